@@ -1,0 +1,229 @@
+"""ctypes bindings of the CPU oracle (cgs_oracle.c) and a runner for the
+reference driver (ref_driver.cpp).
+
+TEST INFRASTRUCTURE.  Imported only by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, as the checker.  The product package never
+imports this module.
+
+``Oracle(precision=64)`` loads liboracle64.so (the FP64 oracle);
+``Oracle(precision=32)`` loads liboracle32.so (the FP32 restatement of the
+reference's arithmetic, used as the timed CPU port).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
+
+KB_W = 4.25          # Reco.cpp:379
+KB_B = 14.9086       # Reco.cpp:378
+KB_ORDER = 5         # Reco.cpp:380
+KB_THRESH = 1e-7     # Reco.cpp:717
+ADJ_SCALE = 1e-3     # Reco.cpp:482
+
+
+def build():
+    """Compile liboracle{64,32}.so (and the reference driver when the
+    reference sources are present)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if os.path.isdir("/root/reference/CGSense"):
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("img", C.c_int32 * 3),
+        ("grid", C.c_int32 * 3),
+        ("n_ch", C.c_int32),
+        ("kb_order", C.c_int32),
+        ("kb_w", C.c_float),
+        ("kb_b", C.c_float),
+        ("kb_thresh", C.c_double),
+        ("adj_scale", C.c_double),
+        ("offcenter", C.c_int32 * 3),
+    ]
+
+
+class Wave(C.Structure):
+    _fields_ = [
+        ("sx", C.c_int32), ("sy", C.c_int32), ("sz", C.c_int32),
+        ("gx", C.c_int32), ("gy", C.c_int32), ("gz", C.c_int32),
+        ("fov_y", C.c_double), ("fov_z", C.c_double),
+        ("n_osc", C.c_int32),
+        ("grad_amp", C.c_double),
+        ("amp_corr_y", C.c_double), ("amp_corr_z", C.c_double),
+        ("shift_y", C.c_double), ("shift_z", C.c_double),
+        ("dwell", C.c_double),
+    ]
+
+
+def make_params(img, grid, n_ch, kb_w=KB_W, kb_b=KB_B, kb_order=KB_ORDER,
+                kb_thresh=KB_THRESH, adj_scale=ADJ_SCALE, offcenter=(0, 0, 0)):
+    p = Params()
+    p.img[:] = list(img)
+    p.grid[:] = list(grid)
+    p.n_ch = n_ch
+    p.kb_order = kb_order
+    p.kb_w = kb_w
+    p.kb_b = kb_b
+    p.kb_thresh = kb_thresh
+    p.adj_scale = adj_scale
+    p.offcenter[:] = list(offcenter)
+    return p
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Taps:
+    """CSR tap lists (ptr[ns+1], idx[T], w[T])."""
+
+    def __init__(self, ptr, idx, w):
+        self.ptr, self.idx, self.w = ptr, idx, w
+
+
+class Oracle:
+    def __init__(self, precision=64):
+        path = os.path.join(BUILD, "liboracle%d.so" % precision)
+        if not os.path.exists(path):
+            build()
+        self.lib = C.CDLL(path)
+        self.real = np.float64 if precision == 64 else np.float32
+        self.cplx = np.complex128 if precision == 64 else np.complex64
+        L = self.lib
+        vp, i64 = C.c_void_p, C.c_int64
+        L.cgso_bessel_i0.restype = C.c_double
+        L.cgso_bessel_i0.argtypes = [C.c_double]
+        L.cgso_conv_function.restype = C.c_float
+        L.cgso_conv_function.argtypes = [vp, vp]
+        L.cgso_tap_counts.restype = i64
+        L.cgso_tap_counts.argtypes = [vp, vp, i64, vp, vp]
+        L.cgso_taps_fill.restype = None
+        L.cgso_taps_fill.argtypes = [vp, vp, i64, vp, vp, vp, vp]
+        L.cgso_kernel_ft.argtypes = [vp, vp]
+        L.cgso_centred_fft.argtypes = [vp, vp, C.c_int, C.c_int]
+        L.cgso_nufft_fwd.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp]
+        L.cgso_nufft_adj.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp]
+        L.cgso_apply_ehde.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp, vp, vp]
+        L.cgso_cg_sense.restype = C.c_int
+        L.cgso_cg_sense.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp, vp, C.c_double, C.c_int,
+                                    vp, vp, vp]
+        L.cgso_wave_caipi.argtypes = [vp, vp]
+
+    # -- kernel ------------------------------------------------------------
+    def taps(self, p, k, mask=None):
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        ns = k.shape[0]
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        counts = np.zeros(ns, np.int32)
+        self.lib.cgso_tap_counts(C.byref(p), _ptr(k), ns, _ptr(m), _ptr(counts))
+        ptr = np.zeros(ns + 1, np.int64)
+        np.cumsum(counts, out=ptr[1:])
+        idx = np.zeros(int(ptr[-1]), np.int32)
+        w = np.zeros(int(ptr[-1]), np.float32)
+        self.lib.cgso_taps_fill(C.byref(p), _ptr(k), ns, _ptr(m), _ptr(ptr), _ptr(idx), _ptr(w))
+        return Taps(ptr, idx, w)
+
+    def kernel_ft(self, p):
+        out = np.zeros(tuple(p.grid), self.cplx)
+        self.lib.cgso_kernel_ft(C.byref(p), _ptr(out))
+        return out
+
+    def centred_fft(self, p, a, sign, rescale):
+        a = np.ascontiguousarray(a, dtype=self.cplx).copy()
+        self.lib.cgso_centred_fft(C.byref(p), _ptr(a), sign, int(rescale))
+        return a
+
+    # -- operators ---------------------------------------------------------
+    def nufft_fwd(self, p, taps, kft, img):
+        ns = taps.ptr.shape[0] - 1
+        img = np.ascontiguousarray(img, dtype=self.cplx)
+        kft = np.ascontiguousarray(kft, dtype=self.cplx)
+        data = np.zeros((p.n_ch, ns), self.cplx)
+        self.lib.cgso_nufft_fwd(C.byref(p), _ptr(taps.ptr), _ptr(taps.idx), _ptr(taps.w), ns,
+                                _ptr(kft), _ptr(img), _ptr(data))
+        return data
+
+    def nufft_adj(self, p, taps, kft, data):
+        ns = taps.ptr.shape[0] - 1
+        data = np.ascontiguousarray(data, dtype=self.cplx)
+        kft = np.ascontiguousarray(kft, dtype=self.cplx)
+        img = np.zeros((p.n_ch,) + tuple(p.img), self.cplx)
+        self.lib.cgso_nufft_adj(C.byref(p), _ptr(taps.ptr), _ptr(taps.idx), _ptr(taps.w), ns,
+                                _ptr(kft), _ptr(data), _ptr(img))
+        return img
+
+    def apply_ehde(self, p, taps, kft, smaps, dcf, x):
+        ns = taps.ptr.shape[0] - 1
+        smaps = np.ascontiguousarray(smaps, dtype=self.cplx)
+        kft = np.ascontiguousarray(kft, dtype=self.cplx)
+        x = np.ascontiguousarray(x, dtype=self.cplx)
+        d = None if dcf is None else np.ascontiguousarray(dcf, dtype=np.float32)
+        q = np.zeros(tuple(p.img), self.cplx)
+        self.lib.cgso_apply_ehde(C.byref(p), _ptr(taps.ptr), _ptr(taps.idx), _ptr(taps.w), ns,
+                                 _ptr(kft), _ptr(smaps), _ptr(d), _ptr(x), _ptr(q))
+        return q
+
+    def cg_sense(self, p, taps, kft, smaps, dcf, data, threshold, max_iter=16):
+        ns = taps.ptr.shape[0] - 1
+        smaps = np.ascontiguousarray(smaps, dtype=self.cplx)
+        kft = np.ascontiguousarray(kft, dtype=self.cplx)
+        data = np.ascontiguousarray(data, dtype=self.cplx)
+        d = None if dcf is None else np.ascontiguousarray(dcf, dtype=np.float32)
+        x = np.zeros(tuple(p.img), self.cplx)
+        res = np.zeros(max(max_iter, 1), np.float64)
+        it = np.zeros(1, np.int32)
+        st = self.lib.cgso_cg_sense(C.byref(p), _ptr(taps.ptr), _ptr(taps.idx), _ptr(taps.w), ns,
+                                    _ptr(kft), _ptr(smaps), _ptr(d), _ptr(data), threshold,
+                                    max_iter, _ptr(x), _ptr(res), _ptr(it))
+        return st, x, res[: it[0]], int(it[0])
+
+    def wave_caipi(self, **kw):
+        w = Wave()
+        for name, _ in Wave._fields_:
+            setattr(w, name, kw[name])
+        n = w.sx * w.sy * w.sz
+        out = np.zeros((n, 3), np.float64)
+        self.lib.cgso_wave_caipi(C.byref(w), _ptr(out))
+        return out
+
+
+# ---------------------------------------------------------------------------
+# Reference driver runner (only where the reference sources were compiled)
+# ---------------------------------------------------------------------------
+
+def ref_available():
+    return os.path.exists(REF_DRIVER)
+
+
+def run_ref(mode, params, arrays, outputs, workdir=None):
+    """Run oracle/_ref/ref_driver <mode> on a temp dir.
+
+    params: dict written to params.txt; arrays: {name: ndarray} written as
+    <name>.bin; outputs: {name: (dtype, count or None)} read back from
+    <name>.bin.  Returns {name: ndarray}.
+    """
+    own = workdir is None
+    d = tempfile.mkdtemp(prefix="cgsref_") if own else workdir
+    with open(os.path.join(d, "params.txt"), "w") as f:
+        for k, v in params.items():
+            f.write("%s %s\n" % (k, repr(v) if isinstance(v, float) else v))
+    for name, a in arrays.items():
+        np.ascontiguousarray(a).tofile(os.path.join(d, name + ".bin"))
+    subprocess.run([REF_DRIVER, mode, d], check=True, stdout=subprocess.DEVNULL)
+    out = {}
+    for name, (dt, cnt) in outputs.items():
+        out[name] = np.fromfile(os.path.join(d, name + ".bin"), dtype=dt,
+                                count=-1 if cnt is None else cnt)
+    if own:
+        import shutil
+        shutil.rmtree(d, ignore_errors=True)
+    return out
