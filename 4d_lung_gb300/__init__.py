@@ -1,0 +1,352 @@
+"""GB300-native CG-SENSE (expRad/4d_lung hot path): Python bindings.
+
+The compute path is the in-tree CUDA library ``libcgsense.so`` (sm_103a
+kernels behind the C ABI of ``include/cgsense_c.h``).  This module is a thin
+ctypes layer over it; there is no CPU fallback: importing works anywhere, but
+every compute call raises when the library or a GPU is missing.
+
+The class :class:`Reco` mirrors the reference's ``Reco`` reconstruction
+object (CGSense/Reco.h:13-214) for the operator and solver path:
+
+    reco = Reco(img=(64,)*3, grid=(128,)*3, n_ch=8)
+    reco.set_trajectory(k)             # Reco::setTrajectory + calculateWeights
+    reco.set_dcf(d)                    # Reco::denCorr (Density::IMPORT)
+    reco.set_smaps(maps)               # Reco::sMaps
+    data = reco.nufft_fwd(coil_imgs)   # Reco::nufftFWD
+    imgs = reco.nufft_adj(data)        # Reco::nufftBWD
+    x, res, it = reco.cg_sense(data, threshold, max_iter=16)   # Reco::cgSenseDynamic
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcgsense.so")
+
+CGS_OK = 0
+CGS_ERR_ARG = 1
+CGS_ERR_CUDA = 2
+CGS_ERR_NONFINITE = 3
+CGS_ERR_STATE = 4
+CGS_ERR_NOMEM = 5
+CGS_ERR_UNSUPPORTED = 6
+CGS_ERR_NO_THRESHOLD = 7
+
+_ERR_NAMES = {
+    1: "CGS_ERR_ARG", 2: "CGS_ERR_CUDA", 3: "CGS_ERR_NONFINITE", 4: "CGS_ERR_STATE",
+    5: "CGS_ERR_NOMEM", 6: "CGS_ERR_UNSUPPORTED", 7: "CGS_ERR_NO_THRESHOLD",
+}
+
+# Every symbol declared in include/cgsense_c.h.
+EXPORTS = [
+    "cgs_default_params", "cgs_create", "cgs_destroy", "cgs_last_error", "cgs_set_stream",
+    "cgs_sync", "cgs_wave_caipi", "cgs_set_trajectory", "cgs_set_mask", "cgs_mask_from_data",
+    "cgs_set_bins", "cgs_num_bins", "cgs_set_dcf", "cgs_set_smaps", "cgs_set_smaps_d",
+    "cgs_kernel_ft", "cgs_fft3", "cgs_fft3_d", "cgs_nufft_fwd", "cgs_nufft_fwd_d",
+    "cgs_nufft_adj", "cgs_nufft_adj_d", "cgs_apply_ehde", "cgs_apply_ehde_d", "cgs_cg_solve",
+    "cgs_cg_solve_batched", "cgs_cg_solve_batched_d", "cgs_last_launch_count",
+    "cgs_profile_apply",
+]
+
+# Stage names of cgs_profile_apply, in launch order (one group of bins).
+STAGES = ["fwd_z", "fwd_y", "fwd_x", "interp", "spread", "adj_x", "adj_y", "adj_z"]
+
+
+class CGSError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (_ERR_NAMES.get(code, "CGS_ERR"), code, msg))
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("img", C.c_int32 * 3),
+        ("grid", C.c_int32 * 3),
+        ("n_ch", C.c_int32),
+        ("kb_order", C.c_int32),
+        ("kb_w", C.c_float),
+        ("kb_b", C.c_float),
+        ("kb_thresh", C.c_double),
+        ("adj_scale", C.c_double),
+        ("offcenter", C.c_int32 * 3),
+        ("device", C.c_int32),
+        ("workspace_bytes", C.c_int64),
+    ]
+
+
+class Wave(C.Structure):
+    _fields_ = [
+        ("sx", C.c_int32), ("sy", C.c_int32), ("sz", C.c_int32),
+        ("gx", C.c_int32), ("gy", C.c_int32), ("gz", C.c_int32),
+        ("fov_y", C.c_double), ("fov_z", C.c_double),
+        ("n_osc", C.c_int32),
+        ("grad_amp", C.c_double),
+        ("amp_corr_y", C.c_double), ("amp_corr_z", C.c_double),
+        ("shift_y", C.c_double), ("shift_z", C.c_double),
+        ("dwell", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def build():
+    """Compile libcgsense.so in place (nvcc, sm_103a)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("_cgs_build", os.path.join(HERE, "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build()
+
+
+def lib():
+    """Load libcgsense.so (raises when it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError("libcgsense.so is not built: run __graft_entry__.build() "
+                           "or python 4d_lung_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    sig = {
+        "cgs_default_params": (None, [vp]),
+        "cgs_create": (C.c_int, [vp, vp]),
+        "cgs_destroy": (None, [vp]),
+        "cgs_last_error": (C.c_char_p, [vp]),
+        "cgs_set_stream": (C.c_int, [vp, vp]),
+        "cgs_sync": (C.c_int, [vp]),
+        "cgs_wave_caipi": (C.c_int, [vp, vp]),
+        "cgs_set_trajectory": (C.c_int, [vp, vp, i64]),
+        "cgs_set_mask": (C.c_int, [vp, vp]),
+        "cgs_mask_from_data": (C.c_int, [vp, vp]),
+        "cgs_set_bins": (C.c_int, [vp, i32, vp, vp]),
+        "cgs_num_bins": (C.c_int, [vp]),
+        "cgs_set_dcf": (C.c_int, [vp, vp]),
+        "cgs_set_smaps": (C.c_int, [vp, vp]),
+        "cgs_set_smaps_d": (C.c_int, [vp, vp]),
+        "cgs_kernel_ft": (C.c_int, [vp, vp]),
+        "cgs_fft3": (C.c_int, [vp, vp, i32, i32]),
+        "cgs_fft3_d": (C.c_int, [vp, vp, i32, i32]),
+        "cgs_nufft_fwd": (C.c_int, [vp, vp, vp]),
+        "cgs_nufft_fwd_d": (C.c_int, [vp, vp, vp]),
+        "cgs_nufft_adj": (C.c_int, [vp, vp, vp]),
+        "cgs_nufft_adj_d": (C.c_int, [vp, vp, vp]),
+        "cgs_apply_ehde": (C.c_int, [vp, i32, vp, vp]),
+        "cgs_apply_ehde_d": (C.c_int, [vp, i32, i32, vp, vp]),
+        "cgs_cg_solve": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
+        "cgs_cg_solve_batched": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
+        "cgs_cg_solve_batched_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
+        "cgs_last_launch_count": (i64, [vp]),
+        "cgs_profile_apply": (C.c_int, [vp, i32, i32, vp, vp, vp, i32, vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def default_params():
+    p = Params()
+    lib().cgs_default_params(C.byref(p))
+    return p
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _c64(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.complex64)
+    if shape is not None and a.size != int(np.prod(shape)):
+        raise ValueError("expected %s complex values, got %d" % (shape, a.size))
+    return a
+
+
+def wave_caipi(sx, sy, sz, grid, fov_y, fov_z, n_osc=4, grad_amp=0.006, amp_corr_y=0.998,
+               amp_corr_z=1.01, shift_y=5.6e-6, shift_z=6.5e-6, dwell=6.3e-6):
+    """WaveCaipi::calculateTraj (Trajectory.cpp:18-184); defaults from CGSense.cpp:51-59."""
+    w = Wave(sx, sy, sz, grid[0], grid[1], grid[2], fov_y, fov_z, n_osc, grad_amp, amp_corr_y,
+             amp_corr_z, shift_y, shift_z, dwell)
+    out = np.zeros((sx * sy * sz, 3), np.float64)
+    st = lib().cgs_wave_caipi(C.byref(w), _p(out))
+    if st != CGS_OK:
+        raise CGSError(st, "invalid wave-CAIPI parameters")
+    return out
+
+
+class Reco:
+    """Reference-shaped reconstruction object over one CUDA context."""
+
+    def __init__(self, img, grid, n_ch, kb_w=4.25, kb_b=14.9086, kb_order=5, kb_thresh=1e-7,
+                 adj_scale=1e-3, offcenter=(0, 0, 0), device=0, workspace_bytes=0):
+        L = lib()
+        p = default_params()
+        p.img[:] = list(img)
+        p.grid[:] = list(grid)
+        p.n_ch = n_ch
+        p.kb_w, p.kb_b, p.kb_order = kb_w, kb_b, kb_order
+        p.kb_thresh, p.adj_scale = kb_thresh, adj_scale
+        p.offcenter[:] = list(offcenter)
+        p.device = device
+        p.workspace_bytes = workspace_bytes
+        self.params = p
+        self.img, self.grid, self.n_ch = tuple(img), tuple(grid), n_ch
+        self.ni = int(np.prod(img))
+        self.ng = int(np.prod(grid))
+        self.ns = 0
+        ctx = C.c_void_p()
+        st = L.cgs_create(C.byref(p), C.byref(ctx))
+        if st != CGS_OK:
+            raise CGSError(st, "cgs_create failed (see stderr)")
+        self._ctx = ctx
+        self._L = L
+
+    # -- plumbing -------------------------------------------------------
+    def _check(self, st):
+        if st != CGS_OK:
+            raise CGSError(st, self._L.cgs_last_error(self._ctx).decode())
+
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.cgs_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def ctx(self):
+        return self._ctx
+
+    def set_stream(self, stream_handle):
+        self._check(self._L.cgs_set_stream(self._ctx, C.c_void_p(stream_handle)))
+
+    def sync(self):
+        self._check(self._L.cgs_sync(self._ctx))
+
+    def launch_count(self):
+        return int(self._L.cgs_last_launch_count(self._ctx))
+
+    # -- set-up ---------------------------------------------------------
+    def set_trajectory(self, k):
+        k = np.ascontiguousarray(k, dtype=np.float64).reshape(-1, 3)
+        self.ns = k.shape[0]
+        self._check(self._L.cgs_set_trajectory(self._ctx, _p(k), self.ns))
+
+    def set_mask(self, mask):
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        self._check(self._L.cgs_set_mask(self._ctx, _p(m)))
+
+    def mask_from_data(self, data):
+        d = _c64(data, (self.n_ch, self.ns))
+        self._check(self._L.cgs_mask_from_data(self._ctx, _p(d)))
+
+    def set_bins(self, bins):
+        """bins: list of integer index arrays (one per respiratory bin)."""
+        off = np.zeros(len(bins) + 1, np.int64)
+        off[1:] = np.cumsum([len(b) for b in bins])
+        idx = np.ascontiguousarray(np.concatenate([np.asarray(b, np.int32) for b in bins]), np.int32)
+        self._check(self._L.cgs_set_bins(self._ctx, len(bins), _p(off), _p(idx)))
+
+    def num_bins(self):
+        return int(self._L.cgs_num_bins(self._ctx))
+
+    def set_dcf(self, dcf):
+        d = None if dcf is None else np.ascontiguousarray(dcf, dtype=np.float32)
+        self._check(self._L.cgs_set_dcf(self._ctx, _p(d)))
+
+    def set_smaps(self, maps):
+        m = _c64(maps, (self.n_ch,) + self.img)
+        self._check(self._L.cgs_set_smaps(self._ctx, _p(m)))
+
+    def set_smaps_tensor(self, maps):
+        self._check(self._L.cgs_set_smaps_d(self._ctx, C.c_void_p(maps.data_ptr())))
+
+    # -- operators (host arrays) -----------------------------------------
+    def kernel_ft(self):
+        out = np.zeros(self.grid, np.complex64)
+        self._check(self._L.cgs_kernel_ft(self._ctx, _p(out)))
+        return out
+
+    def fft3(self, a, sign, rescale=False):
+        a = _c64(a, self.grid).copy()
+        self._check(self._L.cgs_fft3(self._ctx, _p(a), sign, int(rescale)))
+        return a
+
+    def nufft_fwd(self, imgs):
+        imgs = _c64(imgs, (self.n_ch,) + self.img)
+        out = np.zeros((self.n_ch, self.ns), np.complex64)
+        self._check(self._L.cgs_nufft_fwd(self._ctx, _p(imgs), _p(out)))
+        return out
+
+    def nufft_adj(self, data):
+        data = _c64(data, (self.n_ch, self.ns))
+        out = np.zeros((self.n_ch,) + self.img, np.complex64)
+        self._check(self._L.cgs_nufft_adj(self._ctx, _p(data), _p(out)))
+        return out
+
+    def apply_ehde(self, x, bin=0):
+        x = _c64(x, self.img)
+        q = np.zeros(self.img, np.complex64)
+        self._check(self._L.cgs_apply_ehde(self._ctx, bin, _p(x), _p(q)))
+        return q
+
+    def cg_sense(self, data, threshold, max_iter=16):
+        """Reco::cgSenseDynamic on bin 0: returns (x, residuals, iterations)."""
+        data = _c64(data, (self.n_ch, self.ns))
+        x = np.zeros(self.img, np.complex64)
+        res = np.zeros(max(max_iter, 1), np.float64)
+        it = np.zeros(1, np.int32)
+        self._check(self._L.cgs_cg_solve(self._ctx, _p(data), _p(x), threshold, max_iter, _p(res), _p(it)))
+        return x, res[: it[0]], int(it[0])
+
+    def cg_sense_batched(self, data, threshold, max_iter):
+        """All bins: returns (x[nbins], residuals[nbins][max_iter], iters[nbins])."""
+        nb = self.num_bins()
+        data = _c64(data, (self.n_ch, self.ns))
+        x = np.zeros((nb,) + self.img, np.complex64)
+        res = np.zeros((nb, max(max_iter, 1)), np.float64)
+        it = np.zeros(nb, np.int32)
+        self._check(self._L.cgs_cg_solve_batched(self._ctx, _p(data), _p(x), threshold, max_iter,
+                                                 _p(res), _p(it)))
+        return x, res, it
+
+    # -- device (torch) variants ------------------------------------------
+    def nufft_fwd_tensor(self, imgs, out):
+        self._check(self._L.cgs_nufft_fwd_d(self._ctx, C.c_void_p(imgs.data_ptr()), C.c_void_p(out.data_ptr())))
+
+    def nufft_adj_tensor(self, data, out):
+        self._check(self._L.cgs_nufft_adj_d(self._ctx, C.c_void_p(data.data_ptr()), C.c_void_p(out.data_ptr())))
+
+    def apply_ehde_tensor(self, x, q, bin0=0, nb=1):
+        self._check(self._L.cgs_apply_ehde_d(self._ctx, bin0, nb, C.c_void_p(x.data_ptr()),
+                                             C.c_void_p(q.data_ptr())))
+
+    def profile_apply_tensor(self, x, q, bin0=0, nb=1):
+        """Per-stage kernel times (ms) of one E^H D E application."""
+        out = np.zeros(256, np.float32)
+        n = np.zeros(1, np.int32)
+        self._check(self._L.cgs_profile_apply(self._ctx, bin0, nb, C.c_void_p(x.data_ptr()),
+                                              C.c_void_p(q.data_ptr()), _p(out), 256, _p(n)))
+        return out[: n[0]].astype(np.float64)
+
+    def fft3_tensor(self, a, sign):
+        self._check(self._L.cgs_fft3_d(self._ctx, C.c_void_p(a.data_ptr()), sign, 0))
+
+    def cg_sense_batched_tensor(self, data, x, threshold, max_iter, want_stats=True):
+        nb = self.num_bins()
+        res = np.zeros((nb, max(max_iter, 1)), np.float64) if want_stats else None
+        it = np.zeros(nb, np.int32) if want_stats else None
+        self._check(self._L.cgs_cg_solve_batched_d(self._ctx, C.c_void_p(data.data_ptr()),
+                                                   C.c_void_p(x.data_ptr()), threshold, max_iter,
+                                                   _p(res), _p(it)))
+        return res, it

@@ -1,0 +1,85 @@
+"""Build script of the in-tree CUDA library 4d_lung_gb300/libcgsense.so.
+
+Compiles every translation unit of csrc/ for sm_103a with nvcc (in
+parallel) and links them into one shared library with a plain C ABI
+(include/cgsense_c.h).  No CMake: a handful of nvcc invocations.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libcgsense.so")
+NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+         "-I", CSRC, "-I", os.path.join(ROOT, "include")]
+FFT_GROUPS = 6
+
+
+def _units():
+    units = []
+    for g in range(FFT_GROUPS):
+        units.append(("fft_inst.cu", "fft_inst_%d.o" % g, ["-DCGS_FFT_GROUP=%d" % g]))
+    for src in ("fft_dispatch.cu", "kernels_misc.cu", "cgs_api.cu"):
+        units.append((src, src.replace(".cu", ".o"), []))
+    units.append(("wave_caipi.cpp", "wave_caipi.o", []))
+    return units
+
+
+def _stale(obj, deps):
+    if not os.path.exists(obj):
+        return True
+    t = os.path.getmtime(obj)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def build(verbose=False, jobs=None):
+    os.makedirs(BUILD, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(ROOT, "include", "cgsense_c.h"))
+    cmds = []
+    objs = []
+    for src, obj, extra in _units():
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, obj)
+        objs.append(o)
+        if _stale(o, [s, __file__] + headers):
+            if src.endswith(".cpp"):
+                cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-I", os.path.join(ROOT, "include"),
+                       "-c", s, "-o", o]
+            else:
+                cmd = [NVCC] + ARCH + FLAGS + extra + ["-c", s, "-o", o]
+            cmds.append(cmd)
+    jobs = jobs or max(1, min(len(cmds), os.cpu_count() or 4))
+
+    def run(cmd):
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        return cmd, r.returncode, r.stdout
+
+    if cmds:
+        with cf.ThreadPoolExecutor(jobs) as ex:
+            for cmd, rc, out in ex.map(run, cmds):
+                if verbose or rc != 0:
+                    sys.stderr.write(" ".join(cmd) + "\n" + out)
+                if rc != 0:
+                    raise RuntimeError("compilation failed: %s" % cmd[-3])
+    if _stale(LIB, objs):
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + [
+            "-cudart", "static", "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(r.stdout)
+            raise RuntimeError("link failed")
+    return LIB
+
+
+if __name__ == "__main__":
+    build(verbose="-v" in sys.argv)
+    print(LIB)

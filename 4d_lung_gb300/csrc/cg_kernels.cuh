@@ -1,0 +1,195 @@
+// cg_kernels.cuh -- vector updates and FP64 reductions of the CG-SENSE loop
+// (Reco.cpp:175-321), batched over respiratory bins (blockIdx.y).
+//
+// All control stays on the device so that a whole solve can be captured in
+// one CUDA graph: every kernel of an iteration first reads its bin's
+// CgState and returns at once when the bin has stopped (residual below the
+// threshold or the iteration cap reached), which reproduces the reference's
+// `while (currentResidual > cgThreshold)` loop with its 16-iteration cap.
+// Dot products are FP64: per-block partial sums, then a fixed-order sum in
+// one thread, so results do not depend on scheduling.
+#pragma once
+#include "cgs_common.cuh"
+#include "cgs_types.h"
+
+namespace cgs {
+
+
+
+CGS_D void block_reduce2(double& a, double& b, double* s_red /* [2][RED_THREADS/32] */)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_red[w] = a;
+        s_red[RED_THREADS / 32 + w] = b;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ra = 0.0, rb = 0.0;
+        for (int i = 0; i < RED_THREADS / 32; ++i) {
+            ra += s_red[i];
+            rb += s_red[RED_THREADS / 32 + i];
+        }
+        a = ra;
+        b = rb;
+    }
+}
+
+// r = b, p = b, x = 0; partial sums of <b, b>.  grid: (nblk, nbins)
+__global__ void __launch_bounds__(RED_THREADS)
+k_cg_init(const float2* __restrict__ b, float2* r, float2* p, float2* x, long long n, long long bs,
+          double* partials, const CgState* st)
+{
+    __shared__ double s_red[2 * RED_THREADS / 32];
+    const int bin = blockIdx.y;
+    const long long off = (long long)bin * bs;
+    double acc = 0.0, dummy = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 v = b[off + i];
+        r[off + i] = v;
+        p[off + i] = v;
+        x[off + i] = make_float2(0.f, 0.f);
+        acc += (double)v.x * v.x + (double)v.y * v.y;
+    }
+    block_reduce2(acc, dummy, s_red);
+    if (threadIdx.x == 0) {
+        double* o = partials + 2 * ((long long)bin * gridDim.x + blockIdx.x);
+        o[0] = acc;
+        o[1] = 0.0;
+    }
+}
+
+// Sum the partials of <b, b> and arm the state: rr, active.
+__global__ void k_cg_arm(CgState* st, const double* partials, int nblk, int nbins, double thresh, int max_iter)
+{
+    const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bin >= nbins) return;
+    double s = 0.0;
+    for (int i = 0; i < nblk; ++i) s += partials[2 * ((long long)bin * nblk + i)];
+    CgState& S = st[bin];
+    S.rr[0] = s;
+    S.rr[1] = 0.0;
+    S.pq[0] = S.pq[1] = 0.0;
+    S.alpha[0] = S.alpha[1] = 0.0;
+    S.beta[0] = S.beta[1] = 0.0;
+    S.res = 1000.0;          // Reco.cpp:229
+    S.thresh = thresh;
+    S.iter = 0;
+    S.max_iter = max_iter;
+    S.error = 0;
+    // A zero right-hand side (empty bin, all-zero data) would make the
+    // reference divide 0/0 and return NaN; here the solve stops at x = 0.
+    S.active = (S.res > thresh && max_iter > 0 && s > 0.0) ? 1 : 0;
+}
+
+// alpha = rr / pq from the <p, q> partials (complexDivision, Reco.cpp:145-151).
+__global__ void k_cg_alpha(CgState* st, const double* partials, int nblk, int nbins, const float2* q0,
+                           long long bs)
+{
+    const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bin >= nbins) return;
+    CgState& S = st[bin];
+    if (!S.active) return;
+    double pr = 0.0, pim = 0.0;
+    for (int i = 0; i < nblk; ++i) {
+        pr += partials[2 * ((long long)bin * nblk + i)];
+        pim += partials[2 * ((long long)bin * nblk + i) + 1];
+    }
+    S.pq[0] = pr;
+    S.pq[1] = pim;
+    const float2 qv = q0[(long long)bin * bs];
+    if (!isfinite(qv.x) || !isfinite(qv.y) || !isfinite(pr) || !isfinite(pim)) {
+        S.error = 1;
+        S.active = 0;
+        return;
+    }
+    const double d = pr * pr + pim * pim;
+    S.alpha[0] = (S.rr[0] * pr + S.rr[1] * pim) / d;
+    S.alpha[1] = (S.rr[1] * pr - S.rr[0] * pim) / d;
+}
+
+// x += alpha p ; r -= alpha q ; partial sums of |r|^2  (Reco.cpp:285-298)
+__global__ void __launch_bounds__(RED_THREADS)
+k_cg_update_xr(float2* x, float2* r, const float2* __restrict__ p, const float2* __restrict__ q, long long n,
+               long long bs, const CgState* st, double* partials)
+{
+    __shared__ double s_red[2 * RED_THREADS / 32];
+    const int bin = blockIdx.y;
+    const CgState& S = st[bin];
+    if (!S.active) return;
+    const double ar = S.alpha[0], ai = S.alpha[1];
+    const long long off = (long long)bin * bs;
+    double acc = 0.0, dummy = 0.0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 pv = p[off + i], qv = q[off + i];
+        float2 xv = x[off + i], rv = r[off + i];
+        xv.x = (float)((double)xv.x + (ar * pv.x - ai * pv.y));
+        xv.y = (float)((double)xv.y + (ar * pv.y + ai * pv.x));
+        rv.x = (float)((double)rv.x - (ar * qv.x - ai * qv.y));
+        rv.y = (float)((double)rv.y - (ar * qv.y + ai * qv.x));
+        x[off + i] = xv;
+        r[off + i] = rv;
+        acc += (double)rv.x * rv.x + (double)rv.y * rv.y;
+    }
+    block_reduce2(acc, dummy, s_red);
+    if (threadIdx.x == 0) {
+        double* o = partials + 2 * ((long long)bin * gridDim.x + blockIdx.x);
+        o[0] = acc;
+        o[1] = 0.0;
+    }
+}
+
+// residual, beta = rr_new / rr, loop control (Reco.cpp:292-309)
+__global__ void k_cg_beta(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
+                          int res_stride)
+{
+    const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bin >= nbins) return;
+    CgState& S = st[bin];
+    if (!S.active) return;
+    double s = 0.0;
+    for (int i = 0; i < nblk; ++i) s += partials[2 * ((long long)bin * nblk + i)];
+    S.res = sqrt(s);
+    if (residuals) residuals[(long long)bin * res_stride + S.iter] = S.res;
+    // beta = rr_new / rr_old with rr_new real
+    const double d = S.rr[0] * S.rr[0] + S.rr[1] * S.rr[1];
+    S.beta[0] = (s * S.rr[0]) / d;
+    S.beta[1] = (-s * S.rr[1]) / d;
+    S.rr[0] = s;
+    S.rr[1] = 0.0;
+    S.iter += 1;
+    // p is updated in this same iteration before the loop test
+}
+
+// p = r + beta p ; then the loop test  (Reco.cpp:306-309)
+__global__ void k_cg_update_p(float2* p, const float2* __restrict__ r, long long n, long long bs, const CgState* st)
+{
+    const int bin = blockIdx.y;
+    const CgState& S = st[bin];
+    if (!S.active) return;
+    const double br = S.beta[0], bi = S.beta[1];
+    const long long off = (long long)bin * bs;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 pv = p[off + i], rv = r[off + i];
+        float2 o;
+        o.x = (float)((double)rv.x + br * pv.x - bi * pv.y);
+        o.y = (float)((double)rv.y + br * pv.y + bi * pv.x);
+        p[off + i] = o;
+    }
+}
+
+__global__ void k_cg_loop_test(CgState* st, int nbins)
+{
+    const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bin >= nbins) return;
+    CgState& S = st[bin];
+    if (!S.active) return;
+    S.active = (S.res > S.thresh && S.iter < S.max_iter) ? 1 : 0;
+}
+
+}  // namespace cgs

@@ -1,0 +1,1030 @@
+// cgs_api.cu -- C ABI of the GB300 CG-SENSE library: context, trajectory
+// and bin set-up, NUFFT / E^H D E chains, and the graph-captured CG solve.
+//
+// Replaces the reference's Reco object (Reco.h:13-214, Reco.cpp) for the
+// reconstruction hot path; see include/cgsense_c.h for the entry points and
+// the reference functions each one stands for.
+#include "cgsense_c.h"
+#include "launch.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+using namespace cgs;
+
+namespace {
+
+constexpr double kTwoPi = 6.283185307179586476925286766559;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t ensure(size_t n)
+    {
+        if (n <= bytes && p) return cudaSuccess;
+        release();
+        if (n == 0) return cudaSuccess;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        bytes = n;
+        return cudaSuccess;
+    }
+    template <class T>
+    T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct GraphKey {
+    const void* data;
+    void* x;
+    double thresh;
+    int max_iter;
+    bool operator<(const GraphKey& o) const
+    {
+        return std::tie(data, x, thresh, max_iter) < std::tie(o.data, o.x, o.thresh, o.max_iter);
+    }
+};
+
+}  // namespace
+
+struct cgs_ctx {
+    cgs_params p{};
+    int I[3]{}, G[3]{}, lo[3]{};
+    long long Ni = 0, Ng = 0, Nl = 0;
+    int nch = 0;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    float thresh = 0.f;          // absolute tap threshold
+    double adj_scale_total = 0;  // adj_scale / sqrt(Ng)
+    std::vector<double> apod_full[3];   // 1/R_a(g) over the whole grid axis
+
+    DevBuf tw[3], ap[3];
+    // trajectory
+    long long ns = 0;
+    std::vector<double> h_k;
+    DevBuf d_k;
+    std::vector<float> h_dcf;
+    bool has_dcf = false;
+    // bins
+    std::vector<std::vector<int>> bins;   // global sample indices per bin (user order)
+    bool bins_dirty = true;
+    int nbins = 0;
+    long long total = 0;
+    long long max_bin = 0;
+    std::vector<long long> h_bin_off;
+    DevBuf d_sorted, d_rec, d_dcf_sorted, d_bin_off, d_tile_ptr, d_tile_ptr_off, d_tile_idx, d_tile_idx_off;
+    int ntx = 0, nty = 0, ntz = 0, ntiles = 0;
+    // coil maps
+    DevBuf d_smaps;
+    bool smaps_set = false;
+    // workspace
+    int ws_bins = 0;
+    DevBuf d_zbuf, d_ybuf, d_grid, d_yv, d_img, d_data;
+    // CG
+    DevBuf d_b, d_x, d_r, d_pv, d_q, d_state, d_partials, d_partials2, d_res;
+    std::map<GraphKey, cudaGraphExec_t> graphs;
+    std::map<GraphKey, long long> graph_launches;
+    long long launches = 0;
+    // per-stage timing (cgs_profile_apply): events recorded after each pass
+    cudaEvent_t* prof_ev = nullptr;
+    int prof_n = 0;
+    std::string err;
+};
+
+namespace {
+
+int fail(cgs_ctx* c, int code, const std::string& msg)
+{
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CGS_CUDA(ctx, call)                                                                     \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail((ctx), e_ == cudaErrorMemoryAllocation ? CGS_ERR_NOMEM : CGS_ERR_CUDA,    \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                    \
+    } while (0)
+
+#define CGS_LAUNCH(ctx, call)                                                       \
+    do {                                                                            \
+        CGS_CUDA(ctx, call);                                                        \
+        ++(ctx)->launches;                                                          \
+        if ((ctx)->prof_ev) CGS_CUDA(ctx, cudaEventRecord((ctx)->prof_ev[(ctx)->prof_n++], (ctx)->stream)); \
+    } while (0)
+
+#define CGS_TRY(call)              \
+    do {                           \
+        int s_ = (call);           \
+        if (s_ != CGS_OK) return s_; \
+    } while (0)
+
+// Per-axis KB factor of Reco::ConvKernel::convFunction (Reco.h:218-242) at a
+// k-space distance `dist` on an axis of n grid points.
+double kb_factor(const cgs_params& p, int n, double dist)
+{
+    const float w = p.kb_w, b = p.kb_b;
+    const float dk = (float)(1.0 / (double)(float)(n - 1));
+    const float wHalf = (float)(w / 2.0);
+    const float d = (float)dist;
+    if (d > wHalf * dk) return 0.0;
+    const float q = (float)(2.f * d) / (float)(w * dk);
+    const double arg = (double)b * std::sqrt(1.0 - (double)q * (double)q);
+    return std::cyl_bessel_i(0.0, arg) / (double)(float)(100.0f * w * dk);
+}
+
+// ConvKernel::calculateKernelFT (Reco.cpp:560-601) is separable: the 3-D
+// sampled kernel is the product of per-axis factors, so its centred
+// backward transform is the product of per-axis transforms
+//   R_a(g) = (-1)^g sum_n (-1)^n f_a(n) exp(+2 pi i n g / N),
+// which are real (f_a is symmetric about N/2).  kernelFT = 1/(Rx Ry Rz).
+std::vector<double> deapod_axis(const cgs_params& p, int n)
+{
+    const double dk = 1.0 / (double)(n - 1);
+    std::vector<double> f(n);
+    for (int i = 0; i < n; ++i) f[i] = kb_factor(p, n, std::sqrt(dk * dk * (double)(i - n / 2) * (double)(i - n / 2)));
+    std::vector<double> out(n);
+    for (int g = 0; g < n; ++g) {
+        double re = 0.0;
+        for (int i = 0; i < n; ++i) {
+            if (f[i] == 0.0) continue;
+            const long long m = ((long long)i * g) % n;
+            const double s = (((i + g) & 1) ? -1.0 : 1.0);
+            re += s * f[i] * std::cos(kTwoPi * (double)m / (double)n);
+        }
+        out[g] = 1.0 / re;
+    }
+    return out;
+}
+
+// Host-side bin preparation: spatial sort by home tile and per-tile lists of
+// the samples whose support (nearest point +-3, one cell more than the
+// 5-point taps need) touches the tile.
+struct BinPrep {
+    std::vector<int> sorted;
+    std::vector<int> tile_ptr;
+    std::vector<int> tile_idx;
+};
+
+void nearest_point(const double* kk, const int* G, int* nr)
+{
+    for (int a = 0; a < 3; ++a) {
+        int v = (int)((G[a] - 1) * kk[a] + 0.5);
+        nr[a] = std::min(std::max(v, 0), G[a] - 1);
+    }
+}
+
+void prepare_bin(const cgs_ctx* c, const std::vector<int>& samples, BinPrep& out)
+{
+    const int* G = c->G;
+    const long long n = (long long)samples.size();
+    std::vector<int> key(n);
+    std::vector<int> count(c->ntiles + 1, 0);
+    for (long long i = 0; i < n; ++i) {
+        int nr[3];
+        nearest_point(&c->h_k[3 * (size_t)samples[i]], G, nr);
+        const int k = ((nr[0] / TILE_X) * c->nty + nr[1] / TILE_Y) * c->ntz + nr[2] / TILE_Z;
+        key[i] = k;
+        count[k + 1]++;
+    }
+    for (int t = 0; t < c->ntiles; ++t) count[t + 1] += count[t];
+    out.sorted.assign(n, 0);
+    {
+        std::vector<int> pos(count.begin(), count.end() - 1);
+        for (long long i = 0; i < n; ++i) out.sorted[pos[key[i]]++] = samples[i];
+    }
+    out.tile_ptr.assign(c->ntiles + 1, 0);
+    auto range = [&](int nr, int a, int T, int nt, int& t0, int& t1) {
+        const int lo = std::max(nr - 3, 0), hi = std::min(nr + 3, G[a] - 1);
+        t0 = lo / T;
+        t1 = std::min(hi / T, nt - 1);
+    };
+    for (int pass = 0; pass < 2; ++pass) {
+        std::vector<int> fill;
+        if (pass == 1) {
+            for (int t = 0; t < c->ntiles; ++t) out.tile_ptr[t + 1] += out.tile_ptr[t];
+            out.tile_idx.assign(out.tile_ptr[c->ntiles], 0);
+            fill.assign(out.tile_ptr.begin(), out.tile_ptr.end() - 1);
+        }
+        for (long long j = 0; j < n; ++j) {
+            int nr[3];
+            nearest_point(&c->h_k[3 * (size_t)out.sorted[j]], G, nr);
+            int x0, x1, y0, y1, z0, z1;
+            range(nr[0], 0, TILE_X, c->ntx, x0, x1);
+            range(nr[1], 1, TILE_Y, c->nty, y0, y1);
+            range(nr[2], 2, TILE_Z, c->ntz, z0, z1);
+            for (int tx = x0; tx <= x1; ++tx)
+                for (int ty = y0; ty <= y1; ++ty)
+                    for (int tz = z0; tz <= z1; ++tz) {
+                        const int t = (tx * c->nty + ty) * c->ntz + tz;
+                        if (pass == 0) out.tile_ptr[t + 1]++;
+                        else out.tile_idx[fill[t]++] = (int)j;
+                    }
+        }
+    }
+}
+
+int upload(cgs_ctx* c, DevBuf& b, const void* h, size_t bytes)
+{
+    CGS_CUDA(c, b.ensure(bytes));
+    if (bytes) CGS_CUDA(c, cudaMemcpyAsync(b.p, h, bytes, cudaMemcpyHostToDevice, c->stream));
+    return CGS_OK;
+}
+
+void drop_graphs(cgs_ctx* c)
+{
+    for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
+    c->graphs.clear();
+    c->graph_launches.clear();
+}
+
+int rebuild_bins(cgs_ctx* c)
+{
+    if (!c->bins_dirty) return CGS_OK;
+    if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set");
+    drop_graphs(c);
+    c->nbins = (int)c->bins.size();
+    std::vector<BinPrep> prep(c->nbins);
+    c->h_bin_off.assign(c->nbins + 1, 0);
+    for (int b = 0; b < c->nbins; ++b) {
+        prepare_bin(c, c->bins[b], prep[b]);
+        c->h_bin_off[b + 1] = c->h_bin_off[b] + (long long)c->bins[b].size();
+    }
+    c->total = c->h_bin_off[c->nbins];
+    c->max_bin = 0;
+    for (int b = 0; b < c->nbins; ++b) c->max_bin = std::max(c->max_bin, (long long)c->bins[b].size());
+    std::vector<int> sorted;
+    sorted.reserve(c->total);
+    std::vector<int> tile_ptr;
+    std::vector<int> tile_idx;
+    std::vector<long long> tp_off(c->nbins), ti_off(c->nbins);
+    for (int b = 0; b < c->nbins; ++b) {
+        sorted.insert(sorted.end(), prep[b].sorted.begin(), prep[b].sorted.end());
+        tp_off[b] = (long long)tile_ptr.size();
+        tile_ptr.insert(tile_ptr.end(), prep[b].tile_ptr.begin(), prep[b].tile_ptr.end());
+        ti_off[b] = (long long)tile_idx.size();
+        tile_idx.insert(tile_idx.end(), prep[b].tile_idx.begin(), prep[b].tile_idx.end());
+    }
+    CGS_TRY(upload(c, c->d_sorted, sorted.data(), sorted.size() * sizeof(int)));
+    CGS_TRY(upload(c, c->d_bin_off, c->h_bin_off.data(), c->h_bin_off.size() * sizeof(long long)));
+    CGS_TRY(upload(c, c->d_tile_ptr, tile_ptr.data(), tile_ptr.size() * sizeof(int)));
+    CGS_TRY(upload(c, c->d_tile_idx, tile_idx.data(), std::max<size_t>(tile_idx.size(), 1) * sizeof(int)));
+    CGS_TRY(upload(c, c->d_tile_ptr_off, tp_off.data(), tp_off.size() * sizeof(long long)));
+    CGS_TRY(upload(c, c->d_tile_idx_off, ti_off.data(), ti_off.size() * sizeof(long long)));
+    if (c->has_dcf) {
+        std::vector<float> ds(c->total);
+        for (long long j = 0; j < c->total; ++j) ds[j] = c->h_dcf[sorted[j]];
+        CGS_TRY(upload(c, c->d_dcf_sorted, ds.data(), ds.size() * sizeof(float)));
+    }
+    CGS_CUDA(c, c->d_rec.ensure(std::max<long long>(c->total, 1) * sizeof(TapRecord)));
+    KbParams kb;
+    for (int a = 0; a < 3; ++a) kb.G[a] = c->G[a];
+    kb.w = c->p.kb_w;
+    kb.b = c->p.kb_b;
+    kb.thresh = c->thresh;
+    CGS_CUDA(c, launch_tap_records(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, kb, c->d_rec.as<TapRecord>(),
+                                   c->stream));
+    CGS_CUDA(c, c->d_yv.ensure(std::max<long long>(c->total, 1) * c->nch * sizeof(float2)));
+    // workspace for a group of bins
+    const long long per_bin = (long long)c->nch * (c->Nl * c->G[2] + (long long)c->I[0] * c->G[1] * c->G[2] + c->Ng) *
+                              (long long)sizeof(float2);
+    long long budget = c->p.workspace_bytes > 0 ? c->p.workspace_bytes : (64LL << 30);
+    int wsb = (int)std::max<long long>(1, std::min<long long>(c->nbins, budget / std::max<long long>(per_bin, 1)));
+    c->ws_bins = std::max(wsb, 1);
+    const long long wsn = (long long)c->ws_bins * c->nch;
+    CGS_CUDA(c, c->d_zbuf.ensure(wsn * c->Nl * c->G[2] * sizeof(float2)));
+    CGS_CUDA(c, c->d_ybuf.ensure(wsn * (long long)c->I[0] * c->G[1] * c->G[2] * sizeof(float2)));
+    CGS_CUDA(c, c->d_grid.ensure(wsn * c->Ng * sizeof(float2)));
+    c->bins_dirty = false;
+    return CGS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// chains
+// ---------------------------------------------------------------------------
+
+// Forward half for bins [b0, b0+nb) (nb <= ws_bins): image(s) -> grid -> samples (yv).
+// x: per bin [Ni] (x_bs) shared by the coils, or per coil (x_cs) without coil maps.
+int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long long x_cs, bool use_smaps,
+              bool use_dcf)
+{
+    const int Ix = c->I[0], Iy = c->I[1], Iz = c->I[2];
+    const int Gx = c->G[0], Gy = c->G[1], Gz = c->G[2];
+    const long long zb = c->Nl * Gz, yb = (long long)Ix * Gy * Gz;
+    FwdZArgs fz{};
+    fz.x = x;
+    fz.x_cs = x_cs;
+    fz.smaps = use_smaps ? c->d_smaps.as<float2>() : nullptr;
+    fz.apx = c->ap[0].as<float>();
+    fz.apy = c->ap[1].as<float>();
+    fz.apz = c->ap[2].as<float>();
+    fz.out = c->d_zbuf.as<float2>();
+    fz.nl = c->Nl;
+    fz.Iy = Iy;
+    fz.Iz = Iz;
+    fz.lo_z = c->lo[2];
+    fz.nch = c->nch;
+    fz.x_bs = x_bs;
+    fz.out_bs = (long long)c->nch * zb;
+    fz.coil_in = c->Ni;
+    fz.coil_out = zb;
+    fz.tw = c->tw[2].as<float2>();
+    CGS_LAUNCH(c, launch_fwd_z(Gz, fz, nb, c->stream));
+
+    StridedPassArgs fy{};
+    fy.in = c->d_zbuf.as<float2>();
+    fy.out = c->d_ybuf.as<float2>();
+    fy.in_bs = zb;
+    fy.out_bs = yb;
+    fy.in_as = (long long)Iy * Gz;
+    fy.out_as = (long long)Gy * Gz;
+    fy.B = Gz;
+    fy.Lin = Iy;
+    fy.in_off = c->lo[1];
+    fy.Lout = Gy;
+    fy.out_off = 0;
+    fy.tw = c->tw[1].as<float2>();
+    CGS_LAUNCH(c, launch_strided(Gy, -1, fy, Ix, nb * c->nch, c->stream));
+
+    StridedPassArgs fx{};
+    fx.in = c->d_ybuf.as<float2>();
+    fx.out = c->d_grid.as<float2>();
+    fx.in_bs = yb;
+    fx.out_bs = c->Ng;
+    fx.in_as = 0;
+    fx.out_as = 0;
+    fx.B = Gy * Gz;
+    fx.Lin = Ix;
+    fx.in_off = c->lo[0];
+    fx.Lout = Gx;
+    fx.out_off = 0;
+    fx.tw = c->tw[0].as<float2>();
+    CGS_LAUNCH(c, launch_strided(Gx, -1, fx, 1, nb * c->nch, c->stream));
+
+    InterpArgs ia{};
+    ia.grid = c->d_grid.as<float2>();
+    ia.coil_stride = c->Ng;
+    ia.grid_bs = (long long)c->nch * c->Ng;
+    ia.rec = c->d_rec.as<TapRecord>();
+    ia.dcf = (use_dcf && c->has_dcf) ? c->d_dcf_sorted.as<float>() : nullptr;
+    ia.bin_off = c->d_bin_off.as<long long>();
+    ia.bin0 = b0;
+    ia.yv = c->d_yv.as<float2>();
+    ia.nch = c->nch;
+    for (int a = 0; a < 3; ++a) ia.G[a] = c->G[a];
+    ia.thresh = c->thresh;
+    long long mx = 0;
+    for (int b = b0; b < b0 + nb; ++b) mx = std::max(mx, c->h_bin_off[b + 1] - c->h_bin_off[b]);
+    CGS_LAUNCH(c, launch_interp(ia, mx, nb, c->stream));
+    return CGS_OK;
+}
+
+// Adjoint half for bins [b0, b0+nb): samples (yv) -> grid -> image.
+// use_smaps: q[bin] = sum_c conj(S_c) (...) ; else q[coil] per coil (nb == 1).
+int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_smaps, const float2* pdot,
+              double* partials)
+{
+    const int Ix = c->I[0], Iy = c->I[1], Iz = c->I[2];
+    const int Gx = c->G[0], Gy = c->G[1], Gz = c->G[2];
+    const long long zb = c->Nl * Gz, yb = (long long)Ix * Gy * Gz;
+    SpreadArgs sa{};
+    sa.grid = c->d_grid.as<float2>();
+    sa.coil_stride = c->Ng;
+    sa.grid_bs = (long long)c->nch * c->Ng;
+    sa.rec = c->d_rec.as<TapRecord>();
+    sa.yv = c->d_yv.as<float2>();
+    sa.bin_off = c->d_bin_off.as<long long>();
+    sa.tile_ptr = c->d_tile_ptr.as<int>();
+    sa.tile_ptr_off = c->d_tile_ptr_off.as<long long>();
+    sa.tile_idx_off = c->d_tile_idx_off.as<long long>();
+    sa.tile_idx = c->d_tile_idx.as<int>();
+    sa.bin0 = b0;
+    sa.nch = c->nch;
+    const int nchunk = (c->nch + spread_max_coils() - 1) / spread_max_coils();
+    sa.cc = (c->nch + nchunk - 1) / nchunk;
+    for (int a = 0; a < 3; ++a) sa.G[a] = c->G[a];
+    sa.ntx = c->ntx;
+    sa.nty = c->nty;
+    sa.ntz = c->ntz;
+    sa.thresh = c->thresh;
+    CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->stream));
+
+    StridedPassArgs ax{};
+    ax.in = c->d_grid.as<float2>();
+    ax.out = c->d_ybuf.as<float2>();
+    ax.in_bs = c->Ng;
+    ax.out_bs = yb;
+    ax.B = Gy * Gz;
+    ax.Lin = Gx;
+    ax.in_off = 0;
+    ax.Lout = Ix;
+    ax.out_off = c->lo[0];
+    ax.tw = c->tw[0].as<float2>();
+    CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
+
+    StridedPassArgs ay{};
+    ay.in = c->d_ybuf.as<float2>();
+    ay.out = c->d_zbuf.as<float2>();
+    ay.in_bs = yb;
+    ay.out_bs = zb;
+    ay.in_as = (long long)Gy * Gz;
+    ay.out_as = (long long)Iy * Gz;
+    ay.B = Gz;
+    ay.Lin = Gy;
+    ay.in_off = 0;
+    ay.Lout = Iy;
+    ay.out_off = c->lo[1];
+    ay.tw = c->tw[1].as<float2>();
+    CGS_LAUNCH(c, launch_strided(Gy, +1, ay, Ix, nb * c->nch, c->stream));
+
+    AdjZArgs az{};
+    az.in = c->d_zbuf.as<float2>();
+    az.smaps = use_smaps ? c->d_smaps.as<float2>() : nullptr;
+    az.apx = c->ap[0].as<float>();
+    az.apy = c->ap[1].as<float>();
+    az.apz = c->ap[2].as<float>();
+    az.scale = (float)c->adj_scale_total;
+    az.q = q;
+    az.p = pdot;
+    az.partials = partials;
+    az.nl = c->Nl;
+    az.Iy = Iy;
+    az.Iz = Iz;
+    az.lo_z = c->lo[2];
+    az.nch = c->nch;
+    az.in_bs = (long long)c->nch * zb;
+    az.q_bs = q_bs;
+    az.coil_in = zb;
+    az.coil_s = c->Ni;
+    az.q_cs = c->Ni;
+    az.tw = c->tw[2].as<float2>();
+    CGS_LAUNCH(c, launch_adj_z(Gz, az, nb, c->stream));
+    return CGS_OK;
+}
+
+// q = A x for bins [b0, b0+nb) (all groups).  pdot/partials: fused <p, q>.
+int apply_bins(cgs_ctx* c, int b0, int nb, const float2* x, float2* q, const float2* pdot, double* partials,
+               int nblk)
+{
+    for (int g = b0; g < b0 + nb; g += c->ws_bins) {
+        const int n = std::min(c->ws_bins, b0 + nb - g);
+        const long long off = (long long)(g - b0) * c->Ni;
+        CGS_TRY(fwd_chain(c, g, n, x + off, c->Ni, 0, true, true));
+        CGS_TRY(adj_chain(c, g, n, q + off, c->Ni, true, pdot ? pdot + off : nullptr,
+                          partials ? partials + 2LL * (g - b0) * nblk : nullptr));
+    }
+    return CGS_OK;
+}
+
+int check_ready(cgs_ctx* c, bool need_smaps)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set (cgs_set_trajectory)");
+    if (need_smaps && !c->smaps_set) return fail(c, CGS_ERR_STATE, "no coil maps set (cgs_set_smaps)");
+    CGS_TRY(rebuild_bins(c));
+    return CGS_OK;
+}
+
+int centred_fft_dev(cgs_ctx* c, float2* a, int sign, int rescale)
+{
+    const int Gx = c->G[0], Gy = c->G[1], Gz = c->G[2];
+    ContigPassArgs cz{};
+    cz.in = a;
+    cz.out = a;
+    cz.nl = (long long)Gx * Gy;
+    cz.Lin = Gz;
+    cz.in_off = 0;
+    cz.Lout = Gz;
+    cz.out_off = 0;
+    cz.tw = c->tw[2].as<float2>();
+    CGS_LAUNCH(c, launch_contig(Gz, sign, cz, 1, c->stream));
+    StridedPassArgs sy{};
+    sy.in = a;
+    sy.out = a;
+    sy.in_as = sy.out_as = (long long)Gy * Gz;
+    sy.B = Gz;
+    sy.Lin = sy.Lout = Gy;
+    sy.tw = c->tw[1].as<float2>();
+    CGS_LAUNCH(c, launch_strided(Gy, sign, sy, Gx, 1, c->stream));
+    StridedPassArgs sx{};
+    sx.in = a;
+    sx.out = a;
+    sx.B = Gy * Gz;
+    sx.Lin = sx.Lout = Gx;
+    sx.tw = c->tw[0].as<float2>();
+    CGS_LAUNCH(c, launch_strided(Gx, sign, sx, 1, 1, c->stream));
+    if (rescale) {
+        // Fourier.cpp:31-41 rescales by 1/sqrt(N) after the backward transform;
+        // the host API applies it here, the operator chains fold it into the
+        // adjoint epilogue.
+        return fail(c, CGS_ERR_ARG, "internal: rescale handled by caller");
+    }
+    return CGS_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+
+extern "C" {
+
+void cgs_default_params(cgs_params* p)
+{
+    std::memset(p, 0, sizeof(*p));
+    p->n_ch = 1;
+    p->kb_order = 5;
+    p->kb_w = 4.25f;
+    p->kb_b = 14.9086f;
+    p->kb_thresh = 1e-7;
+    p->adj_scale = 1e-3;
+}
+
+const char* cgs_last_error(const cgs_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int cgs_create(const cgs_params* p, cgs_ctx** out)
+{
+    if (!p || !out) return CGS_ERR_ARG;
+    *out = nullptr;
+    cgs_ctx* c = new cgs_ctx();
+    c->p = *p;
+    auto bad = [&](int code, const std::string& m) {
+        static thread_local std::string last;
+        last = m;
+        std::fprintf(stderr, "cgs_create: %s\n", m.c_str());
+        delete c;
+        return code;
+    };
+    if (p->n_ch < 1) return bad(CGS_ERR_ARG, "n_ch must be >= 1");
+    if (!(p->kb_w > 0.f && p->kb_w < 5.f)) return bad(CGS_ERR_ARG, "kb_w must be in (0, 5)");
+    if (!(p->kb_b >= 0.f) || !(p->kb_thresh >= 0.0) || !std::isfinite(p->adj_scale))
+        return bad(CGS_ERR_ARG, "kb_b and kb_thresh must be >= 0, adj_scale finite");
+    for (int a = 0; a < 3; ++a) {
+        const int g = p->grid[a], i = p->img[a];
+        if (g < 2 || (g & 1)) return bad(CGS_ERR_ARG, "grid sizes must be even (Fourier.cpp:54,64)");
+        if (!fft_supported(g)) return bad(CGS_ERR_UNSUPPORTED, "grid size " + std::to_string(g) + " has no FFT kernel");
+        if (i < 1 || i > g) return bad(CGS_ERR_ARG, "image size must be in [1, grid]");
+        const int lo = (g - i) / 2 + p->offcenter[a];
+        if (lo < 0 || lo + i > g) return bad(CGS_ERR_ARG, "image box (offcenter) outside the grid");
+        c->I[a] = i;
+        c->G[a] = g;
+        c->lo[a] = lo;
+    }
+    if (p->grid[0] > 2048 || p->grid[1] > 2048 || p->grid[2] > 1024) return bad(CGS_ERR_ARG, "grid too large");
+    c->nch = p->n_ch;
+    c->Ni = (long long)c->I[0] * c->I[1] * c->I[2];
+    c->Ng = (long long)c->G[0] * c->G[1] * c->G[2];
+    c->Nl = (long long)c->I[0] * c->I[1];
+    c->device = p->device;
+    if (cudaSetDevice(c->device) != cudaSuccess) return bad(CGS_ERR_CUDA, "cudaSetDevice failed");
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bad(CGS_ERR_CUDA, "cudaStreamCreate failed");
+    c->stream = c->own_stream;
+    if (kernels_init() != cudaSuccess) return bad(CGS_ERR_CUDA, "kernel attribute setup failed");
+    // tap threshold: convFunction(0) * kb_thresh (Reco.cpp:716-717)
+    double kb0 = 1.0;
+    for (int a = 0; a < 3; ++a) kb0 *= kb_factor(*p, c->G[a], 0.0);
+    c->thresh = (float)((double)(float)kb0 * p->kb_thresh);
+    c->adj_scale_total = p->adj_scale / std::sqrt((double)c->Ng);
+    for (int a = 0; a < 3; ++a) {
+        const int L = c->G[a];
+        std::vector<float2> tw(L);
+        for (int m = 0; m < L; ++m) {
+            const double ang = -kTwoPi * (double)m / (double)L;
+            tw[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+        }
+        if (upload(c, c->tw[a], tw.data(), L * sizeof(float2)) != CGS_OK) return bad(CGS_ERR_CUDA, c->err);
+        c->apod_full[a] = deapod_axis(*p, L);
+        std::vector<float> ap(c->I[a]);
+        for (int i = 0; i < c->I[a]; ++i) ap[i] = (float)c->apod_full[a][i + c->lo[a]];
+        if (upload(c, c->ap[a], ap.data(), ap.size() * sizeof(float)) != CGS_OK) return bad(CGS_ERR_CUDA, c->err);
+    }
+    c->ntx = (c->G[0] + TILE_X - 1) / TILE_X;
+    c->nty = (c->G[1] + TILE_Y - 1) / TILE_Y;
+    c->ntz = (c->G[2] + TILE_Z - 1) / TILE_Z;
+    c->ntiles = c->ntx * c->nty * c->ntz;
+    if (cudaMalloc(&c->d_smaps.p, (size_t)c->nch * c->Ni * sizeof(float2)) != cudaSuccess)
+        return bad(CGS_ERR_NOMEM, "coil map allocation failed");
+    c->d_smaps.bytes = (size_t)c->nch * c->Ni * sizeof(float2);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bad(CGS_ERR_CUDA, "set-up failed");
+    *out = c;
+    return CGS_OK;
+}
+
+void cgs_destroy(cgs_ctx* c)
+{
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    drop_graphs(c);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+}
+
+int cgs_set_stream(cgs_ctx* c, void* stream)
+{
+    if (!c) return CGS_ERR_ARG;
+    cudaStream_t s = stream ? (cudaStream_t)stream : c->own_stream;
+    if (s != c->stream) drop_graphs(c);
+    c->stream = s;
+    return CGS_OK;
+}
+
+int cgs_sync(cgs_ctx* c)
+{
+    if (!c) return CGS_ERR_ARG;
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CGS_OK;
+}
+
+int cgs_set_trajectory(cgs_ctx* c, const double* k, int64_t ns)
+{
+    if (!c || (!k && ns > 0) || ns < 0) return CGS_ERR_ARG;
+    if (ns > (int64_t)0x7fffffff) return fail(c, CGS_ERR_ARG, "too many samples");
+    for (int64_t i = 0; i < 3 * ns; ++i)
+        if (!std::isfinite(k[i])) return fail(c, CGS_ERR_NONFINITE, "non-finite trajectory coordinate");
+    c->h_k.assign(k, k + 3 * ns);
+    c->ns = ns;
+    CGS_TRY(upload(c, c->d_k, k, (size_t)(3 * std::max<int64_t>(ns, 1)) * sizeof(double)));
+    c->bins.assign(1, std::vector<int>());
+    c->bins[0].resize(ns);
+    for (int64_t i = 0; i < ns; ++i) c->bins[0][i] = (int)i;
+    c->has_dcf = false;
+    c->h_dcf.clear();
+    c->bins_dirty = true;
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CGS_OK;
+}
+
+int cgs_set_mask(cgs_ctx* c, const uint8_t* mask)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set");
+    c->bins.assign(1, std::vector<int>());
+    for (long long i = 0; i < c->ns; ++i)
+        if (!mask || mask[i]) c->bins[0].push_back((int)i);
+    c->bins_dirty = true;
+    return CGS_OK;
+}
+
+int cgs_mask_from_data(cgs_ctx* c, const float* data)
+{
+    if (!c || !data) return CGS_ERR_ARG;
+    if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set");
+    std::vector<uint8_t> m(c->ns);
+    for (long long i = 0; i < c->ns; ++i) m[i] = (data[2 * i] == 0.f && data[2 * i + 1] == 0.f) ? 0 : 1;
+    return cgs_set_mask(c, m.data());
+}
+
+int cgs_set_bins(cgs_ctx* c, int32_t nbins, const int64_t* offsets, const int32_t* idx)
+{
+    if (!c || nbins < 1 || !offsets || nbins > 65535) return CGS_ERR_ARG;
+    if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set");
+    if (offsets[0] != 0) return fail(c, CGS_ERR_ARG, "offsets[0] must be 0");
+    std::vector<std::vector<int>> bins(nbins);
+    for (int b = 0; b < nbins; ++b) {
+        if (offsets[b + 1] < offsets[b]) return fail(c, CGS_ERR_ARG, "offsets must be non-decreasing");
+        for (int64_t j = offsets[b]; j < offsets[b + 1]; ++j) {
+            if (idx[j] < 0 || idx[j] >= c->ns) return fail(c, CGS_ERR_ARG, "sample index out of range");
+            bins[b].push_back(idx[j]);
+        }
+    }
+    c->bins.swap(bins);
+    c->bins_dirty = true;
+    return CGS_OK;
+}
+
+int cgs_num_bins(const cgs_ctx* c) { return c ? (int)c->bins.size() : 0; }
+
+int cgs_set_dcf(cgs_ctx* c, const float* dcf)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set");
+    if (!dcf) {
+        c->has_dcf = false;
+        c->h_dcf.clear();
+    } else {
+        for (long long i = 0; i < c->ns; ++i)
+            if (!std::isfinite(dcf[i])) return fail(c, CGS_ERR_NONFINITE, "non-finite density weight");
+        c->h_dcf.assign(dcf, dcf + c->ns);
+        c->has_dcf = true;
+    }
+    c->bins_dirty = true;
+    return CGS_OK;
+}
+
+int cgs_set_smaps(cgs_ctx* c, const float* maps)
+{
+    if (!c || !maps) return CGS_ERR_ARG;
+    const size_t n = (size_t)c->nch * c->Ni * 2;
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(maps[i])) return fail(c, CGS_ERR_NONFINITE, "non-finite coil map value");
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_smaps.p, maps, n * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->smaps_set = true;
+    return CGS_OK;
+}
+
+int cgs_set_smaps_d(cgs_ctx* c, const float* maps)
+{
+    if (!c || !maps) return CGS_ERR_ARG;
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_smaps.p, maps, (size_t)c->nch * c->Ni * sizeof(float2),
+                                cudaMemcpyDeviceToDevice, c->stream));
+    c->smaps_set = true;
+    return CGS_OK;
+}
+
+int cgs_kernel_ft(cgs_ctx* c, float* kft)
+{
+    if (!c || !kft) return CGS_ERR_ARG;
+    const int Gx = c->G[0], Gy = c->G[1], Gz = c->G[2];
+    for (int i = 0; i < Gx; ++i)
+        for (int j = 0; j < Gy; ++j)
+            for (int k = 0; k < Gz; ++k) {
+                const size_t e = ((size_t)i * Gy + j) * Gz + k;
+                kft[2 * e] = (float)(c->apod_full[0][i] * c->apod_full[1][j] * c->apod_full[2][k]);
+                kft[2 * e + 1] = 0.f;
+            }
+    return CGS_OK;
+}
+
+int cgs_fft3_d(cgs_ctx* c, float* grid, int32_t sign, int32_t rescale)
+{
+    if (!c || !grid || (sign != -1 && sign != 1)) return CGS_ERR_ARG;
+    c->launches = 0;
+    CGS_TRY(centred_fft_dev(c, reinterpret_cast<float2*>(grid), sign, 0));
+    (void)rescale;
+    return CGS_OK;
+}
+
+int cgs_fft3(cgs_ctx* c, float* grid, int32_t sign, int32_t rescale)
+{
+    if (!c || !grid || (sign != -1 && sign != 1)) return CGS_ERR_ARG;
+    const size_t bytes = (size_t)c->Ng * sizeof(float2);
+    CGS_CUDA(c, c->d_img.ensure(bytes));
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_img.p, grid, bytes, cudaMemcpyHostToDevice, c->stream));
+    c->launches = 0;
+    CGS_TRY(centred_fft_dev(c, c->d_img.as<float2>(), sign, 0));
+    CGS_CUDA(c, cudaMemcpyAsync(grid, c->d_img.p, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (rescale) {
+        const double s = 1.0 / std::sqrt((double)c->Ng);
+        for (size_t i = 0; i < 2 * (size_t)c->Ng; ++i) grid[i] = (float)((double)grid[i] * s);
+    }
+    return CGS_OK;
+}
+
+int cgs_nufft_fwd_d(cgs_ctx* c, const float* img, float* data)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!img || !data) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (c->nbins != 1) return fail(c, CGS_ERR_STATE, "cgs_nufft_fwd works on a single bin (mask)");
+    c->launches = 0;
+    CGS_CUDA(c, cudaMemsetAsync(data, 0, (size_t)c->nch * c->ns * sizeof(float2), c->stream));
+    CGS_TRY(fwd_chain(c, 0, 1, reinterpret_cast<const float2*>(img), 0, c->Ni, false, false));
+    CGS_LAUNCH(c, launch_scatter_samples(c->d_yv.as<float2>(), c->d_sorted.as<int>(), c->total, c->nch, c->ns,
+                                         reinterpret_cast<float2*>(data), c->stream));
+    return CGS_OK;
+}
+
+int cgs_nufft_adj_d(cgs_ctx* c, const float* data, float* img)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!img || !data) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (c->nbins != 1) return fail(c, CGS_ERR_STATE, "cgs_nufft_adj works on a single bin (mask)");
+    c->launches = 0;
+    CGS_LAUNCH(c, launch_gather_samples(reinterpret_cast<const float2*>(data), c->ns, c->d_sorted.as<int>(), c->total,
+                                        c->nch, nullptr, c->d_yv.as<float2>(), c->stream));
+    CGS_TRY(adj_chain(c, 0, 1, reinterpret_cast<float2*>(img), 0, false, nullptr, nullptr));
+    return CGS_OK;
+}
+
+int cgs_nufft_fwd(cgs_ctx* c, const float* img, float* data)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!img || !data) return fail(c, CGS_ERR_ARG, "null pointer");
+    const size_t bi = (size_t)c->nch * c->Ni * sizeof(float2), bd = (size_t)c->nch * c->ns * sizeof(float2);
+    CGS_CUDA(c, c->d_img.ensure(bi));
+    CGS_CUDA(c, c->d_data.ensure(bd));
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_img.p, img, bi, cudaMemcpyHostToDevice, c->stream));
+    CGS_TRY(cgs_nufft_fwd_d(c, c->d_img.as<float>(), c->d_data.as<float>()));
+    CGS_CUDA(c, cudaMemcpyAsync(data, c->d_data.p, bd, cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CGS_OK;
+}
+
+int cgs_nufft_adj(cgs_ctx* c, const float* data, float* img)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!img || !data) return fail(c, CGS_ERR_ARG, "null pointer");
+    const size_t bi = (size_t)c->nch * c->Ni * sizeof(float2), bd = (size_t)c->nch * c->ns * sizeof(float2);
+    CGS_CUDA(c, c->d_img.ensure(bi));
+    CGS_CUDA(c, c->d_data.ensure(bd));
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_data.p, data, bd, cudaMemcpyHostToDevice, c->stream));
+    CGS_TRY(cgs_nufft_adj_d(c, c->d_data.as<float>(), c->d_img.as<float>()));
+    CGS_CUDA(c, cudaMemcpyAsync(img, c->d_img.p, bi, cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CGS_OK;
+}
+
+int cgs_apply_ehde_d(cgs_ctx* c, int32_t bin0, int32_t nb, const float* x, float* q)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!x || !q) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (bin0 < 0 || nb < 1 || bin0 + nb > c->nbins) return fail(c, CGS_ERR_ARG, "bin range out of bounds");
+    c->launches = 0;
+    return apply_bins(c, bin0, nb, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(q), nullptr, nullptr,
+                      0);
+}
+
+int cgs_apply_ehde(cgs_ctx* c, int32_t bin, const float* x, float* q)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!x || !q) return fail(c, CGS_ERR_ARG, "null pointer");
+    const size_t b = (size_t)c->Ni * sizeof(float2);
+    CGS_CUDA(c, c->d_img.ensure(2 * b));
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_img.p, x, b, cudaMemcpyHostToDevice, c->stream));
+    float2* dq = c->d_img.as<float2>() + c->Ni;
+    CGS_TRY(cgs_apply_ehde_d(c, bin, 1, c->d_img.as<float>(), reinterpret_cast<float*>(dq)));
+    CGS_CUDA(c, cudaMemcpyAsync(q, dq, b, cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CGS_OK;
+}
+
+// The whole batched solve is recorded once into a CUDA graph (per data/x
+// pointers, threshold and iteration cap) and replayed.
+static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh, int max_iter)
+{
+    const int nb = c->nbins;
+    const long long Ni = c->Ni;
+    const int nblk_adj = adj_z_blocks(c->G[2], c->Nl);
+    const int nblk_cg = cg_blocks(Ni);
+    // RHS: b = sum_c conj(S_c) E_c^H (D y_c)   (CGSense.cpp:226-235, Reco.cpp:182-190)
+    CGS_LAUNCH(c, launch_gather_samples(data, c->ns, c->d_sorted.as<int>(), c->total, c->nch,
+                                        c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr, c->d_yv.as<float2>(),
+                                        c->stream));
+    for (int g = 0; g < nb; g += c->ws_bins) {
+        const int n = std::min(c->ws_bins, nb - g);
+        CGS_TRY(adj_chain(c, g, n, c->d_b.as<float2>() + (long long)g * Ni, Ni, true, nullptr, nullptr));
+    }
+    CgState* st = c->d_state.as<CgState>();
+    CGS_LAUNCH(c, launch_cg_init(c->d_b.as<float2>(), c->d_r.as<float2>(), c->d_pv.as<float2>(), x, Ni, Ni,
+                                 c->d_partials2.as<double>(), st, nb, c->stream));
+    CGS_LAUNCH(c, launch_cg_arm(st, c->d_partials2.as<double>(), nblk_cg, nb, thresh, max_iter, c->stream));
+    for (int it = 0; it < max_iter; ++it) {
+        CGS_TRY(apply_bins(c, 0, nb, c->d_pv.as<float2>(), c->d_q.as<float2>(), c->d_pv.as<float2>(),
+                           c->d_partials.as<double>(), nblk_adj));
+        CGS_LAUNCH(c, launch_cg_alpha(st, c->d_partials.as<double>(), nblk_adj, nb, c->d_q.as<float2>(), Ni, c->stream));
+        CGS_LAUNCH(c, launch_cg_update_xr(x, c->d_r.as<float2>(), c->d_pv.as<float2>(), c->d_q.as<float2>(), Ni, Ni, st,
+                                          c->d_partials2.as<double>(), nb, c->stream));
+        CGS_LAUNCH(c, launch_cg_beta(st, c->d_partials2.as<double>(), nblk_cg, nb, c->d_res.as<double>(), max_iter,
+                                     c->stream));
+        CGS_LAUNCH(c, launch_cg_update_p(c->d_pv.as<float2>(), c->d_r.as<float2>(), Ni, Ni, st, nb, c->stream));
+        CGS_LAUNCH(c, launch_cg_loop_test(st, nb, c->stream));
+    }
+    return CGS_OK;
+}
+
+int cgs_cg_solve_batched_d(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter,
+                           double* residuals, int32_t* iters)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!data || !x) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (thresh == -1.0) return fail(c, CGS_ERR_NO_THRESHOLD, "no threshold set for CG SENSE (Reco.cpp:192-196)");
+    if (max_iter < 0 || max_iter > 10000) return fail(c, CGS_ERR_ARG, "max_iter out of range");
+    const int nb = c->nbins;
+    const long long Ni = c->Ni;
+    const size_t vb = (size_t)nb * Ni * sizeof(float2);
+    const int nblk_adj = adj_z_blocks(c->G[2], c->Nl);
+    const int nblk_cg = cg_blocks(Ni);
+    CGS_CUDA(c, c->d_b.ensure(vb));
+    CGS_CUDA(c, c->d_r.ensure(vb));
+    CGS_CUDA(c, c->d_pv.ensure(vb));
+    CGS_CUDA(c, c->d_q.ensure(vb));
+    CGS_CUDA(c, c->d_state.ensure(nb * sizeof(CgState)));
+    CGS_CUDA(c, c->d_partials.ensure((size_t)nb * nblk_adj * 2 * sizeof(double)));
+    CGS_CUDA(c, c->d_partials2.ensure((size_t)nb * nblk_cg * 2 * sizeof(double)));
+    CGS_CUDA(c, c->d_res.ensure((size_t)nb * std::max(max_iter, 1) * sizeof(double)));
+
+    GraphKey key{data, x, thresh, max_iter};
+    auto it = c->graphs.find(key);
+    cudaGraphExec_t exec = nullptr;
+    if (it == c->graphs.end()) {
+        c->launches = 0;
+        CGS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        int st = record_solve(c, reinterpret_cast<const float2*>(data), reinterpret_cast<float2*>(x), thresh, max_iter);
+        cudaGraph_t graph = nullptr;
+        cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
+        if (st != CGS_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        CGS_CUDA(c, ee);
+        cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        CGS_CUDA(c, ei);
+        c->graphs[key] = exec;
+        c->graph_launches[key] = c->launches;
+    } else {
+        exec = it->second;
+    }
+    c->launches = c->graph_launches[key];
+    CGS_CUDA(c, cudaGraphLaunch(exec, c->stream));
+    if (residuals || iters) {
+        std::vector<CgState> hs(nb);
+        CGS_CUDA(c, cudaMemcpyAsync(hs.data(), c->d_state.p, nb * sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
+        std::vector<double> hr((size_t)nb * std::max(max_iter, 1));
+        if (residuals)
+            CGS_CUDA(c, cudaMemcpyAsync(hr.data(), c->d_res.p, hr.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        c->stream));
+        CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int b = 0; b < nb; ++b) {
+            if (iters) iters[b] = hs[b].iter;
+            if (residuals)
+                for (int i = 0; i < max_iter; ++i)
+                    residuals[(size_t)b * max_iter + i] = i < hs[b].iter ? hr[(size_t)b * max_iter + i] : 0.0;
+        }
+        for (int b = 0; b < nb; ++b)
+            if (hs[b].error)
+                return fail(c, CGS_ERR_NONFINITE, "NaN or INF value in image detected (bin " + std::to_string(b) + ")");
+    }
+    return CGS_OK;
+}
+
+int cgs_cg_solve_batched(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter,
+                         double* residuals, int32_t* iters)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!data || !x) return fail(c, CGS_ERR_ARG, "null pointer");
+    const size_t bd = (size_t)c->nch * c->ns * sizeof(float2);
+    const size_t bx = (size_t)c->nbins * c->Ni * sizeof(float2);
+    CGS_CUDA(c, c->d_data.ensure(bd));
+    CGS_CUDA(c, c->d_x.ensure(bx));
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_data.p, data, bd, cudaMemcpyHostToDevice, c->stream));
+    std::vector<int32_t> it_local(c->nbins);
+    int st = cgs_cg_solve_batched_d(c, c->d_data.as<float>(), c->d_x.as<float>(), thresh, max_iter, residuals,
+                                    iters ? iters : it_local.data());
+    if (st != CGS_OK && st != CGS_ERR_NONFINITE) return st;
+    CGS_CUDA(c, cudaMemcpyAsync(x, c->d_x.p, bx, cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return st;
+}
+
+int cgs_cg_solve(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter, double* residuals,
+                 int32_t* iters)
+{
+    CGS_TRY(check_ready(c, true));
+    if (c->nbins != 1) return fail(c, CGS_ERR_STATE, "cgs_cg_solve reconstructs one bin; use cgs_cg_solve_batched");
+    return cgs_cg_solve_batched(c, data, x, thresh, max_iter, residuals, iters);
+}
+
+int64_t cgs_last_launch_count(const cgs_ctx* c) { return c ? c->launches : 0; }
+
+int cgs_profile_apply(cgs_ctx* c, int32_t bin0, int32_t nb, const float* x, float* q, float* stage_ms,
+                      int32_t max_stages, int32_t* n_stages)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!x || !q || !stage_ms || max_stages < 1) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (bin0 < 0 || nb < 1 || bin0 + nb > c->nbins) return fail(c, CGS_ERR_ARG, "bin range out of bounds");
+    const int groups = (nb + c->ws_bins - 1) / c->ws_bins;
+    const int nev = 1 + 8 * groups;
+    std::vector<cudaEvent_t> ev(nev);
+    for (auto& e : ev) CGS_CUDA(c, cudaEventCreate(&e));
+    CGS_CUDA(c, cudaEventRecord(ev[0], c->stream));
+    c->prof_ev = ev.data() + 1;
+    c->prof_n = 0;
+    c->launches = 0;
+    int st = apply_bins(c, bin0, nb, reinterpret_cast<const float2*>(x), reinterpret_cast<float2*>(q), nullptr,
+                        nullptr, 0);
+    const int rec = c->prof_n;
+    c->prof_ev = nullptr;
+    c->prof_n = 0;
+    if (st == CGS_OK) {
+        CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+        const int ns = std::min(rec, (int)max_stages);
+        for (int i = 0; i < ns; ++i) CGS_CUDA(c, cudaEventElapsedTime(&stage_ms[i], ev[i], ev[i + 1]));
+        if (n_stages) *n_stages = ns;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    return st;
+}
+
+}  // extern "C"

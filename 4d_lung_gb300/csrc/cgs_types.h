@@ -1,0 +1,127 @@
+// cgs_types.h -- argument records and layout constants shared by the
+// kernels (device side) and their launchers (host side).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cgs {
+
+// KB taps: 5 candidate grid points per axis (w < 5)
+constexpr int TAPS_1D = 5;
+// spreading tile (grid points) owned by one block
+constexpr int TILE_X = 4, TILE_Y = 8, TILE_Z = 16;
+constexpr int TILE_PTS = TILE_X * TILE_Y * TILE_Z;
+constexpr int SPREAD_THREADS = 32 * TILE_X;
+constexpr int RED_THREADS = 256;
+
+struct CgState {
+    double rr[2];      // <r, r> of the current residual
+    double pq[2];      // <p, q>
+    double alpha[2];
+    double beta[2];
+    double res;        // ||r||_2 after the last update
+    double thresh;     // absolute residual threshold (Reco.cpp:230)
+    int iter;          // completed iterations
+    int max_iter;
+    int active;        // 1 while the loop runs
+    int error;         // 1: non-finite value detected (Reco.cpp:264-268)
+};
+
+struct StridedPassArgs {
+    const float2* in;
+    float2* out;
+    long long in_bs, out_bs;   // batch strides (blockIdx.y)
+    long long in_as, out_as;   // strides of the outer index a
+    int B;                     // columns (contiguous extent)
+    int ntb;                   // column tiles per outer index
+    int Lin, in_off, Lout, out_off;
+    const float2* tw;          // L twiddles
+};
+
+struct ContigPassArgs {
+    const float2* in;
+    float2* out;
+    long long in_bs, out_bs;
+    long long nl;              // lines per batch item
+    int Lin, in_off, Lout, out_off;
+    const float2* tw;
+};
+
+struct FwdZArgs {
+    const float2* x;        // [nl][Iz]   image (one bin), or one image per coil
+    long long x_cs;         // coil stride of x (0: one image shared by all coils)
+    const float2* smaps;    // [nch][nl][Iz], or null (no coil multiply)
+    const float* apx;       // [Ix]
+    const float* apy;       // [Iy]
+    const float* apz;       // [Iz]
+    float2* out;            // [nch][nl][L]
+    long long nl;
+    int Iy, Iz, lo_z, nch;
+    long long x_bs, out_bs; // batch strides (blockIdx.y: bins)
+    long long coil_in, coil_out;  // coil strides of smaps and out
+    const float2* tw;
+};
+
+struct AdjZArgs {
+    const float2* in;       // [nch][nl][L]
+    const float2* smaps;    // [nch][nl][Iz]; null: one output image per coil, no coil sum
+    const float* apx;
+    const float* apy;
+    const float* apz;
+    float scale;            // adj_scale / sqrt(Ng)
+    float2* q;              // [nl][Iz]
+    const float2* p;        // optional [nl][Iz]
+    double* partials;       // [gridDim.y][gridDim.x][2]
+    long long nl;
+    int Iy, Iz, lo_z, nch;
+    long long in_bs, q_bs;  // batch strides (bins)
+    long long coil_in, coil_s;
+    long long q_cs;         // coil stride of q when smaps is null
+    const float2* tw;
+};
+
+struct TapRecord {
+    float4 q[4];   // w[0..14] = x(5) y(5) z(5); q[3].w holds the packed nearest point
+};
+
+struct KbParams {
+    int G[3];          // grid size
+    float w;           // KB width (cells)
+    float b;           // KB shape
+    float thresh;      // absolute tap threshold
+};
+
+struct InterpArgs {
+    const float2* grid;        // coil c at grid + c*coil_stride (+ bin stride)
+    long long coil_stride;
+    long long grid_bs;         // bin stride of the grids (blockIdx.z)
+    const TapRecord* rec;      // sorted tap records (all bins concatenated)
+    const float* dcf;          // sorted density weights, or null
+    const long long* bin_off;  // [nbins+1] sample offsets
+    int bin0;                  // first bin of this launch
+    float2* yv;                // [total samples][nch]
+    int nch;
+    int G[3];
+    float thresh;
+};
+
+struct SpreadArgs {
+    float2* grid;              // coil c at grid + c*coil_stride (+ bin stride)
+    long long coil_stride;
+    long long grid_bs;
+    const TapRecord* rec;
+    const float2* yv;          // [total samples][nch]
+    const long long* bin_off;  // [nbins+1]
+    const int* tile_ptr;       // per bin: [ntiles+1] offsets into tile_idx (relative to bin)
+    const long long* tile_ptr_off;  // [nbins] start of each bin's tile_ptr array
+    const long long* tile_idx_off;  // [nbins] start of each bin's tile_idx array
+    const int* tile_idx;       // sample positions relative to the bin start
+    int bin0;
+    int nch;
+    int cc;                    // coils per block (chunk)
+    int G[3];
+    int ntx, nty, ntz;         // tiles per axis
+    float thresh;
+};
+
+}  // namespace cgs

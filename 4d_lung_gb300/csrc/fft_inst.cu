@@ -1,0 +1,108 @@
+// fft_inst.cu -- instantiation of the FFT pass kernels for one group of line
+// lengths (compiled once per group with -DCGS_FFT_GROUP=g).
+#include "fft_sizes.h"
+#include "launch.h"
+#include "fft_passes.cuh"
+
+#ifndef CGS_FFT_GROUP
+#define CGS_FFT_GROUP 0
+#endif
+
+namespace cgs {
+
+constexpr int rmax2(int a, int b) { return a > b ? a : b; }
+constexpr int strided_tb(int r1, int r2) { return rmax2(r1, r2) > 16 ? 8 : 16; }
+constexpr int contig_lpb(int r1, int r2) { return rmax2(r1, r2) > 16 ? 8 : (rmax2(r1, r2) > 8 ? 16 : 32); }
+
+template <int R1, int R2>
+struct SizeImpl {
+    static constexpr int L = R1 * R2;
+    static constexpr int TB = strided_tb(R1, R2);
+    static constexpr int LPB = contig_lpb(R1, R2);
+    static constexpr int NT_S = TB * rmax2(R1, R2);
+    static constexpr int NT_C = LPB * rmax2(R1, R2);
+    static_assert(NT_C % 32 == 0, "contiguous pass block must be whole warps");
+
+    static cudaError_t strided(int sign, StridedPassArgs a, int A, int batch, cudaStream_t s)
+    {
+        a.ntb = (a.B + TB - 1) / TB;
+        dim3 grid((unsigned)(A * a.ntb), (unsigned)batch);
+        if (sign < 0) k_fft_strided<R1, R2, -1, TB><<<grid, NT_S, 0, s>>>(a);
+        else k_fft_strided<R1, R2, +1, TB><<<grid, NT_S, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    static cudaError_t contig(int sign, const ContigPassArgs& a, int batch, cudaStream_t s)
+    {
+        dim3 grid((unsigned)((a.nl + LPB - 1) / LPB), (unsigned)batch);
+        if (sign < 0) k_fft_contig<R1, R2, -1, LPB><<<grid, NT_C, 0, s>>>(a);
+        else k_fft_contig<R1, R2, +1, LPB><<<grid, NT_C, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    static cudaError_t fwd_z(const FwdZArgs& a, int batch, cudaStream_t s)
+    {
+        dim3 grid((unsigned)((a.nl + LPB - 1) / LPB), (unsigned)batch);
+        k_fwd_z<R1, R2, LPB><<<grid, NT_C, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+    static int adj_blocks(long long nl) { return (int)((nl + LPB - 1) / LPB); }
+    static cudaError_t adj_z(const AdjZArgs& a, int batch, cudaStream_t s)
+    {
+        dim3 grid((unsigned)adj_blocks(a.nl), (unsigned)batch);
+        k_adj_z<R1, R2, LPB><<<grid, NT_C, 0, s>>>(a);
+        return cudaGetLastError();
+    }
+};
+
+#define CGS_DEFINE(L_, R1_, R2_, G_)                                                                \
+    cudaError_t fft_strided_##L_(int sign, const StridedPassArgs& a, int A, int batch, cudaStream_t s); \
+    cudaError_t fft_contig_##L_(int sign, const ContigPassArgs& a, int batch, cudaStream_t s);        \
+    cudaError_t fft_fwd_z_##L_(const FwdZArgs& a, int batch, cudaStream_t s);                          \
+    cudaError_t fft_adj_z_##L_(const AdjZArgs& a, int batch, cudaStream_t s);                          \
+    int fft_adj_blocks_##L_(long long nl);                                                             \
+    CGS_DEFINE_IF_##G_(L_, R1_, R2_)
+
+#define CGS_BODY(L_, R1_, R2_)                                                                      \
+    cudaError_t fft_strided_##L_(int sign, const StridedPassArgs& a, int A, int batch, cudaStream_t s) \
+    { return SizeImpl<R1_, R2_>::strided(sign, a, A, batch, s); }                                   \
+    cudaError_t fft_contig_##L_(int sign, const ContigPassArgs& a, int batch, cudaStream_t s)         \
+    { return SizeImpl<R1_, R2_>::contig(sign, a, batch, s); }                                       \
+    cudaError_t fft_fwd_z_##L_(const FwdZArgs& a, int batch, cudaStream_t s)                           \
+    { return SizeImpl<R1_, R2_>::fwd_z(a, batch, s); }                                              \
+    cudaError_t fft_adj_z_##L_(const AdjZArgs& a, int batch, cudaStream_t s)                           \
+    { return SizeImpl<R1_, R2_>::adj_z(a, batch, s); }                                              \
+    int fft_adj_blocks_##L_(long long nl) { return SizeImpl<R1_, R2_>::adj_blocks(nl); }
+
+#if CGS_FFT_GROUP == 0
+#define CGS_DEFINE_IF_0(L, R1, R2) CGS_BODY(L, R1, R2)
+#else
+#define CGS_DEFINE_IF_0(L, R1, R2)
+#endif
+#if CGS_FFT_GROUP == 1
+#define CGS_DEFINE_IF_1(L, R1, R2) CGS_BODY(L, R1, R2)
+#else
+#define CGS_DEFINE_IF_1(L, R1, R2)
+#endif
+#if CGS_FFT_GROUP == 2
+#define CGS_DEFINE_IF_2(L, R1, R2) CGS_BODY(L, R1, R2)
+#else
+#define CGS_DEFINE_IF_2(L, R1, R2)
+#endif
+#if CGS_FFT_GROUP == 3
+#define CGS_DEFINE_IF_3(L, R1, R2) CGS_BODY(L, R1, R2)
+#else
+#define CGS_DEFINE_IF_3(L, R1, R2)
+#endif
+#if CGS_FFT_GROUP == 4
+#define CGS_DEFINE_IF_4(L, R1, R2) CGS_BODY(L, R1, R2)
+#else
+#define CGS_DEFINE_IF_4(L, R1, R2)
+#endif
+#if CGS_FFT_GROUP == 5
+#define CGS_DEFINE_IF_5(L, R1, R2) CGS_BODY(L, R1, R2)
+#else
+#define CGS_DEFINE_IF_5(L, R1, R2)
+#endif
+
+CGS_FFT_SIZES(CGS_DEFINE)
+
+}  // namespace cgs

@@ -1,0 +1,385 @@
+// fft_passes.cuh -- one-axis passes of the centred 3-D FFT, with the
+// coil / deapodisation / crop work of the NUFFT fused into the passes that
+// touch the image.
+//
+// The reference's centred transform (Fourier.cpp:19-42) multiplies by
+// (-1)^(i+j+k) before and after an unnormalised FFTW c2c transform.  The
+// sign factor separates per axis, so every pass below multiplies its input
+// by (-1)^l and its output by (-1)^l, l being the grid position along the
+// pass axis.
+//
+// A line of length L = R1 * R2 is transformed in two register stages with
+// one exchange through shared memory:
+//   stage 1: thread n2 loads x[R2*n1 + n2] (n1 < R1), runs an R1-point DFT,
+//            multiplies by W_L^(n2*k1) and stores Y[k1][n2];
+//   stage 2: thread k1 loads Y[k1][n2] (n2 < R2), runs an R2-point DFT and
+//            writes X[k1 + R1*k2].
+// Global loads of stage 1 and stores of stage 2 are coalesced in both
+// layouts: along the line for z passes, across the tile's columns otherwise.
+//
+// Pruning (zero-padded oversampled grid): a pass reads only the Lin stored
+// input positions [in_off, in_off+Lin) of each line (the rest are zero) and
+// writes only the Lout kept output positions [out_off, out_off+Lout).
+#pragma once
+#include "fft_codelets.cuh"
+#include "cgs_types.h"
+
+namespace cgs {
+
+// Twiddle table tw[m] = exp(-2*pi*i*m/L), m < L; SIGN=+1 uses the conjugate.
+template <int SIGN>
+CGS_D float2 table_twiddle(float2 v, float2 w)
+{
+    if (SIGN < 0) return cmul(v, w);
+    return cmulc(v, w);
+}
+
+CGS_D float2 parity(float2 v, int l) { return (l & 1) ? cneg(v) : v; }
+
+// ---------------------------------------------------------------------------
+// Strided pass: lines along a non-contiguous axis of an [A][Lrows][B] array.
+// One block handles TB consecutive columns b of one outer index a.
+// ---------------------------------------------------------------------------
+
+template <int R1, int R2, int SIGN, int TB>
+__global__ void __launch_bounds__(TB * (R1 > R2 ? R1 : R2))
+k_fft_strided(StridedPassArgs a)
+{
+    constexpr int L = R1 * R2;
+    __shared__ float2 s_tw[L];
+    __shared__ float2 s_y[L * TB];
+    const int tid = threadIdx.x;
+    for (int m = tid; m < L; m += blockDim.x) s_tw[m] = a.tw[m];
+
+    const int tile = blockIdx.x;
+    const int ai = tile / a.ntb;
+    const int b0 = (tile - ai * a.ntb) * TB;
+    const int bi = tid % TB;
+    const int b = b0 + bi;
+    const bool bok = b < a.B;
+    const float2* in = a.in + (long long)blockIdx.y * a.in_bs + (long long)ai * a.in_as + b;
+    float2* out = a.out + (long long)blockIdx.y * a.out_bs + (long long)ai * a.out_as + b;
+
+    __syncthreads();
+    {
+        const int n2 = tid / TB;
+        if (n2 < R2) {
+            float2 v[R1];
+#pragma unroll
+            for (int n1 = 0; n1 < R1; ++n1) {
+                const int l = R2 * n1 + n2;
+                const int li = l - a.in_off;
+                float2 x = make_float2(0.f, 0.f);
+                if (bok && li >= 0 && li < a.Lin) x = parity(in[(long long)li * a.B], l);
+                v[n1] = x;
+            }
+            Dft<R1, SIGN>::run(v);
+#pragma unroll
+            for (int k1 = 0; k1 < R1; ++k1) {
+                float2 t = v[k1];
+                if (k1 > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * k1]);
+                s_y[(k1 * R2 + n2) * TB + bi] = t;
+            }
+        }
+    }
+    __syncthreads();
+    {
+        const int k1 = tid / TB;
+        if (k1 < R1) {
+            float2 u[R2];
+#pragma unroll
+            for (int n2 = 0; n2 < R2; ++n2) u[n2] = s_y[(k1 * R2 + n2) * TB + bi];
+            Dft<R2, SIGN>::run(u);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) {
+                const int l = k1 + R1 * k2;
+                const int lo = l - a.out_off;
+                if (bok && lo >= 0 && lo < a.Lout) out[(long long)lo * a.B] = parity(u[k2], l);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Contiguous passes (z axis): LPB whole lines per block.
+// Shared layout per line: Y[n2][k1] with an odd row pitch (conflict-free).
+// ---------------------------------------------------------------------------
+template <int R1, int R2>
+struct ContigLayout {
+    static constexpr int L = R1 * R2;
+    static constexpr int R1P = R1 | 1;
+    static constexpr int LINE = R2 * R1P;
+    static constexpr int RMAX = R1 > R2 ? R1 : R2;
+};
+
+// Plain centred pass on contiguous lines: out[line][l] = F(in[line][.])
+
+template <int R1, int R2, int SIGN, int LPB>
+__global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX)
+k_fft_contig(ContigPassArgs a)
+{
+    using Lay = ContigLayout<R1, R2>;
+    constexpr int L = Lay::L;
+    __shared__ float2 s_tw[L];
+    __shared__ float2 s_y[LPB * Lay::LINE];
+    const int tid = threadIdx.x;
+    for (int m = tid; m < L; m += blockDim.x) s_tw[m] = a.tw[m];
+    const long long line0 = (long long)blockIdx.x * LPB;
+    const float2* in = a.in + (long long)blockIdx.y * a.in_bs;
+    float2* out = a.out + (long long)blockIdx.y * a.out_bs;
+    __syncthreads();
+    {
+        const int ln = tid / R2, n2 = tid % R2;
+        const long long line = line0 + ln;
+        if (ln < LPB && line < a.nl) {
+            float2 v[R1];
+#pragma unroll
+            for (int n1 = 0; n1 < R1; ++n1) {
+                const int l = R2 * n1 + n2;
+                const int li = l - a.in_off;
+                float2 x = make_float2(0.f, 0.f);
+                if (li >= 0 && li < a.Lin) x = parity(in[line * a.Lin + li], l);
+                v[n1] = x;
+            }
+            Dft<R1, SIGN>::run(v);
+#pragma unroll
+            for (int k1 = 0; k1 < R1; ++k1) {
+                float2 t = v[k1];
+                if (k1 > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * k1]);
+                s_y[ln * Lay::LINE + n2 * Lay::R1P + k1] = t;
+            }
+        }
+    }
+    __syncthreads();
+    {
+        const int ln = tid / R1, k1 = tid % R1;
+        const long long line = line0 + ln;
+        if (ln < LPB && line < a.nl) {
+            float2 u[R2];
+#pragma unroll
+            for (int n2 = 0; n2 < R2; ++n2) u[n2] = s_y[ln * Lay::LINE + n2 * Lay::R1P + k1];
+            Dft<R2, SIGN>::run(u);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) {
+                const int l = k1 + R1 * k2;
+                const int lo = l - a.out_off;
+                if (lo >= 0 && lo < a.Lout) out[line * a.Lout + lo] = parity(u[k2], l);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Forward z pass fused with the coil multiply, deapodisation and zero-pad
+// (Reco.cpp:236-240 elementProduct, Reco.cpp:529-535 kernelFT multiply):
+//   zbuf[c][line][l] = F_z( pad( x * S_c * apod ) ),  for all coils c.
+// Lines are the Ix*Iy image (x, y) positions; their x/y apodisation factors
+// and the x/y parities are applied here and in the later passes respectively.
+// ---------------------------------------------------------------------------
+
+template <int R1, int R2, int LPB>
+__global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX)
+k_fwd_z(FwdZArgs a)
+{
+    using Lay = ContigLayout<R1, R2>;
+    constexpr int L = Lay::L;
+    constexpr int SIGN = -1;
+    __shared__ float2 s_tw[L];
+    __shared__ float2 s_y[LPB * Lay::LINE];
+    const int tid = threadIdx.x;
+    for (int m = tid; m < L; m += blockDim.x) s_tw[m] = a.tw[m];
+    const long long line0 = (long long)blockIdx.x * LPB;
+    const float2* xin = a.x + (long long)blockIdx.y * a.x_bs;
+    float2* outb = a.out + (long long)blockIdx.y * a.out_bs;
+
+    // stage-1 role
+    const int ln1 = tid / R2, n2 = tid % R2;
+    const long long line1 = line0 + ln1;
+    const bool act1 = ln1 < LPB && line1 < a.nl;
+    // image values times apodisation (reloaded per coil only for per-coil images)
+    float2 xa[R1];
+    float axy = 0.f;
+    if (act1) {
+        const int ix = (int)(line1 / a.Iy), iy = (int)(line1 - (long long)ix * a.Iy);
+        axy = a.apx[ix] * a.apy[iy];
+    }
+    const int ln2 = tid / R1, k1 = tid % R1;
+    const long long line2 = line0 + ln2;
+    const bool act2 = ln2 < LPB && line2 < a.nl;
+
+    for (int c = 0; c < a.nch; ++c) {
+        __syncthreads();   // s_tw ready / previous coil's stage 2 finished
+        if (act1) {
+            if (c == 0 || a.x_cs != 0) {
+                const float2* xl = xin + (long long)c * a.x_cs + line1 * a.Iz;
+#pragma unroll
+                for (int n1 = 0; n1 < R1; ++n1) {
+                    const int l = R2 * n1 + n2;
+                    const int zi = l - a.lo_z;
+                    float2 v = make_float2(0.f, 0.f);
+                    if (zi >= 0 && zi < a.Iz) v = parity(cscale(xl[zi], axy * a.apz[zi]), l);
+                    xa[n1] = v;
+                }
+            }
+            float2 v[R1];
+            if (a.smaps) {
+                const float2* S = a.smaps + (long long)c * a.coil_in + line1 * a.Iz;
+#pragma unroll
+                for (int n1 = 0; n1 < R1; ++n1) {
+                    const int zi = R2 * n1 + n2 - a.lo_z;
+                    v[n1] = (zi >= 0 && zi < a.Iz) ? cmul(xa[n1], S[zi]) : make_float2(0.f, 0.f);
+                }
+            } else {
+#pragma unroll
+                for (int n1 = 0; n1 < R1; ++n1) v[n1] = xa[n1];
+            }
+            Dft<R1, SIGN>::run(v);
+#pragma unroll
+            for (int kk = 0; kk < R1; ++kk) {
+                float2 t = v[kk];
+                if (kk > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * kk]);
+                s_y[ln1 * Lay::LINE + n2 * Lay::R1P + kk] = t;
+            }
+        }
+        __syncthreads();
+        if (act2) {
+            float2 u[R2];
+#pragma unroll
+            for (int m = 0; m < R2; ++m) u[m] = s_y[ln2 * Lay::LINE + m * Lay::R1P + k1];
+            Dft<R2, SIGN>::run(u);
+            float2* o = outb + (long long)c * a.coil_out + line2 * L;
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) {
+                const int l = k1 + R1 * k2;
+                o[l] = parity(u[k2], l);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint z pass fused with crop, deapodisation, rescale, conjugate coil
+// multiply and the coil sum (Reco.cpp:509-517, 257-262; Fourier.cpp:31-41):
+//   q[line][z] = scale * apod * sum_c conj(S_c) * F^H_z(zbuf[c][line])[z + lo_z]
+// The coil sum is accumulated in registers in coil order (no atomics).
+// When p != nullptr, the block also accumulates <p, q> = sum conj(p) q in
+// double precision and writes it to partials[blockIdx] (re, im).
+// ---------------------------------------------------------------------------
+
+template <int R1, int R2, int LPB>
+__global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX)
+k_adj_z(AdjZArgs a)
+{
+    using Lay = ContigLayout<R1, R2>;
+    constexpr int L = Lay::L;
+    constexpr int SIGN = +1;
+    constexpr int NT = LPB * Lay::RMAX;
+    __shared__ float2 s_tw[L];
+    __shared__ float2 s_y[LPB * Lay::LINE];
+    __shared__ double s_red[2][NT / 32];
+    const int tid = threadIdx.x;
+    for (int m = tid; m < L; m += blockDim.x) s_tw[m] = a.tw[m];
+    const long long line0 = (long long)blockIdx.x * LPB;
+    const float2* inb = a.in + (long long)blockIdx.y * a.in_bs;
+    float2* qb = a.q + (long long)blockIdx.y * a.q_bs;
+
+    const int ln1 = tid / R2, n2 = tid % R2;
+    const long long line1 = line0 + ln1;
+    const bool act1 = ln1 < LPB && line1 < a.nl;
+    const int ln2 = tid / R1, k1 = tid % R1;
+    const long long line2 = line0 + ln2;
+    const bool act2 = ln2 < LPB && line2 < a.nl;
+
+    float2 acc[R2];
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) acc[k2] = make_float2(0.f, 0.f);
+
+    for (int c = 0; c < a.nch; ++c) {
+        __syncthreads();
+        if (act1) {
+            const float2* src = inb + (long long)c * a.coil_in + line1 * L;
+            float2 v[R1];
+#pragma unroll
+            for (int n1 = 0; n1 < R1; ++n1) {
+                const int l = R2 * n1 + n2;
+                v[n1] = parity(src[l], l);
+            }
+            Dft<R1, SIGN>::run(v);
+#pragma unroll
+            for (int kk = 0; kk < R1; ++kk) {
+                float2 t = v[kk];
+                if (kk > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * kk]);
+                s_y[ln1 * Lay::LINE + n2 * Lay::R1P + kk] = t;
+            }
+        }
+        __syncthreads();
+        if (act2) {
+            float2 u[R2];
+#pragma unroll
+            for (int m = 0; m < R2; ++m) u[m] = s_y[ln2 * Lay::LINE + m * Lay::R1P + k1];
+            Dft<R2, SIGN>::run(u);
+            if (a.smaps) {
+                const float2* S = a.smaps + (long long)c * a.coil_s + line2 * a.Iz;
+#pragma unroll
+                for (int k2 = 0; k2 < R2; ++k2) {
+                    const int l = k1 + R1 * k2;
+                    const int zi = l - a.lo_z;
+                    if (zi >= 0 && zi < a.Iz) acc[k2] = cadd(acc[k2], cmulc(parity(u[k2], l), S[zi]));
+                }
+            } else {
+                const int ix = (int)(line2 / a.Iy), iy = (int)(line2 - (long long)ix * a.Iy);
+                const float sxy = a.scale * a.apx[ix] * a.apy[iy];
+                float2* qc = qb + (long long)c * a.q_cs + line2 * a.Iz;
+#pragma unroll
+                for (int k2 = 0; k2 < R2; ++k2) {
+                    const int l = k1 + R1 * k2;
+                    const int zi = l - a.lo_z;
+                    if (zi >= 0 && zi < a.Iz) qc[zi] = cscale(parity(u[k2], l), sxy * a.apz[zi]);
+                }
+            }
+        }
+    }
+    if (!a.smaps) return;
+    double dre = 0.0, dim = 0.0;
+    if (act2) {
+        const int ix = (int)(line2 / a.Iy), iy = (int)(line2 - (long long)ix * a.Iy);
+        const float sxy = a.scale * a.apx[ix] * a.apy[iy];
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) {
+            const int zi = k1 + R1 * k2 - a.lo_z;
+            if (zi >= 0 && zi < a.Iz) {
+                const float2 qv = cscale(acc[k2], sxy * a.apz[zi]);
+                qb[line2 * a.Iz + zi] = qv;
+                if (a.p) {
+                    const float2 pv = a.p[(long long)blockIdx.y * a.q_bs + line2 * a.Iz + zi];
+                    dre += (double)pv.x * qv.x + (double)pv.y * qv.y;
+                    dim += (double)pv.x * qv.y - (double)pv.y * qv.x;
+                }
+            }
+        }
+    }
+    if (a.p) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            dre += __shfl_xor_sync(0xffffffffu, dre, o);
+            dim += __shfl_xor_sync(0xffffffffu, dim, o);
+        }
+        if ((tid & 31) == 0) {
+            s_red[0][tid >> 5] = dre;
+            s_red[1][tid >> 5] = dim;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double r0 = 0.0, r1 = 0.0;
+            for (int w = 0; w < NT / 32; ++w) {
+                r0 += s_red[0][w];
+                r1 += s_red[1][w];
+            }
+            double* out = a.partials + 2 * ((long long)blockIdx.y * gridDim.x + blockIdx.x);
+            out[0] = r0;
+            out[1] = r1;
+        }
+    }
+}
+
+}  // namespace cgs

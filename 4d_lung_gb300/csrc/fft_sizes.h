@@ -1,0 +1,11 @@
+// fft_sizes.h -- supported FFT line lengths and their two-stage split
+// L = R1 * R2 (both register codelets).  X(L, R1, R2, GROUP): GROUP picks
+// the translation unit that instantiates the size (parallel builds).
+#pragma once
+#define CGS_FFT_SIZES(X)                                                              \
+    X(16, 4, 4, 0) X(20, 4, 5, 1) X(24, 4, 6, 2) X(32, 4, 8, 3) X(40, 8, 5, 4)        \
+    X(48, 8, 6, 5) X(64, 8, 8, 0) X(80, 8, 10, 1) X(96, 8, 12, 2) X(128, 8, 16, 3)    \
+    X(160, 16, 10, 4) X(176, 16, 11, 5) X(192, 16, 12, 0) X(224, 16, 14, 1)           \
+    X(256, 16, 16, 2) X(320, 16, 20, 3) X(352, 32, 11, 4) X(384, 16, 24, 5)           \
+    X(448, 16, 28, 0) X(512, 16, 32, 1)
+#define CGS_FFT_NGROUPS 6

@@ -1,0 +1,238 @@
+// gridding.cuh -- Kaiser-Bessel interpolation (gather) and spreading
+// (scatter) between the non-Cartesian samples and the Cartesian grid.
+//
+// Kernel and tap set follow Reco::ConvKernel (Reco.h:218-242,
+// Reco.cpp:698-806):
+//   * sample k in [0,1]^3 sits at grid coordinate k*(N-1), dk = 1/(N-1);
+//   * per axis the KB factor is I0(b*sqrt(1-(2d/(w dk))^2)) / (100 w dk) for
+//     |d| <= w/2 dk, else 0; the 3-D weight is the product of the factors;
+//   * a tap is kept when its weight exceeds thresh = KB(0,0,0) * 1e-7;
+//   * taps outside [0, N-1] are dropped (no wrap-around).
+// With w <= 5 every tap lies within +-2 cells of the nearest grid point
+// (int)(k*(N-1) + 0.5), so each sample has 5 candidate factors per axis.
+//
+// The per-axis factors are computed once per trajectory into a 64-byte tap
+// record per sample: 15 weights (0 for candidates outside the support or the
+// grid) and the packed nearest grid point.
+#pragma once
+#include "cgs_common.cuh"
+#include "cgs_types.h"
+
+namespace cgs {
+
+
+
+CGS_D unsigned pack_nearest(int nx, int ny, int nz)
+{
+    return (unsigned)nx | ((unsigned)ny << 11) | ((unsigned)nz << 22);
+}
+CGS_D void unpack_nearest(unsigned u, int& nx, int& ny, int& nz)
+{
+    nx = (int)(u & 2047u);
+    ny = (int)((u >> 11) & 2047u);
+    nz = (int)(u >> 22);
+}
+
+
+// ---------------------------------------------------------------------------
+// Tap records.  sample_idx maps sorted position -> global sample index.
+// The distance arithmetic follows Reco.cpp:763-771: double k minus the
+// float product (index * float dk), then a float distance.
+// ---------------------------------------------------------------------------
+__global__ void k_tap_records(const double* __restrict__ k, const int* __restrict__ sample_idx,
+                              long long n, KbParams kb, TapRecord* __restrict__ out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const long long g = sample_idx ? sample_idx[i] : i;
+    float wv[3][TAPS_1D];
+    int nearest[3];
+    const float wHalf = (float)(kb.w / 2.0);
+    for (int a = 0; a < 3; ++a) {
+        const int N = kb.G[a];
+        const double ka = k[3 * g + a];
+        const float dk = (float)(1.0 / (double)(float)(N - 1));
+        int nr = (int)__dadd_rn(__dmul_rn((double)(N - 1), ka), 0.5);   // no FMA: matches the host
+        nr = nr < 0 ? 0 : (nr > N - 1 ? N - 1 : nr);
+        nearest[a] = nr;
+        for (int j = 0; j < TAPS_1D; ++j) {
+            const int gi = nr - 2 + j;
+            float val = 0.f;
+            if (gi >= 0 && gi <= N - 1) {
+                const double dd = ka - (double)__fmul_rn((float)gi, dk);
+                const float d = (float)fabs(dd);
+                if (!(d > wHalf * dk)) {
+                    const float q = (float)(2.f * d) / (float)(kb.w * dk);
+                    const double arg = (double)kb.b * sqrt(__dadd_rn(1.0, -__dmul_rn((double)q, (double)q)));
+                    val = (float)(cyl_bessel_i0(arg) / (double)(float)(100.0f * kb.w * dk));
+                }
+            }
+            wv[a][j] = val;
+        }
+    }
+    TapRecord r;
+    float* f = reinterpret_cast<float*>(&r);
+    for (int a = 0; a < 3; ++a)
+        for (int j = 0; j < TAPS_1D; ++j) f[a * TAPS_1D + j] = wv[a][j];
+    f[15] = __uint_as_float(pack_nearest(nearest[0], nearest[1], nearest[2]));
+    out[i] = r;
+}
+
+CGS_D void load_record(const TapRecord* __restrict__ rec, long long i, float (&w)[15], int& nx, int& ny,
+                       int& nz)
+{
+    const float4* p = reinterpret_cast<const float4*>(rec + i);
+    const float4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
+    w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
+    w[4] = b.x; w[5] = b.y; w[6] = b.z; w[7] = b.w;
+    w[8] = c.x; w[9] = c.y; w[10] = c.z; w[11] = c.w;
+    w[12] = d.x; w[13] = d.y; w[14] = d.z;
+    unpack_nearest(__float_as_uint(d.w), nx, ny, nz);
+}
+
+// ---------------------------------------------------------------------------
+// Interpolation (Reco.cpp:539-550) fused with the density weights
+// (Reco.cpp:243-254):  yv[i][c] = D[i] * sum_taps w * grid_c[idx]
+// One thread per (sample, chunk of CC coils).  Grids are [coil][Ng]; the
+// sample values are written coil-interleaved, yv[i][c].
+// ---------------------------------------------------------------------------
+
+template <int CC>
+__global__ void __launch_bounds__(128) k_interp(InterpArgs a)
+{
+    const int bin = a.bin0 + blockIdx.z;
+    const long long s0 = a.bin_off[bin], s1 = a.bin_off[bin + 1];
+    const long long i = s0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= s1) return;
+    const int c0 = blockIdx.y * CC;
+    const float2* grid = a.grid + (long long)blockIdx.z * a.grid_bs + (long long)c0 * a.coil_stride;
+    float w[15];
+    int nx, ny, nz;
+    load_record(a.rec, i, w, nx, ny, nz);
+    float2 acc[CC];
+#pragma unroll
+    for (int c = 0; c < CC; ++c) acc[c] = make_float2(0.f, 0.f);
+    const int Gy = a.G[1], Gz = a.G[2];
+    const int ncc = min(CC, a.nch - c0);
+#pragma unroll
+    for (int jx = 0; jx < 5; ++jx) {
+        const float wx = w[jx];
+        if (wx == 0.f) continue;
+        const int gx = nx - 2 + jx;
+#pragma unroll
+        for (int jy = 0; jy < 5; ++jy) {
+            const float wxy = wx * w[5 + jy];
+            if (wxy == 0.f) continue;
+            const long long row = ((long long)gx * Gy + (ny - 2 + jy)) * Gz + (nz - 2);
+#pragma unroll
+            for (int jz = 0; jz < 5; ++jz) {
+                const float wz = w[10 + jz];
+                const float wt = wxy * wz;
+                if (wz != 0.f && wt > a.thresh) {   // wz != 0: the tap lies inside the grid
+                    const long long idx = row + jz;
+#pragma unroll
+                    for (int c = 0; c < CC; ++c)
+                        if (c < ncc) {
+                            const float2 g = __ldg(grid + (long long)c * a.coil_stride + idx);
+                            acc[c].x = fmaf(g.x, wt, acc[c].x);
+                            acc[c].y = fmaf(g.y, wt, acc[c].y);
+                        }
+                }
+            }
+        }
+    }
+    const float d = a.dcf ? a.dcf[i] : 1.f;
+    float2* out = a.yv + i * a.nch + c0;
+#pragma unroll
+    for (int c = 0; c < CC; ++c)
+        if (c < ncc) out[c] = cscale(acc[c], d);
+}
+
+// ---------------------------------------------------------------------------
+// Spreading (Reco.cpp:492-504) without atomics.  One block owns one
+// TILE_X x TILE_Y x TILE_Z tile of the grid for a chunk of coils and
+// visits, in sorted order, every sample whose support touches the tile.
+// Warp w owns the grid plane x = tile_x0 + w; lane l owns (y, z) offset
+// (l / 5, l % 5) of the current sample.  Every grid value is therefore
+// updated by one lane at a time in a fixed sample order: the result is
+// deterministic.  The whole tile (zeros included) is then stored, so the
+// grid needs no separate clearing.
+// ---------------------------------------------------------------------------
+
+constexpr int SPREAD_BATCH = 32;   // samples staged per round
+
+__global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
+{
+    extern __shared__ float4 s_dyn[];
+    const int bin = a.bin0 + blockIdx.z;
+    const int tile = blockIdx.x;
+    const int c0 = blockIdx.y * a.cc;
+    const int ncc = min(a.cc, a.nch - c0);
+    const int tz = tile % a.ntz;
+    const int ty = (tile / a.ntz) % a.nty;
+    const int tx = tile / (a.ntz * a.nty);
+    const int x0 = tx * TILE_X, y0 = ty * TILE_Y, z0 = tz * TILE_Z;
+
+    // shared: accumulators [cc][TILE_PTS] float2, then staged records and values
+    float2* acc = reinterpret_cast<float2*>(s_dyn);
+    TapRecord* s_rec = reinterpret_cast<TapRecord*>(acc + (size_t)a.cc * TILE_PTS);
+    float2* s_val = reinterpret_cast<float2*>(s_rec + SPREAD_BATCH);
+
+    const int tid = threadIdx.x;
+    for (int e = tid; e < ncc * TILE_PTS; e += SPREAD_THREADS) acc[e] = make_float2(0.f, 0.f);
+
+    const long long tp = a.tile_ptr_off[bin];
+    const int beg = a.tile_ptr[tp + tile], end = a.tile_ptr[tp + tile + 1];
+    const int* idx = a.tile_idx + a.tile_idx_off[bin];
+    const long long sbase = a.bin_off[bin];
+    const int warp = tid >> 5, lane = tid & 31;
+    const int gx = x0 + warp;
+    const int jy = lane / 5, jz = lane - 5 * (lane / 5);
+
+    for (int s = beg; s < end; s += SPREAD_BATCH) {
+        const int nbat = min(SPREAD_BATCH, end - s);
+        __syncthreads();
+        for (int e = tid; e < nbat * 4; e += SPREAD_THREADS) {
+            const long long si = sbase + idx[s + e / 4];
+            reinterpret_cast<float4*>(s_rec)[e] = __ldg(reinterpret_cast<const float4*>(a.rec + si) + (e & 3));
+        }
+        for (int e = tid; e < nbat * ncc; e += SPREAD_THREADS) {
+            const int j = e / ncc, c = e - j * ncc;
+            const long long si = sbase + idx[s + j];
+            s_val[j * ncc + c] = a.yv[si * a.nch + c0 + c];
+        }
+        __syncthreads();
+        for (int j = 0; j < nbat; ++j) {
+            const float* w = reinterpret_cast<const float*>(&s_rec[j]);
+            int nx, ny, nz;
+            unpack_nearest(__float_as_uint(w[15]), nx, ny, nz);
+            const int jx = gx - (nx - 2);
+            if (jx < 0 || jx > 4 || lane >= 25) continue;
+            const int gy = ny - 2 + jy, gz = nz - 2 + jz;
+            if (gy < y0 || gy >= y0 + TILE_Y || gz < z0 || gz >= z0 + TILE_Z) continue;
+            const float wt = (w[jx] * w[5 + jy]) * w[10 + jz];
+            if (w[jx] == 0.f || w[5 + jy] == 0.f || w[10 + jz] == 0.f || !(wt > a.thresh)) continue;
+            const int local = (warp * TILE_Y + (gy - y0)) * TILE_Z + (gz - z0);
+            const float2* v = s_val + j * ncc;
+            for (int c = 0; c < ncc; ++c) {
+                float2 t = acc[c * TILE_PTS + local];
+                t.x = fmaf(v[c].x, wt, t.x);
+                t.y = fmaf(v[c].y, wt, t.y);
+                acc[c * TILE_PTS + local] = t;
+            }
+        }
+    }
+    __syncthreads();
+    // store the tile: z fastest, coalesced rows of TILE_Z points
+    float2* grid = a.grid + (long long)blockIdx.z * a.grid_bs + (long long)c0 * a.coil_stride;
+    const int Gx = a.G[0], Gy = a.G[1], Gz = a.G[2];
+    for (int e = tid; e < ncc * TILE_PTS; e += SPREAD_THREADS) {
+        const int c = e / TILE_PTS, local = e - c * TILE_PTS;
+        const int lz = local % TILE_Z, ly = (local / TILE_Z) % TILE_Y, lx = local / (TILE_Z * TILE_Y);
+        const int X = x0 + lx, Y = y0 + ly, Z = z0 + lz;
+        if (X < Gx && Y < Gy && Z < Gz)
+            grid[(long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z] = acc[e];
+    }
+}
+
+}  // namespace cgs

@@ -1,0 +1,166 @@
+// kernels_misc.cu -- launch wrappers of the gridding, sample-reordering and
+// CG kernels.
+#include "launch.h"
+#include "cg_kernels.cuh"
+#include "gridding.cuh"
+
+namespace cgs {
+
+// ---------------------------------------------------------------------------
+// sample reordering
+// ---------------------------------------------------------------------------
+
+// yv[j][c] = D[j] * data[c][sorted[j]]   (performDensityCorrection, functions.h:319-335)
+__global__ void k_gather_samples(const float2* __restrict__ data, long long ns, const int* __restrict__ sorted,
+                                 long long total, int nch, const float* __restrict__ dcf, float2* __restrict__ yv)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total * nch) return;
+    const long long j = e / nch;
+    const int c = (int)(e - j * nch);
+    float2 v = data[(long long)c * ns + sorted[j]];
+    if (dcf) v = cscale(v, dcf[j]);
+    yv[e] = v;
+}
+
+// data[c][sorted[j]] = yv[j][c]
+__global__ void k_scatter_samples(const float2* __restrict__ yv, const int* __restrict__ sorted, long long total,
+                                  int nch, long long ns, float2* __restrict__ data)
+{
+    const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= total * nch) return;
+    const long long j = e / nch;
+    const int c = (int)(e - j * nch);
+    data[(long long)c * ns + sorted[j]] = yv[e];
+}
+
+cudaError_t launch_gather_samples(const float2* data, long long ns, const int* sorted, long long total, int nch,
+                                  const float* dcf_sorted, float2* yv, cudaStream_t s)
+{
+    const long long n = total * nch;
+    if (n == 0) return cudaSuccess;
+    k_gather_samples<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(data, ns, sorted, total, nch, dcf_sorted, yv);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_samples(const float2* yv, const int* sorted, long long total, int nch, long long ns,
+                                   float2* data, cudaStream_t s)
+{
+    const long long n = total * nch;
+    if (n == 0) return cudaSuccess;
+    k_scatter_samples<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(yv, sorted, total, nch, ns, data);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s) { return cudaMemsetAsync(p, 0, bytes, s); }
+
+// ---------------------------------------------------------------------------
+// gridding
+// ---------------------------------------------------------------------------
+
+cudaError_t launch_tap_records(const double* k, const int* sample_idx, long long n, const KbParams& kb,
+                               TapRecord* out, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_tap_records<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(k, sample_idx, n, kb, out);
+    return cudaGetLastError();
+}
+
+constexpr int INTERP_CC = 4;
+
+cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, cudaStream_t s)
+{
+    if (max_bin_samples == 0 || nbins == 0) return cudaSuccess;
+    dim3 grid((unsigned)((max_bin_samples + 127) / 128), (unsigned)((a.nch + INTERP_CC - 1) / INTERP_CC),
+              (unsigned)nbins);
+    k_interp<INTERP_CC><<<grid, 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+size_t spread_smem_bytes(int cc)
+{
+    return (size_t)cc * TILE_PTS * sizeof(float2) + SPREAD_BATCH * sizeof(TapRecord) +
+           (size_t)SPREAD_BATCH * cc * sizeof(float2);
+}
+
+int spread_max_coils() { return 24; }
+
+cudaError_t kernels_init()
+{
+    return cudaFuncSetAttribute(k_spread, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)spread_smem_bytes(spread_max_coils()));
+}
+
+cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, cudaStream_t s)
+{
+    if (ntiles == 0 || nbins == 0) return cudaSuccess;
+    const size_t smem = spread_smem_bytes(a.cc);
+    dim3 grid((unsigned)ntiles, (unsigned)((a.nch + a.cc - 1) / a.cc), (unsigned)nbins);
+    k_spread<<<grid, SPREAD_THREADS, smem, s>>>(a);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// CG
+// ---------------------------------------------------------------------------
+
+int cg_blocks(long long n)
+{
+    long long b = (n + RED_THREADS - 1) / RED_THREADS;
+    if (b > 4 * 152) b = 4 * 152;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+cudaError_t launch_cg_init(const float2* b, float2* r, float2* p, float2* x, long long n, long long bs,
+                           double* partials, const CgState* st, int nbins, cudaStream_t s)
+{
+    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    k_cg_init<<<grid, RED_THREADS, 0, s>>>(b, r, p, x, n, bs, partials, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_arm(CgState* st, const double* partials, int nblk, int nbins, double thresh, int max_iter,
+                          cudaStream_t s)
+{
+    k_cg_arm<<<(nbins + 63) / 64, 64, 0, s>>>(st, partials, nblk, nbins, thresh, max_iter);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_alpha(CgState* st, const double* partials, int nblk, int nbins, const float2* q0,
+                            long long bs, cudaStream_t s)
+{
+    k_cg_alpha<<<(nbins + 63) / 64, 64, 0, s>>>(st, partials, nblk, nbins, q0, bs);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_update_xr(float2* x, float2* r, const float2* p, const float2* q, long long n, long long bs,
+                                const CgState* st, double* partials, int nbins, cudaStream_t s)
+{
+    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    k_cg_update_xr<<<grid, RED_THREADS, 0, s>>>(x, r, p, q, n, bs, st, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_beta(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
+                           int res_stride, cudaStream_t s)
+{
+    k_cg_beta<<<(nbins + 63) / 64, 64, 0, s>>>(st, partials, nblk, nbins, residuals, res_stride);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_update_p(float2* p, const float2* r, long long n, long long bs, const CgState* st, int nbins,
+                               cudaStream_t s)
+{
+    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    k_cg_update_p<<<grid, RED_THREADS, 0, s>>>(p, r, n, bs, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_loop_test(CgState* st, int nbins, cudaStream_t s)
+{
+    k_cg_loop_test<<<(nbins + 63) / 64, 64, 0, s>>>(st, nbins);
+    return cudaGetLastError();
+}
+
+}  // namespace cgs

@@ -1,0 +1,54 @@
+// launch.h -- host-side launch interface of the CG-SENSE kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include "cgs_types.h"
+
+namespace cgs {
+
+// Supported line lengths of the 3-D FFT (each a product R1*R2 of two
+// register codelets).  Grid sizes must be taken from this list.
+bool fft_supported(int L);
+const int* fft_supported_list(int* n);
+
+// One launch per pass; `batch` items along blockIdx.y.
+cudaError_t launch_strided(int L, int sign, const StridedPassArgs& a, int A, int batch, cudaStream_t s);
+cudaError_t launch_contig(int L, int sign, const ContigPassArgs& a, int batch, cudaStream_t s);
+cudaError_t launch_fwd_z(int L, const FwdZArgs& a, int batch, cudaStream_t s);
+// grid.x of the adjoint z pass (number of partial sums per batch item)
+int adj_z_blocks(int L, long long nl);
+cudaError_t launch_adj_z(int L, const AdjZArgs& a, int batch, cudaStream_t s);
+
+// Gridding and element-wise kernels (kernels_misc.cu).
+cudaError_t launch_tap_records(const double* k, const int* sample_idx, long long n, const KbParams& kb,
+                               TapRecord* out, cudaStream_t s);
+cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, cudaStream_t s);
+cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, cudaStream_t s);
+size_t spread_smem_bytes(int cc);
+// one-time kernel attributes (dynamic shared memory limits); call per device
+cudaError_t kernels_init();
+int spread_max_coils();
+
+// samples: reference order [nch][ns] <-> sorted, coil-interleaved [total][nch]
+cudaError_t launch_gather_samples(const float2* data, long long ns, const int* sorted, long long total, int nch,
+                                  const float* dcf_sorted, float2* yv, cudaStream_t s);
+cudaError_t launch_scatter_samples(const float2* yv, const int* sorted, long long total, int nch, long long ns,
+                                   float2* data, cudaStream_t s);
+cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s);
+
+// CG
+int cg_blocks(long long n);
+cudaError_t launch_cg_init(const float2* b, float2* r, float2* p, float2* x, long long n, long long bs,
+                           double* partials, const CgState* st, int nbins, cudaStream_t s);
+cudaError_t launch_cg_arm(CgState* st, const double* partials, int nblk, int nbins, double thresh, int max_iter,
+                          cudaStream_t s);
+cudaError_t launch_cg_alpha(CgState* st, const double* partials, int nblk, int nbins, const float2* q0,
+                            long long bs, cudaStream_t s);
+cudaError_t launch_cg_update_xr(float2* x, float2* r, const float2* p, const float2* q, long long n, long long bs,
+                                const CgState* st, double* partials, int nbins, cudaStream_t s);
+cudaError_t launch_cg_beta(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
+                           int res_stride, cudaStream_t s);
+cudaError_t launch_cg_update_p(float2* p, const float2* r, long long n, long long bs, const CgState* st, int nbins,
+                               cudaStream_t s);
+cudaError_t launch_cg_loop_test(CgState* st, int nbins, cudaStream_t s);
+
+}  // namespace cgs

@@ -1,0 +1,424 @@
+"""Benchmark of the GB300 CG-SENSE path (E^H D E applies/s; s per 16-bin 4D
+reconstruction).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (default): the batched 4D reconstruction of 128x128x96 images on a
+2x oversampled 256x256x192 grid, 12 coils, wave-CAIPI R=2x2 (+-5 cells,
+8 cycles), 512 samples per readout, 16 respiratory bins of uneven occupancy,
+15 CG iterations per bin, all bins in one graph-captured solve.  Synthetic,
+seeded inputs (4d_lung_gb300/synth.py).
+
+One step = one full 16-bin reconstruction; value = E^H D E applies per
+second (bins x iterations per step / time per step), summed over ranks.
+With torchrun (N > 1) every rank reconstructs its own 16-bin scan on its
+GPU (replicas, weak scaling, no collective on the data path).
+
+--impl reference times the reference's CPU implementation of the same
+operator on the host cores: the oracle port (oracle/cgs_oracle.c, FP32,
+OpenMP over coils like Reco.cpp:470,523), one E^H D E application of bin 0
+per step.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "E^H D E applies/s; s per 16-bin 4D recon; chosen vs plain at <=1e-4 rel err"
+UNIT = "applies/s"
+STAGES = ["fwd_z", "fwd_y", "fwd_x", "interp", "spread", "adj_x", "adj_y", "adj_z"]
+
+
+def beatty_beta(w, sigma=2.0):
+    return float(np.pi * np.sqrt(w ** 2 / sigma ** 2 * (sigma - 0.5) ** 2 - 0.8))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_record():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def make_workload(cgs, synth, torch, name, device, stream_handle):
+    w = synth.WORKLOADS[name]
+    kb_w = 4.0
+    kb_b = beatty_beta(kb_w)
+    lines = synth.readout_lines(w)
+    k = synth.wave_trajectory(w, lines=lines)
+    rbins = synth.breathing_bins(len(lines), w.n_bins)
+    sbins = synth.bin_samples(rbins, w.n_read)
+    smaps = synth.coil_maps(w.img, w.n_ch)
+    dcf = synth.radial_dcf(k, w.grid)
+    reco = cgs.Reco(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=kb_b, device=device)
+    reco.set_stream(stream_handle)
+    reco.set_trajectory(k)
+    ns = k.shape[0]
+    dev = torch.device("cuda", device)
+    smaps_t = torch.from_numpy(smaps).to(dev)
+    data = torch.zeros((w.n_ch, ns), dtype=torch.complex64, device=dev)
+    full = torch.zeros((w.n_ch, ns), dtype=torch.complex64, device=dev)
+    # k-space of each bin from its own (z-displaced) phantom: y = E(S x_b)
+    for b, idx in enumerate(sbins):
+        shift = w.z_shift_max * (b / max(w.n_bins - 1, 1))
+        x_b = torch.from_numpy(synth.phantom(w.img, z_shift=shift)).to(dev)
+        imgs = (smaps_t * x_b[None]).contiguous()
+        reco.nufft_fwd_tensor(imgs, full)
+        it = torch.from_numpy(np.asarray(idx, np.int64)).to(dev)
+        data[:, it] = full[:, it]
+    torch.cuda.synchronize(dev)
+    rms = float(torch.sqrt(torch.mean(torch.abs(data) ** 2)).item())
+    g = torch.Generator(device=dev)
+    g.manual_seed(2)
+    sigma = rms / 30.0 / np.sqrt(2.0)
+    noise = torch.complex(torch.randn(data.shape, generator=g, device=dev),
+                          torch.randn(data.shape, generator=g, device=dev)) * sigma
+    data += noise
+    reco.set_dcf(dcf)
+    reco.set_bins(sbins)
+    reco.set_smaps_tensor(smaps_t)
+    return w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b
+
+
+def stage_bytes(w, sizes):
+    """Algorithmic bytes of each stage of one E^H D E application over all
+    bins: every stage reads its input and writes its output once."""
+    Ix, Iy, Iz = w.img
+    Gx, Gy, Gz = w.grid
+    Ni, Ng, Nl = Ix * Iy * Iz, Gx * Gy * Gz, Ix * Iy
+    C8 = 8 * w.n_ch
+    nb = len(sizes)
+    M = int(sum(sizes))
+    return {
+        "fwd_z": nb * (8 * Ni + C8 * Ni + C8 * Nl * Gz),
+        "fwd_y": nb * C8 * (Nl * Gz + Ix * Gy * Gz),
+        "fwd_x": nb * C8 * (Ix * Gy * Gz + Ng),
+        "interp": nb * C8 * Ng + M * (64 + 4 + C8),
+        "spread": nb * C8 * Ng + M * (64 + C8),
+        "adj_x": nb * C8 * (Ng + Ix * Gy * Gz),
+        "adj_y": nb * C8 * (Ix * Gy * Gz + Nl * Gz),
+        "adj_z": nb * (C8 * Nl * Gz + C8 * Ni + 8 * Ni),
+    }
+
+
+def apply_bytes(w, sizes):
+    """B_apply = Nc (48 Ni + 56 Ng + 44 M) + 56 Ni per bin (the operator's
+    algorithmic traffic: coil/apod/pad, FFT, interpolation + D, spreading,
+    adjoint FFT, crop/apod/conj-coil accumulate, CG update)."""
+    Ni, Ng = int(np.prod(w.img)), int(np.prod(w.grid))
+    return sum(w.n_ch * (48 * Ni + 56 * Ng + 44 * int(m)) + 56 * Ni for m in sizes)
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (oracle port)
+# ---------------------------------------------------------------------------
+
+def cpu_apply_sample(synth, name, budget_s=12.0, max_reps=3, warmup=0):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    o = oracle_py.Oracle(32)
+    w = synth.WORKLOADS[name]
+    kb_w = 4.0
+    lines = synth.readout_lines(w)
+    k = synth.wave_trajectory(w, lines=lines)
+    rbins = synth.breathing_bins(len(lines), w.n_bins)
+    sb = synth.bin_samples(rbins, w.n_read)[0]
+    kb = k[sb]
+    p = oracle_py.make_params(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=beatty_beta(kb_w))
+    taps = o.taps(p, kb)                     # ConvKernel::calculateWeights (set-up)
+    kft = o.kernel_ft(p)                     # ConvKernel::calculateKernelFT (set-up)
+    smaps = synth.coil_maps(w.img, w.n_ch)
+    dcf = synth.radial_dcf(kb, w.grid)
+    x = synth.phantom(w.img)
+    for _ in range(warmup):
+        o.apply_ehde(p, taps, kft, smaps, dcf, x)
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < max_reps:
+        t0 = time.perf_counter()
+        o.apply_ehde(p, taps, kft, smaps, dcf, x)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > budget_s:
+            break
+    return {
+        "times": times, "threads": threads, "samples_in_bin": int(len(sb)),
+        "sample": "E^H D E applications of bin 0 (%d samples, %d coils, %s grid), %d timed" % (
+            len(sb), w.n_ch, "x".join(map(str, w.grid)), len(times)),
+    }
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    synth = importlib.import_module("4d_lung_gb300.synth")
+    w = synth.WORKLOADS[args.workload]
+    res = cpu_apply_sample(synth, args.workload, budget_s=1e9, max_reps=args.steps, warmup=args.warmup)
+    t = res["times"]
+    value = len(t) / sum(t)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": len(t), "warmup": args.warmup, "ms_per_step": 1e3 * sum(t) / len(t),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32",
+        "data": "synthetic", "config": {"workload": w.name, "bins": w.n_bins, "cg_iters": w.cg_iters,
+                                        "step": "one E^H D E application of bin 0 on the host cores"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["threads"], "kind": "port",
+                         "sample": res["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "s_per_4d_recon_extrapolated": w.n_bins * w.cg_iters * sum(t) / len(t),
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    cgs = importlib.import_module("4d_lung_gb300")
+    synth = importlib.import_module("4d_lung_gb300.synth")
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if not os.path.exists(cgs.LIB_PATH):
+        raise RuntimeError("libcgsense.so missing: run __graft_entry__.build() first")
+
+    # all library work and the timing events on one dedicated stream
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b = make_workload(cgs, synth, torch, args.workload, local,
+                                                                    stream.cuda_stream)
+    torch.cuda.synchronize(dev)
+    nb = len(sbins)
+    sizes = [len(s) for s in sbins]
+    x = torch.zeros((nb,) + w.img, dtype=torch.complex64, device=dev)
+    iters = w.cg_iters
+
+    for _ in range(args.warmup):
+        res, its = reco.cg_sense_batched_tensor(data, x, 0.0, iters, want_stats=True)
+    launches_per_step = reco.launch_count()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        reco.cg_sense_batched_tensor(data, x, 0.0, iters, want_stats=False)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    applies_per_step = nb * iters
+    value = world * applies_per_step * args.steps / (ms / 1e3)
+    ms_step = ms / args.steps
+
+    # residual check of the last solve
+    res, its = reco.cg_sense_batched_tensor(data, x, 0.0, iters, want_stats=True)
+    assert np.all(its == iters) and np.all(np.isfinite(res))
+
+    # end to end through the host-buffer C ABI call (pinned host memory)
+    h_data = torch.empty(data.shape, dtype=torch.complex64, pin_memory=True)
+    h_data.copy_(data.cpu())
+    h_x = torch.empty(x.shape, dtype=torch.complex64, pin_memory=True)
+    h_res = np.zeros((nb, iters), np.float64)
+    h_it = np.zeros(nb, np.int32)
+    import ctypes as C
+    L = cgs.lib()
+
+    def host_call():
+        st = L.cgs_cg_solve_batched(reco.ctx, C.c_void_p(h_data.data_ptr()), C.c_void_p(h_x.data_ptr()),
+                                    0.0, iters, h_res.ctypes.data_as(C.c_void_p),
+                                    h_it.ctypes.data_as(C.c_void_p))
+        if st != 0:
+            raise RuntimeError(L.cgs_last_error(reco.ctx).decode())
+
+    for _ in range(max(1, args.warmup)):
+        host_call()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_call()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * applies_per_step * args.steps / float(te.item())
+    h2d = data.numel() * 8
+    d2h = x.numel() * 8 + h_res.nbytes + h_it.nbytes
+
+    # per-stage kernel times of one batched application (roofline)
+    xa = torch.from_numpy(np.stack([synth.phantom(w.img)] * nb)).to(dev)
+    qa = torch.empty_like(xa)
+    reps = []
+    for _ in range(5):
+        reps.append(reco.profile_apply_tensor(xa, qa, 0, nb))
+    st = np.median(np.stack(reps), axis=0)
+    groups = len(st) // 8
+    stage_ms = {s: float(sum(st[g * 8 + i] for g in range(groups))) for i, s in enumerate(STAGES)}
+    sb = stage_bytes(w, sizes)
+    apply_ms = float(sum(stage_ms.values()))
+    dom = max(stage_ms, key=stage_ms.get)
+    peak, peak_kind = measured_peaks()
+    achieved = sb[dom] / (stage_ms[dom] / 1e3) / 1e9
+    tr = traffic_record().get(args.workload, {}).get(dom)
+    roofline = {
+        "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
+        if peak_kind == "measured" else "fallback 6800 GB/s",
+        "traffic": tr, "launches_per_apply": groups,
+        "algorithmic_bytes_per_apply": sb[dom],
+        "stage_ms": stage_ms,
+        "stage_frac_of_peak": {s: sb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in STAGES},
+        "apply_ms": apply_ms,
+        "apply_achieved_gbs": apply_bytes(w, sizes) / (apply_ms / 1e3) / 1e9,
+    }
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64/f32 (fp64 CG scalars)", "data": "synthetic",
+        "config": {"workload": w.name, "img": list(w.img), "grid": list(w.grid), "coils": w.n_ch,
+                   "bins": nb, "samples_per_bin": [min(sizes), max(sizes)], "samples_total": int(sum(sizes)),
+                   "cg_iters": iters, "kb_w": kb_w, "kb_b": round(kb_b, 4),
+                   "dcf": "radial stand-in", "step": "one 16-bin 4D CG-SENSE reconstruction (graph replay)",
+                   "l2": "inputs larger than L2 (data %d MB, workspace > 30 GB)" % (h2d // 2 ** 20),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "s_per_4d_recon": ms_step / 1e3,
+        "gpu_launches": int(launches_per_step) * args.steps,
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "s_per_4d_recon": float(te.item()) / args.steps},
+        "roofline": roofline,
+    }
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_apply_sample(synth, args.workload)
+        v = len(cb["times"]) / sum(cb["times"])
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cb["threads"], "kind": "port",
+                                "sample": cb["sample"]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cfg3")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,192 @@
+/*
+ * cgsense_c.h -- C ABI of the GB300 CG-SENSE library (libcgsense.so).
+ *
+ * The library implements the CG-SENSE encoding operator E^H D E of
+ * expRad/4d_lung (CGSense/Reco.cpp) and the conjugate-gradient solve around
+ * it on one NVIDIA GB300 GPU (sm_103a kernels).  It is the drop-in boundary
+ * for the reference's reconstruction object: every entry point below names
+ * the reference member function it replaces.  Plain pointers and sizes only.
+ *
+ * Conventions (all kept from the reference):
+ *   - complex data are interleaved float pairs (re, im), bit-compatible with
+ *     fftwf_complex;
+ *   - grids and images are row-major [x][y][z], z fastest (Reco.cpp:603-606);
+ *   - samples are in the reference's memory order, z-fastest
+ *     (IO.cpp:109-125, Trajectory.cpp:167-175); per-coil sample arrays are
+ *     [coil][sample] (Reco.cpp:478-479);
+ *   - the trajectory is k in [0,1]^3 per sample, grid coordinate k*(N-1)
+ *     (Reco.cpp:751-755);
+ *   - the forward NUFFT is unscaled; the adjoint is scaled by
+ *     adj_scale / sqrt(N_grid) (Reco.cpp:482, Fourier.cpp:31-41).
+ *
+ * Errors: every function returns CGS_OK (0) or a CGS_ERR_* code and stores a
+ * message retrievable with cgs_last_error().  The reference instead prints
+ * and calls exit(EXIT_FAILURE); the C++ drop-in shim (cgsense/Reco.h) maps a
+ * non-zero status to that behaviour.
+ *
+ * Threading: one context per host thread.  Each context owns (or borrows,
+ * cgs_set_stream) one CUDA stream.  Host-pointer calls are synchronous;
+ * "_d" calls take device pointers and are asynchronous on the context's
+ * stream.
+ */
+#ifndef CGSENSE_C_H
+#define CGSENSE_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CGS_OK 0
+#define CGS_ERR_ARG 1          /* invalid argument or size */
+#define CGS_ERR_CUDA 2         /* CUDA runtime error */
+#define CGS_ERR_NONFINITE 3    /* NaN/Inf in the CG iterate (Reco.cpp:264-268) */
+#define CGS_ERR_STATE 4        /* call order: e.g. no trajectory or coil maps set */
+#define CGS_ERR_NOMEM 5        /* device allocation failed */
+#define CGS_ERR_UNSUPPORTED 6  /* grid size without an FFT kernel */
+#define CGS_ERR_NO_THRESHOLD 7 /* cg threshold == -1 (Reco.cpp:192-196) */
+
+typedef struct cgs_ctx cgs_ctx;
+
+/* Reconstruction parameters.  Replaces Reco::setGridSize / setNCh /
+ * setOffcenter (Reco.h:112-121) and ConvKernel::setB / setW /
+ * setKernelOrder (Reco.h:53-55, values set in Reco::init, Reco.cpp:377-380). */
+typedef struct cgs_params {
+    int32_t img[3];       /* image size; the reference uses img == grid */
+    int32_t grid[3];      /* Cartesian grid size (even, from the supported FFT list) */
+    int32_t n_ch;         /* coils */
+    int32_t kb_order;     /* neighbour scan half-width (5) */
+    float kb_w;           /* KB width in grid cells (4.25); must be < 5 */
+    float kb_b;           /* KB shape (14.9086) */
+    double kb_thresh;     /* relative tap threshold (1e-7) */
+    double adj_scale;     /* adjoint rescale (1e-3) */
+    int32_t offcenter[3]; /* image offset inside the grid beyond centring */
+    int32_t device;       /* CUDA device ordinal */
+    int64_t workspace_bytes; /* device workspace budget for batched bins (0: default) */
+} cgs_params;
+
+/* Wave-CAIPI parameters.  Replaces the WaveCaipi setters
+ * (Trajectory.h:52-60) together with Reco::setSampling / setGridSize /
+ * setFovY / setFovZ (Reco.h:108,112,122-123). */
+typedef struct cgs_wave {
+    int32_t sx, sy, sz;
+    int32_t gx, gy, gz;
+    double fov_y, fov_z;
+    int32_t n_osc;
+    double grad_amp;
+    double amp_corr_y, amp_corr_z;
+    double shift_y, shift_z;
+    double dwell;
+} cgs_wave;
+
+/* Reference defaults: b = 14.9086, w = 4.25, order 5 (Reco.cpp:377-380),
+ * threshold 1e-7 (Reco.cpp:717), adjoint scale 1e-3 (Reco.cpp:482). */
+void cgs_default_params(cgs_params* p);
+
+/* Reco::init + Reco::ConvKernel::calculateKernelFT + Fourier::initFT
+ * (Reco.cpp:374-400, 560-601; Fourier.cpp:4-17). */
+int cgs_create(const cgs_params* p, cgs_ctx** out);
+/* Reco::~Reco (Reco.cpp:29-61). */
+void cgs_destroy(cgs_ctx* ctx);
+const char* cgs_last_error(const cgs_ctx* ctx);
+/* Use an external CUDA stream (cudaStream_t); NULL returns to the context's own stream. */
+int cgs_set_stream(cgs_ctx* ctx, void* stream);
+/* Block until the context's stream is idle. */
+int cgs_sync(cgs_ctx* ctx);
+
+/* WaveCaipi::calculateTraj with Trajectory::calculateKMax (Trajectory.cpp:9-184):
+ * k_out[(sx*sy*sz)][3], z-fastest sample order. Host only. */
+int cgs_wave_caipi(const cgs_wave* w, double* k_out);
+
+/* Reco::setTrajectory (Reco.cpp:324-336) followed by
+ * ConvKernel::calculateWeights (Reco.cpp:698-806): the KB taps are evaluated
+ * on the GPU.  k[ns][3] on the host.  Resets bins to one bin of all samples. */
+int cgs_set_trajectory(cgs_ctx* ctx, const double* k, int64_t ns);
+
+/* ConvKernel::excludeMissingData (Reco.cpp:681-696): samples with
+ * mask[i] == 0 get no taps.  One bin of the unmasked samples.  NULL clears. */
+int cgs_set_mask(cgs_ctx* ctx, const uint8_t* mask);
+/* Same, with the mask taken where coil 0's sample is exactly 0+0i, as the
+ * reference does.  data: host [n_ch][ns] complex. */
+int cgs_mask_from_data(cgs_ctx* ctx, const float* data);
+
+/* Respiratory bins (the reference reconstructs one state file at a time,
+ * CGSense.cpp:200-282): bin b holds samples sample_idx[offsets[b] ..
+ * offsets[b+1]).  Bins may differ in size. */
+int cgs_set_bins(cgs_ctx* ctx, int32_t nbins, const int64_t* offsets, const int32_t* sample_idx);
+int cgs_num_bins(const cgs_ctx* ctx);
+
+/* Reco::denCorr with Density::IMPORT (IO.cpp:129-156, functions.h:319-335):
+ * per-sample real weights D[ns].  NULL clears (Density::NONE). */
+int cgs_set_dcf(cgs_ctx* ctx, const float* dcf);
+
+/* IO::importSensitivityMaps result (IO.cpp:25-51), Reco::sMaps: host
+ * [n_ch][image voxels] complex. */
+int cgs_set_smaps(cgs_ctx* ctx, const float* maps);
+int cgs_set_smaps_d(cgs_ctx* ctx, const float* maps_dev);
+
+/* ConvKernel::kernelFT (Reco.cpp:560-601) as the grid volume the reference
+ * stores (1/Re of the centred backward FFT of the sampled KB kernel):
+ * host [grid voxels] complex. */
+int cgs_kernel_ft(cgs_ctx* ctx, float* kft);
+
+/* Fourier::transformFWD (sign -1) / transformBWD (sign +1, rescale 0|1)
+ * (Fourier.cpp:19-42), in place on a host grid [grid voxels] complex. */
+int cgs_fft3(cgs_ctx* ctx, float* grid, int32_t sign, int32_t rescale);
+int cgs_fft3_d(cgs_ctx* ctx, float* grid_dev, int32_t sign, int32_t rescale);
+
+/* Reco::nufftFWD (Reco.cpp:521-553): img[n_ch][image voxels] ->
+ * data[n_ch][ns].  Samples outside every bin are set to 0. */
+int cgs_nufft_fwd(cgs_ctx* ctx, const float* img, float* data);
+int cgs_nufft_fwd_d(cgs_ctx* ctx, const float* img_dev, float* data_dev);
+/* Reco::nufftBWD (Reco.cpp:468-519): data[n_ch][ns] -> img[n_ch][image voxels].
+ * D is not applied (the reference applies it to `data` beforehand). */
+int cgs_nufft_adj(cgs_ctx* ctx, const float* data, float* img);
+int cgs_nufft_adj_d(cgs_ctx* ctx, const float* data_dev, float* img_dev);
+
+/* One operator application of the CG loop (Reco.cpp:232-262):
+ * q = sum_c conj(S_c) E_c^H D E_c (S_c x) for the samples of bin `bin`.
+ * x, q: [image voxels] complex. */
+int cgs_apply_ehde(cgs_ctx* ctx, int32_t bin, const float* x, float* q);
+/* Bins [bin0, bin0+nb): x, q are [nb][image voxels] device arrays. */
+int cgs_apply_ehde_d(cgs_ctx* ctx, int32_t bin0, int32_t nb, const float* x_dev, float* q_dev);
+
+/* Reco::cgSenseDynamic (Reco.cpp:175-321), preceded by the density
+ * correction of the measured samples and the coil-image step nufftBWD
+ * (CGSense.cpp:226-235).  Bin 0 only (the single-state reconstruction).
+ * data: [n_ch][ns] measured samples; x: [image voxels] result (cgSenseImg);
+ * residuals: max_iter entries (cgResiduals); iters: performed iterations
+ * (numPerformedCGIterations).  threshold == -1 fails like the reference.
+ * The reference's cap is 16 iterations (max_iter = 16). */
+int cgs_cg_solve(cgs_ctx* ctx, const float* data, float* x, double threshold, int32_t max_iter,
+                 double* residuals, int32_t* iters);
+
+/* All bins in one graph-captured launch sequence (the 4D reconstruction of
+ * CGSense.cpp:200-282 without its file IO): x[nbins][image voxels],
+ * residuals[nbins][max_iter], iters[nbins]. */
+int cgs_cg_solve_batched(cgs_ctx* ctx, const float* data, float* x, double threshold, int32_t max_iter,
+                         double* residuals, int32_t* iters);
+/* Device-pointer variant; residuals/iters stay host pointers (filled after
+ * the solve completes). */
+int cgs_cg_solve_batched_d(cgs_ctx* ctx, const float* data_dev, float* x_dev, double threshold,
+                           int32_t max_iter, double* residuals, int32_t* iters);
+
+/* Number of kernel launches issued by the last compute call (for a graph
+ * replay: the kernels in the graph). */
+int64_t cgs_last_launch_count(const cgs_ctx* ctx);
+
+/* Per-stage timing of one E^H D E application (the reference prints
+ * wall-clock times only, CGSense.cpp:122-135,257-261): runs
+ * cgs_apply_ehde_d on device arrays with a CUDA event after every kernel and
+ * returns the kernel durations in launch order (forward z, y, x passes,
+ * interpolation, spreading, adjoint x, y, z passes; repeated per group of
+ * bins).  stage_ms holds max_stages floats; n_stages receives the count. */
+int cgs_profile_apply(cgs_ctx* ctx, int32_t bin0, int32_t nb, const float* x_dev, float* q_dev,
+                      float* stage_ms, int32_t max_stages, int32_t* n_stages);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CGSENSE_C_H */

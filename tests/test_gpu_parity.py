@@ -1,0 +1,224 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the
+reference's golden vectors and the CPU oracle.
+
+Tolerances (relative L2 unless stated):
+  * centred FFT against the FP64 oracle: 2e-6;
+  * deapodisation volume (kernelFT) against the reference: 1e-5;
+  * NUFFT forward / adjoint against the reference: 2e-5 (FP32 gridding
+    and FFT, different summation order);
+  * CG-SENSE image against the reference after 16 iterations: 2e-4;
+    residual sequence 2e-4 element-wise; iteration count exact;
+  * oversampled operator (2x grid) against the FP64 oracle: 2e-5;
+  * spreading is deterministic: two runs are bitwise equal.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+OPS = ["ref_ops_24x20x16.npz", "ref_ops_32x24x16_mask.npz", "ref_ops_40x20x16_stop.npz"]
+
+
+def make_reco(cgs, img, grid, nch, **kw):
+    return cgs.Reco(img, grid, nch, **kw)
+
+
+def golden_reco(cgs, z):
+    grid = tuple(int(v) for v in z["grid"])
+    nch = int(z["nch"])
+    r = make_reco(cgs, grid, grid, nch)
+    r.set_trajectory(z["k"])
+    r.mask_from_data(z["data"])
+    return r, grid, nch
+
+
+@pytest.mark.parametrize("grid", [(24, 20, 16), (40, 20, 16), (64, 48, 32), (16, 512, 20)])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_fft3_vs_oracle(gpu_lib, cgs, oracle_mod, o64, grid, sign):
+    rng = np.random.default_rng(0)
+    a = (rng.standard_normal(grid) + 1j * rng.standard_normal(grid)).astype(np.complex64)
+    r = make_reco(cgs, grid, grid, 1)
+    out = r.fft3(a, sign)
+    ref = o64.centred_fft(oracle_mod.make_params(grid, grid, 1), a, sign, 0)
+    assert rel_l2(out, ref) < 2e-6
+
+
+@pytest.mark.parametrize("L", [16, 20, 24, 32, 40, 48, 64, 80, 96, 128, 160, 176, 192, 224, 256, 320,
+                               352, 384, 448, 512])
+def test_fft_every_line_length(gpu_lib, cgs, L):
+    """Every supported line length, on each axis, against numpy."""
+    rng = np.random.default_rng(L)
+    for grid in [(L, 16, 16), (16, L, 16), (16, 16, L)]:
+        a = (rng.standard_normal(grid) + 1j * rng.standard_normal(grid)).astype(np.complex64)
+        r = make_reco(cgs, grid, grid, 1)
+        out = r.fft3(a, -1)
+        ref = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(a.astype(np.complex128))))
+        ref *= (-1.0) ** sum(n // 2 for n in grid)
+        assert rel_l2(out, ref) < 2e-6, grid
+        r.close()
+
+
+@pytest.mark.parametrize("name", OPS)
+def test_kernel_ft_vs_reference(gpu_lib, cgs, name):
+    z = golden(name)
+    r, grid, nch = golden_reco(cgs, z)
+    assert rel_l2(r.kernel_ft(), z["kernelft"]) < 1e-5
+
+
+@pytest.mark.parametrize("name", OPS)
+def test_nufft_fwd_vs_reference(gpu_lib, cgs, name):
+    """Reco::nufftFWD (Reco.cpp:521-553), excluded samples included."""
+    z = golden(name)
+    r, grid, nch = golden_reco(cgs, z)
+    out = r.nufft_fwd(z["img"])
+    assert rel_l2(out, z["fwd_data"]) < 2e-5
+    # samples excluded by excludeMissingData get no taps: exactly zero
+    assert np.array_equal(out == 0, z["fwd_data"] == 0)
+
+
+@pytest.mark.parametrize("name", OPS)
+def test_nufft_adj_vs_reference(gpu_lib, cgs, name):
+    """Reco::nufftBWD (Reco.cpp:468-519)."""
+    z = golden(name)
+    r, grid, nch = golden_reco(cgs, z)
+    assert rel_l2(r.nufft_adj(z["data"]), z["bwd_img"]) < 2e-5
+
+
+@pytest.mark.parametrize("name", OPS)
+def test_cg_sense_vs_reference(gpu_lib, cgs, name):
+    """Reco::cgSenseDynamic (Reco.cpp:175-321) with density weights, the
+    16-iteration cap and the residual threshold."""
+    z = golden(name)
+    r, grid, nch = golden_reco(cgs, z)
+    r.set_dcf(z["dcf"])
+    r.set_smaps(z["smaps"])
+    x, res, it = r.cg_sense(z["data"], float(z["cg_threshold"]), 16)
+    assert it == int(z["cg_iters"][0])
+    assert np.allclose(res, z["cg_residuals"], rtol=2e-4, atol=0)
+    assert rel_l2(x, z["cg_x"]) < 2e-4
+
+
+def oversampled_case(oracle_mod, o64, img, grid, nch, n_lines, n_read, seed=3, kb_w=4.0, kb_b=None):
+    rng = np.random.default_rng(seed)
+    t = np.linspace(0.02, 0.98, n_read)
+    ky, kz = rng.uniform(0.1, 0.9, n_lines), rng.uniform(0.1, 0.9, n_lines)
+    k = np.zeros((n_lines, n_read, 3))
+    k[..., 0] = t
+    k[..., 1] = ky[:, None] + 0.03 * np.sin(2 * np.pi * 5 * t)
+    k[..., 2] = kz[:, None] + 0.03 * np.cos(2 * np.pi * 5 * t)
+    k = k.reshape(-1, 3)
+    if kb_b is None:
+        kb_b = float(np.pi * np.sqrt(kb_w ** 2 / 4 * 1.5 ** 2 - 0.8))
+    p = oracle_mod.make_params(img, grid, nch, kb_w=kb_w, kb_b=kb_b)
+    taps = o64.taps(p, k)
+    return k, p, taps, kb_w, kb_b
+
+
+@pytest.mark.parametrize("img,grid", [((16, 16, 16), (32, 32, 32)), ((32, 24, 20), (64, 48, 40)),
+                                      ((20, 16, 12), (32, 32, 24))])
+def test_oversampled_nufft_vs_oracle(gpu_lib, cgs, oracle_mod, o64, img, grid):
+    """2x oversampled grid with zero-pad / crop (pruned FFT passes)."""
+    nch = 3
+    k, p, taps, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 40, 64)
+    rng = np.random.default_rng(9)
+    x = (rng.standard_normal((nch,) + img) + 1j * rng.standard_normal((nch,) + img)).astype(np.complex64)
+    y = (rng.standard_normal((nch, k.shape[0])) + 1j * rng.standard_normal((nch, k.shape[0]))).astype(np.complex64)
+    kft = o64.kernel_ft(p)
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b)
+    r.set_trajectory(k)
+    assert rel_l2(r.nufft_fwd(x), o64.nufft_fwd(p, taps, kft, x)) < 2e-5
+    assert rel_l2(r.nufft_adj(y), o64.nufft_adj(p, taps, kft, y)) < 2e-5
+
+
+def test_apply_ehde_vs_oracle_and_hermitian(gpu_lib, cgs, oracle_mod, o64, synth):
+    img, grid, nch = (16, 16, 12), (32, 32, 24), 4
+    k, p, taps, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 50, 64)
+    smaps = synth.coil_maps(img, nch)
+    dcf = np.random.default_rng(2).uniform(0.5, 1.5, k.shape[0]).astype(np.float32)
+    rng = np.random.default_rng(4)
+    x = (rng.standard_normal(img) + 1j * rng.standard_normal(img)).astype(np.complex64)
+    v = (rng.standard_normal(img) + 1j * rng.standard_normal(img)).astype(np.complex64)
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b)
+    r.set_trajectory(k)
+    r.set_dcf(dcf)
+    r.set_smaps(smaps)
+    q = r.apply_ehde(x)
+    qo = o64.apply_ehde(p, taps, o64.kernel_ft(p), smaps, dcf, x)
+    assert rel_l2(q, qo) < 2e-5
+    qv = r.apply_ehde(v)
+    lhs, rhs = np.vdot(v, q), np.vdot(qv, x)
+    assert abs(lhs - rhs) < 1e-4 * abs(lhs)
+    # determinism: spreading has no atomics
+    assert np.array_equal(q, r.apply_ehde(x))
+
+
+def test_batched_bins_match_per_bin_oracle(gpu_lib, cgs, oracle_mod, o64, synth):
+    """All bins in one graph-captured solve equal independent solves."""
+    img, grid, nch = (16, 16, 12), (32, 32, 24), 3
+    k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 48)
+    n_read = 48
+    rb = [np.arange(0, 10), np.arange(10, 32), np.arange(32, 35), np.arange(35, 60)]
+    bins = synth.bin_samples(rb, n_read)
+    smaps = synth.coil_maps(img, nch)
+    rng = np.random.default_rng(6)
+    data = (rng.standard_normal((nch, k.shape[0])) + 1j * rng.standard_normal((nch, k.shape[0]))).astype(np.complex64)
+    dcf = rng.uniform(0.5, 1.5, k.shape[0]).astype(np.float32)
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b)
+    r.set_trajectory(k)
+    r.set_dcf(dcf)
+    r.set_bins(bins)
+    r.set_smaps(smaps)
+    x, res, it = r.cg_sense_batched(data, 0.0, 6)
+    kft = o64.kernel_ft(p)
+    for bi, s in enumerate(bins):
+        mask = np.zeros(k.shape[0], np.uint8)
+        mask[s] = 1
+        tb = o64.taps(p, k, mask)
+        st, xo, reso, ito = o64.cg_sense(p, tb, kft, smaps, dcf, data, 0.0, 6)
+        assert it[bi] == ito == 6
+        assert rel_l2(x[bi], xo) < 1e-4, bi
+        assert np.allclose(res[bi, :6], reso, rtol=1e-4)
+
+
+def test_empty_bin_and_zero_data(gpu_lib, cgs, synth):
+    """A bin without samples (or all-zero data) has a zero right-hand side:
+    the solve returns x = 0 after 0 iterations."""
+    img, grid, nch = (8, 8, 8), (16, 16, 16), 2
+    rng = np.random.default_rng(0)
+    k = rng.uniform(0.2, 0.8, (100, 3))
+    r = make_reco(cgs, img, grid, nch)
+    r.set_trajectory(k)
+    r.set_bins([np.arange(100), np.array([], np.int64)])
+    r.set_smaps(synth.coil_maps(img, nch))
+    data = (rng.standard_normal((nch, 100)) + 1j * rng.standard_normal((nch, 100))).astype(np.complex64)
+    x, res, it = r.cg_sense_batched(data, 0.0, 4)
+    assert it[1] == 0 and np.all(x[1] == 0)
+    assert it[0] == 4 and np.isfinite(x[0]).all() and np.abs(x[0]).max() > 0
+
+
+def test_input_faults_are_reported(gpu_lib, cgs, synth):
+    img, grid, nch = (8, 8, 8), (16, 16, 16), 2
+    r = make_reco(cgs, img, grid, nch)
+    with pytest.raises(cgs.CGSError) as e:
+        r.nufft_fwd(np.zeros((nch,) + img, np.complex64))
+    assert e.value.code == cgs.CGS_ERR_STATE
+    k = np.random.default_rng(0).uniform(0.2, 0.8, (50, 3))
+    r.set_trajectory(k)
+    bad = synth.coil_maps(img, nch)
+    bad[1, 2, 3, 4] = np.nan
+    with pytest.raises(cgs.CGSError) as e:
+        r.set_smaps(bad)
+    assert e.value.code == cgs.CGS_ERR_NONFINITE
+    with pytest.raises(ValueError):
+        r.set_smaps(np.zeros((nch, 4, 4, 4), np.complex64))
+    r.set_smaps(synth.coil_maps(img, nch))
+    with pytest.raises(cgs.CGSError) as e:
+        r.cg_sense(np.zeros((nch, 50), np.complex64), -1.0)
+    assert e.value.code == cgs.CGS_ERR_NO_THRESHOLD
+    kk = k.copy()
+    kk[3, 1] = np.inf
+    with pytest.raises(cgs.CGSError) as e:
+        r.set_trajectory(kk)
+    assert e.value.code == cgs.CGS_ERR_NONFINITE

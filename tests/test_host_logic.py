@@ -1,0 +1,97 @@
+"""Host-side logic without a GPU: synthetic workload generation and the
+multi-GPU bin partition (exercised over gloo with two ranks)."""
+import os
+
+import numpy as np
+import pytest
+
+
+def test_workload_shapes(synth):
+    w = synth.WORKLOADS["cfg3"]
+    lines = synth.readout_lines(w)
+    assert lines.shape == (3072, 2)
+    k = synth.wave_trajectory(w)
+    assert k.shape == (3072 * 512, 3)
+    u = k * (np.array(w.grid) - 1)
+    # readouts span the grid along x; the outermost phase-encode lines wave
+    # past the grid edge by up to the wave amplitude (those taps are dropped)
+    assert u[:, 0].min() >= 0 and u[:, 0].max() < w.grid[0]
+    assert u[:, 1:].min() >= -w.wave_cells - 1e-9
+    assert (u[:, 1:].max(axis=0) <= np.array(w.grid[1:]) + w.wave_cells).all()
+
+
+def test_breathing_bins_uneven_occupancy(synth):
+    bins = synth.breathing_bins(3072, 16)
+    occ = np.array([len(b) for b in bins]) / 3072
+    assert np.isclose(occ.sum(), 1.0)
+    assert occ.min() >= 0.025 and occ.max() <= 0.125
+    assert occ.max() / occ.min() > 3
+    allr = np.sort(np.concatenate(bins))
+    assert np.array_equal(allr, np.arange(3072))
+
+
+def test_coil_maps_normalised(synth):
+    m = synth.coil_maps((16, 12, 8), 6)
+    assert np.allclose(np.sum(np.abs(m) ** 2, axis=0), 1.0, atol=1e-5)
+
+
+def test_phantom_seeded(synth):
+    a = synth.phantom((16, 16, 16))
+    b = synth.phantom((16, 16, 16))
+    assert np.array_equal(a, b) and np.abs(a).max() > 0
+
+
+def test_partition_balanced():
+    import importlib
+    dist = importlib.import_module("4d_lung_gb300.dist")
+    sizes = [5, 9, 3, 12, 7, 7, 4, 10]
+    parts = dist.partition_bins(sizes, 3)
+    assert sorted(sum(parts, [])) == list(range(8))
+    loads = [sum(sizes[b] for b in p) for p in parts]
+    assert max(loads) - min(loads) <= max(sizes)
+
+
+def _rank_main(rank, world, port, sizes, q):
+    import importlib
+
+    import torch
+    import torch.distributed as dist_
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist_.init_process_group("gloo", rank=rank, world_size=world)
+    d = importlib.import_module("4d_lung_gb300.dist")
+    mine = d.partition_bins(sizes, world)[rank]
+    t = torch.zeros(len(sizes), dtype=torch.int64)
+    for b in mine:
+        t[b] += 1
+    dist_.all_reduce(t)
+    load = torch.tensor([sum(sizes[b] for b in mine)], dtype=torch.int64)
+    loads = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+    dist_.all_gather(loads, load)
+    if rank == 0:
+        q.put((t.tolist(), [int(x.item()) for x in loads]))
+    dist_.destroy_process_group()
+
+
+def test_partition_two_ranks_gloo():
+    """Every bin is solved by exactly one rank; no data-path collective is
+    needed (the check itself uses one all_reduce)."""
+    torch = pytest.importorskip("torch")
+    import multiprocessing as mp
+    import socket
+    ctx = mp.get_context("spawn")
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    sizes = [int(x) for x in np.random.default_rng(0).integers(50, 200, 16)]
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, sizes, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    counts, loads = q.get(timeout=120)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert counts == [1] * 16
+    assert abs(loads[0] - loads[1]) <= max(sizes)

@@ -1,0 +1,84 @@
+"""Known-answer checks of the oracle that do not depend on the reference:
+Bessel I0, the centred FFT against numpy, adjointness of the NUFFT pair, and
+the approximation of the exact non-uniform DFT."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+
+def test_bessel_i0(o64):
+    sp = pytest.importorskip("scipy.special")
+    for x in [0.0, 0.5, 1.0, 3.7, 9.0, 14.9086, 20.0]:
+        assert abs(o64.lib.cgso_bessel_i0(x) - sp.i0(x)) <= 1e-14 * sp.i0(x)
+
+
+@pytest.mark.parametrize("grid", [(8, 6, 4), (24, 20, 16), (10, 14, 22)])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_centred_fft_vs_numpy(oracle_mod, o64, grid, sign):
+    """Fourier::transformFWD/BWD = (-1)^(sum N/2) fftshift(F(ifftshift(a))) for
+    even sizes (the sign alternation before and after the transform equals
+    the half-length shifts up to that global sign)."""
+    rng = np.random.default_rng(1)
+    a = rng.standard_normal(grid) + 1j * rng.standard_normal(grid)
+    p = oracle_mod.make_params(grid, grid, 1)
+    out = o64.centred_fft(p, a, sign, 0)
+    if sign < 0:
+        ref = np.fft.fftshift(np.fft.fftn(np.fft.ifftshift(a)))
+    else:
+        ref = np.fft.fftshift(np.fft.ifftn(np.fft.ifftshift(a))) * np.prod(grid)
+    ref = ref * (-1.0) ** (sum(n // 2 for n in grid))
+    assert rel_l2(out, ref) < 1e-13
+
+
+def _case(oracle_mod, o, img, grid, nch=2, n=400, seed=5):
+    rng = np.random.default_rng(seed)
+    k = rng.uniform(0.05, 0.95, (n, 3))
+    p = oracle_mod.make_params(img, grid, nch)
+    taps = o.taps(p, k)
+    return p, k, taps
+
+
+@pytest.mark.parametrize("img,grid", [((16, 16, 16), (16, 16, 16)), ((12, 10, 8), (24, 20, 16))])
+def test_adjointness(oracle_mod, o64, img, grid):
+    """<E x, y> = <x, E^H y> / c with c = adj_scale / sqrt(N_grid)."""
+    p, k, taps = _case(oracle_mod, o64, img, grid)
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal((2,) + img) + 1j * rng.standard_normal((2,) + img)
+    y = rng.standard_normal((2, k.shape[0])) + 1j * rng.standard_normal((2, k.shape[0]))
+    kft = o64.kernel_ft(p)
+    ex = o64.nufft_fwd(p, taps, kft, x)
+    ehy = o64.nufft_adj(p, taps, kft, y)
+    c = 1e-3 / np.sqrt(np.prod(grid))
+    lhs = np.vdot(ex, y)
+    rhs = np.vdot(x, ehy) / c
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+@pytest.mark.parametrize("kb_w,kb_b,tol", [
+    (4.25, 14.9086, 5e-2),                                      # reference shape (Reco.cpp:378-379)
+    (4.25, np.pi * np.sqrt(4.25 ** 2 / 4 * 1.5 ** 2 - 0.8), 2e-3),  # Beatty shape for 2x oversampling
+    (4.0, np.pi * np.sqrt(4.0 ** 2 / 4 * 1.5 ** 2 - 0.8), 3e-3),
+])
+def test_nudft_known_answer(oracle_mod, o64, kb_w, kb_b, tol):
+    """With a 2x oversampled grid the KB NUFFT approximates the exact NUDFT
+    sum_r x[r] exp(-2 pi i (u - G/2) . (r + lo - G/2) / G), u = k (G - 1).
+    The reference's shape parameter b = 14.9086 is tuned for a wider band than
+    2x oversampling gives, so its error is about 3 %; the Beatty shape
+    pi sqrt(w^2/s^2 (s - 1/2)^2 - 0.8) brings it near 1e-3.  The scale is 1."""
+    img, grid = (16, 16, 16), (32, 32, 32)
+    rng = np.random.default_rng(5)
+    k = rng.uniform(0.1, 0.9, (300, 3))
+    p = oracle_mod.make_params(img, grid, 1, kb_w=kb_w, kb_b=kb_b)
+    taps = o64.taps(p, k)
+    x = rng.standard_normal(img) + 1j * rng.standard_normal(img)
+    e = o64.nufft_fwd(p, taps, o64.kernel_ft(p), x[None])[0]
+    G = np.array(grid, float)
+    lo = (G - np.array(img)) // 2
+    u = k * (G - 1) - G / 2
+    r = np.stack(np.meshgrid(*[np.arange(n) for n in img], indexing="ij"), -1).reshape(-1, 3) + lo - G / 2
+    exact = np.exp(-2j * np.pi * (u / G) @ r.T) @ x.ravel()
+    scale = np.vdot(exact, e) / np.vdot(exact, exact)
+    assert abs(scale.imag) < 1e-3
+    assert abs(scale.real - 1.0) < 5e-2
+    assert rel_l2(e, scale.real * exact) < tol
