@@ -48,7 +48,7 @@ EXPORTS = [
     "cgs_kernel_ft", "cgs_fft3", "cgs_fft3_d", "cgs_nufft_fwd", "cgs_nufft_fwd_d",
     "cgs_nufft_adj", "cgs_nufft_adj_d", "cgs_apply_ehde", "cgs_apply_ehde_d", "cgs_cg_solve",
     "cgs_cg_solve_batched", "cgs_cg_solve_batched_d", "cgs_last_launch_count",
-    "cgs_profile_apply",
+    "cgs_profile_apply", "cgs_cg_solve_images", "cgs_alloc_host", "cgs_free_host",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -142,6 +142,9 @@ def lib():
         "cgs_cg_solve_batched_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
         "cgs_last_launch_count": (i64, [vp]),
         "cgs_profile_apply": (C.c_int, [vp, i32, i32, vp, vp, vp, i32, vp]),
+        "cgs_cg_solve_images": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
+        "cgs_alloc_host": (vp, [C.c_size_t]),
+        "cgs_free_host": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -307,6 +310,16 @@ class Reco:
         res = np.zeros(max(max_iter, 1), np.float64)
         it = np.zeros(1, np.int32)
         self._check(self._L.cgs_cg_solve(self._ctx, _p(data), _p(x), threshold, max_iter, _p(res), _p(it)))
+        return x, res[: it[0]], int(it[0])
+
+    def cg_sense_images(self, coil_imgs, threshold, max_iter=16):
+        """Reco::cgSenseDynamic from coil images (the reference's own input)."""
+        imgs = _c64(coil_imgs, (self.n_ch,) + self.img)
+        x = np.zeros(self.img, np.complex64)
+        res = np.zeros(max(max_iter, 1), np.float64)
+        it = np.zeros(1, np.int32)
+        self._check(self._L.cgs_cg_solve_images(self._ctx, _p(imgs), _p(x), threshold, max_iter,
+                                                _p(res), _p(it)))
         return x, res[: it[0]], int(it[0])
 
     def cg_sense_batched(self, data, threshold, max_iter):

@@ -30,6 +30,7 @@ def _units():
     for src in ("fft_dispatch.cu", "kernels_misc.cu", "cgs_api.cu"):
         units.append((src, src.replace(".cu", ".o"), []))
     units.append(("wave_caipi.cpp", "wave_caipi.o", []))
+    units.append(("reco_shim.cpp", "reco_shim.o", []))
     return units
 
 
@@ -44,6 +45,7 @@ def build(verbose=False, jobs=None):
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "cgsense_c.h"))
+    headers.append(os.path.join(ROOT, "include", "cgsense", "Reco.h"))
     cmds = []
     objs = []
     for src, obj, extra in _units():
@@ -53,7 +55,7 @@ def build(verbose=False, jobs=None):
         if _stale(o, [s, __file__] + headers):
             if src.endswith(".cpp"):
                 cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-I", os.path.join(ROOT, "include"),
-                       "-c", s, "-o", o]
+                       "-I", "/usr/local/cuda/include", "-c", s, "-o", o]
             else:
                 cmd = [NVCC] + ARCH + FLAGS + extra + ["-c", s, "-o", o]
             cmds.append(cmd)

@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
@@ -54,9 +55,11 @@ struct GraphKey {
     void* x;
     double thresh;
     int max_iter;
+    int rhs_from_images;
     bool operator<(const GraphKey& o) const
     {
-        return std::tie(data, x, thresh, max_iter) < std::tie(o.data, o.x, o.thresh, o.max_iter);
+        return std::tie(data, x, thresh, max_iter, rhs_from_images) <
+               std::tie(o.data, o.x, o.thresh, o.max_iter, o.rhs_from_images);
     }
 };
 
@@ -871,19 +874,25 @@ int cgs_apply_ehde(cgs_ctx* c, int32_t bin, const float* x, float* q)
 
 // The whole batched solve is recorded once into a CUDA graph (per data/x
 // pointers, threshold and iteration cap) and replayed.
-static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh, int max_iter)
+static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh, int max_iter,
+                        bool rhs_from_images)
 {
     const int nb = c->nbins;
     const long long Ni = c->Ni;
     const int nblk_adj = adj_z_blocks(c->G[2], c->Nl);
     const int nblk_cg = cg_blocks(Ni);
-    // RHS: b = sum_c conj(S_c) E_c^H (D y_c)   (CGSense.cpp:226-235, Reco.cpp:182-190)
-    CGS_LAUNCH(c, launch_gather_samples(data, c->ns, c->d_sorted.as<int>(), c->total, c->nch,
-                                        c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr, c->d_yv.as<float2>(),
-                                        c->stream));
-    for (int g = 0; g < nb; g += c->ws_bins) {
-        const int n = std::min(c->ws_bins, nb - g);
-        CGS_TRY(adj_chain(c, g, n, c->d_b.as<float2>() + (long long)g * Ni, Ni, true, nullptr, nullptr));
+    if (rhs_from_images) {
+        // b = sum_c conj(S_c) img_c from given coil images (Reco.cpp:182-190)
+        CGS_LAUNCH(c, launch_coil_combine(data, c->d_smaps.as<float2>(), c->nch, Ni, c->d_b.as<float2>(), c->stream));
+    } else {
+        // RHS: b = sum_c conj(S_c) E_c^H (D y_c)   (CGSense.cpp:226-235, Reco.cpp:182-190)
+        CGS_LAUNCH(c, launch_gather_samples(data, c->ns, c->d_sorted.as<int>(), c->total, c->nch,
+                                            c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr,
+                                            c->d_yv.as<float2>(), c->stream));
+        for (int g = 0; g < nb; g += c->ws_bins) {
+            const int n = std::min(c->ws_bins, nb - g);
+            CGS_TRY(adj_chain(c, g, n, c->d_b.as<float2>() + (long long)g * Ni, Ni, true, nullptr, nullptr));
+        }
     }
     CgState* st = c->d_state.as<CgState>();
     CGS_LAUNCH(c, launch_cg_init(c->d_b.as<float2>(), c->d_r.as<float2>(), c->d_pv.as<float2>(), x, Ni, Ni,
@@ -903,8 +912,8 @@ static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh
     return CGS_OK;
 }
 
-int cgs_cg_solve_batched_d(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter,
-                           double* residuals, int32_t* iters)
+static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter, double* residuals,
+                   int32_t* iters, bool rhs_from_images)
 {
     CGS_TRY(check_ready(c, true));
     if (!data || !x) return fail(c, CGS_ERR_ARG, "null pointer");
@@ -924,13 +933,15 @@ int cgs_cg_solve_batched_d(cgs_ctx* c, const float* data, float* x, double thres
     CGS_CUDA(c, c->d_partials2.ensure((size_t)nb * nblk_cg * 2 * sizeof(double)));
     CGS_CUDA(c, c->d_res.ensure((size_t)nb * std::max(max_iter, 1) * sizeof(double)));
 
-    GraphKey key{data, x, thresh, max_iter};
+    if (rhs_from_images && nb != 1) return fail(c, CGS_ERR_STATE, "coil-image right-hand side needs one bin");
+    GraphKey key{data, x, thresh, max_iter, rhs_from_images ? 1 : 0};
     auto it = c->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
     if (it == c->graphs.end()) {
         c->launches = 0;
         CGS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-        int st = record_solve(c, reinterpret_cast<const float2*>(data), reinterpret_cast<float2*>(x), thresh, max_iter);
+        int st = record_solve(c, reinterpret_cast<const float2*>(data), reinterpret_cast<float2*>(x), thresh, max_iter,
+                              rhs_from_images);
         cudaGraph_t graph = nullptr;
         cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
         if (st != CGS_OK) {
@@ -969,6 +980,31 @@ int cgs_cg_solve_batched_d(cgs_ctx* c, const float* data, float* x, double thres
     return CGS_OK;
 }
 
+int cgs_cg_solve_batched_d(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter,
+                           double* residuals, int32_t* iters)
+{
+    return solve_d(c, data, x, thresh, max_iter, residuals, iters, false);
+}
+
+int cgs_cg_solve_images(cgs_ctx* c, const float* coil_imgs, float* x, double thresh, int32_t max_iter,
+                        double* residuals, int32_t* iters)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!coil_imgs || !x) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (c->nbins != 1) return fail(c, CGS_ERR_STATE, "cgs_cg_solve_images reconstructs one bin");
+    const size_t bi = (size_t)c->nch * c->Ni * sizeof(float2), bx = (size_t)c->Ni * sizeof(float2);
+    CGS_CUDA(c, c->d_img.ensure(bi));
+    CGS_CUDA(c, c->d_x.ensure(bx));
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_img.p, coil_imgs, bi, cudaMemcpyHostToDevice, c->stream));
+    int32_t it_local = 0;
+    int st = solve_d(c, c->d_img.as<float>(), c->d_x.as<float>(), thresh, max_iter, residuals,
+                     iters ? iters : &it_local, true);
+    if (st != CGS_OK && st != CGS_ERR_NONFINITE) return st;
+    CGS_CUDA(c, cudaMemcpyAsync(x, c->d_x.p, bx, cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return st;
+}
+
 int cgs_cg_solve_batched(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter,
                          double* residuals, int32_t* iters)
 {
@@ -997,6 +1033,28 @@ int cgs_cg_solve(cgs_ctx* c, const float* data, float* x, double thresh, int32_t
 }
 
 int64_t cgs_last_launch_count(const cgs_ctx* c) { return c ? c->launches : 0; }
+
+void* cgs_alloc_host(size_t bytes)
+{
+    void* p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        p = std::malloc(bytes ? bytes : 1);   // no usable GPU: ordinary memory
+    }
+    return p;
+}
+
+void cgs_free_host(void* p)
+{
+    if (!p) return;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost) {
+        cudaFreeHost(p);
+    } else {
+        cudaGetLastError();
+        std::free(p);
+    }
+}
 
 int cgs_profile_apply(cgs_ctx* c, int32_t bin0, int32_t nb, const float* x, float* q, float* stage_ms,
                       int32_t max_stages, int32_t* n_stages)

@@ -54,6 +54,28 @@ cudaError_t launch_scatter_samples(const float2* yv, const int* sorted, long lon
 
 cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s) { return cudaMemsetAsync(p, 0, bytes, s); }
 
+// b = sum_c conj(S_c) img_c, coils summed in order (Reco.cpp:182-190)
+__global__ void k_coil_combine(const float2* __restrict__ imgs, const float2* __restrict__ smaps, int nch,
+                               long long n, float2* __restrict__ b)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = 0; c < nch; ++c) {
+        const float2 s = smaps[(long long)c * n + i], g = imgs[(long long)c * n + i];
+        acc.x += s.x * g.x + s.y * g.y;
+        acc.y += s.x * g.y - s.y * g.x;
+    }
+    b[i] = acc;
+}
+
+cudaError_t launch_coil_combine(const float2* imgs, const float2* smaps, int nch, long long n, float2* b,
+                                cudaStream_t s)
+{
+    k_coil_combine<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(imgs, smaps, nch, n, b);
+    return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // gridding
 // ---------------------------------------------------------------------------

@@ -34,6 +34,8 @@ cudaError_t launch_gather_samples(const float2* data, long long ns, const int* s
 cudaError_t launch_scatter_samples(const float2* yv, const int* sorted, long long total, int nch, long long ns,
                                    float2* data, cudaStream_t s);
 cudaError_t launch_zero(void* p, size_t bytes, cudaStream_t s);
+cudaError_t launch_coil_combine(const float2* imgs, const float2* smaps, int nch, long long n, float2* b,
+                                cudaStream_t s);
 
 // CG
 int cg_blocks(long long n);

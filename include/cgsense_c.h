@@ -163,6 +163,13 @@ int cgs_apply_ehde_d(cgs_ctx* ctx, int32_t bin0, int32_t nb, const float* x_dev,
 int cgs_cg_solve(cgs_ctx* ctx, const float* data, float* x, double threshold, int32_t max_iter,
                  double* residuals, int32_t* iters);
 
+/* Reco::cgSenseDynamic exactly as the reference calls it: its inputs are the
+ * coil images `img` already produced by nufftBWD from density-corrected
+ * samples (CGSense.cpp:226-235) and the coil maps; the loop applies D from
+ * cgs_set_dcf.  coil_imgs: host [n_ch][image voxels]; bin 0 only. */
+int cgs_cg_solve_images(cgs_ctx* ctx, const float* coil_imgs, float* x, double threshold, int32_t max_iter,
+                        double* residuals, int32_t* iters);
+
 /* All bins in one graph-captured launch sequence (the 4D reconstruction of
  * CGSense.cpp:200-282 without its file IO): x[nbins][image voxels],
  * residuals[nbins][max_iter], iters[nbins]. */
@@ -172,6 +179,12 @@ int cgs_cg_solve_batched(cgs_ctx* ctx, const float* data, float* x, double thres
  * the solve completes). */
 int cgs_cg_solve_batched_d(cgs_ctx* ctx, const float* data_dev, float* x_dev, double threshold,
                            int32_t max_iter, double* residuals, int32_t* iters);
+
+/* fftwf_alloc_complex / fftwf_free counterparts for host buffers handed to
+ * the library (Reco.cpp:441,447,454): page-locked memory when a GPU is
+ * present, so that transfers run at full speed. */
+void* cgs_alloc_host(size_t bytes);
+void cgs_free_host(void* p);
 
 /* Number of kernel launches issued by the last compute call (for a graph
  * replay: the kernels in the graph). */
