@@ -34,10 +34,11 @@ CGS_ERR_STATE = 4
 CGS_ERR_NOMEM = 5
 CGS_ERR_UNSUPPORTED = 6
 CGS_ERR_NO_THRESHOLD = 7
+CGS_ERR_TIMEOUT = 8
 
 _ERR_NAMES = {
     1: "CGS_ERR_ARG", 2: "CGS_ERR_CUDA", 3: "CGS_ERR_NONFINITE", 4: "CGS_ERR_STATE",
-    5: "CGS_ERR_NOMEM", 6: "CGS_ERR_UNSUPPORTED", 7: "CGS_ERR_NO_THRESHOLD",
+    5: "CGS_ERR_NOMEM", 6: "CGS_ERR_UNSUPPORTED", 7: "CGS_ERR_NO_THRESHOLD", 8: "CGS_ERR_TIMEOUT",
 }
 
 # Every symbol declared in include/cgsense_c.h.
@@ -49,6 +50,7 @@ EXPORTS = [
     "cgs_nufft_adj", "cgs_nufft_adj_d", "cgs_apply_ehde", "cgs_apply_ehde_d", "cgs_cg_solve",
     "cgs_cg_solve_batched", "cgs_cg_solve_batched_d", "cgs_last_launch_count",
     "cgs_profile_apply", "cgs_cg_solve_images", "cgs_alloc_host", "cgs_free_host",
+    "cgs_cg_solve_plain_d",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -145,6 +147,7 @@ def lib():
         "cgs_cg_solve_images": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
         "cgs_alloc_host": (vp, [C.c_size_t]),
         "cgs_free_host": (None, [vp]),
+        "cgs_cg_solve_plain_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -354,6 +357,15 @@ class Reco:
 
     def fft3_tensor(self, a, sign):
         self._check(self._L.cgs_fft3_d(self._ctx, C.c_void_p(a.data_ptr()), sign, 0))
+
+    def cg_sense_plain_tensor(self, data, x, threshold, max_iter):
+        """The plain per-bin form (comparison point); returns (residuals, iters)."""
+        nb = self.num_bins()
+        res = np.zeros((nb, max(max_iter, 1)), np.float64)
+        it = np.zeros(nb, np.int32)
+        self._check(self._L.cgs_cg_solve_plain_d(self._ctx, C.c_void_p(data.data_ptr()), C.c_void_p(x.data_ptr()),
+                                                 threshold, max_iter, _p(res), _p(it)))
+        return res, it
 
     def cg_sense_batched_tensor(self, data, x, threshold, max_iter, want_stats=True):
         nb = self.num_bins()

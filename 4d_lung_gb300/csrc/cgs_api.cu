@@ -78,6 +78,7 @@ struct cgs_ctx {
     std::vector<double> apod_full[3];   // 1/R_a(g) over the whole grid axis
 
     DevBuf tw[3], ap[3];
+    DevBuf d_err;                // set by a kernel whose bounded wait timed out
     // trajectory
     long long ns = 0;
     std::vector<double> h_k;
@@ -104,6 +105,10 @@ struct cgs_ctx {
     std::map<GraphKey, cudaGraphExec_t> graphs;
     std::map<GraphKey, long long> graph_launches;
     long long launches = 0;
+    // plain per-bin form (cgs_cg_solve_plain_d)
+    cufftHandle plain_plan = 0;
+    bool plain_plan_ok = false;
+    DevBuf d_plain_grid, d_plain_y, d_plain_dot;
     // per-stage timing (cgs_profile_apply): events recorded after each pass
     cudaEvent_t* prof_ev = nullptr;
     int prof_n = 0;
@@ -363,6 +368,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fy.in_off = c->lo[1];
     fy.Lout = Gy;
     fy.out_off = 0;
+    fy.err = c->d_err.as<int>();
     fy.tw = c->tw[1].as<float2>();
     CGS_LAUNCH(c, launch_strided(Gy, -1, fy, Ix, nb * c->nch, c->stream));
 
@@ -378,6 +384,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fx.in_off = c->lo[0];
     fx.Lout = Gx;
     fx.out_off = 0;
+    fx.err = c->d_err.as<int>();
     fx.tw = c->tw[0].as<float2>();
     CGS_LAUNCH(c, launch_strided(Gx, -1, fx, 1, nb * c->nch, c->stream));
 
@@ -439,6 +446,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
     ax.in_off = 0;
     ax.Lout = Ix;
     ax.out_off = c->lo[0];
+    ax.err = c->d_err.as<int>();
     ax.tw = c->tw[0].as<float2>();
     CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
 
@@ -454,6 +462,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
     ay.in_off = 0;
     ay.Lout = Iy;
     ay.out_off = c->lo[1];
+    ay.err = c->d_err.as<int>();
     ay.tw = c->tw[1].as<float2>();
     CGS_LAUNCH(c, launch_strided(Gy, +1, ay, Ix, nb * c->nch, c->stream));
 
@@ -496,6 +505,20 @@ int apply_bins(cgs_ctx* c, int b0, int nb, const float2* x, float2* q, const flo
     return CGS_OK;
 }
 
+// A pipelined pass whose bounded wait ran out sets the context's flag; read
+// it at the host synchronisation points.
+int check_timeout(cgs_ctx* c)
+{
+    int h = 0;
+    CGS_CUDA(c, cudaMemcpyAsync(&h, c->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (h) {
+        CGS_CUDA(c, cudaMemsetAsync(c->d_err.p, 0, sizeof(int), c->stream));
+        return fail(c, CGS_ERR_TIMEOUT, "a pipelined FFT pass timed out waiting for its copies");
+    }
+    return CGS_OK;
+}
+
 int check_ready(cgs_ctx* c, bool need_smaps)
 {
     if (!c) return CGS_ERR_ARG;
@@ -525,6 +548,7 @@ int centred_fft_dev(cgs_ctx* c, float2* a, int sign, int rescale)
     sy.B = Gz;
     sy.Lin = sy.Lout = Gy;
     sy.tw = c->tw[1].as<float2>();
+    sy.err = c->d_err.as<int>();
     CGS_LAUNCH(c, launch_strided(Gy, sign, sy, Gx, 1, c->stream));
     StridedPassArgs sx{};
     sx.in = a;
@@ -532,6 +556,7 @@ int centred_fft_dev(cgs_ctx* c, float2* a, int sign, int rescale)
     sx.B = Gy * Gz;
     sx.Lin = sx.Lout = Gx;
     sx.tw = c->tw[0].as<float2>();
+    sx.err = c->d_err.as<int>();
     CGS_LAUNCH(c, launch_strided(Gx, sign, sx, 1, 1, c->stream));
     if (rescale) {
         // Fourier.cpp:31-41 rescales by 1/sqrt(N) after the backward transform;
@@ -624,6 +649,8 @@ int cgs_create(const cgs_params* p, cgs_ctx** out)
     c->nty = (c->G[1] + TILE_Y - 1) / TILE_Y;
     c->ntz = (c->G[2] + TILE_Z - 1) / TILE_Z;
     c->ntiles = c->ntx * c->nty * c->ntz;
+    if (c->d_err.ensure(sizeof(int)) != cudaSuccess || cudaMemset(c->d_err.p, 0, sizeof(int)) != cudaSuccess)
+        return bad(CGS_ERR_NOMEM, "error flag allocation failed");
     if (cudaMalloc(&c->d_smaps.p, (size_t)c->nch * c->Ni * sizeof(float2)) != cudaSuccess)
         return bad(CGS_ERR_NOMEM, "coil map allocation failed");
     c->d_smaps.bytes = (size_t)c->nch * c->Ni * sizeof(float2);
@@ -638,6 +665,7 @@ void cgs_destroy(cgs_ctx* c)
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     drop_graphs(c);
+    if (c->plain_plan_ok) cufftDestroy(c->plain_plan);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -655,7 +683,7 @@ int cgs_sync(cgs_ctx* c)
 {
     if (!c) return CGS_ERR_ARG;
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return CGS_OK;
+    return check_timeout(c);
 }
 
 int cgs_set_trajectory(cgs_ctx* c, const double* k, int64_t ns)
@@ -788,6 +816,7 @@ int cgs_fft3(cgs_ctx* c, float* grid, int32_t sign, int32_t rescale)
     CGS_TRY(centred_fft_dev(c, c->d_img.as<float2>(), sign, 0));
     CGS_CUDA(c, cudaMemcpyAsync(grid, c->d_img.p, bytes, cudaMemcpyDeviceToHost, c->stream));
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    CGS_TRY(check_timeout(c));
     if (rescale) {
         const double s = 1.0 / std::sqrt((double)c->Ng);
         for (size_t i = 0; i < 2 * (size_t)c->Ng; ++i) grid[i] = (float)((double)grid[i] * s);
@@ -831,7 +860,7 @@ int cgs_nufft_fwd(cgs_ctx* c, const float* img, float* data)
     CGS_TRY(cgs_nufft_fwd_d(c, c->d_img.as<float>(), c->d_data.as<float>()));
     CGS_CUDA(c, cudaMemcpyAsync(data, c->d_data.p, bd, cudaMemcpyDeviceToHost, c->stream));
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return CGS_OK;
+    return check_timeout(c);
 }
 
 int cgs_nufft_adj(cgs_ctx* c, const float* data, float* img)
@@ -845,7 +874,7 @@ int cgs_nufft_adj(cgs_ctx* c, const float* data, float* img)
     CGS_TRY(cgs_nufft_adj_d(c, c->d_data.as<float>(), c->d_img.as<float>()));
     CGS_CUDA(c, cudaMemcpyAsync(img, c->d_img.p, bi, cudaMemcpyDeviceToHost, c->stream));
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return CGS_OK;
+    return check_timeout(c);
 }
 
 int cgs_apply_ehde_d(cgs_ctx* c, int32_t bin0, int32_t nb, const float* x, float* q)
@@ -869,7 +898,7 @@ int cgs_apply_ehde(cgs_ctx* c, int32_t bin, const float* x, float* q)
     CGS_TRY(cgs_apply_ehde_d(c, bin, 1, c->d_img.as<float>(), reinterpret_cast<float*>(dq)));
     CGS_CUDA(c, cudaMemcpyAsync(q, dq, b, cudaMemcpyDeviceToHost, c->stream));
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
-    return CGS_OK;
+    return check_timeout(c);
 }
 
 // The whole batched solve is recorded once into a CUDA graph (per data/x
@@ -973,6 +1002,7 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
                 for (int i = 0; i < max_iter; ++i)
                     residuals[(size_t)b * max_iter + i] = i < hs[b].iter ? hr[(size_t)b * max_iter + i] : 0.0;
         }
+        CGS_TRY(check_timeout(c));
         for (int b = 0; b < nb; ++b)
             if (hs[b].error)
                 return fail(c, CGS_ERR_NONFINITE, "NaN or INF value in image detected (bin " + std::to_string(b) + ")");
@@ -1022,6 +1052,97 @@ int cgs_cg_solve_batched(cgs_ctx* c, const float* data, float* x, double thresh,
     CGS_CUDA(c, cudaMemcpyAsync(x, c->d_x.p, bx, cudaMemcpyDeviceToHost, c->stream));
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
     return st;
+}
+
+int cgs_cg_solve_plain_d(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter,
+                         double* residuals, int32_t* iters)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!data || !x) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (thresh == -1.0) return fail(c, CGS_ERR_NO_THRESHOLD, "no threshold set for CG SENSE (Reco.cpp:192-196)");
+    if (max_iter < 0 || max_iter > 10000) return fail(c, CGS_ERR_ARG, "max_iter out of range");
+    const int nb = c->nbins;
+    const long long Ni = c->Ni;
+    const int nblk_cg = cg_blocks(Ni);
+    const int nblk_dot = cg_blocks(Ni);
+    if (!c->plain_plan_ok) {
+        if (cufftPlan3d(&c->plain_plan, c->G[0], c->G[1], c->G[2], CUFFT_C2C) != CUFFT_SUCCESS)
+            return fail(c, CGS_ERR_CUDA, "cufftPlan3d failed");
+        c->plain_plan_ok = true;
+    }
+    if (cufftSetStream(c->plain_plan, c->stream) != CUFFT_SUCCESS) return fail(c, CGS_ERR_CUDA, "cufftSetStream failed");
+    CGS_CUDA(c, c->d_plain_grid.ensure(c->Ng * sizeof(float2)));
+    CGS_CUDA(c, c->d_plain_y.ensure(std::max<long long>(c->max_bin, 1) * sizeof(float2)));
+    CGS_CUDA(c, c->d_plain_dot.ensure((size_t)nblk_dot * 2 * sizeof(double)));
+    CGS_CUDA(c, c->d_b.ensure(Ni * sizeof(float2)));
+    CGS_CUDA(c, c->d_r.ensure(Ni * sizeof(float2)));
+    CGS_CUDA(c, c->d_pv.ensure(Ni * sizeof(float2)));
+    CGS_CUDA(c, c->d_q.ensure(Ni * sizeof(float2)));
+    CGS_CUDA(c, c->d_state.ensure(sizeof(CgState)));
+    CGS_CUDA(c, c->d_partials2.ensure((size_t)nblk_cg * 2 * sizeof(double)));
+    CGS_CUDA(c, c->d_res.ensure((size_t)nb * std::max(max_iter, 1) * sizeof(double)));
+    PlainArgs P{};
+    for (int a = 0; a < 3; ++a) {
+        P.g.I[a] = c->I[a];
+        P.g.G[a] = c->G[a];
+        P.g.lo[a] = c->lo[a];
+        P.ap[a] = c->ap[a].as<float>();
+    }
+    P.g.Ni = Ni;
+    P.g.Ng = c->Ng;
+    P.nch = c->nch;
+    P.smaps = c->d_smaps.as<float2>();
+    P.scale = (float)c->adj_scale_total;
+    P.thresh = c->thresh;
+    P.plan = c->plain_plan;
+    P.s = c->stream;
+    P.grid = c->d_plain_grid.as<float2>();
+    P.y = c->d_plain_y.as<float2>();
+    c->launches = 0;
+    CgState* st = c->d_state.as<CgState>();
+    std::vector<double> hres;
+    for (int b = 0; b < nb; ++b) {
+        const long long off = c->h_bin_off[b], n = c->h_bin_off[b + 1] - off;
+        const TapRecord* rec = c->d_rec.as<TapRecord>() + off;
+        const float* dcf = c->has_dcf ? c->d_dcf_sorted.as<float>() + off : nullptr;
+        const int* sorted = c->d_sorted.as<int>() + off;
+        float2* xb = reinterpret_cast<float2*>(x) + (long long)b * Ni;
+        double* resb = c->d_res.as<double>() + (long long)b * std::max(max_iter, 1);
+        CGS_CUDA(c, plain_rhs(P, rec, dcf, sorted, n, reinterpret_cast<const float2*>(data), c->ns, c->d_b.as<float2>(),
+                              &c->launches));
+        CGS_LAUNCH(c, launch_cg_init(c->d_b.as<float2>(), c->d_r.as<float2>(), c->d_pv.as<float2>(), xb, Ni, Ni,
+                                     c->d_partials2.as<double>(), st, 1, c->stream));
+        CGS_LAUNCH(c, launch_cg_arm(st, c->d_partials2.as<double>(), nblk_cg, 1, thresh, max_iter, c->stream));
+        CgState hs{};
+        for (int it = 0; it < max_iter; ++it) {
+            // host-side loop test every iteration, as the reference's while loop
+            CGS_CUDA(c, cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
+            CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+            if (!hs.active) break;
+            CGS_CUDA(c, plain_apply(P, rec, dcf, n, c->d_pv.as<float2>(), c->d_q.as<float2>(), &c->launches));
+            CGS_LAUNCH(c, plain_dot(c->d_pv.as<float2>(), c->d_q.as<float2>(), Ni, c->d_plain_dot.as<double>(), nblk_dot,
+                                    c->stream));
+            CGS_LAUNCH(c, launch_cg_alpha(st, c->d_plain_dot.as<double>(), nblk_dot, 1, c->d_q.as<float2>(), Ni,
+                                          c->stream));
+            CGS_LAUNCH(c, launch_cg_update_xr(xb, c->d_r.as<float2>(), c->d_pv.as<float2>(), c->d_q.as<float2>(), Ni, Ni,
+                                              st, c->d_partials2.as<double>(), 1, c->stream));
+            CGS_LAUNCH(c, launch_cg_beta(st, c->d_partials2.as<double>(), nblk_cg, 1, resb, max_iter, c->stream));
+            CGS_LAUNCH(c, launch_cg_update_p(c->d_pv.as<float2>(), c->d_r.as<float2>(), Ni, Ni, st, 1, c->stream));
+            CGS_LAUNCH(c, launch_cg_loop_test(st, 1, c->stream));
+        }
+        CGS_CUDA(c, cudaMemcpyAsync(&hs, st, sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
+        if (residuals) {
+            hres.assign(std::max(max_iter, 1), 0.0);
+            CGS_CUDA(c, cudaMemcpyAsync(hres.data(), resb, hres.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                        c->stream));
+        }
+        CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (iters) iters[b] = hs.iter;
+        if (residuals)
+            for (int i = 0; i < max_iter; ++i) residuals[(size_t)b * max_iter + i] = i < hs.iter ? hres[i] : 0.0;
+        if (hs.error) return fail(c, CGS_ERR_NONFINITE, "NaN or INF value in image detected (bin " + std::to_string(b) + ")");
+    }
+    return CGS_OK;
 }
 
 int cgs_cg_solve(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter, double* residuals,

@@ -11,6 +11,10 @@ constexpr int TAPS_1D = 5;
 // spreading tile (grid points) owned by one block
 constexpr int TILE_X = 4, TILE_Y = 8, TILE_Z = 16;
 constexpr int TILE_PTS = TILE_X * TILE_Y * TILE_Z;
+// shared accumulator pitch along z: 16 + 5, so that the 5x5 (y, z) lanes of a
+// sample fall on distinct 8-byte bank pairs (two wavefronts, no conflicts)
+constexpr int TILE_ZP = TILE_Z + 5;
+constexpr int ACC_PTS = TILE_X * TILE_Y * TILE_ZP;
 constexpr int SPREAD_THREADS = 32 * TILE_X;
 constexpr int RED_THREADS = 256;
 
@@ -36,6 +40,7 @@ struct StridedPassArgs {
     int ntb;                   // column tiles per outer index
     int Lin, in_off, Lout, out_off;
     const float2* tw;          // L twiddles
+    int* err;                  // error flag of the pipelined pass (null: plain loads)
 };
 
 struct ContigPassArgs {

@@ -10,13 +10,23 @@ namespace cgs {
     cudaError_t fft_contig_##L_(int sign, const ContigPassArgs& a, int batch, cudaStream_t s);        \
     cudaError_t fft_fwd_z_##L_(const FwdZArgs& a, int batch, cudaStream_t s);                          \
     cudaError_t fft_adj_z_##L_(const AdjZArgs& a, int batch, cudaStream_t s);                          \
-    int fft_adj_blocks_##L_(long long nl);
+    int fft_adj_blocks_##L_(long long nl);                                                             \
+    cudaError_t fft_init_##L_();
 CGS_FFT_SIZES(CGS_DECLARE)
 
 static const int kSizes[] = {
 #define CGS_LIST(L_, R1_, R2_, G_) L_,
     CGS_FFT_SIZES(CGS_LIST)
 };
+
+cudaError_t fft_init_all()
+{
+    cudaError_t e = cudaSuccess;
+#define CGS_INIT(L_, R1_, R2_, G_) if (e == cudaSuccess) e = fft_init_##L_();
+    CGS_FFT_SIZES(CGS_INIT)
+#undef CGS_INIT
+    return e;
+}
 
 bool fft_supported(int L)
 {

@@ -10,6 +10,23 @@
 
 namespace cgs {
 
+static int sm_count()
+{
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// The bulk-copy pipelined pass measured slower than the plain pass on GB300
+// (one 128-byte copy per row saturates the copy engine's request rate); it
+// stays off until the tensor-map version replaces it.
+constexpr bool kUsePipe = false;
+
 constexpr int rmax2(int a, int b) { return a > b ? a : b; }
 constexpr int strided_tb(int r1, int r2) { return rmax2(r1, r2) > 16 ? 8 : 16; }
 constexpr int contig_lpb(int r1, int r2) { return rmax2(r1, r2) > 16 ? 8 : (rmax2(r1, r2) > 8 ? 16 : 32); }
@@ -23,9 +40,43 @@ struct SizeImpl {
     static constexpr int NT_C = LPB * rmax2(R1, R2);
     static_assert(NT_C % 32 == 0, "contiguous pass block must be whole warps");
 
+    static constexpr int NSTAGE = 3;
+    using Pipe = PipeLayout<R1, R2, TB, NSTAGE>;
+
+    static cudaError_t init()
+    {
+        const int smem = (int)Pipe::smem_bytes(L);
+        cudaError_t e = cudaFuncSetAttribute(k_fft_strided_pipe<R1, R2, -1, TB, NSTAGE>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_fft_strided_pipe<R1, R2, +1, TB, NSTAGE>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        return e;
+    }
+
     static cudaError_t strided(int sign, StridedPassArgs a, int A, int batch, cudaStream_t s)
     {
         a.ntb = (a.B + TB - 1) / TB;
+        // bulk copies need 16-byte aligned rows: base pointer, B, strides even
+        const bool aligned = ((reinterpret_cast<uintptr_t>(a.in) & 15) == 0) && (a.B % 2 == 0) &&
+                             (a.in_as % 2 == 0) && (a.in_bs % 2 == 0) && a.Lin > 0;
+        if (kUsePipe && a.err && aligned) {
+            const size_t smem = Pipe::smem_bytes(a.Lin);
+            int per_sm = 0;
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                &per_sm, sign < 0 ? k_fft_strided_pipe<R1, R2, -1, TB, NSTAGE> : k_fft_strided_pipe<R1, R2, +1, TB, NSTAGE>,
+                Pipe::NT, smem);
+            if (e != cudaSuccess) return e;
+            const long long tiles_per_item = (long long)A * a.ntb;
+            const long long ntiles = tiles_per_item * batch;
+            long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
+            if (nblk > ntiles) nblk = ntiles;
+            if (sign < 0)
+                k_fft_strided_pipe<R1, R2, -1, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, ntiles, (int)tiles_per_item);
+            else
+                k_fft_strided_pipe<R1, R2, +1, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, ntiles, (int)tiles_per_item);
+            return cudaGetLastError();
+        }
         dim3 grid((unsigned)(A * a.ntb), (unsigned)batch);
         if (sign < 0) k_fft_strided<R1, R2, -1, TB><<<grid, NT_S, 0, s>>>(a);
         else k_fft_strided<R1, R2, +1, TB><<<grid, NT_S, 0, s>>>(a);
@@ -59,6 +110,7 @@ struct SizeImpl {
     cudaError_t fft_fwd_z_##L_(const FwdZArgs& a, int batch, cudaStream_t s);                          \
     cudaError_t fft_adj_z_##L_(const AdjZArgs& a, int batch, cudaStream_t s);                          \
     int fft_adj_blocks_##L_(long long nl);                                                             \
+    cudaError_t fft_init_##L_();                                                                       \
     CGS_DEFINE_IF_##G_(L_, R1_, R2_)
 
 #define CGS_BODY(L_, R1_, R2_)                                                                      \
@@ -70,7 +122,8 @@ struct SizeImpl {
     { return SizeImpl<R1_, R2_>::fwd_z(a, batch, s); }                                              \
     cudaError_t fft_adj_z_##L_(const AdjZArgs& a, int batch, cudaStream_t s)                           \
     { return SizeImpl<R1_, R2_>::adj_z(a, batch, s); }                                              \
-    int fft_adj_blocks_##L_(long long nl) { return SizeImpl<R1_, R2_>::adj_blocks(nl); }
+    int fft_adj_blocks_##L_(long long nl) { return SizeImpl<R1_, R2_>::adj_blocks(nl); }               \
+    cudaError_t fft_init_##L_() { return SizeImpl<R1_, R2_>::init(); }
 
 #if CGS_FFT_GROUP == 0
 #define CGS_DEFINE_IF_0(L, R1, R2) CGS_BODY(L, R1, R2)

@@ -23,6 +23,7 @@
 #pragma once
 #include "fft_codelets.cuh"
 #include "cgs_types.h"
+#include "ptx_async.cuh"
 
 namespace cgs {
 
@@ -97,6 +98,131 @@ k_fft_strided(StridedPassArgs a)
                 if (bok && lo >= 0 && lo < a.Lout) out[(long long)lo * a.B] = parity(u[k2], l);
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined strided pass.  Persistent blocks walk the tiles (batch item,
+// outer index, TB-column strip) round-robin.  The Lin stored rows of a tile
+// are fetched by the asynchronous copy engine (one 16-byte-aligned bulk copy
+// per row, completion counted on an mbarrier), NSTAGE tiles ahead, so that
+// the HBM requests of later tiles overlap the FFT of the current one.  The
+// two register stages are those of k_fft_strided.  Every wait is bounded
+// (2 s); on a timeout the block sets *err, lets its copies land and exits.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long PIPE_WAIT_NS = 2000000000ull;
+
+template <int R1, int R2, int TB, int NSTAGE>
+struct PipeLayout {
+    static constexpr int L = R1 * R2;
+    static constexpr int NT = TB * (R1 > R2 ? R1 : R2);
+    static size_t smem_bytes(int Lin)
+    {
+        return ((size_t)NSTAGE * Lin * TB + (size_t)L * TB + L) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
+    }
+};
+
+template <int R1, int R2, int SIGN, int TB, int NSTAGE>
+__global__ void __launch_bounds__(PipeLayout<R1, R2, TB, NSTAGE>::NT)
+k_fft_strided_pipe(StridedPassArgs a, long long ntiles, int tiles_per_item)
+{
+    constexpr int L = R1 * R2;
+    constexpr int NT = PipeLayout<R1, R2, TB, NSTAGE>::NT;
+    extern __shared__ float4 s_pipe[];
+    const int stage_elems = a.Lin * TB;
+    float2* s_in = reinterpret_cast<float2*>(s_pipe);
+    float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
+    float2* s_tw = s_y + L * TB;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&s_bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const long long my_n = ntiles > (long long)blockIdx.x ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+
+    auto issue = [&](long long k) {
+        const long long t = blockIdx.x + k * gridDim.x;
+        const long long item = t / tiles_per_item;
+        const int rem = (int)(t - item * tiles_per_item);
+        const int ai = rem / a.ntb;
+        const int b0 = (rem - ai * a.ntb) * TB;
+        const int ncols = min(TB, a.B - b0);
+        const float2* src = a.in + item * a.in_bs + (long long)ai * a.in_as + b0;
+        const int s = (int)(k % NSTAGE);
+        const uint32_t row_bytes = (uint32_t)ncols * (uint32_t)sizeof(float2);
+        if (lane == 0) mbar_arrive_expect_tx(&s_bar[s], row_bytes * (uint32_t)a.Lin);
+        __syncwarp();
+        float2* dst = s_in + (size_t)s * stage_elems;
+        for (int li = lane; li < a.Lin; li += 32)
+            bulk_copy_g2s(dst + (size_t)li * TB, src + (long long)li * a.B, row_bytes, &s_bar[s]);
+    };
+
+    if (warp == 0)
+        for (long long k = 0; k < NSTAGE - 1 && k < my_n; ++k) issue(k);
+    for (long long k = 0; k < my_n; ++k) {
+        const int s = (int)(k % NSTAGE);
+        if (warp == 0 && k + NSTAGE - 1 < my_n) issue(k + NSTAGE - 1);
+        const bool ok = mbar_wait_bounded(&s_bar[s], (uint32_t)((k / NSTAGE) & 1), PIPE_WAIT_NS);
+        if (__syncthreads_or(!ok)) {
+            // timeout: report, let the copies already issued land, leave
+            if (tid == 0) {
+                atomicExch(a.err, 1);
+                for (long long j = k; j < my_n && j < k + NSTAGE - 1 + 1; ++j)
+                    mbar_wait_bounded(&s_bar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1), PIPE_WAIT_NS);
+            }
+            return;
+        }
+        const long long t = blockIdx.x + k * gridDim.x;
+        const long long item = t / tiles_per_item;
+        const int rem = (int)(t - item * tiles_per_item);
+        const int ai = rem / a.ntb;
+        const int b0 = (rem - ai * a.ntb) * TB;
+        const int bi = tid % TB;
+        const int b = b0 + bi;
+        const bool bok = b < a.B;
+        const float2* sin_s = s_in + (size_t)s * stage_elems;
+        {
+            const int n2 = tid / TB;
+            if (n2 < R2) {
+                float2 v[R1];
+#pragma unroll
+                for (int n1 = 0; n1 < R1; ++n1) {
+                    const int l = R2 * n1 + n2;
+                    const int li = l - a.in_off;
+                    float2 x = make_float2(0.f, 0.f);
+                    if (bok && li >= 0 && li < a.Lin) x = parity(sin_s[li * TB + bi], l);
+                    v[n1] = x;
+                }
+                Dft<R1, SIGN>::run(v);
+#pragma unroll
+                for (int k1 = 0; k1 < R1; ++k1) {
+                    float2 tv = v[k1];
+                    if (k1 > 0) tv = table_twiddle<SIGN>(tv, s_tw[n2 * k1]);
+                    s_y[(k1 * R2 + n2) * TB + bi] = tv;
+                }
+            }
+        }
+        __syncthreads();
+        {
+            const int k1 = tid / TB;
+            if (k1 < R1) {
+                float2 u[R2];
+#pragma unroll
+                for (int n2 = 0; n2 < R2; ++n2) u[n2] = s_y[(k1 * R2 + n2) * TB + bi];
+                Dft<R2, SIGN>::run(u);
+                float2* out = a.out + item * a.out_bs + (long long)ai * a.out_as + b;
+#pragma unroll
+                for (int k2 = 0; k2 < R2; ++k2) {
+                    const int l = k1 + R1 * k2;
+                    const int lo = l - a.out_off;
+                    if (bok && lo >= 0 && lo < a.Lout) out[(long long)lo * a.B] = parity(u[k2], l);
+                }
+            }
+        }
+        __syncthreads();
     }
 }
 

@@ -17,21 +17,10 @@
 #pragma once
 #include "cgs_common.cuh"
 #include "cgs_types.h"
+#include "gridding_common.cuh"
 
 namespace cgs {
 
-
-
-CGS_D unsigned pack_nearest(int nx, int ny, int nz)
-{
-    return (unsigned)nx | ((unsigned)ny << 11) | ((unsigned)nz << 22);
-}
-CGS_D void unpack_nearest(unsigned u, int& nx, int& ny, int& nz)
-{
-    nx = (int)(u & 2047u);
-    ny = (int)((u >> 11) & 2047u);
-    nz = (int)(u >> 22);
-}
 
 
 // ---------------------------------------------------------------------------
@@ -76,18 +65,6 @@ __global__ void k_tap_records(const double* __restrict__ k, const int* __restric
         for (int j = 0; j < TAPS_1D; ++j) f[a * TAPS_1D + j] = wv[a][j];
     f[15] = __uint_as_float(pack_nearest(nearest[0], nearest[1], nearest[2]));
     out[i] = r;
-}
-
-CGS_D void load_record(const TapRecord* __restrict__ rec, long long i, float (&w)[15], int& nx, int& ny,
-                       int& nz)
-{
-    const float4* p = reinterpret_cast<const float4*>(rec + i);
-    const float4 a = __ldg(p + 0), b = __ldg(p + 1), c = __ldg(p + 2), d = __ldg(p + 3);
-    w[0] = a.x; w[1] = a.y; w[2] = a.z; w[3] = a.w;
-    w[4] = b.x; w[5] = b.y; w[6] = b.z; w[7] = b.w;
-    w[8] = c.x; w[9] = c.y; w[10] = c.z; w[11] = c.w;
-    w[12] = d.x; w[13] = d.y; w[14] = d.z;
-    unpack_nearest(__float_as_uint(d.w), nx, ny, nz);
 }
 
 // ---------------------------------------------------------------------------
@@ -175,11 +152,11 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
 
     // shared: accumulators [cc][TILE_PTS] float2, then staged records and values
     float2* acc = reinterpret_cast<float2*>(s_dyn);
-    TapRecord* s_rec = reinterpret_cast<TapRecord*>(acc + (size_t)a.cc * TILE_PTS);
+    TapRecord* s_rec = reinterpret_cast<TapRecord*>(acc + (size_t)a.cc * ACC_PTS);
     float2* s_val = reinterpret_cast<float2*>(s_rec + SPREAD_BATCH);
 
     const int tid = threadIdx.x;
-    for (int e = tid; e < ncc * TILE_PTS; e += SPREAD_THREADS) acc[e] = make_float2(0.f, 0.f);
+    for (int e = tid; e < ncc * ACC_PTS; e += SPREAD_THREADS) acc[e] = make_float2(0.f, 0.f);
 
     const long long tp = a.tile_ptr_off[bin];
     const int beg = a.tile_ptr[tp + tile], end = a.tile_ptr[tp + tile + 1];
@@ -212,13 +189,13 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
             if (gy < y0 || gy >= y0 + TILE_Y || gz < z0 || gz >= z0 + TILE_Z) continue;
             const float wt = (w[jx] * w[5 + jy]) * w[10 + jz];
             if (w[jx] == 0.f || w[5 + jy] == 0.f || w[10 + jz] == 0.f || !(wt > a.thresh)) continue;
-            const int local = (warp * TILE_Y + (gy - y0)) * TILE_Z + (gz - z0);
+            const int local = (warp * TILE_Y + (gy - y0)) * TILE_ZP + (gz - z0);
             const float2* v = s_val + j * ncc;
             for (int c = 0; c < ncc; ++c) {
-                float2 t = acc[c * TILE_PTS + local];
+                float2 t = acc[c * ACC_PTS + local];
                 t.x = fmaf(v[c].x, wt, t.x);
                 t.y = fmaf(v[c].y, wt, t.y);
-                acc[c * TILE_PTS + local] = t;
+                acc[c * ACC_PTS + local] = t;
             }
         }
     }
@@ -231,7 +208,8 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
         const int lz = local % TILE_Z, ly = (local / TILE_Z) % TILE_Y, lx = local / (TILE_Z * TILE_Y);
         const int X = x0 + lx, Y = y0 + ly, Z = z0 + lz;
         if (X < Gx && Y < Gy && Z < Gz)
-            grid[(long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z] = acc[e];
+            grid[(long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z] =
+                acc[c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + lz];
     }
 }
 

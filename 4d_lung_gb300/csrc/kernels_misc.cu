@@ -101,7 +101,7 @@ cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nb
 
 size_t spread_smem_bytes(int cc)
 {
-    return (size_t)cc * TILE_PTS * sizeof(float2) + SPREAD_BATCH * sizeof(TapRecord) +
+    return (size_t)cc * ACC_PTS * sizeof(float2) + SPREAD_BATCH * sizeof(TapRecord) +
            (size_t)SPREAD_BATCH * cc * sizeof(float2);
 }
 
@@ -109,8 +109,10 @@ int spread_max_coils() { return 24; }
 
 cudaError_t kernels_init()
 {
-    return cudaFuncSetAttribute(k_spread, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)spread_smem_bytes(spread_max_coils()));
+    cudaError_t e = cudaFuncSetAttribute(k_spread, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)spread_smem_bytes(spread_max_coils()));
+    if (e == cudaSuccess) e = fft_init_all();
+    return e;
 }
 
 cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, cudaStream_t s)

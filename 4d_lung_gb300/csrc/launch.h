@@ -2,12 +2,15 @@
 #pragma once
 #include <cuda_runtime.h>
 #include "cgs_types.h"
+#include <cufft.h>
 
 namespace cgs {
 
 // Supported line lengths of the 3-D FFT (each a product R1*R2 of two
 // register codelets).  Grid sizes must be taken from this list.
 bool fft_supported(int L);
+// per-device kernel attributes of the FFT passes (dynamic shared memory)
+cudaError_t fft_init_all();
 const int* fft_supported_list(int* n);
 
 // One launch per pass; `batch` items along blockIdx.y.
@@ -52,5 +55,30 @@ cudaError_t launch_cg_beta(CgState* st, const double* partials, int nblk, int nb
 cudaError_t launch_cg_update_p(float2* p, const float2* r, long long n, long long bs, const CgState* st, int nbins,
                                cudaStream_t s);
 cudaError_t launch_cg_loop_test(CgState* st, int nbins, cudaStream_t s);
+
+// Plain per-bin form (plain.cu): unfused kernels + cuFFT, comparison only.
+struct PlainGeom {
+    int I[3], G[3], lo[3];
+    long long Ni, Ng;
+};
+
+struct PlainArgs {
+    PlainGeom g;
+    int nch;
+    const float2* smaps;
+    const float* ap[3];
+    float scale;
+    float thresh;
+    cufftHandle plan;
+    cudaStream_t s;
+    float2* grid;   // [Ng]
+    float2* y;      // [max bin samples]
+};
+
+cudaError_t plain_apply(const PlainArgs& P, const TapRecord* rec, const float* dcf, long long n, const float2* x,
+                        float2* q, long long* launches);
+cudaError_t plain_rhs(const PlainArgs& P, const TapRecord* rec, const float* dcf, const int* sorted, long long n,
+                      const float2* data, long long ns, float2* b, long long* launches);
+cudaError_t plain_dot(const float2* p, const float2* q, long long n, double* partials, int nblocks, cudaStream_t s);
 
 }  // namespace cgs

@@ -319,6 +319,27 @@ def run_ours(args):
     res, its = reco.cg_sense_batched_tensor(data, x, 0.0, iters, want_stats=True)
     assert np.all(its == iters) and np.all(np.isfinite(res))
 
+    # the plain per-bin GPU form (frozen comparison point): same solve
+    plain = None
+    if not args.no_plain:
+        xp = torch.zeros_like(x)
+        reco.cg_sense_plain_tensor(data, xp, 0.0, 1)          # warm-up (cuFFT plan, first touch)
+        torch.cuda.synchronize(dev)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        pres, pits = reco.cg_sense_plain_tensor(data, xp, 0.0, iters)
+        p1.record(stream)
+        torch.cuda.synchronize(dev)
+        t_plain = p0.elapsed_time(p1) / 1e3
+        err = float(torch.linalg.vector_norm(x - xp) / torch.linalg.vector_norm(xp))
+        plain = {"s_per_4d_recon": t_plain, "applies_per_s": applies_per_step / t_plain,
+                 "speedup_chosen_vs_plain": t_plain / (ms_step / 1e3),
+                 "rel_l2_chosen_vs_plain": err, "iters": [int(v) for v in pits],
+                 "launches": reco.launch_count(),
+                 "form": "per-bin, per-coil launches, unfused, cuFFT full-grid c2c, global-atomic spreading, "
+                         "host loop test per iteration"}
+
     # end to end through the host-buffer C ABI call (pinned host memory)
     h_data = torch.empty(data.shape, dtype=torch.complex64, pin_memory=True)
     h_data.copy_(data.cpu())
@@ -393,6 +414,7 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "s_per_4d_recon": float(te.item()) / args.steps},
         "roofline": roofline,
+        "plain": plain,
     }
     if rank == 0 and not args.no_cpu:
         cb = cpu_apply_sample(synth, args.workload)
@@ -414,6 +436,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="cfg3")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain per-bin GPU form")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

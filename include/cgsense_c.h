@@ -47,6 +47,7 @@ extern "C" {
 #define CGS_ERR_NOMEM 5        /* device allocation failed */
 #define CGS_ERR_UNSUPPORTED 6  /* grid size without an FFT kernel */
 #define CGS_ERR_NO_THRESHOLD 7 /* cg threshold == -1 (Reco.cpp:192-196) */
+#define CGS_ERR_TIMEOUT 8      /* a kernel's bounded wait for its asynchronous copies ran out */
 
 typedef struct cgs_ctx cgs_ctx;
 
@@ -185,6 +186,14 @@ int cgs_cg_solve_batched_d(cgs_ctx* ctx, const float* data_dev, float* x_dev, do
  * present, so that transfers run at full speed. */
 void* cgs_alloc_host(size_t bytes);
 void cgs_free_host(void* p);
+
+/* The plain per-bin GPU form of cgs_cg_solve_batched_d, kept as the
+ * comparison point: bins one after another, coils one after another,
+ * unfused kernels, full-grid cuFFT transforms, global-atomic spreading, a
+ * host round trip per iteration (the reference's loop structure,
+ * Reco.cpp:175-321, 468-553).  Same arguments and results. */
+int cgs_cg_solve_plain_d(cgs_ctx* ctx, const float* data_dev, float* x_dev, double threshold, int32_t max_iter,
+                         double* residuals, int32_t* iters);
 
 /* Number of kernel launches issued by the last compute call (for a graph
  * replay: the kernels in the graph). */
