@@ -50,7 +50,7 @@ EXPORTS = [
     "cgs_nufft_adj", "cgs_nufft_adj_d", "cgs_apply_ehde", "cgs_apply_ehde_d", "cgs_cg_solve",
     "cgs_cg_solve_batched", "cgs_cg_solve_batched_d", "cgs_last_launch_count",
     "cgs_profile_apply", "cgs_cg_solve_images", "cgs_alloc_host", "cgs_free_host",
-    "cgs_cg_solve_plain_d",
+    "cgs_fft3_noalloc", "cgs_cg_solve_plain_d",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -147,6 +147,7 @@ def lib():
         "cgs_cg_solve_images": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
         "cgs_alloc_host": (vp, [C.c_size_t]),
         "cgs_free_host": (None, [vp]),
+        "cgs_fft3_noalloc": (C.c_int, [vp, vp, vp, i32, vp]),
         "cgs_cg_solve_plain_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
     }
     for name, (res, args) in sig.items():

@@ -208,6 +208,22 @@ int64_t cgs_last_launch_count(const cgs_ctx* ctx);
 int cgs_profile_apply(cgs_ctx* ctx, int32_t bin0, int32_t nb, const float* x_dev, float* q_dev,
                       float* stage_ms, int32_t max_stages, int32_t* n_stages);
 
+/* Centred 3-D FFT (sign -1 forward, +1 backward, unscaled) that allocates no
+ * device memory, for callers that cannot let a library allocate: code
+ * running under a host application that owns all device memory through its
+ * own allocator, or a latency-critical loop that must not pay for
+ * cudaMalloc/cudaFree.  No counterpart in the reference.  in and out are
+ * device arrays of grid[0]*grid[1]*grid[2] complex values (they may be the
+ * same array); no context is needed.  The intermediate grid lives in a fixed
+ * file-scope device array of 2^19 complex values (4 MiB, held by every GPU
+ * that loads the library); larger grids are rejected with CGS_ERR_ARG, sizes
+ * without an FFT kernel with CGS_ERR_UNSUPPORTED (messages go to stderr).
+ * The first call on a device looks up that array's device address, so make
+ * that first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised.  stream is a
+ * cudaStream_t (NULL: the default stream); the call is asynchronous. */
+int cgs_fft3_noalloc(const float* in_dev, float* out_dev, const int32_t* grid, int32_t sign, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
