@@ -50,7 +50,7 @@ EXPORTS = [
     "cgs_nufft_adj", "cgs_nufft_adj_d", "cgs_apply_ehde", "cgs_apply_ehde_d", "cgs_cg_solve",
     "cgs_cg_solve_batched", "cgs_cg_solve_batched_d", "cgs_last_launch_count",
     "cgs_profile_apply", "cgs_cg_solve_images", "cgs_alloc_host", "cgs_free_host",
-    "cgs_fft3_noalloc", "cgs_cg_solve_plain_d",
+    "cgs_fft3_noalloc", "cgs_cg_solve_plain_d", "cgs_voronoi_dcf",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -149,6 +149,7 @@ def lib():
         "cgs_free_host": (None, [vp]),
         "cgs_fft3_noalloc": (C.c_int, [vp, vp, vp, i32, vp]),
         "cgs_cg_solve_plain_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
+        "cgs_voronoi_dcf": (C.c_int, [vp, i64, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -184,6 +185,17 @@ def wave_caipi(sx, sy, sz, grid, fov_y, fov_z, n_osc=4, grad_amp=0.006, amp_corr
     st = lib().cgs_wave_caipi(C.byref(w), _p(out))
     if st != CGS_OK:
         raise CGSError(st, "invalid wave-CAIPI parameters")
+    return out
+
+
+def voronoi_dcf(k):
+    """estimateDensityV3D (functions.h:161-258): normalised Voronoi volumes,
+    0 on the convex hull."""
+    k = np.ascontiguousarray(k, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros(k.shape[0], np.float32)
+    st = lib().cgs_voronoi_dcf(_p(k), k.shape[0], _p(out))
+    if st != CGS_OK:
+        raise CGSError(st, "cgs_voronoi_dcf failed")
     return out
 
 

@@ -31,6 +31,7 @@ def _units():
         units.append((src, src.replace(".cu", ".o"), []))
     units.append(("wave_caipi.cpp", "wave_caipi.o", []))
     units.append(("reco_shim.cpp", "reco_shim.o", []))
+    units.append(("voronoi.cpp", "voronoi.o", ["-fopenmp"]))
     return units
 
 
@@ -55,7 +56,7 @@ def build(verbose=False, jobs=None):
         if _stale(o, [s, __file__] + headers):
             if src.endswith(".cpp"):
                 cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-I", os.path.join(ROOT, "include"),
-                       "-I", "/usr/local/cuda/include", "-c", s, "-o", o]
+                       "-I", "/usr/local/cuda/include"] + extra + ["-c", s, "-o", o]
             else:
                 cmd = [NVCC] + ARCH + FLAGS + extra + ["-c", s, "-o", o]
             cmds.append(cmd)
@@ -74,7 +75,7 @@ def build(verbose=False, jobs=None):
                     raise RuntimeError("compilation failed: %s" % cmd[-3])
     if _stale(LIB, objs):
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + [
-            "-cudart", "static", "-lcufft", "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+            "-cudart", "static", "-lcufft", "-lgomp", "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout)

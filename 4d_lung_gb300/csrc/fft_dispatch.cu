@@ -28,6 +28,53 @@ cudaError_t fft_init_all()
     return e;
 }
 
+// cuTensorMapEncodeTiled from the driver (no link-time dependency on libcuda)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int batch, int TB, int* box_rows)
+{
+    // TMA rows start on 16-byte boundaries: base pointer, row pitch and
+    // strides must be multiples of 16 bytes (even element counts)
+    if ((reinterpret_cast<uintptr_t>(a.in) & 15) || (a.B & 1) || a.Lin < 1) return false;
+    const long long as = A > 1 ? a.in_as : (long long)a.Lin * a.B;
+    const long long bs = batch > 1 ? a.in_bs : (long long)A * as;
+    if ((as & 1) || (bs & 1)) return false;
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    int br = a.Lin;
+    if (br > 256)
+        for (br = 256; br > 1 && a.Lin % br != 0; --br) {
+        }
+    const cuuint64_t dims[4] = {(cuuint64_t)a.B, (cuuint64_t)a.Lin, (cuuint64_t)A, (cuuint64_t)batch};
+    const cuuint64_t strides[3] = {(cuuint64_t)a.B * 8, (cuuint64_t)as * 8, (cuuint64_t)bs * 8};
+    const cuuint32_t box[4] = {(cuuint32_t)TB, (cuuint32_t)br, 1, 1};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<float2*>(a.in), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    *box_rows = br;
+    return true;
+}
+
 bool fft_supported(int L)
 {
     for (int s : kSizes)

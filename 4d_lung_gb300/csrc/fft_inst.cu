@@ -22,11 +22,6 @@ static int sm_count()
     return n;
 }
 
-// The bulk-copy pipelined pass measured slower than the plain pass on GB300
-// (one 128-byte copy per row saturates the copy engine's request rate); it
-// stays off until the tensor-map version replaces it.
-constexpr bool kUsePipe = false;
-
 constexpr int rmax2(int a, int b) { return a > b ? a : b; }
 constexpr int strided_tb(int r1, int r2) { return rmax2(r1, r2) > 16 ? 8 : 16; }
 constexpr int contig_lpb(int r1, int r2) { return rmax2(r1, r2) > 16 ? 8 : (rmax2(r1, r2) > 8 ? 16 : 32); }
@@ -40,16 +35,16 @@ struct SizeImpl {
     static constexpr int NT_C = LPB * rmax2(R1, R2);
     static_assert(NT_C % 32 == 0, "contiguous pass block must be whole warps");
 
-    static constexpr int NSTAGE = 3;
+    static constexpr int NSTAGE = 2;
     using Pipe = PipeLayout<R1, R2, TB, NSTAGE>;
 
     static cudaError_t init()
     {
         const int smem = (int)Pipe::smem_bytes(L);
-        cudaError_t e = cudaFuncSetAttribute(k_fft_strided_pipe<R1, R2, -1, TB, NSTAGE>,
+        cudaError_t e = cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, -1, TB, NSTAGE>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_fft_strided_pipe<R1, R2, +1, TB, NSTAGE>,
+            e = cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, +1, TB, NSTAGE>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         return e;
     }
@@ -57,14 +52,13 @@ struct SizeImpl {
     static cudaError_t strided(int sign, StridedPassArgs a, int A, int batch, cudaStream_t s)
     {
         a.ntb = (a.B + TB - 1) / TB;
-        // bulk copies need 16-byte aligned rows: base pointer, B, strides even
-        const bool aligned = ((reinterpret_cast<uintptr_t>(a.in) & 15) == 0) && (a.B % 2 == 0) &&
-                             (a.in_as % 2 == 0) && (a.in_bs % 2 == 0) && a.Lin > 0;
-        if (kUsePipe && a.err && aligned) {
+        CUtensorMap map;
+        int box_rows = 0;
+        if (a.err && encode_strided_map(&map, a, A, batch, TB, &box_rows)) {
             const size_t smem = Pipe::smem_bytes(a.Lin);
             int per_sm = 0;
             cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per_sm, sign < 0 ? k_fft_strided_pipe<R1, R2, -1, TB, NSTAGE> : k_fft_strided_pipe<R1, R2, +1, TB, NSTAGE>,
+                &per_sm, sign < 0 ? k_fft_strided_tma<R1, R2, -1, TB, NSTAGE> : k_fft_strided_tma<R1, R2, +1, TB, NSTAGE>,
                 Pipe::NT, smem);
             if (e != cudaSuccess) return e;
             const long long tiles_per_item = (long long)A * a.ntb;
@@ -72,9 +66,11 @@ struct SizeImpl {
             long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
             if (nblk > ntiles) nblk = ntiles;
             if (sign < 0)
-                k_fft_strided_pipe<R1, R2, -1, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, ntiles, (int)tiles_per_item);
+                k_fft_strided_tma<R1, R2, -1, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, map, ntiles,
+                                                                                             (int)tiles_per_item, box_rows);
             else
-                k_fft_strided_pipe<R1, R2, +1, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, ntiles, (int)tiles_per_item);
+                k_fft_strided_tma<R1, R2, +1, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, map, ntiles,
+                                                                                             (int)tiles_per_item, box_rows);
             return cudaGetLastError();
         }
         dim3 grid((unsigned)(A * a.ntb), (unsigned)batch);

@@ -24,6 +24,7 @@
 #include "fft_codelets.cuh"
 #include "cgs_types.h"
 #include "ptx_async.cuh"
+#include <cuda.h>
 
 namespace cgs {
 
@@ -102,13 +103,15 @@ k_fft_strided(StridedPassArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// Pipelined strided pass.  Persistent blocks walk the tiles (batch item,
-// outer index, TB-column strip) round-robin.  The Lin stored rows of a tile
-// are fetched by the asynchronous copy engine (one 16-byte-aligned bulk copy
-// per row, completion counted on an mbarrier), NSTAGE tiles ahead, so that
-// the HBM requests of later tiles overlap the FFT of the current one.  The
-// two register stages are those of k_fft_strided.  Every wait is bounded
-// (2 s); on a timeout the block sets *err, lets its copies land and exits.
+// TMA-pipelined strided pass.  Persistent blocks walk the tiles (batch item,
+// outer index, TB-column strip) round-robin.  A tile's Lin stored rows are
+// one 4-D tensor-map box (or a few, each at most 256 rows) fetched by the TMA
+// unit into shared memory, NSTAGE tiles ahead of the FFT, completion counted
+// on an mbarrier.  The two register stages are those of k_fft_strided.
+// Every wait is bounded (2 s); on a timeout the block sets *err, lets its
+// issued copies land and exits.
+// The tensor map views the input as [items][A][Lin][B] (B innermost) with a
+// box of TB x box_rows x 1 x 1 elements of 8 bytes.
 // ---------------------------------------------------------------------------
 constexpr unsigned long long PIPE_WAIT_NS = 2000000000ull;
 
@@ -116,25 +119,28 @@ template <int R1, int R2, int TB, int NSTAGE>
 struct PipeLayout {
     static constexpr int L = R1 * R2;
     static constexpr int NT = TB * (R1 > R2 ? R1 : R2);
+    // 1 KiB slack to align the TMA destination to 1 KiB
     static size_t smem_bytes(int Lin)
     {
-        return ((size_t)NSTAGE * Lin * TB + (size_t)L * TB + L) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
+        return 1024 + ((size_t)NSTAGE * Lin * TB + (size_t)L * TB + L) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
     }
 };
 
 template <int R1, int R2, int SIGN, int TB, int NSTAGE>
 __global__ void __launch_bounds__(PipeLayout<R1, R2, TB, NSTAGE>::NT)
-k_fft_strided_pipe(StridedPassArgs a, long long ntiles, int tiles_per_item)
+k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, long long ntiles,
+                  int tiles_per_item, int box_rows)
 {
     constexpr int L = R1 * R2;
     constexpr int NT = PipeLayout<R1, R2, TB, NSTAGE>::NT;
     extern __shared__ float4 s_pipe[];
+    const uintptr_t base = (reinterpret_cast<uintptr_t>(s_pipe) + 1023) & ~(uintptr_t)1023;
     const int stage_elems = a.Lin * TB;
-    float2* s_in = reinterpret_cast<float2*>(s_pipe);
+    float2* s_in = reinterpret_cast<float2*>(base);
     float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
     float2* s_tw = s_y + L * TB;
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
     for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) mbar_init(&s_bar[s], 1);
@@ -143,34 +149,30 @@ k_fft_strided_pipe(StridedPassArgs a, long long ntiles, int tiles_per_item)
     __syncthreads();
     const long long my_n = ntiles > (long long)blockIdx.x ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
 
-    auto issue = [&](long long k) {
+    auto issue = [&](long long k) {   // thread 0 only
         const long long t = blockIdx.x + k * gridDim.x;
-        const long long item = t / tiles_per_item;
-        const int rem = (int)(t - item * tiles_per_item);
+        const int item = (int)(t / tiles_per_item);
+        const int rem = (int)(t - (long long)item * tiles_per_item);
         const int ai = rem / a.ntb;
         const int b0 = (rem - ai * a.ntb) * TB;
-        const int ncols = min(TB, a.B - b0);
-        const float2* src = a.in + item * a.in_bs + (long long)ai * a.in_as + b0;
         const int s = (int)(k % NSTAGE);
-        const uint32_t row_bytes = (uint32_t)ncols * (uint32_t)sizeof(float2);
-        if (lane == 0) mbar_arrive_expect_tx(&s_bar[s], row_bytes * (uint32_t)a.Lin);
-        __syncwarp();
+        mbar_arrive_expect_tx(&s_bar[s], (uint32_t)(stage_elems * sizeof(float2)));
         float2* dst = s_in + (size_t)s * stage_elems;
-        for (int li = lane; li < a.Lin; li += 32)
-            bulk_copy_g2s(dst + (size_t)li * TB, src + (long long)li * a.B, row_bytes, &s_bar[s]);
+        for (int r0 = 0; r0 < a.Lin; r0 += box_rows)
+            tma_load_4d(dst + (size_t)r0 * TB, &tmap, b0, r0, ai, item, &s_bar[s]);
     };
 
-    if (warp == 0)
+    if (tid == 0)
         for (long long k = 0; k < NSTAGE - 1 && k < my_n; ++k) issue(k);
     for (long long k = 0; k < my_n; ++k) {
         const int s = (int)(k % NSTAGE);
-        if (warp == 0 && k + NSTAGE - 1 < my_n) issue(k + NSTAGE - 1);
+        if (tid == 0 && k + NSTAGE - 1 < my_n) issue(k + NSTAGE - 1);
         const bool ok = mbar_wait_bounded(&s_bar[s], (uint32_t)((k / NSTAGE) & 1), PIPE_WAIT_NS);
         if (__syncthreads_or(!ok)) {
             // timeout: report, let the copies already issued land, leave
             if (tid == 0) {
                 atomicExch(a.err, 1);
-                for (long long j = k; j < my_n && j < k + NSTAGE - 1 + 1; ++j)
+                for (long long j = k; j < my_n && j < k + NSTAGE; ++j)
                     mbar_wait_bounded(&s_bar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1), PIPE_WAIT_NS);
             }
             return;
@@ -193,7 +195,7 @@ k_fft_strided_pipe(StridedPassArgs a, long long ntiles, int tiles_per_item)
                     const int l = R2 * n1 + n2;
                     const int li = l - a.in_off;
                     float2 x = make_float2(0.f, 0.f);
-                    if (bok && li >= 0 && li < a.Lin) x = parity(sin_s[li * TB + bi], l);
+                    if (li >= 0 && li < a.Lin) x = parity(sin_s[li * TB + bi], l);
                     v[n1] = x;
                 }
                 Dft<R1, SIGN>::run(v);

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include "cgs_types.h"
 #include <cufft.h>
+#include <cuda.h>
 
 namespace cgs {
 
@@ -11,6 +12,9 @@ namespace cgs {
 bool fft_supported(int L);
 // per-device kernel attributes of the FFT passes (dynamic shared memory)
 cudaError_t fft_init_all();
+// 4-D tensor map [batch][A][Lin][B] of a strided pass's input with a
+// TB x box_rows box; false when the buffer or strides are not 16-byte aligned
+bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int batch, int TB, int* box_rows);
 const int* fft_supported_list(int* n);
 
 // One launch per pass; `batch` items along blockIdx.y.

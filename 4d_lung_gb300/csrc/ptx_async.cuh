@@ -54,13 +54,14 @@ CGS_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
     return true;
 }
 
-// bytes (multiple of 16) from global to shared; both addresses 16-byte aligned
-CGS_D void bulk_copy_g2s(void* dst_smem, const void* src_gmem, uint32_t bytes, uint64_t* bar)
+// 4-D tensor-map tile load (TMA) into shared memory, completion on `bar`.
+// Coordinates are element indices, innermost first.
+CGS_D void tma_load_4d(void* dst_smem, const void* tmap, int c0, int c1, int c2, int c3, uint64_t* bar)
 {
     asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(
             smem_addr(dst_smem)),
-        "l"(src_gmem), "r"(bytes), "r"(smem_addr(bar))
+        "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
         : "memory");
 }
 

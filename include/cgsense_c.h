@@ -119,6 +119,12 @@ int cgs_mask_from_data(cgs_ctx* ctx, const float* data);
 int cgs_set_bins(cgs_ctx* ctx, int32_t nbins, const int64_t* offsets, const int32_t* sample_idx);
 int cgs_num_bins(const cgs_ctx* ctx);
 
+/* estimateDensityV3D (functions.h:161-258, Density::VORONOI3D): the Voronoi
+ * cell volume of every sample of k[n][3], 0 for samples on the convex hull,
+ * divided by the largest volume.  Host computation (OpenMP); usable per bin
+ * by passing that bin's coordinates. */
+int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf);
+
 /* Reco::denCorr with Density::IMPORT (IO.cpp:129-156, functions.h:319-335):
  * per-sample real weights D[ns].  NULL clears (Density::NONE). */
 int cgs_set_dcf(cgs_ctx* ctx, const float* dcf);

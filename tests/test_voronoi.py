@@ -1,0 +1,54 @@
+"""Voronoi density weights (estimateDensityV3D, functions.h:161-258): cell
+volumes, 0 on the convex hull, normalised by the maximum.  CGAL (the
+reference's dependency) is not available; the weights are checked against
+scipy's qhull Voronoi diagram and against a lattice of known cell volume."""
+import numpy as np
+import pytest
+
+
+def scipy_volumes(pts):
+    sp = pytest.importorskip("scipy.spatial")
+    vor = sp.Voronoi(pts)
+    vols = np.zeros(len(pts))
+    for i, ri in enumerate(vor.point_region):
+        reg = vor.regions[ri]
+        if -1 in reg or len(reg) == 0:
+            continue
+        vols[i] = sp.ConvexHull(vor.vertices[reg]).volume
+    return vols / vols.max()
+
+
+@pytest.mark.parametrize("n,seed", [(400, 1), (2500, 2)])
+def test_voronoi_matches_qhull(cgs, n, seed):
+    pts = np.random.default_rng(seed).uniform(0, 1, (n, 3))
+    d = cgs.voronoi_dcf(pts)
+    ref = scipy_volumes(pts)
+    assert np.array_equal(d == 0, ref == 0)          # same hull samples
+    assert np.abs(d - ref).max() < 1e-6
+
+
+def test_voronoi_lattice_known_answer(cgs):
+    """Interior cells of a jittered-free cubic lattice are unit cubes; the
+    largest volume belongs to such a cell, so interior weights are 1 and the
+    hull samples (the lattice faces) are 0."""
+    g = np.arange(6, dtype=np.float64)
+    pts = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    pts += np.random.default_rng(0).uniform(-1e-9, 1e-9, pts.shape)   # break exact ties
+    d = cgs.voronoi_dcf(pts)
+    on_face = np.any((pts < 0.5) | (pts > 4.5), axis=1)
+    assert np.all(d[on_face] == 0)
+    assert np.allclose(d[~on_face], 1.0, atol=1e-6)
+
+
+def test_voronoi_readout_trajectory(cgs, synth):
+    """A wave-CAIPI bin: weights in [0, 1], hull zeros at the readout ends."""
+    w = synth.scaled(synth.WORKLOADS["cfg3"], (32, 32, 24), (64, 64, 48), n_ch=2, n_bins=4)
+    lines = synth.readout_lines(w)
+    k = synth.wave_trajectory(w, synth.WaveParams(2.0, 2.0), lines=lines)
+    kb = k.reshape(len(lines), w.n_read, 3)[::3].reshape(-1, 3)
+    d = cgs.voronoi_dcf(kb)
+    assert d.min() >= 0 and d.max() == pytest.approx(1.0)
+    ends = kb.reshape(-1, w.n_read, 3)[:, [0, -1]].reshape(-1, 3)
+    dd = d.reshape(-1, w.n_read)[:, [0, -1]]
+    assert np.all(dd == 0)
+    assert (d > 0).mean() > 0.5
