@@ -50,7 +50,8 @@ EXPORTS = [
     "cgs_nufft_adj", "cgs_nufft_adj_d", "cgs_apply_ehde", "cgs_apply_ehde_d", "cgs_cg_solve",
     "cgs_cg_solve_batched", "cgs_cg_solve_batched_d", "cgs_last_launch_count",
     "cgs_profile_apply", "cgs_cg_solve_images", "cgs_alloc_host", "cgs_free_host",
-    "cgs_fft3_noalloc", "cgs_cg_solve_plain_d", "cgs_voronoi_dcf",
+    "cgs_fft3_noalloc", "cgs_cg_solve_plain_d", "cgs_voronoi_dcf", "cgs_cg_solve_trace_d",
+    "cgs_cg_solve_fp64_d",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -150,6 +151,8 @@ def lib():
         "cgs_fft3_noalloc": (C.c_int, [vp, vp, vp, i32, vp]),
         "cgs_cg_solve_plain_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
         "cgs_voronoi_dcf": (C.c_int, [vp, i64, vp]),
+        "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
+        "cgs_cg_solve_fp64_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -378,6 +381,27 @@ class Reco:
         it = np.zeros(nb, np.int32)
         self._check(self._L.cgs_cg_solve_plain_d(self._ctx, C.c_void_p(data.data_ptr()), C.c_void_p(x.data_ptr()),
                                                  threshold, max_iter, _p(res), _p(it)))
+        return res, it
+
+    def cg_sense_trace_tensor(self, data, x, threshold, max_iter, x_trace):
+        """Batched solve that also stores x after every iteration (x_trace:
+        complex64 [max_iter][nbins][voxels] device tensor)."""
+        nb = self.num_bins()
+        res = np.zeros((nb, max(max_iter, 1)), np.float64)
+        it = np.zeros(nb, np.int32)
+        self._check(self._L.cgs_cg_solve_trace_d(self._ctx, C.c_void_p(data.data_ptr()), C.c_void_p(x.data_ptr()),
+                                                 threshold, max_iter, _p(res), _p(it),
+                                                 C.c_void_p(x_trace.data_ptr())))
+        return res, it
+
+    def cg_sense_fp64_tensor(self, data, x64, threshold, max_iter, x_trace=None):
+        """Full-FP64 solve (x64: complex128 device tensor [nbins][voxels])."""
+        nb = self.num_bins()
+        res = np.zeros((nb, max(max_iter, 1)), np.float64)
+        it = np.zeros(nb, np.int32)
+        self._check(self._L.cgs_cg_solve_fp64_d(self._ctx, C.c_void_p(data.data_ptr()), C.c_void_p(x64.data_ptr()),
+                                                threshold, max_iter, _p(res), _p(it),
+                                                None if x_trace is None else C.c_void_p(x_trace.data_ptr())))
         return res, it
 
     def cg_sense_batched_tensor(self, data, x, threshold, max_iter, want_stats=True):

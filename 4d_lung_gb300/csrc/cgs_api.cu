@@ -56,10 +56,11 @@ struct GraphKey {
     double thresh;
     int max_iter;
     int rhs_from_images;
+    void* trace;
     bool operator<(const GraphKey& o) const
     {
-        return std::tie(data, x, thresh, max_iter, rhs_from_images) <
-               std::tie(o.data, o.x, o.thresh, o.max_iter, o.rhs_from_images);
+        return std::tie(data, x, thresh, max_iter, rhs_from_images, trace) <
+               std::tie(o.data, o.x, o.thresh, o.max_iter, o.rhs_from_images, o.trace);
     }
 };
 
@@ -109,6 +110,10 @@ struct cgs_ctx {
     cufftHandle plain_plan = 0;
     bool plain_plan_ok = false;
     DevBuf d_plain_grid, d_plain_y, d_plain_dot;
+    // full-FP64 form (cgs_cg_solve_fp64_d)
+    cufftHandle z_plan = 0;
+    bool z_plan_ok = false;
+    DevBuf d64_grid, d64_y, d64_r, d64_p, d64_q, d64_part;
     // per-stage timing (cgs_profile_apply): events recorded after each pass
     cudaEvent_t* prof_ev = nullptr;
     int prof_n = 0;
@@ -190,6 +195,8 @@ struct BinPrep {
     std::vector<int> tile_ptr;
     std::vector<int> tile_idx;
 };
+
+
 
 void nearest_point(const double* kk, const int* G, int* nr)
 {
@@ -414,41 +421,43 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
     const int Ix = c->I[0], Iy = c->I[1], Iz = c->I[2];
     const int Gx = c->G[0], Gy = c->G[1], Gz = c->G[2];
     const long long zb = c->Nl * Gz, yb = (long long)Ix * Gy * Gz;
-    SpreadArgs sa{};
-    sa.grid = c->d_grid.as<float2>();
-    sa.coil_stride = c->Ng;
-    sa.grid_bs = (long long)c->nch * c->Ng;
-    sa.rec = c->d_rec.as<TapRecord>();
-    sa.yv = c->d_yv.as<float2>();
-    sa.bin_off = c->d_bin_off.as<long long>();
-    sa.tile_ptr = c->d_tile_ptr.as<int>();
-    sa.tile_ptr_off = c->d_tile_ptr_off.as<long long>();
-    sa.tile_idx_off = c->d_tile_idx_off.as<long long>();
-    sa.tile_idx = c->d_tile_idx.as<int>();
-    sa.bin0 = b0;
-    sa.nch = c->nch;
-    const int nchunk = (c->nch + spread_max_coils() - 1) / spread_max_coils();
-    sa.cc = (c->nch + nchunk - 1) / nchunk;
-    for (int a = 0; a < 3; ++a) sa.G[a] = c->G[a];
-    sa.ntx = c->ntx;
-    sa.nty = c->nty;
-    sa.ntz = c->ntz;
-    sa.thresh = c->thresh;
-    CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->stream));
+    {
+        SpreadArgs sa{};
+        sa.grid = c->d_grid.as<float2>();
+        sa.coil_stride = c->Ng;
+        sa.grid_bs = (long long)c->nch * c->Ng;
+        sa.rec = c->d_rec.as<TapRecord>();
+        sa.yv = c->d_yv.as<float2>();
+        sa.bin_off = c->d_bin_off.as<long long>();
+        sa.tile_ptr = c->d_tile_ptr.as<int>();
+        sa.tile_ptr_off = c->d_tile_ptr_off.as<long long>();
+        sa.tile_idx_off = c->d_tile_idx_off.as<long long>();
+        sa.tile_idx = c->d_tile_idx.as<int>();
+        sa.bin0 = b0;
+        sa.nch = c->nch;
+        const int nchunk = (c->nch + spread_max_coils() - 1) / spread_max_coils();
+        sa.cc = (c->nch + nchunk - 1) / nchunk;
+        for (int a = 0; a < 3; ++a) sa.G[a] = c->G[a];
+        sa.ntx = c->ntx;
+        sa.nty = c->nty;
+        sa.ntz = c->ntz;
+        sa.thresh = c->thresh;
+        CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->stream));
 
-    StridedPassArgs ax{};
-    ax.in = c->d_grid.as<float2>();
-    ax.out = c->d_ybuf.as<float2>();
-    ax.in_bs = c->Ng;
-    ax.out_bs = yb;
-    ax.B = Gy * Gz;
-    ax.Lin = Gx;
-    ax.in_off = 0;
-    ax.Lout = Ix;
-    ax.out_off = c->lo[0];
-    ax.err = c->d_err.as<int>();
-    ax.tw = c->tw[0].as<float2>();
-    CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
+        StridedPassArgs ax{};
+        ax.in = c->d_grid.as<float2>();
+        ax.out = c->d_ybuf.as<float2>();
+        ax.in_bs = c->Ng;
+        ax.out_bs = yb;
+        ax.B = Gy * Gz;
+        ax.Lin = Gx;
+        ax.in_off = 0;
+        ax.Lout = Ix;
+        ax.out_off = c->lo[0];
+        ax.err = c->d_err.as<int>();
+        ax.tw = c->tw[0].as<float2>();
+        CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
+    }
 
     StridedPassArgs ay{};
     ay.in = c->d_ybuf.as<float2>();
@@ -666,6 +675,7 @@ void cgs_destroy(cgs_ctx* c)
     cudaStreamSynchronize(c->stream);
     drop_graphs(c);
     if (c->plain_plan_ok) cufftDestroy(c->plain_plan);
+    if (c->z_plan_ok) cufftDestroy(c->z_plan);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -904,7 +914,7 @@ int cgs_apply_ehde(cgs_ctx* c, int32_t bin, const float* x, float* q)
 // The whole batched solve is recorded once into a CUDA graph (per data/x
 // pointers, threshold and iteration cap) and replayed.
 static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh, int max_iter,
-                        bool rhs_from_images)
+                        bool rhs_from_images, float2* x_trace)
 {
     const int nb = c->nbins;
     const long long Ni = c->Ni;
@@ -937,12 +947,15 @@ static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh
                                      c->stream));
         CGS_LAUNCH(c, launch_cg_update_p(c->d_pv.as<float2>(), c->d_r.as<float2>(), Ni, Ni, st, nb, c->stream));
         CGS_LAUNCH(c, launch_cg_loop_test(st, nb, c->stream));
+        if (x_trace)
+            CGS_CUDA(c, cudaMemcpyAsync(x_trace + (long long)it * nb * Ni, x, (size_t)nb * Ni * sizeof(float2),
+                                        cudaMemcpyDeviceToDevice, c->stream));
     }
     return CGS_OK;
 }
 
 static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter, double* residuals,
-                   int32_t* iters, bool rhs_from_images)
+                   int32_t* iters, bool rhs_from_images, float* x_trace = nullptr)
 {
     CGS_TRY(check_ready(c, true));
     if (!data || !x) return fail(c, CGS_ERR_ARG, "null pointer");
@@ -963,14 +976,14 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
     CGS_CUDA(c, c->d_res.ensure((size_t)nb * std::max(max_iter, 1) * sizeof(double)));
 
     if (rhs_from_images && nb != 1) return fail(c, CGS_ERR_STATE, "coil-image right-hand side needs one bin");
-    GraphKey key{data, x, thresh, max_iter, rhs_from_images ? 1 : 0};
+    GraphKey key{data, x, thresh, max_iter, rhs_from_images ? 1 : 0, x_trace};
     auto it = c->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
     if (it == c->graphs.end()) {
         c->launches = 0;
         CGS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         int st = record_solve(c, reinterpret_cast<const float2*>(data), reinterpret_cast<float2*>(x), thresh, max_iter,
-                              rhs_from_images);
+                              rhs_from_images, reinterpret_cast<float2*>(x_trace));
         cudaGraph_t graph = nullptr;
         cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
         if (st != CGS_OK) {
@@ -1014,6 +1027,69 @@ int cgs_cg_solve_batched_d(cgs_ctx* c, const float* data, float* x, double thres
                            double* residuals, int32_t* iters)
 {
     return solve_d(c, data, x, thresh, max_iter, residuals, iters, false);
+}
+
+int cgs_cg_solve_trace_d(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter,
+                         double* residuals, int32_t* iters, float* x_trace)
+{
+    if (!x_trace) return fail(c, CGS_ERR_ARG, "null trace pointer");
+    return solve_d(c, data, x, thresh, max_iter, residuals, iters, false, x_trace);
+}
+
+int cgs_cg_solve_fp64_d(cgs_ctx* c, const float* data, double* x, double thresh, int32_t max_iter,
+                        double* residuals, int32_t* iters, double* x_trace)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!data || !x) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (thresh == -1.0) return fail(c, CGS_ERR_NO_THRESHOLD, "no threshold set for CG SENSE (Reco.cpp:192-196)");
+    if (max_iter < 0 || max_iter > 10000) return fail(c, CGS_ERR_ARG, "max_iter out of range");
+    if (!c->z_plan_ok) {
+        if (cufftPlan3d(&c->z_plan, c->G[0], c->G[1], c->G[2], CUFFT_Z2Z) != CUFFT_SUCCESS)
+            return fail(c, CGS_ERR_CUDA, "cufftPlan3d (Z2Z) failed");
+        c->z_plan_ok = true;
+    }
+    if (cufftSetStream(c->z_plan, c->stream) != CUFFT_SUCCESS) return fail(c, CGS_ERR_CUDA, "cufftSetStream failed");
+    const long long Ni = c->Ni;
+    CGS_CUDA(c, c->d64_grid.ensure(c->Ng * sizeof(double2)));
+    CGS_CUDA(c, c->d64_y.ensure(std::max<long long>(c->max_bin, 1) * sizeof(double2)));
+    CGS_CUDA(c, c->d64_r.ensure(Ni * sizeof(double2)));
+    CGS_CUDA(c, c->d64_p.ensure(Ni * sizeof(double2)));
+    CGS_CUDA(c, c->d64_q.ensure(Ni * sizeof(double2)));
+    CGS_CUDA(c, c->d64_part.ensure(2048 * sizeof(double)));
+    Fp64Args P{};
+    for (int a2 = 0; a2 < 3; ++a2) {
+        P.g.I[a2] = c->I[a2];
+        P.g.G[a2] = c->G[a2];
+        P.g.lo[a2] = c->lo[a2];
+        P.ap[a2] = c->ap[a2].as<float>();
+    }
+    P.g.Ni = Ni;
+    P.g.Ng = c->Ng;
+    P.nch = c->nch;
+    P.smaps = c->d_smaps.as<float2>();
+    P.scale = c->adj_scale_total;
+    P.thresh = c->thresh;
+    P.plan = c->z_plan;
+    P.s = c->stream;
+    P.grid = c->d64_grid.as<double2>();
+    P.y = c->d64_y.as<double2>();
+    for (int b = 0; b < c->nbins; ++b) {
+        const long long off = c->h_bin_off[b], n = c->h_bin_off[b + 1] - off;
+        int it = 0;
+        std::vector<double> res(std::max(max_iter, 1), 0.0);
+        CGS_CUDA(c, fp64_solve_bin(P, c->d_rec.as<TapRecord>() + off, c->has_dcf ? c->d_dcf_sorted.as<float>() + off : nullptr,
+                                   c->d_sorted.as<int>() + off, n, reinterpret_cast<const float2*>(data), c->ns,
+                                   reinterpret_cast<double2*>(x) + (long long)b * Ni, c->d64_r.as<double2>(),
+                                   c->d64_p.as<double2>(), c->d64_q.as<double2>(), c->d64_part.as<double>(), thresh,
+                                   max_iter, res.data(), &it,
+                                   x_trace ? reinterpret_cast<double2*>(x_trace) + (long long)b * Ni : nullptr,
+                                   (long long)c->nbins * Ni));
+        if (iters) iters[b] = it;
+        if (residuals)
+            for (int i = 0; i < max_iter; ++i) residuals[(size_t)b * max_iter + i] = res[i];
+    }
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CGS_OK;
 }
 
 int cgs_cg_solve_images(cgs_ctx* c, const float* coil_imgs, float* x, double thresh, int32_t max_iter,

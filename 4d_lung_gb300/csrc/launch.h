@@ -21,6 +21,7 @@ const int* fft_supported_list(int* n);
 cudaError_t launch_strided(int L, int sign, const StridedPassArgs& a, int A, int batch, cudaStream_t s);
 cudaError_t launch_contig(int L, int sign, const ContigPassArgs& a, int batch, cudaStream_t s);
 cudaError_t launch_fwd_z(int L, const FwdZArgs& a, int batch, cudaStream_t s);
+
 // grid.x of the adjoint z pass (number of partial sums per batch item)
 int adj_z_blocks(int L, long long nl);
 cudaError_t launch_adj_z(int L, const AdjZArgs& a, int batch, cudaStream_t s);
@@ -84,5 +85,23 @@ cudaError_t plain_apply(const PlainArgs& P, const TapRecord* rec, const float* d
 cudaError_t plain_rhs(const PlainArgs& P, const TapRecord* rec, const float* dcf, const int* sorted, long long n,
                       const float2* data, long long ns, float2* b, long long* launches);
 cudaError_t plain_dot(const float2* p, const float2* q, long long n, double* partials, int nblocks, cudaStream_t s);
+
+// Full-FP64 form (fp64.cu): the precision reference on the GPU.
+struct Fp64Args {
+    PlainGeom g;
+    int nch;
+    const float2* smaps;
+    const float* ap[3];
+    double scale;
+    float thresh;
+    cufftHandle plan;
+    cudaStream_t s;
+    double2* grid;
+    double2* y;
+};
+cudaError_t fp64_solve_bin(const Fp64Args& P, const TapRecord* rec, const float* dcf, const int* sorted, long long n,
+                           const float2* data, long long ns, double2* x, double2* r, double2* p, double2* q,
+                           double* partials, double thresh, int max_iter, double* residuals, int* iters,
+                           double2* x_trace, long long trace_stride);
 
 }  // namespace cgs

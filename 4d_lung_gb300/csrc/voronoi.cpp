@@ -70,6 +70,18 @@ struct Cell {
         return m;
     }
 
+    // axis-aligned bounds of the vertices relative to c
+    void bounds(V3 c, V3& lo, V3& hi) const
+    {
+        lo = {1e300, 1e300, 1e300};
+        hi = {-1e300, -1e300, -1e300};
+        for (const auto& v : vtx) {
+            const V3 r = v - c;
+            lo = {std::min(lo.x, r.x), std::min(lo.y, r.y), std::min(lo.z, r.z)};
+            hi = {std::max(hi.x, r.x), std::max(hi.y, r.y), std::max(hi.z, r.z)};
+        }
+    }
+
     bool touches_box() const
     {
         for (char b : fbox)
@@ -226,6 +238,16 @@ extern "C" int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf)
             int c[3];
             cell_of(p, c);
             double r2 = cell.max_dist2(p);
+            V3 blo, bhi;
+            cell.bounds(p, blo, bhi);
+            // the bisector of q can cut the cell only if the cell reaches past
+            // it along n = q - p: max over the cell of (v-p).n > |n|^2 / 2;
+            // the bounding box bounds that maximum in O(1)
+            auto may_cut = [&](const V3& nrm, double l2) {
+                const double sup = std::max(nrm.x * blo.x, nrm.x * bhi.x) + std::max(nrm.y * blo.y, nrm.y * bhi.y) +
+                                   std::max(nrm.z * blo.z, nrm.z * bhi.z);
+                return sup > 0.5 * l2;
+            };
             for (int s = 0; s <= max_shell; ++s) {
                 // shell s: cells at Chebyshev distance s from the home cell,
                 // nearest samples first so that the cell shrinks early
@@ -245,13 +267,19 @@ extern "C" int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf)
                                 if (l2 > 0.0 && l2 < 4.0 * r2) cand.push_back({l2, j});
                             }
                         }
-                std::sort(cand.begin(), cand.end());
+                // the first shells are sorted so that the cell shrinks early;
+                // later shells only meet the O(1) tests below
+                if (s <= 1) std::sort(cand.begin(), cand.end());
                 for (const auto& e : cand) {
-                    if (e.first >= 4.0 * r2) break;   // too far to cut the cell
+                    if (e.first >= 4.0 * r2) continue;   // too far to cut the cell
                     const int64_t j = e.second;
                     const V3 q{k[3 * j], k[3 * j + 1], k[3 * j + 2]};
                     const V3 nrm = q - p;
-                    if (cell.clip(nrm, dot(nrm, (p + q) * 0.5), eps)) r2 = cell.max_dist2(p);
+                    if (!may_cut(nrm, e.first)) continue;
+                    if (cell.clip(nrm, dot(nrm, (p + q) * 0.5), eps)) {
+                        r2 = cell.max_dist2(p);
+                        cell.bounds(p, blo, bhi);
+                    }
                 }
                 // every unvisited sample is at least s*h away; it cannot cut
                 // the cell once that exceeds twice the cell's radius
@@ -293,6 +321,7 @@ extern "C" int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf)
                             break;
                         }
                         r2 = cell.max_dist2(p);
+                        cell.bounds(p, blo, bhi);
                     }
                     if (unbounded) break;
                 }

@@ -201,6 +201,19 @@ void cgs_free_host(void* p);
 int cgs_cg_solve_plain_d(cgs_ctx* ctx, const float* data_dev, float* x_dev, double threshold, int32_t max_iter,
                          double* residuals, int32_t* iters);
 
+/* cgs_cg_solve_batched_d that also stores x after every iteration:
+ * x_trace [max_iter][nbins][image voxels] complex64 (device).  Used to state
+ * the error of every iteration against the FP64 form. */
+int cgs_cg_solve_trace_d(cgs_ctx* ctx, const float* data_dev, float* x_dev, double threshold, int32_t max_iter,
+                         double* residuals, int32_t* iters, float* x_trace_dev);
+
+/* The same solve entirely in FP64 on the GPU (double-complex images, grids,
+ * samples, cuFFT Z2Z, FP64 CG), the precision reference of the complex64
+ * path: x [nbins][image voxels] complex128 (device); x_trace (optional)
+ * [max_iter][nbins][image voxels] complex128. */
+int cgs_cg_solve_fp64_d(cgs_ctx* ctx, const float* data_dev, double* x_dev, double threshold, int32_t max_iter,
+                        double* residuals, int32_t* iters, double* x_trace_dev);
+
 /* Number of kernel launches issued by the last compute call (for a graph
  * replay: the kernels in the graph). */
 int64_t cgs_last_launch_count(const cgs_ctx* ctx);

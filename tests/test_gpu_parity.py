@@ -117,7 +117,9 @@ def oversampled_case(oracle_mod, o64, img, grid, nch, n_lines, n_read, seed=3, k
 
 
 @pytest.mark.parametrize("img,grid", [((16, 16, 16), (32, 32, 32)), ((32, 24, 20), (64, 48, 40)),
-                                      ((20, 16, 12), (32, 32, 24))])
+                                      ((20, 16, 12), (32, 32, 24)),
+                                      # Gx >= 128: spreading fused with the adjoint x pass
+                                      ((64, 16, 16), (128, 32, 32)), ((100, 12, 10), (192, 24, 20))])
 def test_oversampled_nufft_vs_oracle(gpu_lib, cgs, oracle_mod, o64, img, grid):
     """2x oversampled grid with zero-pad / crop (pruned FFT passes)."""
     nch = 3
@@ -132,8 +134,9 @@ def test_oversampled_nufft_vs_oracle(gpu_lib, cgs, oracle_mod, o64, img, grid):
     assert rel_l2(r.nufft_adj(y), o64.nufft_adj(p, taps, kft, y)) < 2e-5
 
 
-def test_apply_ehde_vs_oracle_and_hermitian(gpu_lib, cgs, oracle_mod, o64, synth):
-    img, grid, nch = (16, 16, 12), (32, 32, 24), 4
+@pytest.mark.parametrize("img,grid", [((16, 16, 12), (32, 32, 24)), ((64, 16, 12), (128, 32, 24))])
+def test_apply_ehde_vs_oracle_and_hermitian(gpu_lib, cgs, oracle_mod, o64, synth, img, grid):
+    nch = 4
     k, p, taps, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 50, 64)
     smaps = synth.coil_maps(img, nch)
     dcf = np.random.default_rng(2).uniform(0.5, 1.5, k.shape[0]).astype(np.float32)
@@ -154,9 +157,10 @@ def test_apply_ehde_vs_oracle_and_hermitian(gpu_lib, cgs, oracle_mod, o64, synth
     assert np.array_equal(q, r.apply_ehde(x))
 
 
-def test_batched_bins_match_per_bin_oracle(gpu_lib, cgs, oracle_mod, o64, synth):
+@pytest.mark.parametrize("img,grid", [((16, 16, 12), (32, 32, 24)), ((64, 16, 12), (128, 32, 24))])
+def test_batched_bins_match_per_bin_oracle(gpu_lib, cgs, oracle_mod, o64, synth, img, grid):
     """All bins in one graph-captured solve equal independent solves."""
-    img, grid, nch = (16, 16, 12), (32, 32, 24), 3
+    nch = 3
     k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 48)
     n_read = 48
     rb = [np.arange(0, 10), np.arange(10, 32), np.arange(32, 35), np.arange(35, 60)]
@@ -222,3 +226,43 @@ def test_input_faults_are_reported(gpu_lib, cgs, synth):
     with pytest.raises(cgs.CGSError) as e:
         r.set_trajectory(kk)
     assert e.value.code == cgs.CGS_ERR_NONFINITE
+
+
+def test_precision_form_against_fp64(gpu_lib, cgs, oracle_mod, o64, synth):
+    """The complex64 solve (FP32 gridding and FFT, FP64 CG scalars) against
+    the full-FP64 GPU solve, iteration by iteration: relative L2 <= 1e-4.
+    The FP64 GPU solve itself agrees with the FP64 CPU oracle to 1e-6 (its
+    inputs -- coil maps, deapodisation, tap weights -- are float)."""
+    import torch
+    img, grid, nch = (32, 24, 20), (64, 48, 40), 4
+    k, p, taps, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 64)
+    smaps = synth.coil_maps(img, nch)
+    rng = np.random.default_rng(8)
+    x_true = synth.phantom(img)
+    dcf = rng.uniform(0.5, 1.5, k.shape[0]).astype(np.float32)
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b)
+    r.set_trajectory(k)
+    data = r.nufft_fwd(smaps * x_true[None])
+    data += synth.complex_noise(data.shape, 30.0, float(np.sqrt(np.mean(np.abs(data) ** 2))))
+    r.set_dcf(dcf)
+    r.set_smaps(smaps)
+    iters = 10
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        d = torch.from_numpy(data).cuda()
+        x32 = torch.zeros((1,) + img, dtype=torch.complex64, device="cuda")
+        x64 = torch.zeros((1,) + img, dtype=torch.complex128, device="cuda")
+        t32 = torch.zeros((iters, 1) + img, dtype=torch.complex64, device="cuda")
+        t64 = torch.zeros((iters, 1) + img, dtype=torch.complex128, device="cuda")
+    stream.synchronize()
+    res32, it32 = r.cg_sense_trace_tensor(d, x32, 0.0, iters, t32)
+    res64, it64 = r.cg_sense_fp64_tensor(d, x64, 0.0, iters, t64)
+    stream.synchronize()
+    assert it32[0] == it64[0] == iters
+    a32, a64 = t32.cpu().numpy(), t64.cpu().numpy()
+    errs = [rel_l2(a32[i], a64[i]) for i in range(iters)]
+    assert max(errs) < 1e-4, errs
+    st, xo, reso, ito = o64.cg_sense(p, taps, o64.kernel_ft(p), smaps, dcf, data, 0.0, iters)
+    assert rel_l2(x64.cpu().numpy()[0], xo) < 1e-6
+    assert np.allclose(res64[0, :iters], reso, rtol=1e-6)
