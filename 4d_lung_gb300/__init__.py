@@ -51,7 +51,7 @@ EXPORTS = [
     "cgs_cg_solve_batched", "cgs_cg_solve_batched_d", "cgs_last_launch_count",
     "cgs_profile_apply", "cgs_cg_solve_images", "cgs_alloc_host", "cgs_free_host",
     "cgs_fft3_noalloc", "cgs_cg_solve_plain_d", "cgs_voronoi_dcf", "cgs_cg_solve_trace_d",
-    "cgs_cg_solve_fp64_d",
+    "cgs_cg_solve_fp64_d", "cgs_estimate_density_v3d",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -151,6 +151,7 @@ def lib():
         "cgs_fft3_noalloc": (C.c_int, [vp, vp, vp, i32, vp]),
         "cgs_cg_solve_plain_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
         "cgs_voronoi_dcf": (C.c_int, [vp, i64, vp]),
+        "cgs_estimate_density_v3d": (C.c_int, [vp, i64, C.c_int32, C.c_int32, C.c_double, vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
         "cgs_cg_solve_fp64_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
     }
@@ -199,6 +200,17 @@ def voronoi_dcf(k):
     st = lib().cgs_voronoi_dcf(_p(k), k.shape[0], _p(out))
     if st != CGS_OK:
         raise CGSError(st, "cgs_voronoi_dcf failed")
+    return out
+
+
+def estimate_density_v3d(k, sX, average=False, cutoff=1.0):
+    """estimateDensityV3D with its readout averaging (functions.h:212-232):
+    k holds whole readouts of sX samples each (readout-major order)."""
+    k = np.ascontiguousarray(k, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros(k.shape[0], np.float32)
+    st = lib().cgs_estimate_density_v3d(_p(k), k.shape[0], int(sX), int(bool(average)), float(cutoff), _p(out))
+    if st != CGS_OK:
+        raise CGSError(st, "cgs_estimate_density_v3d failed")
     return out
 
 

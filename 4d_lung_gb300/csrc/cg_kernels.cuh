@@ -6,15 +6,20 @@
 // CgState and returns at once when the bin has stopped (residual below the
 // threshold or the iteration cap reached), which reproduces the reference's
 // `while (currentResidual > cgThreshold)` loop with its 16-iteration cap.
-// Dot products are FP64: per-block partial sums, then a fixed-order sum in
-// one thread, so results do not depend on scheduling.
+// Dot products follow conjScalarProduct (Reco.cpp:131-143): the products of
+// an element are formed in FP32 and accumulated in FP64 -- here a thread
+// adds CG_FCHUNK elements' FP32 terms before each FP64 addition, which keeps
+// the FP64 pipe (a small fraction of GB300's FP32 rate) off the critical
+// path.  Per-block partial sums are then added in a fixed order in one
+// thread, so results do not depend on scheduling.  The vector updates use
+// the FP64 step sizes rounded to FP32 (relative change ~1e-7 per update).
 #pragma once
 #include "cgs_common.cuh"
 #include "cgs_types.h"
 
 namespace cgs {
 
-
+constexpr int CG_FCHUNK = 4;   // elements per FP32 partial of a dot product
 
 CGS_D void block_reduce2(double& a, double& b, double* s_red /* [2][RED_THREADS/32] */)
 {
@@ -49,13 +54,21 @@ k_cg_init(const float2* __restrict__ b, float2* r, float2* p, float2* x, long lo
     const int bin = blockIdx.y;
     const long long off = (long long)bin * bs;
     double acc = 0.0, dummy = 0.0;
+    float fa = 0.f;
+    int cnt = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 v = b[off + i];
         r[off + i] = v;
         p[off + i] = v;
         x[off + i] = make_float2(0.f, 0.f);
-        acc += (double)v.x * v.x + (double)v.y * v.y;
+        fa += v.x * v.x + v.y * v.y;
+        if (++cnt == CG_FCHUNK) {
+            acc += (double)fa;
+            fa = 0.f;
+            cnt = 0;
+        }
     }
+    acc += (double)fa;
     block_reduce2(acc, dummy, s_red);
     if (threadIdx.x == 0) {
         double* o = partials + 2 * ((long long)bin * gridDim.x + blockIdx.x);
@@ -122,20 +135,28 @@ k_cg_update_xr(float2* x, float2* r, const float2* __restrict__ p, const float2*
     const int bin = blockIdx.y;
     const CgState& S = st[bin];
     if (!S.active) return;
-    const double ar = S.alpha[0], ai = S.alpha[1];
+    const float ar = (float)S.alpha[0], ai = (float)S.alpha[1];
     const long long off = (long long)bin * bs;
     double acc = 0.0, dummy = 0.0;
+    float fa = 0.f;
+    int cnt = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 pv = p[off + i], qv = q[off + i];
         float2 xv = x[off + i], rv = r[off + i];
-        xv.x = (float)((double)xv.x + (ar * pv.x - ai * pv.y));
-        xv.y = (float)((double)xv.y + (ar * pv.y + ai * pv.x));
-        rv.x = (float)((double)rv.x - (ar * qv.x - ai * qv.y));
-        rv.y = (float)((double)rv.y - (ar * qv.y + ai * qv.x));
+        xv.x += ar * pv.x - ai * pv.y;
+        xv.y += ar * pv.y + ai * pv.x;
+        rv.x -= ar * qv.x - ai * qv.y;
+        rv.y -= ar * qv.y + ai * qv.x;
         x[off + i] = xv;
         r[off + i] = rv;
-        acc += (double)rv.x * rv.x + (double)rv.y * rv.y;
+        fa += rv.x * rv.x + rv.y * rv.y;
+        if (++cnt == CG_FCHUNK) {
+            acc += (double)fa;
+            fa = 0.f;
+            cnt = 0;
+        }
     }
+    acc += (double)fa;
     block_reduce2(acc, dummy, s_red);
     if (threadIdx.x == 0) {
         double* o = partials + 2 * ((long long)bin * gridDim.x + blockIdx.x);
@@ -172,13 +193,13 @@ __global__ void k_cg_update_p(float2* p, const float2* __restrict__ r, long long
     const int bin = blockIdx.y;
     const CgState& S = st[bin];
     if (!S.active) return;
-    const double br = S.beta[0], bi = S.beta[1];
+    const float br = (float)S.beta[0], bi = (float)S.beta[1];
     const long long off = (long long)bin * bs;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 pv = p[off + i], rv = r[off + i];
         float2 o;
-        o.x = (float)((double)rv.x + br * pv.x - bi * pv.y);
-        o.y = (float)((double)rv.y + br * pv.y + bi * pv.x);
+        o.x = rv.x + (br * pv.x - bi * pv.y);
+        o.y = rv.y + (br * pv.y + bi * pv.x);
         p[off + i] = o;
     }
 }

@@ -358,6 +358,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fz.nch = c->nch;
     fz.x_bs = x_bs;
     fz.out_bs = (long long)c->nch * zb;
+    fz.err = c->d_err.as<int>();
     fz.coil_in = c->Ni;
     fz.coil_out = zb;
     fz.tw = c->tw[2].as<float2>();
@@ -496,6 +497,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
     az.coil_s = c->Ni;
     az.q_cs = c->Ni;
     az.tw = c->tw[2].as<float2>();
+    az.err = c->d_err.as<int>();
     CGS_LAUNCH(c, launch_adj_z(Gz, az, nb, c->stream));
     return CGS_OK;
 }

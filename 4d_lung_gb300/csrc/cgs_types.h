@@ -65,6 +65,7 @@ struct FwdZArgs {
     long long x_bs, out_bs; // batch strides (blockIdx.y: bins)
     long long coil_in, coil_out;  // coil strides of smaps and out
     const float2* tw;
+    int* err;               // timeout flag of the pipelined variant (null: plain kernel)
 };
 
 struct AdjZArgs {
@@ -83,6 +84,7 @@ struct AdjZArgs {
     long long coil_in, coil_s;
     long long q_cs;         // coil stride of q when smaps is null
     const float2* tw;
+    int* err;               // timeout flag of the pipelined variant (null: plain kernel)
 };
 
 struct TapRecord {

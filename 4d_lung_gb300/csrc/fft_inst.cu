@@ -38,6 +38,11 @@ struct SizeImpl {
     static constexpr int NSTAGE = 2;
     using Pipe = PipeLayout<R1, R2, TB, NSTAGE>;
 
+    // pipelined z passes: coil tiles in flight ahead of the FFT
+    static constexpr int ZNST_F = 3, ZNST_A = 2;
+    using ZF = ZPipeLayout<R1, R2, LPB, ZNST_F>;
+    using ZA = ZPipeLayout<R1, R2, LPB, ZNST_A>;
+
     static cudaError_t init()
     {
         const int smem = (int)Pipe::smem_bytes(L);
@@ -46,8 +51,17 @@ struct SizeImpl {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, +1, TB, NSTAGE>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        // the z extent of an image never exceeds the grid's: size for Iz = L
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_fwd_z_pipe<R1, R2, LPB, ZNST_F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ZF::smem_bytes(L, false));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_adj_z_pipe<R1, R2, LPB, ZNST_A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)ZA::smem_bytes(L, true));
         return e;
     }
+
+    static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
     static cudaError_t strided(int sign, StridedPassArgs a, int A, int batch, cudaStream_t s)
     {
@@ -88,6 +102,12 @@ struct SizeImpl {
     static cudaError_t fwd_z(const FwdZArgs& a, int batch, cudaStream_t s)
     {
         dim3 grid((unsigned)((a.nl + LPB - 1) / LPB), (unsigned)batch);
+        // bulk copies need 16-byte aligned tiles: even Iz and coil strides
+        if (a.err && a.smaps && a.x_cs == 0 && a.Iz <= L && (a.Iz & 1) == 0 && (a.coil_in & 1) == 0 &&
+            al16(a.smaps)) {
+            k_fwd_z_pipe<R1, R2, LPB, ZNST_F><<<grid, NT_C, ZF::smem_bytes(a.Iz, false), s>>>(a);
+            return cudaGetLastError();
+        }
         k_fwd_z<R1, R2, LPB><<<grid, NT_C, 0, s>>>(a);
         return cudaGetLastError();
     }
@@ -95,6 +115,11 @@ struct SizeImpl {
     static cudaError_t adj_z(const AdjZArgs& a, int batch, cudaStream_t s)
     {
         dim3 grid((unsigned)adj_blocks(a.nl), (unsigned)batch);
+        if (a.err && a.smaps && a.Iz <= L && (a.Iz & 1) == 0 && (a.coil_s & 1) == 0 && (a.coil_in & 1) == 0 &&
+            (a.in_bs & 1) == 0 && al16(a.smaps) && al16(a.in)) {
+            k_adj_z_pipe<R1, R2, LPB, ZNST_A><<<grid, NT_C, ZA::smem_bytes(a.Iz, true), s>>>(a);
+            return cudaGetLastError();
+        }
         k_adj_z<R1, R2, LPB><<<grid, NT_C, 0, s>>>(a);
         return cudaGetLastError();
     }

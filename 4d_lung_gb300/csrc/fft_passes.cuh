@@ -468,10 +468,13 @@ k_adj_z(AdjZArgs a)
         }
     }
     if (!a.smaps) return;
+    // <p, q>: FP32 products of the thread's R2 elements (as conjScalarProduct,
+    // Reco.cpp:139-140, forms them), accumulated from here on in FP64
     double dre = 0.0, dim = 0.0;
     if (act2) {
         const int ix = (int)(line2 / a.Iy), iy = (int)(line2 - (long long)ix * a.Iy);
         const float sxy = a.scale * a.apx[ix] * a.apy[iy];
+        float fre = 0.f, fim = 0.f;
 #pragma unroll
         for (int k2 = 0; k2 < R2; ++k2) {
             const int zi = k1 + R1 * k2 - a.lo_z;
@@ -480,11 +483,281 @@ k_adj_z(AdjZArgs a)
                 qb[line2 * a.Iz + zi] = qv;
                 if (a.p) {
                     const float2 pv = a.p[(long long)blockIdx.y * a.q_bs + line2 * a.Iz + zi];
-                    dre += (double)pv.x * qv.x + (double)pv.y * qv.y;
-                    dim += (double)pv.x * qv.y - (double)pv.y * qv.x;
+                    fre += pv.x * qv.x + pv.y * qv.y;
+                    fim += pv.x * qv.y - pv.y * qv.x;
                 }
             }
         }
+        dre = (double)fre;
+        dim = (double)fim;
+    }
+    if (a.p) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            dre += __shfl_xor_sync(0xffffffffu, dre, o);
+            dim += __shfl_xor_sync(0xffffffffu, dim, o);
+        }
+        if ((tid & 31) == 0) {
+            s_red[0][tid >> 5] = dre;
+            s_red[1][tid >> 5] = dim;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double r0 = 0.0, r1 = 0.0;
+            for (int w = 0; w < NT / 32; ++w) {
+                r0 += s_red[0][w];
+                r1 += s_red[1][w];
+            }
+            double* out = a.partials + 2 * ((long long)blockIdx.y * gridDim.x + blockIdx.x);
+            out[0] = r0;
+            out[1] = r1;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pipelined z passes.  The per-coil inputs of a block -- its LPB lines of the
+// coil map S_c (forward and adjoint) and of the z-pass buffer (adjoint) --
+// are contiguous, so each is one cp.async.bulk copy into a ring of NST
+// shared-memory stages, NST - 1 coils ahead of the FFT.  Arithmetic and
+// results are those of k_fwd_z / k_adj_z.  Every wait is bounded (2 s); on a
+// timeout the block sets *err, lets its issued copies land and exits.
+// Shared layout: [NST stages][bars][twiddles][exchange rows].
+// ---------------------------------------------------------------------------
+template <int R1, int R2, int LPB, int NST>
+struct ZPipeLayout {
+    using Lay = ContigLayout<R1, R2>;
+    static constexpr int L = Lay::L;
+    static constexpr int NT = LPB * Lay::RMAX;
+    // elements of one stage: S tile (+ z-buffer tile for the adjoint)
+    __host__ __device__ static size_t stage_elems(int Iz, bool adj) { return (size_t)LPB * Iz + (adj ? (size_t)LPB * L : 0); }
+    static size_t smem_bytes(int Iz, bool adj)
+    {
+        return (NST * stage_elems(Iz, adj) + L + (size_t)LPB * Lay::LINE) * sizeof(float2) + 16 * NST;
+    }
+};
+
+template <int R1, int R2, int LPB, int NST>
+__global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX)
+k_fwd_z_pipe(FwdZArgs a)
+{
+    using Lay = ContigLayout<R1, R2>;
+    using ZL = ZPipeLayout<R1, R2, LPB, NST>;
+    constexpr int L = Lay::L;
+    constexpr int SIGN = -1;
+    extern __shared__ float4 s_dyn[];
+    const size_t se = ZL::stage_elems(a.Iz, false);
+    float2* s_stage = reinterpret_cast<float2*>(s_dyn);
+    float2* s_tw = s_stage + NST * se;
+    float2* s_y = s_tw + L;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_y + LPB * Lay::LINE);
+    const int tid = threadIdx.x;
+    for (int m = tid; m < L; m += ZL::NT) s_tw[m] = a.tw[m];
+    const long long line0 = (long long)blockIdx.x * LPB;
+    const int rows = (int)min((long long)LPB, a.nl - line0);
+    const uint32_t tile_bytes = (uint32_t)rows * (uint32_t)a.Iz * (uint32_t)sizeof(float2);
+    const float2* Sb = a.smaps + line0 * a.Iz;
+    if (tid == 0) {
+        for (int s = 0; s < NST; ++s) mbar_init(&s_bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int c) {   // thread 0 only
+        const int st = c % NST;
+        mbar_arrive_expect_tx(&s_bar[st], tile_bytes);
+        bulk_load(s_stage + (size_t)st * se, Sb + (long long)c * a.coil_in, tile_bytes, &s_bar[st]);
+    };
+    if (tid == 0)
+        for (int c = 0; c < NST - 1 && c < a.nch; ++c) issue(c);
+
+    const float2* xin = a.x + (long long)blockIdx.y * a.x_bs;
+    float2* outb = a.out + (long long)blockIdx.y * a.out_bs;
+    const int ln1 = tid / R2, n2 = tid % R2;
+    const long long line1 = line0 + ln1;
+    const bool act1 = ln1 < LPB && line1 < a.nl;
+    float2 xa[R1];
+    if (act1) {
+        const int ix = (int)(line1 / a.Iy), iy = (int)(line1 - (long long)ix * a.Iy);
+        const float axy = a.apx[ix] * a.apy[iy];
+        const float2* xl = xin + line1 * a.Iz;
+#pragma unroll
+        for (int n1 = 0; n1 < R1; ++n1) {
+            const int l = R2 * n1 + n2;
+            const int zi = l - a.lo_z;
+            float2 v = make_float2(0.f, 0.f);
+            if (zi >= 0 && zi < a.Iz) v = parity(cscale(xl[zi], axy * a.apz[zi]), l);
+            xa[n1] = v;
+        }
+    }
+    const int ln2 = tid / R1, k1 = tid % R1;
+    const long long line2 = line0 + ln2;
+    const bool act2 = ln2 < LPB && line2 < a.nl;
+
+    for (int c = 0; c < a.nch; ++c) {
+        const int st = c % NST;
+        // stage (c - 1) % NST was last read in stage 1 of coil c - 1, before
+        // the barrier that followed it: it can be refilled now
+        if (tid == 0 && c + NST - 1 < a.nch) issue(c + NST - 1);
+        const bool ok = mbar_wait_bounded(&s_bar[st], (uint32_t)((c / NST) & 1), PIPE_WAIT_NS);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(a.err, 1);
+                for (int j = c; j < a.nch && j < c + NST; ++j)
+                    mbar_wait_bounded(&s_bar[j % NST], (uint32_t)((j / NST) & 1), PIPE_WAIT_NS);
+            }
+            return;
+        }
+        if (act1) {
+            const float2* S = s_stage + (size_t)st * se + ln1 * a.Iz;
+            float2 v[R1];
+#pragma unroll
+            for (int n1 = 0; n1 < R1; ++n1) {
+                const int zi = R2 * n1 + n2 - a.lo_z;
+                v[n1] = (zi >= 0 && zi < a.Iz) ? cmul(xa[n1], S[zi]) : make_float2(0.f, 0.f);
+            }
+            Dft<R1, SIGN>::run(v);
+#pragma unroll
+            for (int kk = 0; kk < R1; ++kk) {
+                float2 t = v[kk];
+                if (kk > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * kk]);
+                s_y[ln1 * Lay::LINE + n2 * Lay::R1P + kk] = t;
+            }
+        }
+        __syncthreads();
+        if (act2) {
+            float2 u[R2];
+#pragma unroll
+            for (int m = 0; m < R2; ++m) u[m] = s_y[ln2 * Lay::LINE + m * Lay::R1P + k1];
+            Dft<R2, SIGN>::run(u);
+            float2* o = outb + (long long)c * a.coil_out + line2 * L;
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) {
+                const int l = k1 + R1 * k2;
+                o[l] = parity(u[k2], l);
+            }
+        }
+    }
+}
+
+template <int R1, int R2, int LPB, int NST>
+__global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX)
+k_adj_z_pipe(AdjZArgs a)
+{
+    using Lay = ContigLayout<R1, R2>;
+    using ZL = ZPipeLayout<R1, R2, LPB, NST>;
+    constexpr int L = Lay::L;
+    constexpr int SIGN = +1;
+    constexpr int NT = ZL::NT;
+    extern __shared__ float4 s_dyn[];
+    __shared__ double s_red[2][NT / 32];
+    const size_t se = ZL::stage_elems(a.Iz, true);
+    const size_t s_off = (size_t)LPB * L;   // S tile after the z-buffer tile
+    float2* s_stage = reinterpret_cast<float2*>(s_dyn);
+    float2* s_tw = s_stage + NST * se;
+    float2* s_y = s_tw + L;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_y + LPB * Lay::LINE);
+    const int tid = threadIdx.x;
+    for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
+    const long long line0 = (long long)blockIdx.x * LPB;
+    const int rows = (int)min((long long)LPB, a.nl - line0);
+    const uint32_t in_bytes = (uint32_t)rows * (uint32_t)L * (uint32_t)sizeof(float2);
+    const uint32_t s_bytes = (uint32_t)rows * (uint32_t)a.Iz * (uint32_t)sizeof(float2);
+    const float2* inb = a.in + (long long)blockIdx.y * a.in_bs + line0 * L;
+    const float2* Sb = a.smaps + line0 * a.Iz;
+    float2* qb = a.q + (long long)blockIdx.y * a.q_bs;
+    if (tid == 0) {
+        for (int s = 0; s < NST; ++s) mbar_init(&s_bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    auto issue = [&](int c) {   // thread 0 only
+        const int st = c % NST;
+        float2* dst = s_stage + (size_t)st * se;
+        mbar_arrive_expect_tx(&s_bar[st], in_bytes + s_bytes);
+        bulk_load(dst, inb + (long long)c * a.coil_in, in_bytes, &s_bar[st]);
+        bulk_load(dst + s_off, Sb + (long long)c * a.coil_s, s_bytes, &s_bar[st]);
+    };
+    if (tid == 0)
+        for (int c = 0; c < NST - 1 && c < a.nch; ++c) issue(c);
+
+    const int ln1 = tid / R2, n2 = tid % R2;
+    const long long line1 = line0 + ln1;
+    const bool act1 = ln1 < LPB && line1 < a.nl;
+    const int ln2 = tid / R1, k1 = tid % R1;
+    const long long line2 = line0 + ln2;
+    const bool act2 = ln2 < LPB && line2 < a.nl;
+
+    float2 acc[R2];
+#pragma unroll
+    for (int k2 = 0; k2 < R2; ++k2) acc[k2] = make_float2(0.f, 0.f);
+
+    for (int c = 0; c < a.nch; ++c) {
+        const int st = c % NST;
+        // stage (c - 1) % NST is read up to stage 2 of coil c - 1
+        __syncthreads();
+        if (tid == 0 && c + NST - 1 < a.nch) issue(c + NST - 1);
+        const bool ok = mbar_wait_bounded(&s_bar[st], (uint32_t)((c / NST) & 1), PIPE_WAIT_NS);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(a.err, 1);
+                for (int j = c; j < a.nch && j < c + NST; ++j)
+                    mbar_wait_bounded(&s_bar[j % NST], (uint32_t)((j / NST) & 1), PIPE_WAIT_NS);
+            }
+            return;
+        }
+        const float2* tin = s_stage + (size_t)st * se;
+        if (act1) {
+            const float2* src = tin + ln1 * L;
+            float2 v[R1];
+#pragma unroll
+            for (int n1 = 0; n1 < R1; ++n1) {
+                const int l = R2 * n1 + n2;
+                v[n1] = parity(src[l], l);
+            }
+            Dft<R1, SIGN>::run(v);
+#pragma unroll
+            for (int kk = 0; kk < R1; ++kk) {
+                float2 t = v[kk];
+                if (kk > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * kk]);
+                s_y[ln1 * Lay::LINE + n2 * Lay::R1P + kk] = t;
+            }
+        }
+        __syncthreads();
+        if (act2) {
+            float2 u[R2];
+#pragma unroll
+            for (int m = 0; m < R2; ++m) u[m] = s_y[ln2 * Lay::LINE + m * Lay::R1P + k1];
+            Dft<R2, SIGN>::run(u);
+            const float2* S = tin + s_off + ln2 * a.Iz;
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) {
+                const int l = k1 + R1 * k2;
+                const int zi = l - a.lo_z;
+                if (zi >= 0 && zi < a.Iz) acc[k2] = cadd(acc[k2], cmulc(parity(u[k2], l), S[zi]));
+            }
+        }
+    }
+    // <p, q>: FP32 products of the thread's R2 elements, accumulated in FP64
+    double dre = 0.0, dim = 0.0;
+    if (act2) {
+        const int ix = (int)(line2 / a.Iy), iy = (int)(line2 - (long long)ix * a.Iy);
+        const float sxy = a.scale * a.apx[ix] * a.apy[iy];
+        float fre = 0.f, fim = 0.f;
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) {
+            const int zi = k1 + R1 * k2 - a.lo_z;
+            if (zi >= 0 && zi < a.Iz) {
+                const float2 qv = cscale(acc[k2], sxy * a.apz[zi]);
+                qb[line2 * a.Iz + zi] = qv;
+                if (a.p) {
+                    const float2 pv = a.p[(long long)blockIdx.y * a.q_bs + line2 * a.Iz + zi];
+                    fre += pv.x * qv.x + pv.y * qv.y;
+                    fim += pv.x * qv.y - pv.y * qv.x;
+                }
+            }
+        }
+        dre = (double)fre;
+        dim = (double)fim;
     }
     if (a.p) {
 #pragma unroll

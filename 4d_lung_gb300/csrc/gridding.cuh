@@ -138,6 +138,10 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
 
 constexpr int SPREAD_BATCH = 32;   // samples staged per round
 
+// CC: compile-time upper bound of the coils per block (a.cc <= CC); the
+// coil loop is unrolled so that the shared-memory loads, FMAs and stores of
+// all coils of one grid point issue back to back.
+template <int CC>
 __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
 {
     extern __shared__ float4 s_dyn[];
@@ -150,7 +154,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
     const int tx = tile / (a.ntz * a.nty);
     const int x0 = tx * TILE_X, y0 = ty * TILE_Y, z0 = tz * TILE_Z;
 
-    // shared: accumulators [cc][TILE_PTS] float2, then staged records and values
+    // shared: accumulators [cc][ACC_PTS] float2, then staged records and values
     float2* acc = reinterpret_cast<float2*>(s_dyn);
     TapRecord* s_rec = reinterpret_cast<TapRecord*>(acc + (size_t)a.cc * ACC_PTS);
     float2* s_val = reinterpret_cast<float2*>(s_rec + SPREAD_BATCH);
@@ -176,26 +180,37 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
         for (int e = tid; e < nbat * ncc; e += SPREAD_THREADS) {
             const int j = e / ncc, c = e - j * ncc;
             const long long si = sbase + idx[s + j];
-            s_val[j * ncc + c] = a.yv[si * a.nch + c0 + c];
+            s_val[j * CC + c] = a.yv[si * a.nch + c0 + c];
         }
         __syncthreads();
-        for (int j = 0; j < nbat; ++j) {
-            const float* w = reinterpret_cast<const float*>(&s_rec[j]);
-            int nx, ny, nz;
-            unpack_nearest(__float_as_uint(w[15]), nx, ny, nz);
-            const int jx = gx - (nx - 2);
-            if (jx < 0 || jx > 4 || lane >= 25) continue;
-            const int gy = ny - 2 + jy, gz = nz - 2 + jz;
-            if (gy < y0 || gy >= y0 + TILE_Y || gz < z0 || gz >= z0 + TILE_Z) continue;
-            const float wt = (w[jx] * w[5 + jy]) * w[10 + jz];
-            if (w[jx] == 0.f || w[5 + jy] == 0.f || w[10 + jz] == 0.f || !(wt > a.thresh)) continue;
-            const int local = (warp * TILE_Y + (gy - y0)) * TILE_ZP + (gz - z0);
-            const float2* v = s_val + j * ncc;
-            for (int c = 0; c < ncc; ++c) {
-                float2 t = acc[c * ACC_PTS + local];
-                t.x = fmaf(v[c].x, wt, t.x);
-                t.y = fmaf(v[c].y, wt, t.y);
-                acc[c * ACC_PTS + local] = t;
+        if (lane < 25) {
+            for (int j = 0; j < nbat; ++j) {
+                const float* w = reinterpret_cast<const float*>(&s_rec[j]);
+                int nx, ny, nz;
+                unpack_nearest(__float_as_uint(w[15]), nx, ny, nz);
+                const int jx = gx - (nx - 2);
+                if (jx < 0 || jx > 4) continue;
+                const int gy = ny - 2 + jy, gz = nz - 2 + jz;
+                if (gy < y0 || gy >= y0 + TILE_Y || gz < z0 || gz >= z0 + TILE_Z) continue;
+                const float wxv = w[jx], wyv = w[5 + jy], wzv = w[10 + jz];
+                const float wt = (wxv * wyv) * wzv;
+                if (wxv == 0.f || wyv == 0.f || wzv == 0.f || !(wt > a.thresh)) continue;
+                float2* pt = acc + (warp * TILE_Y + (gy - y0)) * TILE_ZP + (gz - z0);
+                const float2* v = s_val + j * CC;
+                float2 t[CC], vv[CC];
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+                    if (c < ncc) {
+                        t[c] = pt[c * ACC_PTS];
+                        vv[c] = v[c];
+                    }
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+                    if (c < ncc) {
+                        t[c].x = fmaf(vv[c].x, wt, t[c].x);
+                        t[c].y = fmaf(vv[c].y, wt, t[c].y);
+                        pt[c * ACC_PTS] = t[c];
+                    }
             }
         }
     }

@@ -99,18 +99,25 @@ cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nb
     return cudaGetLastError();
 }
 
+// coils per spreading block: staged values use a row of SPREAD_CC_MAX
+constexpr int SPREAD_CC_MAX = 12;
+
 size_t spread_smem_bytes(int cc)
 {
+    const int ccp = cc <= 4 ? 4 : (cc <= 8 ? 8 : SPREAD_CC_MAX);
     return (size_t)cc * ACC_PTS * sizeof(float2) + SPREAD_BATCH * sizeof(TapRecord) +
-           (size_t)SPREAD_BATCH * cc * sizeof(float2);
+           (size_t)SPREAD_BATCH * ccp * sizeof(float2);
 }
 
-int spread_max_coils() { return 24; }
+int spread_max_coils() { return SPREAD_CC_MAX; }
 
 cudaError_t kernels_init()
 {
-    cudaError_t e = cudaFuncSetAttribute(k_spread, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)spread_smem_bytes(spread_max_coils()));
+    const int smax = (int)spread_smem_bytes(SPREAD_CC_MAX);
+    cudaError_t e = cudaFuncSetAttribute(k_spread<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_spread<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_spread<SPREAD_CC_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
     if (e == cudaSuccess) e = fft_init_all();
     return e;
 }
@@ -118,9 +125,12 @@ cudaError_t kernels_init()
 cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, cudaStream_t s)
 {
     if (ntiles == 0 || nbins == 0) return cudaSuccess;
+    if (a.cc < 1 || a.cc > SPREAD_CC_MAX) return cudaErrorInvalidValue;
     const size_t smem = spread_smem_bytes(a.cc);
     dim3 grid((unsigned)ntiles, (unsigned)((a.nch + a.cc - 1) / a.cc), (unsigned)nbins);
-    k_spread<<<grid, SPREAD_THREADS, smem, s>>>(a);
+    if (a.cc <= 4) k_spread<4><<<grid, SPREAD_THREADS, smem, s>>>(a);
+    else if (a.cc <= 8) k_spread<8><<<grid, SPREAD_THREADS, smem, s>>>(a);
+    else k_spread<SPREAD_CC_MAX><<<grid, SPREAD_THREADS, smem, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -54,6 +54,16 @@ CGS_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint64_t limit_ns)
     return true;
 }
 
+// Contiguous bulk copy global -> shared (both 16-byte aligned, bytes a
+// multiple of 16), completion counted on `bar`.
+CGS_D void bulk_load(void* dst_smem, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst_smem)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
 // 4-D tensor-map tile load (TMA) into shared memory, completion on `bar`.
 // Coordinates are element indices, innermost first.
 CGS_D void tma_load_4d(void* dst_smem, const void* tmap, int c0, int c1, int c2, int c3, uint64_t* bar)

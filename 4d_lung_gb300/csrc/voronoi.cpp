@@ -180,10 +180,9 @@ struct Cell {
 
 }  // namespace
 
-extern "C" int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf)
+// Voronoi cell volume of every sample (0 on the convex hull).
+static int voronoi_volumes(const double* k, int64_t n, std::vector<double>& volumes)
 {
-    if (!k || !dcf || n < 0) return CGS_ERR_ARG;
-    if (n == 0) return CGS_OK;
     V3 lo{1e300, 1e300, 1e300}, hi{-1e300, -1e300, -1e300};
     for (int64_t i = 0; i < n; ++i) {
         const V3 p{k[3 * i], k[3 * i + 1], k[3 * i + 2]};
@@ -225,7 +224,7 @@ extern "C" int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf)
     // after every sample that could cut them has been used
     const double box_h = 1e3 * diam;
     const double eps = diam * 1e-12;
-    std::vector<double> volumes(n, 0.0);
+    volumes.assign(n, 0.0);
 
 #pragma omp parallel
     {
@@ -329,9 +328,62 @@ extern "C" int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf)
             volumes[i] = cell.touches_box() ? 0.0 : cell.volume(p);
         }
     }
+    return CGS_OK;
+}
+
+static int check_traj(const double* k, int64_t n)
+{
+    for (int64_t i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(k[i])) return CGS_ERR_NONFINITE;
+    return CGS_OK;
+}
+
+// division by the largest value (functions.h:234-245)
+static void normalise_max(const std::vector<double>& v, float* dcf)
+{
     double mx = 0.0;
-    for (int64_t i = 0; i < n; ++i) mx = std::max(mx, volumes[i]);
+    for (double x : v) mx = std::max(mx, x);
     const double inv = mx > 0 ? 1.0 / mx : 0.0;
-    for (int64_t i = 0; i < n; ++i) dcf[i] = (float)(volumes[i] * inv);
+    for (size_t i = 0; i < v.size(); ++i) dcf[i] = (float)(v[i] * inv);
+}
+
+extern "C" int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf)
+{
+    if (!k || !dcf || n < 0) return CGS_ERR_ARG;
+    if (n == 0) return CGS_OK;
+    const int st = check_traj(k, n);
+    if (st != CGS_OK) return st;
+    std::vector<double> vol;
+    voronoi_volumes(k, n, vol);
+    normalise_max(vol, dcf);
+    return CGS_OK;
+}
+
+// estimateDensityV3D with its `average` option (functions.h:212-232): the
+// volumes are summed per readout position i % sX over all readouts, divided
+// by the total, and every sample takes the sum of its position -- positions
+// beyond (sX - 1) * cutoff take the value at that position -- before the
+// division by the maximum.  The reference adds into a float array from
+// several threads without a reduction; here the sums are FP64 and ordered.
+extern "C" int cgs_estimate_density_v3d(const double* k, int64_t n, int32_t sX, int32_t average, double cutoff,
+                                        float* dcf)
+{
+    if (!k || !dcf || n < 0) return CGS_ERR_ARG;
+    if (n == 0) return CGS_OK;
+    if (average && (sX <= 0 || n % sX != 0 || !(cutoff >= 0.0 && cutoff <= 1.0))) return CGS_ERR_ARG;
+    const int st = check_traj(k, n);
+    if (st != CGS_OK) return st;
+    std::vector<double> vol;
+    voronoi_volumes(k, n, vol);
+    if (average) {
+        std::vector<double> avg(sX, 0.0);
+        for (int64_t i = 0; i < n; ++i) avg[i % sX] += vol[i];
+        double tot = 0.0;
+        for (int i = 0; i < sX; ++i) tot += avg[i];
+        const double inv = tot > 0 ? 1.0 / tot : 0.0;
+        const int lim = (int)((sX - 1) * cutoff);
+        for (int64_t i = 0; i < n; ++i) vol[i] = inv * avg[std::min((int)(i % sX), lim)];
+    }
+    normalise_max(vol, dcf);
     return CGS_OK;
 }

@@ -220,13 +220,15 @@ def radial_dcf(k, grid):
     return d.astype(np.float32)
 
 
-def cap_dcf(d, q=99.9):
+def cap_dcf(d, q=99.0):
     """Caps Voronoi weights at the q-th percentile of the positive ones and
     renormalises to max 1.  The raw weights (estimateDensityV3D's definition)
-    give the few bounded cells next to the convex hull volumes 10^3 times the
-    median; with them the weighted normal equations are so ill-conditioned
-    that two FP32 summation orders differ by ~1e-3 after 15 CG iterations
-    (3e-2 against FP64).  Capping the top 0.1 % restores ~3e-6."""
+    of one respiratory bin span five orders of magnitude (cfg3 bins: median
+    ~2e-5 of the largest, 99th percentile ~2e-3): the few bounded cells next
+    to the convex hull are huge.  With them the weighted normal equations are
+    so ill-conditioned that 15 complex64 CG iterations end 8e-2 away from the
+    FP64 solve (cap at the 99.9th percentile); capped at the 99th percentile
+    the difference is 1.5e-6 (the reference's readout averaging: 2.5e-6)."""
     d = np.asarray(d, np.float32)
     pos = d[d > 0]
     if pos.size == 0:

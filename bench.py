@@ -55,7 +55,15 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
+# stage -> kernel family (the roofline's "kernel")
+FAMILY = {"fwd_z": "k_fwd_z_pipe+k_adj_z_pipe", "adj_z": "k_fwd_z_pipe+k_adj_z_pipe",
+          "fwd_y": "k_fft_strided_tma", "fwd_x": "k_fft_strided_tma", "adj_x": "k_fft_strided_tma",
+          "adj_y": "k_fft_strided_tma", "interp": "k_interp", "spread": "k_spread"}
+
+
 def traffic_record():
+    """DRAM bytes (read + write) of each kernel family per application, from
+    an ncu capture (profiles/traffic.json, written by hand from the capture)."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
@@ -389,33 +397,24 @@ def run_ours(args):
     groups = len(st) // 8
     stage_ms = {s: float(sum(st[g * 8 + i] for g in range(groups))) for i, s in enumerate(STAGES)}
     sb = stage_bytes(w, sizes)
-    if stage_ms["adj_x"] < 0.01 * stage_ms["spread"]:
-        # fused kernels: x pass + interpolation (slot partials), slot reduction,
-        # spreading + x pass; profile slots keep the unfused names' order
-        Ix, Iy, Iz = w.img
-        Gx, Gy, Gz = w.grid
-        C8 = 8 * w.n_ch
-        M = int(sum(sizes))
-        nb_ = len(sizes)
-        stage_ms = {"fwd_z": stage_ms["fwd_z"], "fwd_y": stage_ms["fwd_y"],
-                    "fwd_x+interp": stage_ms["fwd_x"], "interp_reduce": stage_ms["interp"],
-                    "spread+adj_x": stage_ms["spread"], "adj_y": stage_ms["adj_y"], "adj_z": stage_ms["adj_z"]}
-        sb = {"fwd_z": sb["fwd_z"], "fwd_y": sb["fwd_y"],
-              "fwd_x+interp": nb_ * C8 * Ix * Gy * Gz + M * (64 + 5 * C8),
-              "interp_reduce": M * (64 + 5 * C8 + C8 + 4),
-              "spread+adj_x": nb_ * C8 * Ix * Gy * Gz + M * (64 + C8),
-              "adj_y": sb["adj_y"], "adj_z": sb["adj_z"]}
     apply_ms = float(sum(stage_ms.values()))
-    dom = max(stage_ms, key=stage_ms.get)
+    # kernel families: the four x/y passes are one kernel template
+    fam = {k: [s for s in STAGES if FAMILY[s] == k] for k in dict.fromkeys(FAMILY.values())}
+    fam_ms = {k: sum(stage_ms[s] for s in v) for k, v in fam.items()}
+    dom = max(fam_ms, key=fam_ms.get)
+    dom_bytes = sum(sb[s] for s in fam[dom])
     peak, peak_kind = measured_peaks()
-    achieved = sb[dom] / (stage_ms[dom] / 1e3) / 1e9
+    achieved = dom_bytes / (fam_ms[dom] / 1e3) / 1e9
     tr = traffic_record().get(args.workload, {}).get(dom)
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
         if peak_kind == "measured" else "fallback 6800 GB/s",
-        "traffic": tr, "launches_per_apply": groups,
-        "algorithmic_bytes_per_apply": sb[dom],
+        "traffic": None if tr is None else tr["dram_bytes_per_apply"],
+        "traffic_source": None if tr is None else tr["source"],
+        "launches_per_apply": len(fam[dom]),
+        "algorithmic_bytes_per_apply": dom_bytes,
+        "kernel_ms": fam_ms,
         "stage_ms": stage_ms,
         "stage_frac_of_peak": {s: sb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
         "apply_ms": apply_ms,
@@ -429,7 +428,7 @@ def run_ours(args):
         "config": {"workload": w.name, "img": list(w.img), "grid": list(w.grid), "coils": w.n_ch,
                    "bins": nb, "samples_per_bin": [min(sizes), max(sizes)], "samples_total": int(sum(sizes)),
                    "cg_iters": iters, "kb_w": kb_w, "kb_b": round(kb_b, 4),
-                   "dcf": ("per-bin Voronoi volumes capped at the 99.9th percentile (host, %.1f s set-up)" % dcf_s)
+                   "dcf": ("per-bin Voronoi volumes capped at the 99th percentile (host, %.1f s set-up)" % dcf_s)
                    if args.dcf == "voronoi"
                    else "radial stand-in",
                    "step": "one 16-bin 4D CG-SENSE reconstruction (graph replay)",

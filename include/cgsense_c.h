@@ -125,6 +125,14 @@ int cgs_num_bins(const cgs_ctx* ctx);
  * by passing that bin's coordinates. */
 int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf);
 
+/* estimateDensityV3D(traj, sX, sY, sZ, average, cutoff) (functions.h:161-258)
+ * with its readout averaging: average != 0 replaces every volume by the sum
+ * over all readouts of the volumes at its readout position i % sX (the
+ * position clamped to (sX - 1) * cutoff), divided by the total, before the
+ * division by the maximum.  n must be a multiple of sX when averaging;
+ * average == 0 is cgs_voronoi_dcf. */
+int cgs_estimate_density_v3d(const double* k, int64_t n, int32_t sX, int32_t average, double cutoff, float* dcf);
+
 /* Reco::denCorr with Density::IMPORT (IO.cpp:129-156, functions.h:319-335):
  * per-sample real weights D[ns].  NULL clears (Density::NONE). */
 int cgs_set_dcf(cgs_ctx* ctx, const float* dcf);

@@ -52,3 +52,27 @@ def test_voronoi_readout_trajectory(cgs, synth):
     dd = d.reshape(-1, w.n_read)[:, [0, -1]]
     assert np.all(dd == 0)
     assert (d > 0).mean() > 0.5
+
+
+@pytest.mark.parametrize("cutoff", [1.0, 0.75])
+def test_density_readout_averaging(cgs, synth, cutoff):
+    """estimateDensityV3D(average=true, cutoff) (functions.h:212-245),
+    restated in numpy from the per-sample volumes: sums per readout position,
+    divided by the total, positions past (sX-1)*cutoff clamped, then divided
+    by the maximum."""
+    w = synth.scaled(synth.WORKLOADS["cfg3"], (32, 32, 24), (64, 64, 48), n_ch=2, n_bins=4)
+    lines = synth.readout_lines(w)
+    k = synth.wave_trajectory(w, synth.WaveParams(2.0, 2.0), lines=lines)
+    sx = w.n_read
+    kb = k.reshape(len(lines), sx, 3)[::5].reshape(-1, 3)
+    raw = cgs.voronoi_dcf(kb).astype(np.float64)       # volumes / max: averaging is scale-free
+    avg = raw.reshape(-1, sx).sum(0)
+    avg /= avg.sum()
+    pos = np.minimum(np.arange(sx), int((sx - 1) * cutoff))
+    ref = np.tile(avg[pos], kb.shape[0] // sx)
+    ref /= ref.max()
+    d = cgs.estimate_density_v3d(kb, sx, average=True, cutoff=cutoff)
+    assert np.abs(d - ref).max() < 1e-6
+    assert np.array_equal(cgs.estimate_density_v3d(kb, sx, average=False), cgs.voronoi_dcf(kb))
+    with pytest.raises(cgs.CGSError):
+        cgs.estimate_density_v3d(kb[:-1], sx, average=True)
