@@ -94,6 +94,12 @@ struct cgs_ctx {
     long long max_bin = 0;
     std::vector<long long> h_bin_off;
     DevBuf d_sorted, d_rec, d_dcf_sorted, d_bin_off, d_tile_ptr, d_tile_ptr_off, d_tile_idx, d_tile_idx_off;
+    DevBuf d_plane_rng;
+    // loss gradients: derivative records, gathered measured samples, partials
+    DevBuf d_drec, d_gy, d_gpart, d_flag;
+    bool drec_valid = false;
+    bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
+    bool tiles_stale = false;    // spreading lists built from older coordinates
     int ntx = 0, nty = 0, ntz = 0, ntiles = 0;
     // coil maps
     DevBuf d_smaps;
@@ -187,16 +193,18 @@ std::vector<double> deapod_axis(const cgs_params& p, int n)
     return out;
 }
 
-// Host-side bin preparation: spatial sort by home tile and per-tile lists of
-// the samples whose support (nearest point +-3, one cell more than the
-// 5-point taps need) touches the tile.
+// Host-side bin preparation.  Samples are sorted by their home spreading
+// tile (the tile of the nearest grid point).  Each tile then gets the list of
+// the samples whose 5-point support touches it, ordered by nearest x (stable
+// in sorted position), and per x plane of the tile the range of that list
+// whose support covers the plane.  The lists use the nearest points of the
+// device's tap records, so that list membership and the taps agree exactly.
 struct BinPrep {
     std::vector<int> sorted;
     std::vector<int> tile_ptr;
     std::vector<int> tile_idx;
+    std::vector<int> plane_rng;   // [ntiles][TILE_X][2]
 };
-
-
 
 void nearest_point(const double* kk, const int* G, int* nr)
 {
@@ -206,7 +214,7 @@ void nearest_point(const double* kk, const int* G, int* nr)
     }
 }
 
-void prepare_bin(const cgs_ctx* c, const std::vector<int>& samples, BinPrep& out)
+void sort_bin(const cgs_ctx* c, const std::vector<int>& samples, BinPrep& out)
 {
     const int* G = c->G;
     const long long n = (long long)samples.size();
@@ -221,26 +229,45 @@ void prepare_bin(const cgs_ctx* c, const std::vector<int>& samples, BinPrep& out
     }
     for (int t = 0; t < c->ntiles; ++t) count[t + 1] += count[t];
     out.sorted.assign(n, 0);
+    std::vector<int> pos(count.begin(), count.end() - 1);
+    for (long long i = 0; i < n; ++i) out.sorted[pos[key[i]]++] = samples[i];
+}
+
+// nearest: packed nearest points of the bin's sorted samples (device records)
+void tile_lists(const cgs_ctx* c, const unsigned* nearest, long long n, BinPrep& out)
+{
+    const int* G = c->G;
+    auto unpack = [](unsigned u, int* nr) {
+        nr[0] = (int)(u & 2047u);
+        nr[1] = (int)((u >> 11) & 2047u);
+        nr[2] = (int)(u >> 22);
+    };
+    // visit the samples in order of nearest x (counting sort, stable)
+    std::vector<int> xcount(G[0] + 1, 0);
+    for (long long j = 0; j < n; ++j) xcount[(nearest[j] & 2047u) + 1]++;
+    for (int x = 0; x < G[0]; ++x) xcount[x + 1] += xcount[x];
+    std::vector<int> byx(n);
     {
-        std::vector<int> pos(count.begin(), count.end() - 1);
-        for (long long i = 0; i < n; ++i) out.sorted[pos[key[i]]++] = samples[i];
+        std::vector<int> p(xcount.begin(), xcount.end() - 1);
+        for (long long j = 0; j < n; ++j) byx[p[nearest[j] & 2047u]++] = (int)j;
     }
-    out.tile_ptr.assign(c->ntiles + 1, 0);
     auto range = [&](int nr, int a, int T, int nt, int& t0, int& t1) {
-        const int lo = std::max(nr - 3, 0), hi = std::min(nr + 3, G[a] - 1);
+        const int lo = std::max(nr - 2, 0), hi = std::min(nr + 2, G[a] - 1);
         t0 = lo / T;
         t1 = std::min(hi / T, nt - 1);
     };
+    out.tile_ptr.assign(c->ntiles + 1, 0);
+    std::vector<int> fill;
     for (int pass = 0; pass < 2; ++pass) {
-        std::vector<int> fill;
         if (pass == 1) {
             for (int t = 0; t < c->ntiles; ++t) out.tile_ptr[t + 1] += out.tile_ptr[t];
             out.tile_idx.assign(out.tile_ptr[c->ntiles], 0);
             fill.assign(out.tile_ptr.begin(), out.tile_ptr.end() - 1);
         }
-        for (long long j = 0; j < n; ++j) {
+        for (long long m = 0; m < n; ++m) {
+            const int j = byx[m];
             int nr[3];
-            nearest_point(&c->h_k[3 * (size_t)out.sorted[j]], G, nr);
+            unpack(nearest[j], nr);
             int x0, x1, y0, y1, z0, z1;
             range(nr[0], 0, TILE_X, c->ntx, x0, x1);
             range(nr[1], 1, TILE_Y, c->nty, y0, y1);
@@ -250,8 +277,24 @@ void prepare_bin(const cgs_ctx* c, const std::vector<int>& samples, BinPrep& out
                     for (int tz = z0; tz <= z1; ++tz) {
                         const int t = (tx * c->nty + ty) * c->ntz + tz;
                         if (pass == 0) out.tile_ptr[t + 1]++;
-                        else out.tile_idx[fill[t]++] = (int)j;
+                        else out.tile_idx[fill[t]++] = j;
                     }
+        }
+    }
+    // plane ranges: the list is sorted by nearest x, so the samples whose
+    // support [nx - 2, nx + 2] covers plane x form one run
+    out.plane_rng.assign((size_t)c->ntiles * TILE_X * 2, 0);
+    for (int t = 0; t < c->ntiles; ++t) {
+        const int b = out.tile_ptr[t], e = out.tile_ptr[t + 1];
+        const int xt0 = (t / (c->nty * c->ntz)) * TILE_X;
+        int lo = b, hi = b;
+        for (int p = 0; p < TILE_X; ++p) {
+            const int x = xt0 + p;
+            while (lo < e && (int)(nearest[out.tile_idx[lo]] & 2047u) < x - 2) ++lo;
+            if (hi < lo) hi = lo;
+            while (hi < e && (int)(nearest[out.tile_idx[hi]] & 2047u) <= x + 2) ++hi;
+            out.plane_rng[((size_t)t * TILE_X + p) * 2] = lo - b;
+            out.plane_rng[((size_t)t * TILE_X + p) * 2 + 1] = (x < G[0] ? hi : lo) - b;
         }
     }
 }
@@ -270,16 +313,32 @@ void drop_graphs(cgs_ctx* c)
     c->graph_launches.clear();
 }
 
+KbParams kb_params(const cgs_ctx* c)
+{
+    KbParams kb;
+    for (int a = 0; a < 3; ++a) kb.G[a] = c->G[a];
+    kb.w = c->p.kb_w;
+    kb.b = c->p.kb_b;
+    kb.thresh = c->thresh;
+    return kb;
+}
+
 int rebuild_bins(cgs_ctx* c)
 {
     if (!c->bins_dirty) return CGS_OK;
+    if (c->k_host_stale) {
+        CGS_CUDA(c, cudaMemcpyAsync(c->h_k.data(), c->d_k.p, c->h_k.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+        c->k_host_stale = false;
+    }
     if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set");
     drop_graphs(c);
     c->nbins = (int)c->bins.size();
     std::vector<BinPrep> prep(c->nbins);
     c->h_bin_off.assign(c->nbins + 1, 0);
     for (int b = 0; b < c->nbins; ++b) {
-        prepare_bin(c, c->bins[b], prep[b]);
+        sort_bin(c, c->bins[b], prep[b]);
         c->h_bin_off[b + 1] = c->h_bin_off[b] + (long long)c->bins[b].size();
     }
     c->total = c->h_bin_off[c->nbins];
@@ -287,35 +346,49 @@ int rebuild_bins(cgs_ctx* c)
     for (int b = 0; b < c->nbins; ++b) c->max_bin = std::max(c->max_bin, (long long)c->bins[b].size());
     std::vector<int> sorted;
     sorted.reserve(c->total);
+    for (int b = 0; b < c->nbins; ++b) sorted.insert(sorted.end(), prep[b].sorted.begin(), prep[b].sorted.end());
+    CGS_TRY(upload(c, c->d_sorted, sorted.data(), std::max<size_t>(sorted.size(), 1) * sizeof(int)));
+    CGS_TRY(upload(c, c->d_bin_off, c->h_bin_off.data(), c->h_bin_off.size() * sizeof(long long)));
+    // tap records (the device's nearest points decide the tile lists)
+    CGS_CUDA(c, c->d_rec.ensure(std::max<long long>(c->total, 1) * sizeof(TapRecord)));
+    const KbParams kb = kb_params(c);
+    CGS_CUDA(c, launch_tap_records(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, kb, c->d_rec.as<TapRecord>(),
+                                   c->stream));
+    c->drec_valid = false;
+    c->tiles_stale = false;
+    std::vector<unsigned> nearest(std::max<long long>(c->total, 1));
+    {
+        DevBuf d_near;
+        CGS_CUDA(c, d_near.ensure(nearest.size() * sizeof(unsigned)));
+        CGS_CUDA(c, launch_record_nearest(c->d_rec.as<TapRecord>(), c->total, d_near.as<unsigned>(), c->stream));
+        CGS_CUDA(c, cudaMemcpyAsync(nearest.data(), d_near.p, nearest.size() * sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int b = 0; b < c->nbins; ++b)
+        tile_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], prep[b]);
     std::vector<int> tile_ptr;
     std::vector<int> tile_idx;
+    std::vector<int> plane_rng;
     std::vector<long long> tp_off(c->nbins), ti_off(c->nbins);
     for (int b = 0; b < c->nbins; ++b) {
-        sorted.insert(sorted.end(), prep[b].sorted.begin(), prep[b].sorted.end());
         tp_off[b] = (long long)tile_ptr.size();
         tile_ptr.insert(tile_ptr.end(), prep[b].tile_ptr.begin(), prep[b].tile_ptr.end());
         ti_off[b] = (long long)tile_idx.size();
         tile_idx.insert(tile_idx.end(), prep[b].tile_idx.begin(), prep[b].tile_idx.end());
+        plane_rng.insert(plane_rng.end(), prep[b].plane_rng.begin(), prep[b].plane_rng.end());
     }
-    CGS_TRY(upload(c, c->d_sorted, sorted.data(), sorted.size() * sizeof(int)));
-    CGS_TRY(upload(c, c->d_bin_off, c->h_bin_off.data(), c->h_bin_off.size() * sizeof(long long)));
     CGS_TRY(upload(c, c->d_tile_ptr, tile_ptr.data(), tile_ptr.size() * sizeof(int)));
     CGS_TRY(upload(c, c->d_tile_idx, tile_idx.data(), std::max<size_t>(tile_idx.size(), 1) * sizeof(int)));
     CGS_TRY(upload(c, c->d_tile_ptr_off, tp_off.data(), tp_off.size() * sizeof(long long)));
     CGS_TRY(upload(c, c->d_tile_idx_off, ti_off.data(), ti_off.size() * sizeof(long long)));
+    CGS_TRY(upload(c, c->d_plane_rng, plane_rng.data(), std::max<size_t>(plane_rng.size(), 2) * sizeof(int)));
     if (c->has_dcf) {
         std::vector<float> ds(c->total);
         for (long long j = 0; j < c->total; ++j) ds[j] = c->h_dcf[sorted[j]];
         CGS_TRY(upload(c, c->d_dcf_sorted, ds.data(), ds.size() * sizeof(float)));
     }
-    CGS_CUDA(c, c->d_rec.ensure(std::max<long long>(c->total, 1) * sizeof(TapRecord)));
-    KbParams kb;
-    for (int a = 0; a < 3; ++a) kb.G[a] = c->G[a];
-    kb.w = c->p.kb_w;
-    kb.b = c->p.kb_b;
-    kb.thresh = c->thresh;
-    CGS_CUDA(c, launch_tap_records(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, kb, c->d_rec.as<TapRecord>(),
-                                   c->stream));
     CGS_CUDA(c, c->d_yv.ensure(std::max<long long>(c->total, 1) * c->nch * sizeof(float2)));
     // workspace for a group of bins
     const long long per_bin = (long long)c->nch * (c->Nl * c->G[2] + (long long)c->I[0] * c->G[1] * c->G[2] + c->Ng) *
@@ -416,8 +489,10 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
 
 // Adjoint half for bins [b0, b0+nb): samples (yv) -> grid -> image.
 // use_smaps: q[bin] = sum_c conj(S_c) (...) ; else q[coil] per coil (nb == 1).
+// scale < 0: the reference's rescale adj_scale / sqrt(Ng) (Reco.cpp:482,
+// Fourier.cpp:34); scale = 1: the exact adjoint of the forward chain.
 int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_smaps, const float2* pdot,
-              double* partials)
+              double* partials, double scale = -1.0)
 {
     const int Ix = c->I[0], Iy = c->I[1], Iz = c->I[2];
     const int Gx = c->G[0], Gy = c->G[1], Gz = c->G[2];
@@ -434,6 +509,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
         sa.tile_ptr_off = c->d_tile_ptr_off.as<long long>();
         sa.tile_idx_off = c->d_tile_idx_off.as<long long>();
         sa.tile_idx = c->d_tile_idx.as<int>();
+        sa.plane_rng = c->d_plane_rng.as<int2>();
         sa.bin0 = b0;
         sa.nch = c->nch;
         const int nchunk = (c->nch + spread_max_coils() - 1) / spread_max_coils();
@@ -482,7 +558,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
     az.apx = c->ap[0].as<float>();
     az.apy = c->ap[1].as<float>();
     az.apz = c->ap[2].as<float>();
-    az.scale = (float)c->adj_scale_total;
+    az.scale = (float)(scale < 0 ? c->adj_scale_total : scale);
     az.q = q;
     az.p = pdot;
     az.partials = partials;
@@ -530,11 +606,14 @@ int check_timeout(cgs_ctx* c)
     return CGS_OK;
 }
 
-int check_ready(cgs_ctx* c, bool need_smaps)
+// need_tiles: the call spreads, so the tile lists must match the current
+// coordinates (after cgs_update_trajectory_d they are rebuilt here).
+int check_ready(cgs_ctx* c, bool need_smaps, bool need_tiles = true)
 {
     if (!c) return CGS_ERR_ARG;
     if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set (cgs_set_trajectory)");
     if (need_smaps && !c->smaps_set) return fail(c, CGS_ERR_STATE, "no coil maps set (cgs_set_smaps)");
+    if (need_tiles && c->tiles_stale) c->bins_dirty = true;
     CGS_TRY(rebuild_bins(c));
     return CGS_OK;
 }
@@ -1282,6 +1361,125 @@ int cgs_profile_apply(cgs_ctx* c, int32_t bin0, int32_t nb, const float* x, floa
     }
     for (auto& e : ev) cudaEventDestroy(e);
     return st;
+}
+
+int cgs_update_trajectory_d(cgs_ctx* c, const double* k)
+{
+    if (!c || !k) return CGS_ERR_ARG;
+    if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set (cgs_set_trajectory)");
+    CGS_CUDA(c, c->d_flag.ensure(sizeof(int)));
+    CGS_CUDA(c, cudaMemsetAsync(c->d_flag.p, 0, sizeof(int), c->stream));
+    CGS_CUDA(c, launch_check_finite(k, 3 * c->ns, c->d_flag.as<int>(), c->stream));
+    int bad = 0;
+    CGS_CUDA(c, cudaMemcpyAsync(&bad, c->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (bad) return fail(c, CGS_ERR_NONFINITE, "non-finite trajectory coordinate");
+    CGS_CUDA(c, cudaMemcpyAsync(c->d_k.p, k, (size_t)(3 * c->ns) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                c->stream));
+    c->k_host_stale = true;
+    c->tiles_stale = true;
+    c->drec_valid = false;
+    if (!c->bins_dirty)   // same samples, same sorted order: new tap records only
+        CGS_CUDA(c, launch_tap_records(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, kb_params(c),
+                                       c->d_rec.as<TapRecord>(), c->stream));
+    return CGS_OK;
+}
+
+int cgs_loss_grad_d(cgs_ctx* c, int32_t bin, const void* x, const void* y, double* loss, void* grad_x, void* grad_k)
+{
+    CGS_TRY(check_ready(c, true, grad_x != nullptr));
+    if (!x || !y || !loss) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (bin < 0 || bin >= c->nbins) return fail(c, CGS_ERR_ARG, "bin out of range");
+    const long long s0 = c->h_bin_off[bin], n = c->h_bin_off[bin + 1] - s0;
+    if (!c->drec_valid) {
+        CGS_CUDA(c, c->d_drec.ensure(std::max<long long>(c->total, 1) * sizeof(TapRecord)));
+        CGS_CUDA(c, launch_tap_grad_records(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, kb_params(c),
+                                            c->d_drec.as<TapRecord>(), c->stream));
+        c->drec_valid = true;
+    }
+    // forward chain of the bin: every coil's grid (the interpolation it ends
+    // with is recomputed below together with the derivatives)
+    CGS_TRY(fwd_chain(c, bin, 1, reinterpret_cast<const float2*>(x), 0, 0, true, false));
+    CGS_CUDA(c, c->d_gy.ensure(std::max<long long>(c->total, 1) * c->nch * sizeof(float2)));
+    CGS_CUDA(c, launch_gather_samples(reinterpret_cast<const float2*>(y), c->ns, c->d_sorted.as<int>() + s0, n, c->nch,
+                                      nullptr, c->d_gy.as<float2>() + s0 * c->nch, c->stream));
+    const int nblk = interp_grad_blocks(n);
+    CGS_CUDA(c, c->d_gpart.ensure((size_t)nblk * sizeof(double)));
+    if (grad_k) CGS_CUDA(c, cudaMemsetAsync(grad_k, 0, (size_t)(3 * c->ns) * sizeof(float), c->stream));
+    InterpGradArgs ga{};
+    ga.grid = c->d_grid.as<float2>();
+    ga.coil_stride = c->Ng;
+    ga.rec = c->d_rec.as<TapRecord>();
+    ga.drec = c->d_drec.as<TapRecord>();
+    ga.ymeas = c->d_gy.as<float2>();
+    ga.dcf = c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr;
+    ga.sorted = c->d_sorted.as<int>();
+    ga.s0 = s0;
+    ga.n = n;
+    ga.nch = c->nch;
+    for (int a = 0; a < 3; ++a) ga.G[a] = c->G[a];
+    ga.thresh = c->thresh;
+    ga.rv = grad_x ? c->d_yv.as<float2>() : nullptr;
+    ga.grad_k = reinterpret_cast<float*>(grad_k);
+    ga.partials = c->d_gpart.as<double>();
+    CGS_LAUNCH(c, launch_interp_grad(ga, c->stream));
+    if (grad_x)   // sum_c conj(S_c) E_c^* (D r_c): the adjoint chain at the exact-adjoint scale
+        CGS_TRY(adj_chain(c, bin, 1, reinterpret_cast<float2*>(grad_x), c->Ni, true, nullptr, nullptr, 1.0));
+    std::vector<double> h(nblk);
+    CGS_CUDA(c, cudaMemcpyAsync(h.data(), c->d_gpart.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    double L = 0.0;
+    for (double v : h) L += v;
+    *loss = L;
+    return check_timeout(c);
+}
+
+int cgs_loss_grad_fp64_d(cgs_ctx* c, int32_t bin, const void* x, const void* y, double* loss, void* grad_x,
+                         void* grad_k)
+{
+    CGS_TRY(check_ready(c, true, false));
+    if (!x || !y || !loss) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (bin < 0 || bin >= c->nbins) return fail(c, CGS_ERR_ARG, "bin out of range");
+    if (!c->z_plan_ok) {
+        if (cufftPlan3d(&c->z_plan, c->G[0], c->G[1], c->G[2], CUFFT_Z2Z) != CUFFT_SUCCESS)
+            return fail(c, CGS_ERR_CUDA, "cufftPlan3d (Z2Z) failed");
+        c->z_plan_ok = true;
+    }
+    if (cufftSetStream(c->z_plan, c->stream) != CUFFT_SUCCESS) return fail(c, CGS_ERR_CUDA, "cufftSetStream failed");
+    const long long s0 = c->h_bin_off[bin], n = c->h_bin_off[bin + 1] - s0;
+    CGS_CUDA(c, c->d64_grid.ensure(c->Ng * sizeof(double2)));
+    CGS_CUDA(c, c->d64_y.ensure(std::max<long long>(c->max_bin, 1) * sizeof(double2)));
+    CGS_CUDA(c, c->d64_part.ensure(std::max<long long>((c->max_bin + 255) / 256, 2048) * sizeof(double)));
+    Fp64Args P{};
+    for (int a2 = 0; a2 < 3; ++a2) {
+        P.g.I[a2] = c->I[a2];
+        P.g.G[a2] = c->G[a2];
+        P.g.lo[a2] = c->lo[a2];
+        P.ap[a2] = c->ap[a2].as<float>();
+    }
+    P.g.Ni = c->Ni;
+    P.g.Ng = c->Ng;
+    P.nch = c->nch;
+    P.smaps = c->d_smaps.as<float2>();
+    P.scale = 1.0;
+    P.thresh = c->thresh;
+    P.plan = c->z_plan;
+    P.s = c->stream;
+    P.grid = c->d64_grid.as<double2>();
+    P.y = c->d64_y.as<double2>();
+    // tap threshold in double: kb_thresh times the kernel's peak (Reco.cpp:716-717)
+    double peak = 1.0;
+    for (int a = 0; a < 3; ++a) {
+        const double dk = 1.0 / (double)(c->G[a] - 1);
+        peak *= std::cyl_bessel_i(0.0, (double)c->p.kb_b) / (100.0 * c->p.kb_w * dk);
+    }
+    CGS_CUDA(c, fp64_loss_grad(P, c->d_k.as<double>(), c->d_sorted.as<int>() + s0, n,
+                               c->has_dcf ? c->d_dcf_sorted.as<float>() + s0 : nullptr, c->p.kb_w, c->p.kb_b,
+                               peak * c->p.kb_thresh, reinterpret_cast<const float2*>(y), c->ns,
+                               reinterpret_cast<const double2*>(x), loss, reinterpret_cast<double2*>(grad_x),
+                               reinterpret_cast<double*>(grad_k), c->d64_part.as<double>(), 0));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return CGS_OK;
 }
 
 }  // extern "C"

@@ -122,13 +122,33 @@ struct SpreadArgs {
     const int* tile_ptr;       // per bin: [ntiles+1] offsets into tile_idx (relative to bin)
     const long long* tile_ptr_off;  // [nbins] start of each bin's tile_ptr array
     const long long* tile_idx_off;  // [nbins] start of each bin's tile_idx array
-    const int* tile_idx;       // sample positions relative to the bin start
+    const int* tile_idx;       // sample positions relative to the bin start, sorted by nearest x
+    const int2* plane_rng;     // [nbins][ntiles][TILE_X]: entries of the tile's list whose
+                               // x support covers plane x0 + p (relative to the list start)
     int bin0;
     int nch;
     int cc;                    // coils per block (chunk)
     int G[3];
     int ntx, nty, ntz;         // tiles per axis
     float thresh;
+};
+
+// Loss gradient pass (grad.cu): one bin's samples [s0, s0 + n) in sorted order.
+struct InterpGradArgs {
+    const float2* grid;        // coil c at grid + c * coil_stride (one bin)
+    long long coil_stride;
+    const TapRecord* rec;      // tap records (sorted order)
+    const TapRecord* drec;     // derivative records (sorted order)
+    const float2* ymeas;       // measured samples [sorted][nch]
+    const float* dcf;          // sorted density weights, or null
+    const int* sorted;         // sorted position -> global sample index
+    long long s0, n;
+    int nch;
+    int G[3];
+    float thresh;
+    float2* rv;                // out: D r [sorted][nch], or null
+    float* grad_k;             // out: [ns][3] by global index, or null
+    double* partials;          // out: [blocks] loss partial sums
 };
 
 }  // namespace cgs

@@ -173,6 +173,120 @@ __global__ void k64_xpay(double2* p, const double2* __restrict__ r, double sr, d
     p[i] = make_double2(r[i].x + sr * a.x - si * a.y, r[i].y + sr * a.y + si * a.x);
 }
 
+
+// KB factor and its derivative in double from a double coordinate (the
+// extension used by the gradient reference; cf. Reco.h:218-242).
+__device__ void kb64(double ka, int gi, double dk, double w, double b, double& f, double& df)
+{
+    const double d = ka - (double)gi * dk;
+    if (fabs(d) > 0.5 * w * dk) {
+        f = df = 0.0;
+        return;
+    }
+    const double t = 2.0 * d / (w * dk);
+    const double s2 = 1.0 - t * t;
+    const double s = s2 > 0.0 ? sqrt(s2) : 0.0;
+    const double C = 100.0 * w * dk;
+    f = cyl_bessel_i0(b * s) / C;
+    const double i1s = s > 1e-12 ? cyl_bessel_i1(b * s) / s : 0.5 * b;
+    df = -i1s * b * t * (2.0 / (w * dk)) / C;
+}
+
+struct Taps64 {
+    double f[3][5], df[3][5];
+    int nr[3];
+};
+
+__device__ void taps64(const double* kk, const PlainGeom& g, double w, double b, Taps64& t)
+{
+    for (int a = 0; a < 3; ++a) {
+        const int N = g.G[a];
+        const double dk = 1.0 / (double)(N - 1);
+        int nr = (int)__dadd_rn(__dmul_rn((double)(N - 1), kk[a]), 0.5);
+        nr = nr < 0 ? 0 : (nr > N - 1 ? N - 1 : nr);
+        t.nr[a] = nr;
+        for (int j = 0; j < 5; ++j) {
+            const int gi = nr - 2 + j;
+            if (gi < 0 || gi > N - 1) {
+                t.f[a][j] = t.df[a][j] = 0.0;
+                continue;
+            }
+            kb64(kk[a], gi, dk, w, b, t.f[a][j], t.df[a][j]);
+        }
+    }
+}
+
+// One coil: loss partials, grad_k += per-coil term, rv = D r (sorted order).
+__global__ void __launch_bounds__(256) k64_loss_grad(const double2* __restrict__ grid, const double* __restrict__ k,
+                                                     const int* __restrict__ sorted, long long n, PlainGeom g,
+                                                     double w, double b, double thresh,
+                                                     const float2* __restrict__ yc, const float* dcf,
+                                                     double* grad_k, double2* rv, double* partials)
+{
+    __shared__ double s_red[8];
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double loss = 0.0;
+    if (j < n) {
+        const long long gi = sorted[j];
+        Taps64 t;
+        taps64(k + 3 * gi, g, w, b, t);
+        double yr = 0, yi = 0, dr[3] = {0, 0, 0}, di[3] = {0, 0, 0};
+        for (int jx = 0; jx < 5; ++jx)
+            for (int jy = 0; jy < 5; ++jy)
+                for (int jz = 0; jz < 5; ++jz) {
+                    const double wt = t.f[0][jx] * t.f[1][jy] * t.f[2][jz];
+                    if (!(wt > thresh)) continue;
+                    const long long idx =
+                        ((long long)(t.nr[0] - 2 + jx) * g.G[1] + (t.nr[1] - 2 + jy)) * g.G[2] + (t.nr[2] - 2 + jz);
+                    const double2 v = grid[idx];
+                    yr += wt * v.x;
+                    yi += wt * v.y;
+                    const double e[3] = {t.df[0][jx] * t.f[1][jy] * t.f[2][jz], t.f[0][jx] * t.df[1][jy] * t.f[2][jz],
+                                         t.f[0][jx] * t.f[1][jy] * t.df[2][jz]};
+                    for (int a = 0; a < 3; ++a) {
+                        dr[a] += e[a] * v.x;
+                        di[a] += e[a] * v.y;
+                    }
+                }
+        const double D = dcf ? (double)dcf[j] : 1.0;
+        const double rr = yr - (double)yc[gi].x, ri = yi - (double)yc[gi].y;
+        loss = 0.5 * D * (rr * rr + ri * ri);
+        if (grad_k)
+            for (int a = 0; a < 3; ++a) grad_k[3 * gi + a] += D * (rr * dr[a] + ri * di[a]);
+        if (rv) rv[j] = make_double2(D * rr, D * ri);
+    }
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = loss;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double sum = 0.0;
+        for (int i = 0; i < 8; ++i) sum += s_red[i];
+        partials[blockIdx.x] = sum;
+    }
+}
+
+// transpose of the interpolation with the double taps (double atomics)
+__global__ void k64_spread_taps(const double2* __restrict__ v, const double* __restrict__ k,
+                                const int* __restrict__ sorted, long long n, PlainGeom g, double w, double b,
+                                double thresh, double2* grid)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    Taps64 t;
+    taps64(k + 3 * (long long)sorted[j], g, w, b, t);
+    const double2 d = v[j];
+    for (int jx = 0; jx < 5; ++jx)
+        for (int jy = 0; jy < 5; ++jy)
+            for (int jz = 0; jz < 5; ++jz) {
+                const double wt = t.f[0][jx] * t.f[1][jy] * t.f[2][jz];
+                if (!(wt > thresh)) continue;
+                const long long idx =
+                    ((long long)(t.nr[0] - 2 + jx) * g.G[1] + (t.nr[1] - 2 + jy)) * g.G[2] + (t.nr[2] - 2 + jz);
+                atomicAdd(&grid[idx].x, wt * d.x);
+                atomicAdd(&grid[idx].y, wt * d.y);
+            }
+}
+
 }  // namespace
 
 
@@ -280,6 +394,45 @@ cudaError_t fp64_solve_bin(const Fp64Args& P, const TapRecord* rec, const float*
     }
     *iters = it;
     return cudaGetLastError();
+}
+
+cudaError_t fp64_loss_grad(const Fp64Args& P, const double* k, const int* sorted, long long n, const float* dcf,
+                           double kb_w, double kb_b, double thresh, const float2* y, long long ns,
+                           const double2* x, double* loss, double2* grad_x, double* grad_k, double* partials,
+                           int /*nblk*/)
+{
+    const PlainGeom& g = P.g;
+    const unsigned nblk = nb64(std::max<long long>(n, 1));
+    std::vector<double> h(nblk);
+    double total = 0.0;
+    cudaError_t e = cudaSuccess;
+    if (grad_k) e = cudaMemsetAsync(grad_k, 0, (size_t)ns * 3 * sizeof(double), P.s);
+    for (int c = 0; c < P.nch && e == cudaSuccess; ++c) {
+        const float2* S = P.smaps + (long long)c * g.Ni;
+        k64_pad<<<nb64(g.Ng), 256, 0, P.s>>>(x, S, P.ap[0], P.ap[1], P.ap[2], g, P.grid);
+        k64_sign<<<nb64(g.Ng), 256, 0, P.s>>>(P.grid, g);
+        if (cufftExecZ2Z(P.plan, (cufftDoubleComplex*)P.grid, (cufftDoubleComplex*)P.grid, CUFFT_FORWARD) != CUFFT_SUCCESS)
+            return cudaErrorUnknown;
+        k64_sign<<<nb64(g.Ng), 256, 0, P.s>>>(P.grid, g);
+        k64_loss_grad<<<nblk, 256, 0, P.s>>>(P.grid, k, sorted, n, g, kb_w, kb_b, thresh, y + (long long)c * ns, dcf,
+                                            grad_k, grad_x ? P.y : nullptr, partials);
+        e = cudaMemcpyAsync(h.data(), partials, nblk * sizeof(double), cudaMemcpyDeviceToHost, P.s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(P.s);
+        for (unsigned i = 0; i < nblk; ++i) total += h[i];
+        if (grad_x) {
+            cudaMemsetAsync(P.grid, 0, g.Ng * sizeof(double2), P.s);
+            if (n > 0) k64_spread_taps<<<nb64(n), 256, 0, P.s>>>(P.y, k, sorted, n, g, kb_w, kb_b, thresh, P.grid);
+            k64_sign<<<nb64(g.Ng), 256, 0, P.s>>>(P.grid, g);
+            if (cufftExecZ2Z(P.plan, (cufftDoubleComplex*)P.grid, (cufftDoubleComplex*)P.grid, CUFFT_INVERSE) !=
+                CUFFT_SUCCESS)
+                return cudaErrorUnknown;
+            k64_sign<<<nb64(g.Ng), 256, 0, P.s>>>(P.grid, g);
+            k64_crop<<<nb64(g.Ni), 256, 0, P.s>>>(P.grid, S, P.ap[0], P.ap[1], P.ap[2], 1.0, g, c == 0, grad_x);
+        }
+    }
+    *loss = total;
+    if (e == cudaSuccess) e = cudaGetLastError();
+    return e;
 }
 
 }  // namespace cgs

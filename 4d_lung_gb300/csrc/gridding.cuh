@@ -127,13 +127,14 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
 
 // ---------------------------------------------------------------------------
 // Spreading (Reco.cpp:492-504) without atomics.  One block owns one
-// TILE_X x TILE_Y x TILE_Z tile of the grid for a chunk of coils and
-// visits, in sorted order, every sample whose support touches the tile.
-// Warp w owns the grid plane x = tile_x0 + w; lane l owns (y, z) offset
-// (l / 5, l % 5) of the current sample.  Every grid value is therefore
-// updated by one lane at a time in a fixed sample order: the result is
-// deterministic.  The whole tile (zeros included) is then stored, so the
-// grid needs no separate clearing.
+// TILE_X x TILE_Y x TILE_Z tile of the grid for a chunk of coils.  The
+// tile's list holds every sample whose support touches the tile, ordered by
+// nearest x; the block stages it in batches.  Warp w owns the grid plane
+// x = tile_x0 + w and walks only its run of the list (the samples whose x
+// support covers the plane); lane l owns (y, z) offset (l / 5, l % 5) of the
+// current sample.  Every grid value is therefore updated by one lane at a
+// time in a fixed sample order: the result is deterministic.  The whole tile
+// (zeros included) is then stored, so the grid needs no separate clearing.
 // ---------------------------------------------------------------------------
 
 constexpr int SPREAD_BATCH = 32;   // samples staged per round
@@ -169,6 +170,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
     const int warp = tid >> 5, lane = tid & 31;
     const int gx = x0 + warp;
     const int jy = lane / 5, jz = lane - 5 * (lane / 5);
+    const int2 run = a.plane_rng[((long long)bin * gridDim.x + tile) * TILE_X + warp];
 
     for (int s = beg; s < end; s += SPREAD_BATCH) {
         const int nbat = min(SPREAD_BATCH, end - s);
@@ -183,8 +185,9 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
             s_val[j * CC + c] = a.yv[si * a.nch + c0 + c];
         }
         __syncthreads();
+        const int j0 = max(run.x - (s - beg), 0), j1 = min(run.y - (s - beg), nbat);
         if (lane < 25) {
-            for (int j = 0; j < nbat; ++j) {
+            for (int j = j0; j < j1; ++j) {
                 const float* w = reinterpret_cast<const float*>(&s_rec[j]);
                 int nx, ny, nz;
                 unpack_nearest(__float_as_uint(w[15]), nx, ny, nz);

@@ -99,6 +99,19 @@ cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nb
     return cudaGetLastError();
 }
 
+__global__ void k_record_nearest(const TapRecord* __restrict__ rec, long long n, unsigned* __restrict__ out)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = __float_as_uint(rec[i].q[3].w);
+}
+
+cudaError_t launch_record_nearest(const TapRecord* rec, long long n, unsigned* out, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_record_nearest<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(rec, n, out);
+    return cudaGetLastError();
+}
+
 // coils per spreading block: staged values use a row of SPREAD_CC_MAX
 constexpr int SPREAD_CC_MAX = 12;
 

@@ -31,6 +31,8 @@ cudaError_t launch_tap_records(const double* k, const int* sample_idx, long long
                                TapRecord* out, cudaStream_t s);
 cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, cudaStream_t s);
 cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, cudaStream_t s);
+// packed nearest grid point of each tap record
+cudaError_t launch_record_nearest(const TapRecord* rec, long long n, unsigned* out, cudaStream_t s);
 size_t spread_smem_bytes(int cc);
 // one-time kernel attributes (dynamic shared memory limits); call per device
 cudaError_t kernels_init();
@@ -86,6 +88,13 @@ cudaError_t plain_rhs(const PlainArgs& P, const TapRecord* rec, const float* dcf
                       const float2* data, long long ns, float2* b, long long* launches);
 cudaError_t plain_dot(const float2* p, const float2* q, long long n, double* partials, int nblocks, cudaStream_t s);
 
+// Loss gradients (grad.cu)
+cudaError_t launch_tap_grad_records(const double* k, const int* sample_idx, long long n, const KbParams& kb,
+                                    TapRecord* out, cudaStream_t s);
+int interp_grad_blocks(long long n);
+cudaError_t launch_interp_grad(const InterpGradArgs& a, cudaStream_t s);
+cudaError_t launch_check_finite(const double* v, long long n, int* bad, cudaStream_t s);
+
 // Full-FP64 form (fp64.cu): the precision reference on the GPU.
 struct Fp64Args {
     PlainGeom g;
@@ -103,5 +112,12 @@ cudaError_t fp64_solve_bin(const Fp64Args& P, const TapRecord* rec, const float*
                            const float2* data, long long ns, double2* x, double2* r, double2* p, double2* q,
                            double* partials, double thresh, int max_iter, double* residuals, int* iters,
                            double2* x_trace, long long trace_stride);
+// FP64 loss and gradients of one bin: KB weights and derivatives in double
+// from the double coordinates; grad_k (double [ns][3], global index) is
+// accumulated over coils; grad_x (double complex [Ni]) written when non-null.
+cudaError_t fp64_loss_grad(const Fp64Args& P, const double* k, const int* sorted, long long n, const float* dcf,
+                           double kb_w, double kb_b, double thresh, const float2* y, long long ns,
+                           const double2* x, double* loss, double2* grad_x, double* grad_k, double* partials,
+                           int nblk);
 
 }  // namespace cgs

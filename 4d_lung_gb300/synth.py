@@ -161,6 +161,52 @@ def wave_trajectory(w: Workload, wave: WaveParams | None = None, lines=None):
     return k.reshape(-1, 3)
 
 
+WAVE_PARAM_NAMES = ("amp_y", "amp_z", "phase_y", "phase_z", "delay_y", "delay_z")
+
+
+def wave_jacobian(w: Workload, wave: WaveParams | None = None, lines=None):
+    """dk/dtheta of wave_trajectory: [n_lines * n_read][3][6] for theta =
+    (amp_y, amp_z, phase_y, phase_z, delay_y, delay_z); kx does not depend
+    on theta."""
+    wave = wave or WaveParams(w.wave_cells, w.wave_cells)
+    if lines is None:
+        lines = readout_lines(w)
+    G = np.array(w.grid, np.float64)
+    n = w.n_read
+    t = np.arange(n) / n
+    om = 2 * np.pi * w.wave_cycles
+    py = om * (t - wave.delay_y) + wave.phase_y
+    pz = om * (t - wave.delay_z) + wave.phase_z
+    J = np.zeros((n, 3, 6))
+    J[:, 1, 0] = np.sin(py) / (G[1] - 1)
+    J[:, 1, 2] = wave.amp_y * np.cos(py) / (G[1] - 1)
+    J[:, 1, 4] = -wave.amp_y * np.cos(py) * om / (G[1] - 1)
+    J[:, 2, 1] = np.cos(pz) / (G[2] - 1)
+    J[:, 2, 3] = -wave.amp_z * np.sin(pz) / (G[2] - 1)
+    J[:, 2, 5] = wave.amp_z * np.sin(pz) * om / (G[2] - 1)
+    return np.broadcast_to(J[None], (lines.shape[0], n, 3, 6)).reshape(-1, 3, 6)
+
+
+def wave_from_vector(v):
+    return WaveParams(*[float(a) for a in v])
+
+
+def perturbed_wave(w: Workload, frac=0.05, seed=5):
+    """Nominal wave parameters perturbed by up to `frac`: amplitudes by a
+    relative frac, phases by frac radians, delays by frac of a wave period."""
+    rng = np.random.default_rng(seed)
+    u = rng.uniform(-1.0, 1.0, 6) * frac
+    nom = WaveParams(w.wave_cells, w.wave_cells)
+    return WaveParams(nom.amp_y * (1 + u[0]), nom.amp_z * (1 + u[1]), u[2], u[3],
+                      u[4] / w.wave_cycles, u[5] / w.wave_cycles)
+
+
+def wave_param_scale(w: Workload):
+    """Natural unit of each wave parameter (cells, cells, rad, rad, period,
+    period): finite-difference steps are taken in these units."""
+    return np.array([1.0, 1.0, 1.0, 1.0, 1.0 / w.wave_cycles, 1.0 / w.wave_cycles])
+
+
 # ---------------------------------------------------------------------------
 # respiratory bins
 # ---------------------------------------------------------------------------

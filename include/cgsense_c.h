@@ -235,6 +235,33 @@ int64_t cgs_last_launch_count(const cgs_ctx* ctx);
 int cgs_profile_apply(cgs_ctx* ctx, int32_t bin0, int32_t nb, const float* x_dev, float* q_dev,
                       float* stage_ms, int32_t max_stages, int32_t* n_stages);
 
+/* --- Differentiation (an extension: the reference has no derivatives) ---
+ * Data-consistency loss of bin `bin`, with E_c the forward operator of
+ * nufftFWD (Reco.cpp:521-553) applied to S_c x and D the density weights:
+ *   L      = 1/2 sum_c sum_i D_i |(E_c S_c x)_i - y_ci|^2
+ *   grad_x = dL/dRe(x) + i dL/dIm(x) = sum_c conj(S_c) E_c^* (D r_c)
+ *            (E^* the exact adjoint: no 1e-3 / sqrt(Ng) rescale)
+ *   grad_k = dL/dk[i][a], k in the reference's [0,1] units; 0 for samples
+ *            outside the bin.
+ * Device pointers: x complex64 [Ni]; y complex64 [n_ch][ns] in the
+ * reference's sample order; grad_x complex64 [Ni] or NULL; grad_k float
+ * [ns][3] or NULL.  FP32 gridding and FFT (the product path); *loss is the
+ * FP64 sum of per-sample FP32 terms. */
+int cgs_loss_grad_d(cgs_ctx* ctx, int32_t bin, const void* x_dev, const void* y_dev, double* loss,
+                    void* grad_x_dev, void* grad_k_dev);
+
+/* The same loss and gradients in FP64 (the gradient reference): x and
+ * grad_x complex128, grad_k double [ns][3]; KB weights and their
+ * derivatives in double from the double coordinates, cuFFT Z2Z. */
+int cgs_loss_grad_fp64_d(cgs_ctx* ctx, int32_t bin, const void* x_dev, const void* y_dev, double* loss,
+                         void* grad_x_dev, void* grad_k_dev);
+
+/* New coordinates for the same samples (device pointer, double [ns][3]),
+ * e.g. one step of trajectory self-calibration: the tap records are
+ * recomputed on the device; the spreading lists are rebuilt lazily by the
+ * next call that spreads. */
+int cgs_update_trajectory_d(cgs_ctx* ctx, const double* k_dev);
+
 /* Centred 3-D FFT (sign -1 forward, +1 backward, unscaled) that allocates no
  * device memory, for callers that cannot let a library allocate: code
  * running under a host application that owns all device memory through its

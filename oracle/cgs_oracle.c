@@ -611,3 +611,178 @@ void cgso_wave_caipi(const cgso_wave* wv, double* k_out)
     }
     free(traj);
 }
+
+/* ---------------------------------------------------------------------- */
+/* Data-consistency loss and gradients (extension; no reference code)      */
+/* ---------------------------------------------------------------------- */
+
+double cgso_bessel_i1(double x)
+{
+    /* I1(x) = sum_m (x/2)^(2m+1) / (m! (m+1)!) */
+    const double h = 0.5 * x, q = h * h;
+    double term = h, sum = h;
+    for (int m = 1; m < 500; ++m) {
+        term *= q / ((double)m * (double)(m + 1));
+        sum += term;
+        if (fabs(term) < fabs(sum) * 1e-17) break;
+    }
+    return sum;
+}
+
+/* KB factor of one axis and its derivative with respect to the sample
+ * coordinate ka, for grid index g: f = I0(b s) / (100 w dk), s = sqrt(1 - t^2),
+ * t = 2 (ka - g dk) / (w dk) (Reco.h:218-242 in double).
+ * df/dka = -(I1(b s) / s) b t (2 / (w dk)) / (100 w dk); I1(b s)/s -> b/2 at s = 0. */
+static void kb_axis(double ka, int g, double dk, double w, double b, double* f, double* df)
+{
+    const double d = ka - (double)g * dk;
+    if (fabs(d) > 0.5 * w * dk) {
+        *f = 0.0;
+        *df = 0.0;
+        return;
+    }
+    const double t = 2.0 * d / (w * dk);
+    const double s2 = 1.0 - t * t;
+    const double s = s2 > 0.0 ? sqrt(s2) : 0.0;
+    const double C = 100.0 * w * dk;
+    *f = cgso_bessel_i0(b * s) / C;
+    const double i1s = s > 1e-12 ? cgso_bessel_i1(b * s) / s : 0.5 * b;
+    *df = -i1s * b * t * (2.0 / (w * dk)) / C;
+}
+
+double cgso_loss_grad(const cgso_params* p, const double* k, int64_t ns, const R* kft, const R* smaps,
+                      const float* dcf, const R* x, const R* y, R* grad_x, double* grad_k)
+{
+    const int nch = p->n_ch;
+    const int* G = p->grid;
+    const size_t ni = n_img(p), ng = n_grid(p);
+    const int order = p->kb_order;
+    const double w = p->kb_w, b = p->kb_b;
+    double dk[3], peak = 1.0;
+    for (int a = 0; a < 3; ++a) {
+        dk[a] = 1.0 / (double)(G[a] - 1);
+        peak *= cgso_bessel_i0(b) / (100.0 * w * dk[a]);
+    }
+    const double thresh = peak * p->kb_thresh;
+    plans3 pl = make_plans(p);
+    double* lossc = (double*)calloc((size_t)nch, sizeof(double));
+    double* gk = grad_k ? (double*)calloc((size_t)nch * ns * 3, sizeof(double)) : NULL;
+    ofc_t* gx = grad_x ? (ofc_t*)calloc((size_t)nch * ni, sizeof(ofc_t)) : NULL;
+#pragma omp parallel for schedule(dynamic)
+    for (int c = 0; c < nch; ++c) {
+        const ofc_t* S = (const ofc_t*)smaps + (size_t)c * ni;
+        const ofc_t* xx = (const ofc_t*)x;
+        const ofc_t* yc = (const ofc_t*)y + (size_t)c * ns;
+        ofc_t* img = (ofc_t*)malloc(sizeof(ofc_t) * ni);
+        ofc_t* grid = (ofc_t*)malloc(sizeof(ofc_t) * ng);
+        for (size_t i = 0; i < ni; ++i) {
+            img[i].re = xx[i].re * S[i].re - xx[i].im * S[i].im;
+            img[i].im = xx[i].re * S[i].im + xx[i].im * S[i].re;
+        }
+        pad_apod(p, (const ofc_t*)kft, img, grid);
+        centred_fft_plans(G, grid, -1, 0, pl.p[0], pl.p[1], pl.p[2]);
+        ofc_t* acc = gx ? (ofc_t*)calloc(ng, sizeof(ofc_t)) : NULL;
+        double lc = 0.0;
+        for (int64_t i = 0; i < ns; ++i) {
+            const double* kk = k + 3 * i;
+            int nr[3];
+            double f[3][16], df[3][16];
+            for (int a = 0; a < 3; ++a) {
+                nr[a] = (int)((G[a] - 1) * kk[a] + 0.5);
+                for (int j = -order; j <= order; ++j) {
+                    const int g = nr[a] + j;
+                    if (g < 0 || g > G[a] - 1) {
+                        f[a][j + order] = df[a][j + order] = 0.0;
+                        continue;
+                    }
+                    kb_axis(kk[a], g, dk[a], w, b, &f[a][j + order], &df[a][j + order]);
+                }
+            }
+            double yr = 0, yi = 0, dr[3] = {0, 0, 0}, di[3] = {0, 0, 0};
+            for (int i1 = 0; i1 <= 2 * order; ++i1)
+                for (int i2 = 0; i2 <= 2 * order; ++i2)
+                    for (int i3 = 0; i3 <= 2 * order; ++i3) {
+                        const double wt = f[0][i1] * f[1][i2] * f[2][i3];
+                        if (!(wt > thresh)) continue;
+                        const size_t gi = ((size_t)(nr[0] - order + i1) * G[1] + (nr[1] - order + i2)) * G[2] +
+                                          (nr[2] - order + i3);
+                        const double gr = grid[gi].re, gim = grid[gi].im;
+                        yr += wt * gr;
+                        yi += wt * gim;
+                        const double dw[3] = {df[0][i1] * f[1][i2] * f[2][i3], f[0][i1] * df[1][i2] * f[2][i3],
+                                              f[0][i1] * f[1][i2] * df[2][i3]};
+                        for (int a = 0; a < 3; ++a) {
+                            dr[a] += dw[a] * gr;
+                            di[a] += dw[a] * gim;
+                        }
+                    }
+            const double D = dcf ? (double)dcf[i] : 1.0;
+            const double rr = yr - (double)yc[i].re, ri = yi - (double)yc[i].im;
+            lc += 0.5 * D * (rr * rr + ri * ri);
+            if (gk)
+                for (int a = 0; a < 3; ++a) gk[((size_t)c * ns + i) * 3 + a] = D * (rr * dr[a] + ri * di[a]);
+            if (acc) {
+                /* spread D r with the same taps (the transpose of the interpolation) */
+                for (int i1 = 0; i1 <= 2 * order; ++i1)
+                    for (int i2 = 0; i2 <= 2 * order; ++i2)
+                        for (int i3 = 0; i3 <= 2 * order; ++i3) {
+                            const double wt = f[0][i1] * f[1][i2] * f[2][i3];
+                            if (!(wt > thresh)) continue;
+                            const size_t gi = ((size_t)(nr[0] - order + i1) * G[1] + (nr[1] - order + i2)) * G[2] +
+                                              (nr[2] - order + i3);
+                            acc[gi].re += (R)(wt * D * rr);
+                            acc[gi].im += (R)(wt * D * ri);
+                        }
+            }
+        }
+        lossc[c] = lc;
+        if (acc) {
+            /* exact adjoint of the unscaled centred forward FFT, then of pad_apod */
+            centred_fft_plans(G, acc, +1, 0, pl.p[0], pl.p[1], pl.p[2]);
+            int lo[3];
+            image_box(p, lo);
+            ofc_t* gc = gx + (size_t)c * ni;
+            const ofc_t* K = (const ofc_t*)kft;
+            for (int i = 0; i < p->img[0]; ++i)
+                for (int j = 0; j < p->img[1]; ++j)
+                    for (int kz = 0; kz < p->img[2]; ++kz) {
+                        const size_t gi = ((size_t)(i + lo[0]) * G[1] + (j + lo[1])) * G[2] + (kz + lo[2]);
+                        const size_t ii = ((size_t)i * p->img[1] + j) * p->img[2] + kz;
+                        /* conj(kft) * acc, then conj(S_c) * (...) */
+                        const double ar = acc[gi].re * K[gi].re + acc[gi].im * K[gi].im;
+                        const double ai = acc[gi].im * K[gi].re - acc[gi].re * K[gi].im;
+                        gc[ii].re = (R)(ar * S[ii].re + ai * S[ii].im);
+                        gc[ii].im = (R)(ai * S[ii].re - ar * S[ii].im);
+                    }
+            free(acc);
+        }
+        free(img);
+        free(grid);
+    }
+    double L = 0.0;
+    for (int c = 0; c < nch; ++c) L += lossc[c];
+    if (gk) {
+        for (int64_t i = 0; i < 3 * ns; ++i) {
+            double s = 0.0;
+            for (int c = 0; c < nch; ++c) s += gk[(size_t)c * ns * 3 + i];
+            grad_k[i] = s;
+        }
+        free(gk);
+    }
+    if (gx) {
+        ofc_t* o = (ofc_t*)grad_x;
+        for (size_t i = 0; i < ni; ++i) {
+            double sr = 0, si = 0;
+            for (int c = 0; c < nch; ++c) {
+                sr += gx[(size_t)c * ni + i].re;
+                si += gx[(size_t)c * ni + i].im;
+            }
+            o[i].re = (R)sr;
+            o[i].im = (R)si;
+        }
+        free(gx);
+    }
+    free(lossc);
+    free_plans(&pl);
+    return L;
+}

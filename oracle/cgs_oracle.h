@@ -102,6 +102,24 @@ int cgso_cg_sense(const cgso_params* p, const int64_t* ptr, const int32_t* idx, 
                   const cgso_real* data, double threshold, int max_iter,
                   cgso_real* x_out, double* residuals, int32_t* iters_out);
 
+/* Data-consistency loss and its gradients -- an extension: the reference has
+ * no derivatives.  E_c is the forward operator of cgso_nufft_fwd applied to
+ * S_c x (zero-pad, kernelFT, centred FFT, KB interpolation; Reco.cpp:521-553):
+ *   L         = 1/2 sum_c sum_i D_i |(E_c S_c x)_i - y_ci|^2
+ *   grad_x    = dL/dRe(x) + i dL/dIm(x) = sum_c conj(S_c) E_c^* (D r_c),
+ *               E^* the exact adjoint (no 1e-3 / sqrt(Ng) rescale)
+ *   grad_k    = dL/dk[i][a], k in the reference's [0,1] units
+ * The KB weights and their derivatives are evaluated in double from the
+ * double coordinates (the reference rounds the distance to float), so L is
+ * smooth in k between changes of the tap set.  dcf NULL: D = 1.  grad_x and
+ * grad_k may be NULL.  Returns L. */
+double cgso_loss_grad(const cgso_params* p, const double* k, int64_t ns, const cgso_real* kft,
+                      const cgso_real* smaps, const float* dcf, const cgso_real* x, const cgso_real* y,
+                      cgso_real* grad_x, double* grad_k);
+
+/* Modified Bessel function I1 by its power series, double precision. */
+double cgso_bessel_i1(double x);
+
 /* WaveCaipi::calculateTraj with Trajectory::calculateKMax (Trajectory.cpp:9-184).
  * k_out: [sx*sy*sz][3] in the reference's z-fastest sample order. */
 void cgso_wave_caipi(const cgso_wave* w, double* k_out);

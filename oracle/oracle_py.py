@@ -117,6 +117,10 @@ class Oracle:
         L.cgso_cg_sense.argtypes = [vp, vp, vp, vp, i64, vp, vp, vp, vp, C.c_double, C.c_int,
                                     vp, vp, vp]
         L.cgso_wave_caipi.argtypes = [vp, vp]
+        L.cgso_loss_grad.restype = C.c_double
+        L.cgso_loss_grad.argtypes = [vp, vp, i64, vp, vp, vp, vp, vp, vp, vp]
+        L.cgso_bessel_i1.restype = C.c_double
+        L.cgso_bessel_i1.argtypes = [C.c_double]
 
     # -- kernel ------------------------------------------------------------
     def taps(self, p, k, mask=None):
@@ -185,6 +189,22 @@ class Oracle:
                                     _ptr(kft), _ptr(smaps), _ptr(d), _ptr(data), threshold,
                                     max_iter, _ptr(x), _ptr(res), _ptr(it))
         return st, x, res[: it[0]], int(it[0])
+
+    def loss_grad(self, p, k, kft, smaps, dcf, x, y, want_x=True, want_k=True):
+        """Data-consistency loss 1/2 sum D |E S x - y|^2 and its gradients
+        (x: complex image, k: [ns][3]); returns (L, grad_x, grad_k)."""
+        k = np.ascontiguousarray(k, dtype=np.float64).reshape(-1, 3)
+        ns = k.shape[0]
+        smaps = np.ascontiguousarray(smaps, dtype=self.cplx)
+        kft = np.ascontiguousarray(kft, dtype=self.cplx)
+        x = np.ascontiguousarray(x, dtype=self.cplx)
+        y = np.ascontiguousarray(y, dtype=self.cplx)
+        d = None if dcf is None else np.ascontiguousarray(dcf, dtype=np.float32)
+        gx = np.zeros(tuple(p.img), self.cplx) if want_x else None
+        gk = np.zeros((ns, 3), np.float64) if want_k else None
+        L = self.lib.cgso_loss_grad(C.byref(p), _ptr(k), ns, _ptr(kft), _ptr(smaps), _ptr(d), _ptr(x),
+                                    _ptr(y), _ptr(gx), _ptr(gk))
+        return L, gx, gk
 
     def wave_caipi(self, **kw):
         w = Wave()
