@@ -51,7 +51,8 @@ EXPORTS = [
     "cgs_cg_solve_batched", "cgs_cg_solve_batched_d", "cgs_last_launch_count",
     "cgs_profile_apply", "cgs_cg_solve_images", "cgs_alloc_host", "cgs_free_host",
     "cgs_fft3_noalloc", "cgs_cg_solve_plain_d", "cgs_voronoi_dcf", "cgs_cg_solve_trace_d",
-    "cgs_cg_solve_fp64_d", "cgs_estimate_density_v3d",
+    "cgs_cg_solve_fp64_d", "cgs_estimate_density_v3d", "cgs_loss_grad_d", "cgs_loss_grad_fp64_d",
+    "cgs_update_trajectory_d", "cgs_set_precision", "cgs_autotune",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -152,6 +153,11 @@ def lib():
         "cgs_cg_solve_plain_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp]),
         "cgs_voronoi_dcf": (C.c_int, [vp, i64, vp]),
         "cgs_estimate_density_v3d": (C.c_int, [vp, i64, C.c_int32, C.c_int32, C.c_double, vp]),
+        "cgs_loss_grad_d": (C.c_int, [vp, C.c_int32, vp, vp, vp, vp, vp]),
+        "cgs_loss_grad_fp64_d": (C.c_int, [vp, C.c_int32, vp, vp, vp, vp, vp]),
+        "cgs_update_trajectory_d": (C.c_int, [vp, vp]),
+        "cgs_set_precision": (C.c_int, [vp, C.c_int32]),
+        "cgs_autotune": (C.c_int, [vp, vp, C.c_int32, vp, vp, vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
         "cgs_cg_solve_fp64_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
     }
@@ -415,6 +421,52 @@ class Reco:
                                                 threshold, max_iter, _p(res), _p(it),
                                                 None if x_trace is None else C.c_void_p(x_trace.data_ptr())))
         return res, it
+
+    # -- differentiation --------------------------------------------------
+    def loss_grad_tensor(self, x, y, grad_x=None, grad_k=None, bin=0):
+        """Data-consistency loss 1/2 sum D |E S x - y|^2 of one bin and its
+        gradients (device tensors: x complex64 image, y complex64 [n_ch][ns],
+        grad_x complex64 image, grad_k float32 [ns][3]); returns the loss."""
+        loss = C.c_double(0.0)
+        self._check(self._L.cgs_loss_grad_d(
+            self._ctx, int(bin), C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), C.byref(loss),
+            None if grad_x is None else C.c_void_p(grad_x.data_ptr()),
+            None if grad_k is None else C.c_void_p(grad_k.data_ptr())))
+        return loss.value
+
+    def loss_grad_fp64_tensor(self, x64, y, grad_x=None, grad_k=None, bin=0):
+        """The FP64 reference of loss_grad_tensor (x64, grad_x complex128,
+        grad_k float64)."""
+        loss = C.c_double(0.0)
+        self._check(self._L.cgs_loss_grad_fp64_d(
+            self._ctx, int(bin), C.c_void_p(x64.data_ptr()), C.c_void_p(y.data_ptr()), C.byref(loss),
+            None if grad_x is None else C.c_void_p(grad_x.data_ptr()),
+            None if grad_k is None else C.c_void_p(grad_k.data_ptr())))
+        return loss.value
+
+    def autotune(self):
+        """Picks the fastest launch shapes for this context; returns
+        {"spread_coils_per_block", "interp_coils_per_thread", "candidates_ms"}."""
+        t = np.zeros(32, np.float32)
+        n = np.zeros(1, np.int32)
+        sc = np.zeros(1, np.int32)
+        ic = np.zeros(1, np.int32)
+        self._check(self._L.cgs_autotune(self._ctx, _p(t), 32, _p(n), _p(sc), _p(ic)))
+        return {"spread_coils_per_block": int(sc[0]), "interp_coils_per_thread": int(ic[0]),
+                "candidates_ms": [float(v) for v in t[: n[0]]]}
+
+    def set_precision(self, compensated):
+        """Compensated (Kahan) spreading on or off."""
+        self._check(self._L.cgs_set_precision(self._ctx, 1 if compensated else 0))
+
+    def update_trajectory_tensor(self, k):
+        """New coordinates (float64 device tensor [ns][3]) for the same samples."""
+        self._check(self._L.cgs_update_trajectory_d(self._ctx, C.c_void_p(k.data_ptr())))
+
+    @property
+    def handle(self):
+        """The C context pointer (for the libtorch operators)."""
+        return int(C.cast(self._ctx, C.c_void_p).value or 0)
 
     def cg_sense_batched_tensor(self, data, x, threshold, max_iter, want_stats=True):
         nb = self.num_bins()

@@ -16,6 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcgsense.so")
+TORCH_LIB = os.path.join(HERE, "libcgsense_torch.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -33,6 +34,17 @@ def _units():
     units.append(("reco_shim.cpp", "reco_shim.o", []))
     units.append(("voronoi.cpp", "voronoi.o", ["-fopenmp"]))
     return units
+
+
+def _torch_paths():
+    """Include and library directories of the installed PyTorch (libtorch)."""
+    import torch
+    from torch.utils import cpp_extension
+    import io
+    import contextlib
+    with contextlib.redirect_stderr(io.StringIO()):
+        inc = cpp_extension.include_paths()
+    return inc, os.path.join(os.path.dirname(torch.__file__), "lib")
 
 
 def _stale(obj, deps):
@@ -60,6 +72,13 @@ def build(verbose=False, jobs=None):
             else:
                 cmd = [NVCC] + ARCH + FLAGS + extra + ["-c", s, "-o", o]
             cmds.append(cmd)
+    # the libtorch operator (torch_ops.cpp) compiles beside the CUDA units
+    tsrc = os.path.join(CSRC, "torch_ops.cpp")
+    tobj = os.path.join(BUILD, "torch_ops.o")
+    tinc, tlib = _torch_paths()
+    if _stale(tobj, [tsrc, __file__, os.path.join(ROOT, "include", "cgsense_c.h")]):
+        cmds.append(["g++", "-std=c++17", "-O2", "-fPIC", "-I", os.path.join(ROOT, "include"),
+                     "-I", "/usr/local/cuda/include"] + sum((["-I", d] for d in tinc), []) + ["-c", tsrc, "-o", tobj])
     jobs = jobs or max(1, min(len(cmds), os.cpu_count() or 4))
 
     def run(cmd):
@@ -80,6 +99,13 @@ def build(verbose=False, jobs=None):
         if r.returncode != 0:
             sys.stderr.write(r.stdout)
             raise RuntimeError("link failed")
+    if _stale(TORCH_LIB, [tobj, LIB]):
+        cmd = ["g++", "-shared", "-o", TORCH_LIB, tobj, "-L", HERE, "-lcgsense", "-L", tlib, "-ltorch", "-ltorch_cpu",
+               "-lc10", "-lc10_cuda", "-Wl,-rpath,$ORIGIN", "-Wl,-rpath," + tlib]
+        r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+        if r.returncode != 0:
+            sys.stderr.write(r.stdout)
+            raise RuntimeError("link of the libtorch operator failed")
     return LIB
 
 

@@ -98,6 +98,11 @@ struct cgs_ctx {
     // loss gradients: derivative records, gathered measured samples, partials
     DevBuf d_drec, d_gy, d_gpart, d_flag;
     bool drec_valid = false;
+    bool kahan = false;          // compensated spreading (cgs_set_precision)
+    // launch shapes (cgs_autotune): coils per spreading block (0: as many as
+    // fit), coils per interpolation thread
+    int spread_cc = 0;
+    int interp_cc = 4;
     bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
     bool tiles_stale = false;    // spreading lists built from older coordinates
     int ntx = 0, nty = 0, ntz = 0, ntiles = 0;
@@ -483,7 +488,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     ia.thresh = c->thresh;
     long long mx = 0;
     for (int b = b0; b < b0 + nb; ++b) mx = std::max(mx, c->h_bin_off[b + 1] - c->h_bin_off[b]);
-    CGS_LAUNCH(c, launch_interp(ia, mx, nb, c->stream));
+    CGS_LAUNCH(c, launch_interp(ia, mx, nb, c->interp_cc, c->stream));
     return CGS_OK;
 }
 
@@ -512,14 +517,15 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
         sa.plane_rng = c->d_plane_rng.as<int2>();
         sa.bin0 = b0;
         sa.nch = c->nch;
-        const int nchunk = (c->nch + spread_max_coils() - 1) / spread_max_coils();
+        const int mc = c->spread_cc > 0 ? std::min(c->spread_cc, spread_max_coils(c->kahan)) : spread_max_coils(c->kahan);
+        const int nchunk = (c->nch + mc - 1) / mc;
         sa.cc = (c->nch + nchunk - 1) / nchunk;
         for (int a = 0; a < 3; ++a) sa.G[a] = c->G[a];
         sa.ntx = c->ntx;
         sa.nty = c->nty;
         sa.ntz = c->ntz;
         sa.thresh = c->thresh;
-        CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->stream));
+        CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->kahan, c->stream));
 
         StridedPassArgs ax{};
         ax.in = c->d_grid.as<float2>();
@@ -1480,6 +1486,95 @@ int cgs_loss_grad_fp64_d(cgs_ctx* c, int32_t bin, const void* x, const void* y, 
                                reinterpret_cast<double*>(grad_k), c->d64_part.as<double>(), 0));
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
     return CGS_OK;
+}
+
+int cgs_set_precision(cgs_ctx* c, int32_t mode)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (mode != CGS_PREC_FP32 && mode != CGS_PREC_COMPENSATED) return fail(c, CGS_ERR_ARG, "unknown precision mode");
+    const bool k = mode == CGS_PREC_COMPENSATED;
+    if (k != c->kahan) {
+        c->kahan = k;
+        drop_graphs(c);
+    }
+    return CGS_OK;
+}
+
+// Project autotuner: times one batched E^H D E application of every bin for
+// each candidate launch shape and keeps the fastest (first coils per
+// spreading block with the interpolation fixed, then coils per
+// interpolation thread).  times_ms (optional, max_times entries) receives
+// the median time of every candidate in that order.
+int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_times, int32_t* spread_cc,
+                 int32_t* interp_cc)
+{
+    CGS_TRY(check_ready(c, true));
+    const long long Ni = c->Ni;
+    const int nb = c->nbins;
+    DevBuf xb, qb;
+    CGS_CUDA(c, xb.ensure((size_t)nb * Ni * sizeof(float2)));
+    CGS_CUDA(c, qb.ensure((size_t)nb * Ni * sizeof(float2)));
+    CGS_CUDA(c, cudaMemsetAsync(xb.p, 0, (size_t)nb * Ni * sizeof(float2), c->stream));
+    cudaEvent_t e0, e1;
+    CGS_CUDA(c, cudaEventCreate(&e0));
+    CGS_CUDA(c, cudaEventCreate(&e1));
+    std::vector<float> all;
+    auto time_apply = [&](float& best) -> int {
+        std::vector<float> t;
+        for (int rep = 0; rep < 4; ++rep) {
+            CGS_CUDA(c, cudaEventRecord(e0, c->stream));
+            CGS_TRY(apply_bins(c, 0, nb, xb.as<float2>(), qb.as<float2>(), nullptr, nullptr, 0));
+            CGS_CUDA(c, cudaEventRecord(e1, c->stream));
+            CGS_CUDA(c, cudaEventSynchronize(e1));
+            float ms = 0.f;
+            CGS_CUDA(c, cudaEventElapsedTime(&ms, e0, e1));
+            if (rep > 0) t.push_back(ms);   // the first run warms up
+        }
+        std::sort(t.begin(), t.end());
+        best = t[t.size() / 2];
+        all.push_back(best);
+        return CGS_OK;
+    };
+    // coils per spreading block: the largest that fits, then halves, thirds
+    std::vector<int> sc;
+    const int mc = std::min(c->nch, spread_max_coils(c->kahan));
+    for (int d = 1; d <= 4; ++d) {
+        const int v = (mc + d - 1) / d;
+        if (std::find(sc.begin(), sc.end(), v) == sc.end()) sc.push_back(v);
+    }
+    float best = 1e30f;
+    int best_sc = sc[0];
+    for (int v : sc) {
+        c->spread_cc = v;
+        float ms;
+        CGS_TRY(time_apply(ms));
+        if (ms < best) {
+            best = ms;
+            best_sc = v;
+        }
+    }
+    c->spread_cc = best_sc;
+    best = 1e30f;
+    int best_ic = c->interp_cc;
+    for (int v : {2, 4, 6, 8}) {
+        c->interp_cc = v;
+        float ms;
+        CGS_TRY(time_apply(ms));
+        if (ms < best) {
+            best = ms;
+            best_ic = v;
+        }
+    }
+    c->interp_cc = best_ic;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    drop_graphs(c);
+    if (times_ms)
+        for (int i = 0; i < (int)all.size() && i < max_times; ++i) times_ms[i] = all[i];
+    if (n_times) *n_times = (int32_t)all.size();
+    if (spread_cc) *spread_cc = c->spread_cc;
+    if (interp_cc) *interp_cc = c->interp_cc;
+    return check_timeout(c);
 }
 
 }  // extern "C"

@@ -43,14 +43,26 @@ struct SizeImpl {
     using ZF = ZPipeLayout<R1, R2, LPB, ZNST_F>;
     using ZA = ZPipeLayout<R1, R2, LPB, ZNST_A>;
 
+    // the TMA strided variants instantiated: forward (input-pruned or not),
+    // adjoint (output-pruned or not)
+    static constexpr bool HAS_IN = R1 % 4 == 0, HAS_OUT = R2 % 4 == 0;
+
+    template <int SIGN, int MODE>
+    static cudaError_t tma_attr(int smem)
+    {
+        return cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, SIGN, TB, NSTAGE, MODE>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    }
+
     static cudaError_t init()
     {
         const int smem = (int)Pipe::smem_bytes(L);
-        cudaError_t e = cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, -1, TB, NSTAGE>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, +1, TB, NSTAGE>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        cudaError_t e = tma_attr<-1, PRUNE_NONE>(smem);
+        if (e == cudaSuccess) e = tma_attr<+1, PRUNE_NONE>(smem);
+        if constexpr (HAS_IN)
+            if (e == cudaSuccess) e = tma_attr<-1, PRUNE_IN>(smem);
+        if constexpr (HAS_OUT)
+            if (e == cudaSuccess) e = tma_attr<+1, PRUNE_OUT>(smem);
         // the z extent of an image never exceeds the grid's: size for Iz = L
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_fwd_z_pipe<R1, R2, LPB, ZNST_F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -63,29 +75,41 @@ struct SizeImpl {
 
     static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
+    // persistent launch: as many blocks as fit, at most one per tile
+    template <int SIGN, int MODE>
+    static cudaError_t tma_run(const StridedPassArgs& a, const CUtensorMap& map, int A, int batch, int box_rows,
+                               cudaStream_t s)
+    {
+        const size_t smem = Pipe::smem_bytes(a.Lin);
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_fft_strided_tma<R1, R2, SIGN, TB, NSTAGE, MODE>, Pipe::NT, smem);
+        if (e != cudaSuccess) return e;
+        const long long tiles_per_item = (long long)A * a.ntb;
+        const long long ntiles = tiles_per_item * batch;
+        long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
+        if (nblk > ntiles) nblk = ntiles;
+        k_fft_strided_tma<R1, R2, SIGN, TB, NSTAGE, MODE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(
+            a, map, ntiles, (int)tiles_per_item, box_rows);
+        return cudaGetLastError();
+    }
+
     static cudaError_t strided(int sign, StridedPassArgs a, int A, int batch, cudaStream_t s)
     {
         a.ntb = (a.B + TB - 1) / TB;
         CUtensorMap map;
         int box_rows = 0;
         if (a.err && encode_strided_map(&map, a, A, batch, TB, &box_rows)) {
-            const size_t smem = Pipe::smem_bytes(a.Lin);
-            int per_sm = 0;
-            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                &per_sm, sign < 0 ? k_fft_strided_tma<R1, R2, -1, TB, NSTAGE> : k_fft_strided_tma<R1, R2, +1, TB, NSTAGE>,
-                Pipe::NT, smem);
-            if (e != cudaSuccess) return e;
-            const long long tiles_per_item = (long long)A * a.ntb;
-            const long long ntiles = tiles_per_item * batch;
-            long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
-            if (nblk > ntiles) nblk = ntiles;
-            if (sign < 0)
-                k_fft_strided_tma<R1, R2, -1, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, map, ntiles,
-                                                                                             (int)tiles_per_item, box_rows);
-            else
-                k_fft_strided_tma<R1, R2, +1, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, map, ntiles,
-                                                                                             (int)tiles_per_item, box_rows);
-            return cudaGetLastError();
+            const bool half_in = 4 * a.in_off == L && 2 * a.Lin == L;
+            const bool half_out = 4 * a.out_off == L && 2 * a.Lout == L;
+            if (sign < 0) {
+                if constexpr (HAS_IN)
+                    if (half_in) return tma_run<-1, PRUNE_IN>(a, map, A, batch, box_rows, s);
+                return tma_run<-1, PRUNE_NONE>(a, map, A, batch, box_rows, s);
+            }
+            if constexpr (HAS_OUT)
+                if (half_out) return tma_run<+1, PRUNE_OUT>(a, map, A, batch, box_rows, s);
+            return tma_run<+1, PRUNE_NONE>(a, map, A, batch, box_rows, s);
         }
         dim3 grid((unsigned)(A * a.ntb), (unsigned)batch);
         if (sign < 0) k_fft_strided<R1, R2, -1, TB><<<grid, NT_S, 0, s>>>(a);

@@ -115,33 +115,63 @@ k_fft_strided(StridedPassArgs a)
 // ---------------------------------------------------------------------------
 constexpr unsigned long long PIPE_WAIT_NS = 2000000000ull;
 
+// Pruning modes of the strided pass, for a 2x oversampled axis with the
+// image centred in the line (rows L/4 .. 3L/4):
+//   PRUNE_NONE  any Lin / in_off / Lout / out_off (predicated rows);
+//   PRUNE_IN    Lin = L/2 rows at in_off = L/4: stage 1 loads only the
+//               n1 in [R1/4, 3R1/4) that hold them (compile-time range);
+//   PRUNE_OUT   Lout = L/2 rows at out_off = L/4: stage 2 stores only the
+//               k2 in [R2/4, 3R2/4) that land there.
+constexpr int PRUNE_NONE = 0, PRUNE_IN = 1, PRUNE_OUT = 2;
+
 template <int R1, int R2, int TB, int NSTAGE>
 struct PipeLayout {
     static constexpr int L = R1 * R2;
     static constexpr int NT = TB * (R1 > R2 ? R1 : R2);
-    // 1 KiB slack to align the TMA destination to 1 KiB
+    // 1 KiB slack to align the TMA destination to 1 KiB; two twiddle tables
     static size_t smem_bytes(int Lin)
     {
-        return 1024 + ((size_t)NSTAGE * Lin * TB + (size_t)L * TB + L) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
+        return 1024 + ((size_t)NSTAGE * Lin * TB + (size_t)L * TB + 2 * L) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
     }
 };
 
-template <int R1, int R2, int SIGN, int TB, int NSTAGE>
-__global__ void __launch_bounds__(PipeLayout<R1, R2, TB, NSTAGE>::NT)
+// The centring signs (-1)^l of input row l = R2 n1 + n2 and output row
+// l = k1 + R1 k2 are (-1)^n2 and (-1)^k1 when R1 and R2 are even: constant
+// per stage-1 thread and per stage-2 row.  Both then fold into the stage-1
+// twiddle W^(n2 k1) of thread n2 and row k1 (the passes are linear), and no
+// element is negated on its own.
+template <int R1, int R2>
+struct SignFold {
+    static constexpr bool value = (R1 % 2 == 0) && (R2 % 2 == 0);
+};
+
+template <int R1, int R2, int SIGN, int TB, int NSTAGE, int MODE>
+__global__ void __launch_bounds__(PipeLayout<R1, R2, TB, NSTAGE>::NT, (MODE == PRUNE_IN && R1 * R2 <= 320) ? 3 : 2)
 k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, long long ntiles,
                   int tiles_per_item, int box_rows)
 {
     constexpr int L = R1 * R2;
     constexpr int NT = PipeLayout<R1, R2, TB, NSTAGE>::NT;
+    constexpr bool FOLD = SignFold<R1, R2>::value;
+    static_assert(MODE != PRUNE_IN || R1 % 4 == 0, "input pruning needs R1 % 4 == 0");
+    static_assert(MODE != PRUNE_OUT || R2 % 4 == 0, "output pruning needs R2 % 4 == 0");
     extern __shared__ float4 s_pipe[];
     const uintptr_t base = (reinterpret_cast<uintptr_t>(s_pipe) + 1023) & ~(uintptr_t)1023;
     const int stage_elems = a.Lin * TB;
     float2* s_in = reinterpret_cast<float2*>(base);
     float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
-    float2* s_tw = s_y + L * TB;
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
+    float2* s_tw = s_y + L * TB;        // W^m, or the signed table [n2][k1] when FOLD
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + 2 * L);
     const int tid = threadIdx.x;
-    for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
+    if (FOLD) {
+        for (int m = tid; m < L; m += NT) {
+            const int n2 = m / R1, k1 = m - n2 * R1;
+            const float2 w = a.tw[n2 * k1];
+            s_tw[m] = ((n2 + k1) & 1) ? cneg(w) : w;
+        }
+    } else {
+        for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
+    }
     if (tid == 0) {
         for (int s = 0; s < NSTAGE; ++s) mbar_init(&s_bar[s], 1);
         fence_mbar_init();
@@ -190,19 +220,34 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
             const int n2 = tid / TB;
             if (n2 < R2) {
                 float2 v[R1];
+                if constexpr (MODE == PRUNE_IN) {
+                    // rows L/4 + R2 m + n2 (m = n1 - R1/4) of the line are the tile's rows
+                    const float2* src = sin_s + n2 * TB + bi;
 #pragma unroll
-                for (int n1 = 0; n1 < R1; ++n1) {
-                    const int l = R2 * n1 + n2;
-                    const int li = l - a.in_off;
-                    float2 x = make_float2(0.f, 0.f);
-                    if (li >= 0 && li < a.Lin) x = parity(sin_s[li * TB + bi], l);
-                    v[n1] = x;
+                    for (int n1 = 0; n1 < R1; ++n1) {
+                        if (n1 >= R1 / 4 && n1 < 3 * R1 / 4) {
+                            const float2 x = src[(R2 * (n1 - R1 / 4)) * TB];
+                            v[n1] = FOLD ? x : parity(x, R2 * n1 + n2);
+                        } else {
+                            v[n1] = make_float2(0.f, 0.f);
+                        }
+                    }
+                } else {
+#pragma unroll
+                    for (int n1 = 0; n1 < R1; ++n1) {
+                        const int l = R2 * n1 + n2;
+                        const int li = l - a.in_off;
+                        float2 x = make_float2(0.f, 0.f);
+                        if (li >= 0 && li < a.Lin) x = sin_s[li * TB + bi];
+                        v[n1] = FOLD ? x : parity(x, l);
+                    }
                 }
                 Dft<R1, SIGN>::run(v);
 #pragma unroll
                 for (int k1 = 0; k1 < R1; ++k1) {
                     float2 tv = v[k1];
-                    if (k1 > 0) tv = table_twiddle<SIGN>(tv, s_tw[n2 * k1]);
+                    if (FOLD) tv = table_twiddle<SIGN>(tv, s_tw[n2 * R1 + k1]);
+                    else if (k1 > 0) tv = table_twiddle<SIGN>(tv, s_tw[n2 * k1]);
                     s_y[(k1 * R2 + n2) * TB + bi] = tv;
                 }
             }
@@ -216,11 +261,22 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
                 for (int n2 = 0; n2 < R2; ++n2) u[n2] = s_y[(k1 * R2 + n2) * TB + bi];
                 Dft<R2, SIGN>::run(u);
                 float2* out = a.out + item * a.out_bs + (long long)ai * a.out_as + b;
+                if constexpr (MODE == PRUNE_OUT) {
+                    // output rows L/4 .. 3L/4: k2 in [R2/4, 3R2/4), row k1 + R1 (k2 - R2/4)
+                    if (bok) {
+                        float2* o = out + (long long)k1 * a.B;
+                        const long long step = (long long)R1 * a.B;
 #pragma unroll
-                for (int k2 = 0; k2 < R2; ++k2) {
-                    const int l = k1 + R1 * k2;
-                    const int lo = l - a.out_off;
-                    if (bok && lo >= 0 && lo < a.Lout) out[(long long)lo * a.B] = parity(u[k2], l);
+                        for (int k2 = R2 / 4; k2 < 3 * R2 / 4; ++k2)
+                            o[(k2 - R2 / 4) * step] = FOLD ? u[k2] : parity(u[k2], k1 + R1 * k2);
+                    }
+                } else {
+#pragma unroll
+                    for (int k2 = 0; k2 < R2; ++k2) {
+                        const int l = k1 + R1 * k2;
+                        const int lo = l - a.out_off;
+                        if (bok && lo >= 0 && lo < a.Lout) out[(long long)lo * a.B] = FOLD ? u[k2] : parity(u[k2], l);
+                    }
                 }
             }
         }

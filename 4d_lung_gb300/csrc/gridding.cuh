@@ -142,7 +142,10 @@ constexpr int SPREAD_BATCH = 32;   // samples staged per round
 // CC: compile-time upper bound of the coils per block (a.cc <= CC); the
 // coil loop is unrolled so that the shared-memory loads, FMAs and stores of
 // all coils of one grid point issue back to back.
-template <int CC>
+// KAHAN: compensated summation (the precision form): every accumulator has
+// a compensation term (the low-order part lost by its last addition), and
+// the stored value is sum - compensation.
+template <int CC, bool KAHAN>
 __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
 {
     extern __shared__ float4 s_dyn[];
@@ -157,11 +160,15 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
 
     // shared: accumulators [cc][ACC_PTS] float2, then staged records and values
     float2* acc = reinterpret_cast<float2*>(s_dyn);
-    TapRecord* s_rec = reinterpret_cast<TapRecord*>(acc + (size_t)a.cc * ACC_PTS);
+    float2* cmp = acc + (size_t)a.cc * ACC_PTS;   // compensation terms (KAHAN only)
+    TapRecord* s_rec = reinterpret_cast<TapRecord*>(acc + (size_t)(KAHAN ? 2 : 1) * a.cc * ACC_PTS);
     float2* s_val = reinterpret_cast<float2*>(s_rec + SPREAD_BATCH);
 
     const int tid = threadIdx.x;
-    for (int e = tid; e < ncc * ACC_PTS; e += SPREAD_THREADS) acc[e] = make_float2(0.f, 0.f);
+    for (int e = tid; e < ncc * ACC_PTS; e += SPREAD_THREADS) {
+        acc[e] = make_float2(0.f, 0.f);
+        if (KAHAN) cmp[e] = make_float2(0.f, 0.f);
+    }
 
     const long long tp = a.tile_ptr_off[bin];
     const int beg = a.tile_ptr[tp + tile], end = a.tile_ptr[tp + tile + 1];
@@ -200,18 +207,29 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
                 if (wxv == 0.f || wyv == 0.f || wzv == 0.f || !(wt > a.thresh)) continue;
                 float2* pt = acc + (warp * TILE_Y + (gy - y0)) * TILE_ZP + (gz - z0);
                 const float2* v = s_val + j * CC;
-                float2 t[CC], vv[CC];
+                float2 t[CC], vv[CC], e[CC];
 #pragma unroll
                 for (int c = 0; c < CC; ++c)
                     if (c < ncc) {
                         t[c] = pt[c * ACC_PTS];
                         vv[c] = v[c];
+                        if (KAHAN) e[c] = pt[(size_t)a.cc * ACC_PTS + c * ACC_PTS];
                     }
 #pragma unroll
                 for (int c = 0; c < CC; ++c)
                     if (c < ncc) {
-                        t[c].x = fmaf(vv[c].x, wt, t[c].x);
-                        t[c].y = fmaf(vv[c].y, wt, t[c].y);
+                        if (KAHAN) {
+                            // y = v w - e;  s = t + y;  e = (s - t) - y;  t = s
+                            const float yx = fmaf(vv[c].x, wt, -e[c].x), yy = fmaf(vv[c].y, wt, -e[c].y);
+                            const float sx = __fadd_rn(t[c].x, yx), sy = __fadd_rn(t[c].y, yy);
+                            e[c].x = __fsub_rn(__fsub_rn(sx, t[c].x), yx);
+                            e[c].y = __fsub_rn(__fsub_rn(sy, t[c].y), yy);
+                            t[c] = make_float2(sx, sy);
+                            pt[(size_t)a.cc * ACC_PTS + c * ACC_PTS] = e[c];
+                        } else {
+                            t[c].x = fmaf(vv[c].x, wt, t[c].x);
+                            t[c].y = fmaf(vv[c].y, wt, t[c].y);
+                        }
                         pt[c * ACC_PTS] = t[c];
                     }
             }
@@ -225,9 +243,12 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
         const int c = e / TILE_PTS, local = e - c * TILE_PTS;
         const int lz = local % TILE_Z, ly = (local / TILE_Z) % TILE_Y, lx = local / (TILE_Z * TILE_Y);
         const int X = x0 + lx, Y = y0 + ly, Z = z0 + lz;
-        if (X < Gx && Y < Gy && Z < Gz)
-            grid[(long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z] =
-                acc[c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + lz];
+        if (X < Gx && Y < Gy && Z < Gz) {
+            const int q = c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + lz;
+            float2 v = acc[q];
+            if (KAHAN) v = make_float2(__fsub_rn(v.x, cmp[q].x), __fsub_rn(v.y, cmp[q].y));
+            grid[(long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z] = v;
+        }
     }
 }
 

@@ -88,14 +88,18 @@ cudaError_t launch_tap_records(const double* k, const int* sample_idx, long long
     return cudaGetLastError();
 }
 
-constexpr int INTERP_CC = 4;
-
-cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, cudaStream_t s)
+// coils per interpolation thread: one of 2, 4, 6, 8 (autotuned per context)
+cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, int cc, cudaStream_t s)
 {
     if (max_bin_samples == 0 || nbins == 0) return cudaSuccess;
-    dim3 grid((unsigned)((max_bin_samples + 127) / 128), (unsigned)((a.nch + INTERP_CC - 1) / INTERP_CC),
-              (unsigned)nbins);
-    k_interp<INTERP_CC><<<grid, 128, 0, s>>>(a);
+    dim3 grid((unsigned)((max_bin_samples + 127) / 128), (unsigned)((a.nch + cc - 1) / cc), (unsigned)nbins);
+    switch (cc) {
+    case 2: k_interp<2><<<grid, 128, 0, s>>>(a); break;
+    case 4: k_interp<4><<<grid, 128, 0, s>>>(a); break;
+    case 6: k_interp<6><<<grid, 128, 0, s>>>(a); break;
+    case 8: k_interp<8><<<grid, 128, 0, s>>>(a); break;
+    default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 
@@ -115,35 +119,49 @@ cudaError_t launch_record_nearest(const TapRecord* rec, long long n, unsigned* o
 // coils per spreading block: staged values use a row of SPREAD_CC_MAX
 constexpr int SPREAD_CC_MAX = 12;
 
-size_t spread_smem_bytes(int cc)
+size_t spread_smem_bytes(int cc, bool kahan)
 {
     const int ccp = cc <= 4 ? 4 : (cc <= 8 ? 8 : SPREAD_CC_MAX);
-    return (size_t)cc * ACC_PTS * sizeof(float2) + SPREAD_BATCH * sizeof(TapRecord) +
+    return (size_t)(kahan ? 2 : 1) * cc * ACC_PTS * sizeof(float2) + SPREAD_BATCH * sizeof(TapRecord) +
            (size_t)SPREAD_BATCH * ccp * sizeof(float2);
 }
 
-int spread_max_coils() { return SPREAD_CC_MAX; }
+int spread_max_coils(bool kahan) { return kahan ? SPREAD_CC_MAX / 2 : SPREAD_CC_MAX; }
+
+template <bool K>
+static cudaError_t spread_attrs(int smax)
+{
+    cudaError_t e = cudaFuncSetAttribute(k_spread<4, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_spread<8, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_spread<SPREAD_CC_MAX, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    return e;
+}
 
 cudaError_t kernels_init()
 {
-    const int smax = (int)spread_smem_bytes(SPREAD_CC_MAX);
-    cudaError_t e = cudaFuncSetAttribute(k_spread<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_spread<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_spread<SPREAD_CC_MAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaError_t e = spread_attrs<false>((int)spread_smem_bytes(SPREAD_CC_MAX, false));
+    if (e == cudaSuccess) e = spread_attrs<true>((int)spread_smem_bytes(SPREAD_CC_MAX / 2, true));
     if (e == cudaSuccess) e = fft_init_all();
     return e;
 }
 
-cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, cudaStream_t s)
+template <bool K>
+static void spread_launch(const SpreadArgs& a, dim3 grid, size_t smem, cudaStream_t s)
+{
+    if (a.cc <= 4) k_spread<4, K><<<grid, SPREAD_THREADS, smem, s>>>(a);
+    else if (a.cc <= 8) k_spread<8, K><<<grid, SPREAD_THREADS, smem, s>>>(a);
+    else k_spread<SPREAD_CC_MAX, K><<<grid, SPREAD_THREADS, smem, s>>>(a);
+}
+
+cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan, cudaStream_t s)
 {
     if (ntiles == 0 || nbins == 0) return cudaSuccess;
-    if (a.cc < 1 || a.cc > SPREAD_CC_MAX) return cudaErrorInvalidValue;
-    const size_t smem = spread_smem_bytes(a.cc);
+    if (a.cc < 1 || a.cc > spread_max_coils(kahan)) return cudaErrorInvalidValue;
+    const size_t smem = spread_smem_bytes(a.cc, kahan);
     dim3 grid((unsigned)ntiles, (unsigned)((a.nch + a.cc - 1) / a.cc), (unsigned)nbins);
-    if (a.cc <= 4) k_spread<4><<<grid, SPREAD_THREADS, smem, s>>>(a);
-    else if (a.cc <= 8) k_spread<8><<<grid, SPREAD_THREADS, smem, s>>>(a);
-    else k_spread<SPREAD_CC_MAX><<<grid, SPREAD_THREADS, smem, s>>>(a);
+    if (kahan) spread_launch<true>(a, grid, smem, s);
+    else spread_launch<false>(a, grid, smem, s);
     return cudaGetLastError();
 }
 

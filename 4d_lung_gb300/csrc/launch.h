@@ -29,14 +29,14 @@ cudaError_t launch_adj_z(int L, const AdjZArgs& a, int batch, cudaStream_t s);
 // Gridding and element-wise kernels (kernels_misc.cu).
 cudaError_t launch_tap_records(const double* k, const int* sample_idx, long long n, const KbParams& kb,
                                TapRecord* out, cudaStream_t s);
-cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, cudaStream_t s);
-cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, cudaStream_t s);
+cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, int cc, cudaStream_t s);
+cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan, cudaStream_t s);
 // packed nearest grid point of each tap record
 cudaError_t launch_record_nearest(const TapRecord* rec, long long n, unsigned* out, cudaStream_t s);
-size_t spread_smem_bytes(int cc);
+size_t spread_smem_bytes(int cc, bool kahan);
 // one-time kernel attributes (dynamic shared memory limits); call per device
 cudaError_t kernels_init();
-int spread_max_coils();
+int spread_max_coils(bool kahan);
 
 // samples: reference order [nch][ns] <-> sorted, coil-interleaved [total][nch]
 cudaError_t launch_gather_samples(const float2* data, long long ns, const int* sorted, long long total, int nch,

@@ -130,7 +130,7 @@ class ClockSampler:
 # workload
 # ---------------------------------------------------------------------------
 
-def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voronoi"):
+def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voronoi", max_bins=0):
     w = synth.WORKLOADS[name]
     kb_w = 4.0
     kb_b = beatty_beta(kb_w)
@@ -138,6 +138,8 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
     k = synth.wave_trajectory(w, lines=lines)
     rbins = synth.breathing_bins(len(lines), w.n_bins)
     sbins = synth.bin_samples(rbins, w.n_read)
+    if max_bins > 0:
+        sbins = sbins[:max_bins]
     smaps = synth.coil_maps(w.img, w.n_ch)
     # per-bin Voronoi weights (estimateDensityV3D, host C++), or the radial stand-in
     t0 = time.perf_counter()
@@ -275,6 +277,175 @@ def run_reference(args):
     return 0
 
 
+def precision_report(reco, data, x, iters, torch, dev):
+    """Relative L2 error of x after every CG iteration against the FP64 GPU
+    form (max over bins), for plain and compensated FP32 spreading."""
+    nb = x.shape[0]
+    t64 = torch.zeros((iters,) + tuple(x.shape), dtype=torch.complex128, device=dev)
+    x64 = torch.zeros(x.shape, dtype=torch.complex128, device=dev)
+    t0 = time.perf_counter()
+    reco.cg_sense_fp64_tensor(data, x64, 0.0, iters, t64)
+    torch.cuda.synchronize(dev)
+    t_fp64 = time.perf_counter() - t0
+    out = {"reference": "full-FP64 GPU form (cuFFT Z2Z, FP64 gridding, vectors and scalars)",
+           "fp64_s_per_recon": t_fp64}
+    for name, comp in (("fp32", False), ("compensated", True)):
+        reco.set_precision(comp)
+        tr = torch.zeros((iters,) + tuple(x.shape), dtype=torch.complex64, device=dev)
+        xx = torch.zeros_like(x)
+        reco.cg_sense_trace_tensor(data, xx, 0.0, iters, tr)
+        torch.cuda.synchronize(dev)
+        errs = []
+        for it in range(iters):
+            d = (tr[it].to(torch.complex128) - t64[it]).reshape(nb, -1)
+            e = torch.linalg.vector_norm(d, dim=1) / torch.linalg.vector_norm(t64[it].reshape(nb, -1), dim=1)
+            errs.append(float(e.max()))
+        out["rel_l2_per_iter_" + name] = errs
+        del tr
+    reco.set_precision(False)
+    out["max_rel_l2_fp32"] = max(out["rel_l2_per_iter_fp32"])
+    out["max_rel_l2_compensated"] = max(out["rel_l2_per_iter_compensated"])
+    del t64
+    return out
+
+
+def differentiation_report(cgs, synth, torch, dev, stream_handle, steps=50):
+    """cfg4 differentiation form: 128x128x96 image, 12 coils, one bin of
+    1.57 M wave-CAIPI samples, the reference's KB kernel (w = 4.25,
+    b = 14.9086); wave parameters perturbed by up to 5 % from nominal.
+    dL/dtheta of L = 1/2 |E(theta) x - y|^2 from the FP32 libtorch operator,
+    the FP64 reference gradient and central finite differences of the FP64
+    loss (step 1e-3 in the parameters' natural units); the time of one loss
+    + gradient evaluation; `steps` Adam steps of trajectory self-calibration."""
+    ag = importlib.import_module("4d_lung_gb300.autograd")
+    w = synth.WORKLOADS["cfg4"]
+    lines = synth.readout_lines(w)
+    kb_w, kb_b = 4.25, 14.9086
+    reco = cgs.Reco(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=kb_b, device=dev.index or 0)
+    reco.set_stream(stream_handle)
+    v_true = torch.tensor([w.wave_cells, w.wave_cells, 0, 0, 0, 0], dtype=torch.float64, device=dev)
+    k_true = ag.wave_trajectory_torch(w, v_true, lines).contiguous()
+    reco.set_trajectory(k_true.cpu().numpy())
+    smaps = torch.from_numpy(synth.coil_maps(w.img, w.n_ch)).to(dev)
+    reco.set_smaps_tensor(smaps)
+    x = torch.from_numpy(synth.phantom(w.img)).to(dev)
+    y = torch.zeros((w.n_ch, k_true.shape[0]), dtype=torch.complex64, device=dev)
+    reco.nufft_fwd_tensor((smaps * x[None]).contiguous(), y)
+    torch.cuda.synchronize(dev)
+    rms = float(torch.sqrt(torch.mean(torch.abs(y) ** 2)))
+    g = torch.Generator(device=dev)
+    g.manual_seed(2)
+    y += torch.complex(torch.randn(y.shape, generator=g, device=dev),
+                       torch.randn(y.shape, generator=g, device=dev)) * (rms / 30 / np.sqrt(2))
+    th = synth.perturbed_wave(w)
+    v0 = np.array([th.amp_y, th.amp_z, th.phase_y, th.phase_z, th.delay_y, th.delay_z])
+    sc = synth.wave_param_scale(w)
+    x64 = x.to(torch.complex128)
+
+    def loss64(vec, grad=False):
+        k = ag.wave_trajectory_torch(w, torch.tensor(vec, dtype=torch.float64, device=dev), lines).contiguous()
+        reco.update_trajectory_tensor(k)
+        gk = torch.zeros((k.shape[0], 3), dtype=torch.float64, device=dev) if grad else None
+        return reco.loss_grad_fp64_tensor(x64, y, None, gk), gk
+
+    L64, gk64 = loss64(v0, grad=True)
+    g64 = np.einsum("ia,iam->m", gk64.cpu().numpy(), synth.wave_jacobian(w, th, lines=lines))
+    fd = np.zeros(6)
+    for m in range(6):
+        h = 1e-3 * sc[m]
+        vp, vm = v0.copy(), v0.copy()
+        vp[m] += h
+        vm[m] -= h
+        fd[m] = (loss64(vp)[0] - loss64(vm)[0]) / (2 * h)
+    # FP32 operator: loss, dL/dx and dL/dtheta through autograd; timed
+    times = []
+    for rep in range(6):
+        v = torch.tensor(v0, dtype=torch.float64, device=dev, requires_grad=True)
+        xr = x.clone().requires_grad_(True)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        loss = ag.dc_loss(reco, xr, ag.wave_trajectory_torch(w, v, lines).contiguous(), y)
+        loss.backward()
+        e1.record()
+        torch.cuda.synchronize(dev)
+        if rep > 0:
+            times.append(e0.elapsed_time(e1))
+    g32 = v.grad.cpu().numpy()
+    # self-calibration (image known): Adam on theta / scale
+    scale = torch.tensor(sc, dtype=torch.float64, device=dev)
+    u = (torch.tensor(v0, dtype=torch.float64, device=dev) / scale).requires_grad_(True)
+    opt = torch.optim.Adam([u], lr=0.01)
+    G = torch.tensor(w.grid, dtype=torch.float64, device=dev) - 1
+
+    def traj_err(uu):
+        k = ag.wave_trajectory_torch(w, uu * scale, lines)
+        return float(torch.sqrt(torch.mean(torch.sum(((k - k_true) * G) ** 2, dim=1))))
+
+    hist_loss, hist_err = [], [traj_err(u.detach())]
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        opt.zero_grad()
+        loss = ag.dc_loss(reco, x, ag.wave_trajectory_torch(w, u * scale, lines).contiguous(), y)
+        loss.backward()
+        opt.step()
+        hist_loss.append(loss.item())
+        hist_err.append(traj_err(u.detach()))
+    t_cal = time.perf_counter() - t0
+    del reco
+    return {
+        "workload": w.name, "samples": int(k_true.shape[0]), "coils": w.n_ch, "kb_w": kb_w, "kb_b": kb_b,
+        "theta0": v0.tolist(), "params": list(synth.WAVE_PARAM_NAMES),
+        "dL_dtheta_fp32": g32.tolist(), "dL_dtheta_fp64": g64.tolist(), "dL_dtheta_fd_fp64": fd.tolist(),
+        "fd_step": "1e-3 in natural units (cells, rad, wave periods)",
+        "rel_err_fp64_vs_fd": (np.abs(g64 - fd) / np.abs(fd)).tolist(),
+        "rel_err_fp32_vs_fp64": (np.abs(g32 - g64) / np.abs(g64)).tolist(),
+        "rel_err_fp32_vs_fd": (np.abs(g32 - fd) / np.abs(fd)).tolist(),
+        "ms_loss_grad_x_theta": float(np.median(times)),
+        "calibration": {"steps": steps, "optimizer": "Adam lr 0.01 on theta / natural unit", "s_total": t_cal,
+                        "loss_first_last": [hist_loss[0], hist_loss[-1]],
+                        "traj_rms_err_cells_first_last": [hist_err[0], hist_err[-1]],
+                        "traj_rms_err_cells": hist_err[:: max(1, steps // 10)]},
+    }
+
+
+def run_diff_only(args):
+    """The differentiation form alone (cfg4), one JSON line."""
+    import torch
+    cgs = importlib.import_module("4d_lung_gb300")
+    synth = importlib.import_module("4d_lung_gb300.synth")
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    rep = differentiation_report(cgs, synth, torch, dev, stream.cuda_stream)
+    print(json.dumps({"metric": "dL/dtheta vs FD and FP64; self-calibration", "differentiation": rep}), flush=True)
+    return 0
+
+
+def run_precision_only(args):
+    """Precision form of a workload (cfg2: 160x160x112, 16 coils, 20 CG
+    iterations): per-iteration relative L2 error of the FP32 and the
+    compensated-spreading solves against the FP64 GPU solve; one JSON line."""
+    import torch
+    cgs = importlib.import_module("4d_lung_gb300")
+    synth = importlib.import_module("4d_lung_gb300.synth")
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s = make_workload(
+        cgs, synth, torch, args.workload, 0, stream.cuda_stream, args.dcf)
+    x = torch.zeros((len(sbins),) + w.img, dtype=torch.complex64, device=dev)
+    rep = precision_report(reco, data, x, w.cg_iters, torch, dev)
+    line = {"metric": "rel L2 vs FP64 per CG iteration (max over bins)", "workload": w.name,
+            "config": {"img": list(w.img), "grid": list(w.grid), "coils": w.n_ch, "bins": len(sbins),
+                       "samples": int(sum(len(s) for s in sbins)), "cg_iters": w.cg_iters, "kb_w": kb_w,
+                       "kb_b": round(kb_b, 4), "dcf": args.dcf}, "precision": rep}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -295,12 +466,14 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
     w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s = make_workload(
-        cgs, synth, torch, args.workload, local, stream.cuda_stream, args.dcf)
+        cgs, synth, torch, args.workload, local, stream.cuda_stream, args.dcf, args.max_bins)
     torch.cuda.synchronize(dev)
     nb = len(sbins)
     sizes = [len(s) for s in sbins]
     x = torch.zeros((nb,) + w.img, dtype=torch.complex64, device=dev)
     iters = w.cg_iters
+    # launch shapes picked by the library's autotuner (timed batched applies)
+    tune = None if args.no_autotune else reco.autotune()
 
     for _ in range(args.warmup):
         res, its = reco.cg_sense_batched_tensor(data, x, 0.0, iters, want_stats=True)
@@ -355,6 +528,17 @@ def run_ours(args):
                  "launches": reco.launch_count(),
                  "form": "per-bin, per-coil launches, unfused, cuFFT full-grid c2c, global-atomic spreading, "
                          "host loop test per iteration"}
+
+    # precision: the chosen form (and its compensated-spreading variant)
+    # against the full-FP64 GPU form, iteration by iteration
+    precision = None
+    if not args.no_precision:
+        precision = precision_report(reco, data, x, iters, torch, dev)
+
+    # differentiation form (cfg4): trajectory gradients and self-calibration
+    diff = None
+    if not args.no_diff:
+        diff = differentiation_report(cgs, synth, torch, dev, stream.cuda_stream)
 
     # end to end through the host-buffer C ABI call (pinned host memory)
     h_data = torch.empty(data.shape, dtype=torch.complex64, pin_memory=True)
@@ -440,6 +624,9 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "s_per_4d_recon": float(te.item()) / args.steps},
         "roofline": roofline,
+        "precision": precision,
+        "autotune": tune,
+        "differentiation": diff,
         "plain": plain,
     }
     if rank == 0 and not args.no_cpu:
@@ -463,11 +650,23 @@ def main():
     ap.add_argument("--workload", default="cfg3")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-bin GPU form")
+    ap.add_argument("--no-precision", action="store_true", help="skip the per-iteration FP64 comparison")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--no-diff", action="store_true", help="skip the differentiation form (cfg4)")
+    ap.add_argument("--diff-only", action="store_true", help="only the differentiation form (one JSON line)")
+    ap.add_argument("--max-bins", type=int, default=0,
+                    help="keep only the first N respiratory bins (small cases for profiling)")
+    ap.add_argument("--precision-only", action="store_true",
+                    help="only the precision form of --workload (one JSON line of per-iteration errors)")
     ap.add_argument("--dcf", default="voronoi", choices=["voronoi", "radial"],
                     help="density weights: per-bin Voronoi volumes or a radial stand-in")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.precision_only:
+        return run_precision_only(args)
+    if args.diff_only:
+        return run_diff_only(args)
     return run_ours(args)
 
 

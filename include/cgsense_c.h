@@ -262,6 +262,23 @@ int cgs_loss_grad_fp64_d(cgs_ctx* ctx, int32_t bin, const void* x_dev, const voi
  * next call that spreads. */
 int cgs_update_trajectory_d(cgs_ctx* ctx, const double* k_dev);
 
+/* Accumulation mode of the spreading (the adjoint gridding, Reco.cpp:492-504):
+ * CGS_PREC_FP32 (default) plain FP32 sums in a fixed order; CGS_PREC_COMPENSATED
+ * Kahan-compensated FP32 sums (the precision form).  FFT passes are FP32 and
+ * the CG scalars FP64 in both. */
+#define CGS_PREC_FP32 0
+#define CGS_PREC_COMPENSATED 1
+int cgs_set_precision(cgs_ctx* ctx, int32_t mode);
+
+/* Autotuner: times one batched E^H D E application of every bin for each
+ * candidate launch shape -- coils per spreading block (all that fit, then
+ * 1/2, 1/3, 1/4 of them), then coils per interpolation thread (2, 4, 6, 8)
+ * -- and keeps the fastest for this context.  times_ms (may be NULL)
+ * receives the median time of each candidate in that order; the chosen
+ * shape is returned in *spread_cc and *interp_cc (may be NULL). */
+int cgs_autotune(cgs_ctx* ctx, float* times_ms, int32_t max_times, int32_t* n_times, int32_t* spread_cc,
+                 int32_t* interp_cc);
+
 /* Centred 3-D FFT (sign -1 forward, +1 backward, unscaled) that allocates no
  * device memory, for callers that cannot let a library allocate: code
  * running under a host application that owns all device memory through its

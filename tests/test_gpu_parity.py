@@ -118,7 +118,7 @@ def oversampled_case(oracle_mod, o64, img, grid, nch, n_lines, n_read, seed=3, k
 
 @pytest.mark.parametrize("img,grid", [((16, 16, 16), (32, 32, 32)), ((32, 24, 20), (64, 48, 40)),
                                       ((20, 16, 12), (32, 32, 24)),
-                                      # Gx >= 128: spreading fused with the adjoint x pass
+                                      # Gx >= 128: wide pruned x passes
                                       ((64, 16, 16), (128, 32, 32)), ((100, 12, 10), (192, 24, 20))])
 def test_oversampled_nufft_vs_oracle(gpu_lib, cgs, oracle_mod, o64, img, grid):
     """2x oversampled grid with zero-pad / crop (pruned FFT passes)."""
@@ -186,6 +186,30 @@ def test_batched_bins_match_per_bin_oracle(gpu_lib, cgs, oracle_mod, o64, synth,
         assert np.allclose(res[bi, :6], reso, rtol=1e-4)
 
 
+def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
+    """The autotuner only changes launch shapes (coils per spreading block,
+    coils per interpolation thread); every coil keeps its summation order,
+    so the batched solve is bitwise unchanged."""
+    img, grid, nch = (32, 24, 20), (64, 48, 40), 7
+    k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 40, 48)
+    bins = synth.bin_samples([np.arange(0, 15), np.arange(15, 40)], 48)
+    smaps = synth.coil_maps(img, nch)
+    rng = np.random.default_rng(9)
+    data = (rng.standard_normal((nch, k.shape[0])) + 1j * rng.standard_normal((nch, k.shape[0]))).astype(np.complex64)
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b)
+    r.set_trajectory(k)
+    r.set_bins(bins)
+    r.set_smaps(smaps)
+    x0, res0, _ = r.cg_sense_batched(data, 0.0, 5)
+    tune = r.autotune()
+    assert tune["spread_coils_per_block"] in range(1, nch + 1)
+    assert tune["interp_coils_per_thread"] in (2, 4, 6, 8)
+    assert len(tune["candidates_ms"]) >= 5 and all(t > 0 for t in tune["candidates_ms"])
+    x1, res1, _ = r.cg_sense_batched(data, 0.0, 5)
+    assert np.array_equal(x0, x1)
+    assert np.array_equal(res0, res1)
+
+
 def test_empty_bin_and_zero_data(gpu_lib, cgs, synth):
     """A bin without samples (or all-zero data) has a zero right-hand side:
     the solve returns x = 0 after 0 iterations."""
@@ -228,7 +252,8 @@ def test_input_faults_are_reported(gpu_lib, cgs, synth):
     assert e.value.code == cgs.CGS_ERR_NONFINITE
 
 
-def test_precision_form_against_fp64(gpu_lib, cgs, oracle_mod, o64, synth):
+@pytest.mark.parametrize("compensated", [False, True])
+def test_precision_form_against_fp64(gpu_lib, cgs, oracle_mod, o64, synth, compensated):
     """The complex64 solve (FP32 gridding and FFT, FP64 CG scalars) against
     the full-FP64 GPU solve, iteration by iteration: relative L2 <= 1e-4.
     The FP64 GPU solve itself agrees with the FP64 CPU oracle to 1e-6 (its
@@ -246,6 +271,7 @@ def test_precision_form_against_fp64(gpu_lib, cgs, oracle_mod, o64, synth):
     data += synth.complex_noise(data.shape, 30.0, float(np.sqrt(np.mean(np.abs(data) ** 2))))
     r.set_dcf(dcf)
     r.set_smaps(smaps)
+    r.set_precision(compensated)
     iters = 10
     stream = torch.cuda.Stream()
     r.set_stream(stream.cuda_stream)
