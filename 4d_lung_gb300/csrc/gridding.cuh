@@ -236,18 +236,37 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
         }
     }
     __syncthreads();
-    // store the tile: z fastest, coalesced rows of TILE_Z points
+    // store the tile: rows of TILE_Z points along z, two points per 16-byte
+    // store; a whole row is in the grid when the grid is a multiple of the
+    // tile along y and z (checked per row otherwise)
+    static_assert(TILE_Z % 2 == 0 && (TILE_Z & (TILE_Z - 1)) == 0 && (TILE_Y & (TILE_Y - 1)) == 0,
+                  "tile sides must be powers of two");
+    constexpr int ZH = TILE_Z / 2;
+    constexpr int ROW_SHIFT = __builtin_ctz(ZH), Y_SHIFT = __builtin_ctz(TILE_Y);
     float2* grid = a.grid + (long long)blockIdx.z * a.grid_bs + (long long)c0 * a.coil_stride;
     const int Gx = a.G[0], Gy = a.G[1], Gz = a.G[2];
-    for (int e = tid; e < ncc * TILE_PTS; e += SPREAD_THREADS) {
-        const int c = e / TILE_PTS, local = e - c * TILE_PTS;
-        const int lz = local % TILE_Z, ly = (local / TILE_Z) % TILE_Y, lx = local / (TILE_Z * TILE_Y);
-        const int X = x0 + lx, Y = y0 + ly, Z = z0 + lz;
-        if (X < Gx && Y < Gy && Z < Gz) {
-            const int q = c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + lz;
-            float2 v = acc[q];
-            if (KAHAN) v = make_float2(__fsub_rn(v.x, cmp[q].x), __fsub_rn(v.y, cmp[q].y));
-            grid[(long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z] = v;
+    const bool pairs = (Gz % 2 == 0) && (reinterpret_cast<uintptr_t>(a.grid) & 15) == 0 && (a.coil_stride % 2 == 0) &&
+                       (a.grid_bs % 2 == 0);
+    for (int e = tid; e < ncc * (TILE_PTS / 2); e += SPREAD_THREADS) {
+        const int zh = e & (ZH - 1);
+        const int row = e >> ROW_SHIFT;                 // (c, lx, ly) rows of TILE_Z points
+        const int ly = row & (TILE_Y - 1);
+        const int lx = (row >> Y_SHIFT) % TILE_X;
+        const int c = (row >> Y_SHIFT) / TILE_X;
+        const int X = x0 + lx, Y = y0 + ly, Z = z0 + 2 * zh;
+        if (X >= Gx || Y >= Gy || Z >= Gz) continue;
+        const int q = c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + 2 * zh;
+        float2 v0 = acc[q], v1 = acc[q + 1];
+        if (KAHAN) {
+            v0 = make_float2(__fsub_rn(v0.x, cmp[q].x), __fsub_rn(v0.y, cmp[q].y));
+            v1 = make_float2(__fsub_rn(v1.x, cmp[q + 1].x), __fsub_rn(v1.y, cmp[q + 1].y));
+        }
+        float2* dst = grid + (long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z;
+        if (pairs) {
+            *reinterpret_cast<float4*>(dst) = make_float4(v0.x, v0.y, v1.x, v1.y);
+        } else {
+            dst[0] = v0;
+            if (Z + 1 < Gz) dst[1] = v1;
         }
     }
 }
