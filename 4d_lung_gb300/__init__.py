@@ -52,7 +52,8 @@ EXPORTS = [
     "cgs_profile_apply", "cgs_cg_solve_images", "cgs_alloc_host", "cgs_free_host",
     "cgs_fft3_noalloc", "cgs_cg_solve_plain_d", "cgs_voronoi_dcf", "cgs_cg_solve_trace_d",
     "cgs_cg_solve_fp64_d", "cgs_estimate_density_v3d", "cgs_loss_grad_d", "cgs_loss_grad_fp64_d",
-    "cgs_update_trajectory_d", "cgs_set_precision", "cgs_autotune",
+    "cgs_update_trajectory_d", "cgs_set_precision", "cgs_autotune", "cgs_rhs_d", "cgs_apply_vjp_k_d",
+    "cgs_rhs_vjp_k_d", "cgs_trajectory_serial",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -158,6 +159,10 @@ def lib():
         "cgs_update_trajectory_d": (C.c_int, [vp, vp]),
         "cgs_set_precision": (C.c_int, [vp, C.c_int32]),
         "cgs_autotune": (C.c_int, [vp, vp, C.c_int32, vp, vp, vp]),
+        "cgs_rhs_d": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp]),
+        "cgs_apply_vjp_k_d": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp, vp]),
+        "cgs_rhs_vjp_k_d": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp, vp]),
+        "cgs_trajectory_serial": (C.c_uint64, [vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
         "cgs_cg_solve_fp64_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
     }

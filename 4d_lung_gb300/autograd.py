@@ -10,6 +10,13 @@ dc_loss is a torch::autograd::Function over cgs_loss_grad_d: the FP32
 gridding/FFT path of the library computes L = 1/2 sum D |E S x - y|^2,
 dL/dx and dL/dk on the GPU; the wave trajectory's dependence on its six
 parameters is plain PyTorch, so autograd chains dL/dk into dL/dtheta.
+
+cg_unrolled runs the batched CG-SENSE solve (Reco.cpp:175-321) as PyTorch
+operations over two libtorch operators, apply_a (E^H D E) and rhs
+(E^H D y), whose backward passes give the trajectory vector-Jacobian
+products; every iteration is checkpointed (recomputed in the backward
+pass), so memory holds four vectors per iteration instead of its
+intermediates.  CG scalars are FP64, vectors complex64.
 """
 from __future__ import annotations
 
@@ -44,6 +51,54 @@ def dc_loss(reco, x, k, y, bin=0):
     k: float64 [ns][3] (all samples of the context), y: complex64 [n_ch][ns]."""
     load_ops()
     return torch.ops.cgsense.dc_loss(reco.handle, int(bin), x, k, y)
+
+
+def apply_a(reco, p, k, bin0=0):
+    """q = A(k) p for bins [bin0, bin0 + len(p)): p complex64 [nb][voxels]."""
+    load_ops()
+    return torch.ops.cgsense.apply_a(reco.handle, int(bin0), int(p.shape[0]), p, k)
+
+
+def rhs(reco, y, k, bin0=0, nb=None):
+    """b = E^H D y of bins [bin0, bin0 + nb): complex64 [nb][voxels]."""
+    load_ops()
+    nb = reco.num_bins() - bin0 if nb is None else nb
+    return torch.ops.cgsense.rhs(reco.handle, int(bin0), int(nb), y, k, int(reco.ni))
+
+
+def _dot(a, b):
+    """Per-bin sum of conj(a) b in FP64 (complex128 [nb])."""
+    return torch.sum(a.conj().to(torch.complex128) * b.to(torch.complex128), dim=-1)
+
+
+def cg_unrolled(reco, k, y, iters, checkpoint=True):
+    """x after `iters` CG-SENSE iterations of every bin (complex64
+    [nbins][voxels]), differentiable in k.  The reference's loop with complex
+    alpha = rr / <p, q> and beta = rr_new / rr (Reco.cpp:232-309); no early
+    stop (the iteration count is fixed for differentiation)."""
+    from torch.utils.checkpoint import checkpoint as ckpt
+    b = rhs(reco, y, k)
+    x = torch.zeros_like(b)
+    r = b
+    p = b
+    rr = _dot(r, r).real
+
+    def step(x, r, p, rr, k):
+        q = apply_a(reco, p.contiguous(), k)
+        alpha = (rr / _dot(p, q)).to(torch.complex64)[:, None]
+        x = x + alpha * p
+        r = r - alpha * q
+        rr_new = _dot(r, r).real
+        beta = (rr_new / rr).to(torch.complex64)[:, None]
+        p = r + beta * p
+        return x, r, p, rr_new
+
+    for _ in range(iters):
+        if checkpoint:
+            x, r, p, rr = ckpt(step, x, r, p, rr, k, use_reentrant=False)
+        else:
+            x, r, p, rr = step(x, r, p, rr, k)
+    return x
 
 
 def wave_trajectory_torch(w, theta, lines=None):

@@ -97,6 +97,7 @@ struct cgs_ctx {
     DevBuf d_plane_rng;
     // loss gradients: derivative records, gathered measured samples, partials
     DevBuf d_drec, d_gy, d_gpart, d_flag;
+    DevBuf d_pa, d_pda;          // stored values / derivatives of E S p (operator VJPs)
     bool drec_valid = false;
     bool kahan = false;          // compensated spreading (cgs_set_precision)
     // launch shapes (cgs_autotune): coils per spreading block (0: as many as
@@ -104,6 +105,7 @@ struct cgs_ctx {
     int spread_cc = 0;
     int interp_cc = 4;
     bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
+    uint64_t traj_serial = 0;    // incremented whenever the coordinates change
     bool tiles_stale = false;    // spreading lists built from older coordinates
     int ntx = 0, nty = 0, ntz = 0, ntiles = 0;
     // coil maps
@@ -669,6 +671,35 @@ int centred_fft_dev(cgs_ctx* c, float2* a, int sign, int rescale)
 // C ABI
 // ===========================================================================
 
+// derivative records for the current coordinates
+int ensure_grad_records(cgs_ctx* c)
+{
+    if (c->drec_valid) return CGS_OK;
+    CGS_CUDA(c, c->d_drec.ensure(std::max<long long>(c->total, 1) * sizeof(TapRecord)));
+    CGS_CUDA(c, launch_tap_grad_records(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, kb_params(c),
+                                        c->d_drec.as<TapRecord>(), c->stream));
+    c->drec_valid = true;
+    return CGS_OK;
+}
+
+PairGradArgs pair_args(const cgs_ctx* c, int b, int slot)
+{
+    PairGradArgs pa{};
+    pa.grid = c->d_grid.as<float2>() + (long long)slot * c->nch * c->Ng;
+    pa.coil_stride = c->Ng;
+    pa.rec = c->d_rec.as<TapRecord>();
+    pa.drec = c->d_drec.as<TapRecord>();
+    pa.dcf = c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr;
+    pa.sorted = c->d_sorted.as<int>();
+    pa.s0 = c->h_bin_off[b];
+    pa.n = c->h_bin_off[b + 1] - pa.s0;
+    pa.nch = c->nch;
+    for (int a = 0; a < 3; ++a) pa.G[a] = c->G[a];
+    pa.thresh = c->thresh;
+    pa.scale = (float)c->adj_scale_total;
+    return pa;
+}
+
 extern "C" {
 
 void cgs_default_params(cgs_params* p)
@@ -791,6 +822,9 @@ int cgs_set_trajectory(cgs_ctx* c, const double* k, int64_t ns)
         if (!std::isfinite(k[i])) return fail(c, CGS_ERR_NONFINITE, "non-finite trajectory coordinate");
     c->h_k.assign(k, k + 3 * ns);
     c->ns = ns;
+    c->k_host_stale = false;
+    c->tiles_stale = false;
+    ++c->traj_serial;
     CGS_TRY(upload(c, c->d_k, k, (size_t)(3 * std::max<int64_t>(ns, 1)) * sizeof(double)));
     c->bins.assign(1, std::vector<int>());
     c->bins[0].resize(ns);
@@ -1385,6 +1419,7 @@ int cgs_update_trajectory_d(cgs_ctx* c, const double* k)
     c->k_host_stale = true;
     c->tiles_stale = true;
     c->drec_valid = false;
+    ++c->traj_serial;
     if (!c->bins_dirty)   // same samples, same sorted order: new tap records only
         CGS_CUDA(c, launch_tap_records(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, kb_params(c),
                                        c->d_rec.as<TapRecord>(), c->stream));
@@ -1397,12 +1432,7 @@ int cgs_loss_grad_d(cgs_ctx* c, int32_t bin, const void* x, const void* y, doubl
     if (!x || !y || !loss) return fail(c, CGS_ERR_ARG, "null pointer");
     if (bin < 0 || bin >= c->nbins) return fail(c, CGS_ERR_ARG, "bin out of range");
     const long long s0 = c->h_bin_off[bin], n = c->h_bin_off[bin + 1] - s0;
-    if (!c->drec_valid) {
-        CGS_CUDA(c, c->d_drec.ensure(std::max<long long>(c->total, 1) * sizeof(TapRecord)));
-        CGS_CUDA(c, launch_tap_grad_records(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, kb_params(c),
-                                            c->d_drec.as<TapRecord>(), c->stream));
-        c->drec_valid = true;
-    }
+    CGS_TRY(ensure_grad_records(c));
     // forward chain of the bin: every coil's grid (the interpolation it ends
     // with is recomputed below together with the derivatives)
     CGS_TRY(fwd_chain(c, bin, 1, reinterpret_cast<const float2*>(x), 0, 0, true, false));
@@ -1576,5 +1606,81 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
     if (interp_cc) *interp_cc = c->interp_cc;
     return check_timeout(c);
 }
+
+int cgs_rhs_d(cgs_ctx* c, int32_t bin0, int32_t nb, const void* y, void* b)
+{
+    CGS_TRY(check_ready(c, true));
+    if (!y || !b) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (bin0 < 0 || nb < 1 || bin0 + nb > c->nbins) return fail(c, CGS_ERR_ARG, "bin range out of bounds");
+    CGS_CUDA(c, launch_gather_samples(reinterpret_cast<const float2*>(y), c->ns, c->d_sorted.as<int>(), c->total,
+                                      c->nch, c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr, c->d_yv.as<float2>(),
+                                      c->stream));
+    for (int g = bin0; g < bin0 + nb; g += c->ws_bins) {
+        const int n = std::min(c->ws_bins, bin0 + nb - g);
+        CGS_TRY(adj_chain(c, g, n, reinterpret_cast<float2*>(b) + (long long)(g - bin0) * c->Ni, c->Ni, true, nullptr,
+                          nullptr));
+    }
+    return check_timeout(c);
+}
+
+int cgs_apply_vjp_k_d(cgs_ctx* c, int32_t bin0, int32_t nb, const void* p, const void* v, void* grad_k)
+{
+    CGS_TRY(check_ready(c, true, false));
+    if (!p || !v || !grad_k) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (bin0 < 0 || nb < 1 || bin0 + nb > c->nbins) return fail(c, CGS_ERR_ARG, "bin range out of bounds");
+    CGS_TRY(ensure_grad_records(c));
+    CGS_CUDA(c, c->d_pa.ensure(std::max<long long>(c->total, 1) * c->nch * sizeof(float2)));
+    CGS_CUDA(c, c->d_pda.ensure(std::max<long long>(c->total, 1) * c->nch * 3 * sizeof(float2)));
+    const float2* P = reinterpret_cast<const float2*>(p);
+    const float2* V = reinterpret_cast<const float2*>(v);
+    for (int g = bin0; g < bin0 + nb; g += c->ws_bins) {
+        const int n = std::min(c->ws_bins, bin0 + nb - g);
+        const long long off = (long long)(g - bin0) * c->Ni;
+        // pass 1: A = E S p and its derivatives, stored per sample
+        CGS_TRY(fwd_chain(c, g, n, P + off, c->Ni, 0, true, false));
+        for (int b = g; b < g + n; ++b) {
+            PairGradArgs pa = pair_args(c, b, b - g);
+            pa.outA = c->d_pa.as<float2>();
+            pa.outdA = c->d_pda.as<float2>();
+            CGS_LAUNCH(c, launch_pair_grad(pa, c->stream));
+        }
+        // pass 2: B = E S v, contracted with (A, dA)
+        CGS_TRY(fwd_chain(c, g, n, V + off, c->Ni, 0, true, false));
+        for (int b = g; b < g + n; ++b) {
+            PairGradArgs pa = pair_args(c, b, b - g);
+            pa.A = c->d_pa.as<float2>();
+            pa.dA = c->d_pda.as<float2>();
+            pa.grad_k = reinterpret_cast<float*>(grad_k);
+            CGS_LAUNCH(c, launch_pair_grad(pa, c->stream));
+        }
+    }
+    return check_timeout(c);
+}
+
+int cgs_rhs_vjp_k_d(cgs_ctx* c, int32_t bin0, int32_t nb, const void* y, const void* v, void* grad_k)
+{
+    CGS_TRY(check_ready(c, true, false));
+    if (!y || !v || !grad_k) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (bin0 < 0 || nb < 1 || bin0 + nb > c->nbins) return fail(c, CGS_ERR_ARG, "bin range out of bounds");
+    CGS_TRY(ensure_grad_records(c));
+    CGS_CUDA(c, c->d_gy.ensure(std::max<long long>(c->total, 1) * c->nch * sizeof(float2)));
+    // measured samples in sorted, coil-interleaved order (D is applied in the contraction)
+    CGS_CUDA(c, launch_gather_samples(reinterpret_cast<const float2*>(y), c->ns, c->d_sorted.as<int>(), c->total,
+                                      c->nch, nullptr, c->d_gy.as<float2>(), c->stream));
+    const float2* V = reinterpret_cast<const float2*>(v);
+    for (int g = bin0; g < bin0 + nb; g += c->ws_bins) {
+        const int n = std::min(c->ws_bins, bin0 + nb - g);
+        CGS_TRY(fwd_chain(c, g, n, V + (long long)(g - bin0) * c->Ni, c->Ni, 0, true, false));
+        for (int b = g; b < g + n; ++b) {
+            PairGradArgs pa = pair_args(c, b, b - g);
+            pa.A = c->d_gy.as<float2>();
+            pa.grad_k = reinterpret_cast<float*>(grad_k);
+            CGS_LAUNCH(c, launch_pair_grad(pa, c->stream));
+        }
+    }
+    return check_timeout(c);
+}
+
+uint64_t cgs_trajectory_serial(const cgs_ctx* c) { return c ? c->traj_serial : 0; }
 
 }  // extern "C"

@@ -151,4 +151,29 @@ struct InterpGradArgs {
     double* partials;          // out: [blocks] loss partial sums
 };
 
+// Trajectory vector-Jacobian products of the operator (grad.cu): one bin's
+// samples [s0, s0 + n) in sorted order; B = E S u and dB = dB/dk come from
+// the grid of the current image u.
+//   store mode (outA != null): outA = B, outdA = dB   [sorted][nch] / [sorted][nch][3]
+//   contract mode: grad_k[g] += scale D_i Re sum_c (conj(B) dA + conj(dB) A)
+//                  (dA may be null: a fixed first factor such as measured data)
+struct PairGradArgs {
+    const float2* grid;
+    long long coil_stride;
+    const TapRecord* rec;
+    const TapRecord* drec;
+    const float2* A;           // [sorted][nch]
+    const float2* dA;          // [sorted][nch][3], or null
+    float2* outA;              // store mode
+    float2* outdA;
+    const float* dcf;
+    const int* sorted;
+    long long s0, n;
+    int nch;
+    int G[3];
+    float thresh;
+    float scale;
+    float* grad_k;             // [ns][3] by global index, accumulated
+};
+
 }  // namespace cgs

@@ -179,4 +179,99 @@ cudaError_t launch_check_finite(const double* v, long long n, int* bad, cudaStre
     return cudaGetLastError();
 }
 
+// Values and coordinate derivatives of E S u at one bin's samples, then
+// either stored (outA) or contracted with a stored pair (A, dA).  One thread
+// per sample; coils in chunks of CC.
+template <int CC>
+__global__ void __launch_bounds__(128) k_pair_grad(PairGradArgs a)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= a.n) return;
+    const long long i = a.s0 + j;
+    float w[15], dw[15];
+    int nx, ny, nz, t0, t1, t2;
+    load_record(a.rec, i, w, nx, ny, nz);
+    load_record(a.drec, i, dw, t0, t1, t2);
+    const float D = a.dcf ? a.dcf[i] : 1.f;
+    const int Gy = a.G[1], Gz = a.G[2];
+    float gk0 = 0.f, gk1 = 0.f, gk2 = 0.f;
+    for (int c0 = 0; c0 < a.nch; c0 += CC) {
+        const int ncc = min(CC, a.nch - c0);
+        const float2* grid = a.grid + (long long)c0 * a.coil_stride;
+        float2 y[CC], d0[CC], d1[CC], d2[CC];
+#pragma unroll
+        for (int c = 0; c < CC; ++c) y[c] = d0[c] = d1[c] = d2[c] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int jx = 0; jx < 5; ++jx) {
+            const float wx = w[jx], dwx = dw[jx];
+            if (wx == 0.f) continue;
+            const int gx = nx - 2 + jx;
+#pragma unroll
+            for (int jy = 0; jy < 5; ++jy) {
+                const float wy = w[5 + jy], dwy = dw[5 + jy];
+                if (wy == 0.f) continue;
+                const long long row = ((long long)gx * Gy + (ny - 2 + jy)) * Gz + (nz - 2);
+#pragma unroll
+                for (int jz = 0; jz < 5; ++jz) {
+                    const float wz = w[10 + jz], dwz = dw[10 + jz];
+                    const float wt = (wx * wy) * wz;
+                    if (wz != 0.f && wt > a.thresh) {
+                        const float ex = (dwx * wy) * wz, ey = (wx * dwy) * wz, ez = (wx * wy) * dwz;
+#pragma unroll
+                        for (int c = 0; c < CC; ++c)
+                            if (c < ncc) {
+                                const float2 g = __ldg(grid + (long long)c * a.coil_stride + row + jz);
+                                y[c].x = fmaf(g.x, wt, y[c].x);
+                                y[c].y = fmaf(g.y, wt, y[c].y);
+                                d0[c].x = fmaf(g.x, ex, d0[c].x);
+                                d0[c].y = fmaf(g.y, ex, d0[c].y);
+                                d1[c].x = fmaf(g.x, ey, d1[c].x);
+                                d1[c].y = fmaf(g.y, ey, d1[c].y);
+                                d2[c].x = fmaf(g.x, ez, d2[c].x);
+                                d2[c].y = fmaf(g.y, ez, d2[c].y);
+                            }
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CC; ++c)
+            if (c < ncc) {
+                const long long e = i * a.nch + c0 + c;
+                if (a.outA) {
+                    a.outA[e] = y[c];
+                    a.outdA[3 * e + 0] = d0[c];
+                    a.outdA[3 * e + 1] = d1[c];
+                    a.outdA[3 * e + 2] = d2[c];
+                } else {
+                    // Re(conj(B) dA + conj(dB) A), B = y, dB = d*
+                    const float2 A = a.A[e];
+                    gk0 += A.x * d0[c].x + A.y * d0[c].y;
+                    gk1 += A.x * d1[c].x + A.y * d1[c].y;
+                    gk2 += A.x * d2[c].x + A.y * d2[c].y;
+                    if (a.dA) {
+                        const float2 e0 = a.dA[3 * e + 0], e1 = a.dA[3 * e + 1], e2 = a.dA[3 * e + 2];
+                        gk0 += y[c].x * e0.x + y[c].y * e0.y;
+                        gk1 += y[c].x * e1.x + y[c].y * e1.y;
+                        gk2 += y[c].x * e2.x + y[c].y * e2.y;
+                    }
+                }
+            }
+    }
+    if (!a.outA) {
+        const long long g = a.sorted[i];
+        const float f = a.scale * D;
+        a.grad_k[3 * g + 0] += f * gk0;
+        a.grad_k[3 * g + 1] += f * gk1;
+        a.grad_k[3 * g + 2] += f * gk2;
+    }
+}
+
+cudaError_t launch_pair_grad(const PairGradArgs& a, cudaStream_t s)
+{
+    if (a.n == 0) return cudaSuccess;
+    k_pair_grad<2><<<(unsigned)((a.n + 127) / 128), 128, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
 }  // namespace cgs

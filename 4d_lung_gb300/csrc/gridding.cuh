@@ -165,9 +165,15 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
     float2* s_val = reinterpret_cast<float2*>(s_rec + SPREAD_BATCH);
 
     const int tid = threadIdx.x;
-    for (int e = tid; e < ncc * ACC_PTS; e += SPREAD_THREADS) {
-        acc[e] = make_float2(0.f, 0.f);
-        if (KAHAN) cmp[e] = make_float2(0.f, 0.f);
+    {
+        // ACC_PTS is even and both regions start 16-byte aligned: zero two points per store
+        float4* a4 = reinterpret_cast<float4*>(acc);
+        float4* c4 = reinterpret_cast<float4*>(cmp);
+        const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int e = tid; e < ncc * (ACC_PTS / 2); e += SPREAD_THREADS) {
+            a4[e] = z4;
+            if (KAHAN) c4[e] = z4;
+        }
     }
 
     const long long tp = a.tile_ptr_off[bin];
@@ -236,37 +242,39 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
         }
     }
     __syncthreads();
-    // store the tile: rows of TILE_Z points along z, two points per 16-byte
-    // store; a whole row is in the grid when the grid is a multiple of the
-    // tile along y and z (checked per row otherwise)
+    // store the tile: every thread keeps one (y, two-point z) position and
+    // walks the coils and every other x plane; two points per 16-byte store
+    // (a whole pair is in the grid when Gz is even)
     static_assert(TILE_Z % 2 == 0 && (TILE_Z & (TILE_Z - 1)) == 0 && (TILE_Y & (TILE_Y - 1)) == 0,
                   "tile sides must be powers of two");
     constexpr int ZH = TILE_Z / 2;
-    constexpr int ROW_SHIFT = __builtin_ctz(ZH), Y_SHIFT = __builtin_ctz(TILE_Y);
+    constexpr int XSTEP = SPREAD_THREADS / (ZH * TILE_Y);
+    static_assert(SPREAD_THREADS % (ZH * TILE_Y) == 0 && TILE_X % XSTEP == 0, "store mapping");
     float2* grid = a.grid + (long long)blockIdx.z * a.grid_bs + (long long)c0 * a.coil_stride;
     const int Gx = a.G[0], Gy = a.G[1], Gz = a.G[2];
     const bool pairs = (Gz % 2 == 0) && (reinterpret_cast<uintptr_t>(a.grid) & 15) == 0 && (a.coil_stride % 2 == 0) &&
                        (a.grid_bs % 2 == 0);
-    for (int e = tid; e < ncc * (TILE_PTS / 2); e += SPREAD_THREADS) {
-        const int zh = e & (ZH - 1);
-        const int row = e >> ROW_SHIFT;                 // (c, lx, ly) rows of TILE_Z points
-        const int ly = row & (TILE_Y - 1);
-        const int lx = (row >> Y_SHIFT) % TILE_X;
-        const int c = (row >> Y_SHIFT) / TILE_X;
-        const int X = x0 + lx, Y = y0 + ly, Z = z0 + 2 * zh;
-        if (X >= Gx || Y >= Gy || Z >= Gz) continue;
-        const int q = c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + 2 * zh;
-        float2 v0 = acc[q], v1 = acc[q + 1];
-        if (KAHAN) {
-            v0 = make_float2(__fsub_rn(v0.x, cmp[q].x), __fsub_rn(v0.y, cmp[q].y));
-            v1 = make_float2(__fsub_rn(v1.x, cmp[q + 1].x), __fsub_rn(v1.y, cmp[q + 1].y));
-        }
-        float2* dst = grid + (long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z;
-        if (pairs) {
-            *reinterpret_cast<float4*>(dst) = make_float4(v0.x, v0.y, v1.x, v1.y);
-        } else {
-            dst[0] = v0;
-            if (Z + 1 < Gz) dst[1] = v1;
+    const int zh = tid % ZH, ly = (tid / ZH) % TILE_Y, lx0 = tid / (ZH * TILE_Y);
+    const int Y = y0 + ly, Z = z0 + 2 * zh;
+    if (Y < Gy && Z < Gz) {
+        for (int c = 0; c < ncc; ++c) {
+            for (int lx = lx0; lx < TILE_X; lx += XSTEP) {
+                const int X = x0 + lx;
+                if (X >= Gx) break;
+                const int q = c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + 2 * zh;
+                float2 v0 = acc[q], v1 = acc[q + 1];
+                if (KAHAN) {
+                    v0 = make_float2(__fsub_rn(v0.x, cmp[q].x), __fsub_rn(v0.y, cmp[q].y));
+                    v1 = make_float2(__fsub_rn(v1.x, cmp[q + 1].x), __fsub_rn(v1.y, cmp[q + 1].y));
+                }
+                float2* dst = grid + (long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z;
+                if (pairs) {
+                    *reinterpret_cast<float4*>(dst) = make_float4(v0.x, v0.y, v1.x, v1.y);
+                } else {
+                    dst[0] = v0;
+                    if (Z + 1 < Gz) dst[1] = v1;
+                }
+            }
         }
     }
 }

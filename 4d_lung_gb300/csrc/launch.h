@@ -94,6 +94,7 @@ cudaError_t launch_tap_grad_records(const double* k, const int* sample_idx, long
 int interp_grad_blocks(long long n);
 cudaError_t launch_interp_grad(const InterpGradArgs& a, cudaStream_t s);
 cudaError_t launch_check_finite(const double* v, long long n, int* bad, cudaStream_t s);
+cudaError_t launch_pair_grad(const PairGradArgs& a, cudaStream_t s);
 
 // Full-FP64 form (fp64.cu): the precision reference on the GPU.
 struct Fp64Args {

@@ -262,6 +262,25 @@ int cgs_loss_grad_fp64_d(cgs_ctx* ctx, int32_t bin, const void* x_dev, const voi
  * next call that spreads. */
 int cgs_update_trajectory_d(cgs_ctx* ctx, const double* k_dev);
 
+/* Right-hand side of the CG solve for bins [bin0, bin0 + nb):
+ * b[bin] = sum_c conj(S_c) E_c^H (D y_c)  (CGSense.cpp:226-235, Reco.cpp:182-190),
+ * with the reference's rescale.  y complex64 [n_ch][ns]; b complex64 [nb][Ni]. */
+int cgs_rhs_d(cgs_ctx* ctx, int32_t bin0, int32_t nb, const void* y_dev, void* b_dev);
+
+/* Trajectory vector-Jacobian products of the solve's building blocks, for
+ * backpropagation through an unrolled CG (all device pointers; grad_k is
+ * float [ns][3] and ACCUMULATED, +=):
+ *   cgs_apply_vjp_k_d: grad_k += d/dk Re<v, A(k) p>, A = E^H D E of
+ *                      cgs_apply_ehde_d, p and v complex64 [nb][Ni];
+ *   cgs_rhs_vjp_k_d:   grad_k += d/dk Re<v, b(k)>, b of cgs_rhs_d. */
+/* Serial number of the context's coordinates: changes whenever
+ * cgs_set_trajectory or cgs_update_trajectory_d sets new ones (callers that
+ * cache an uploaded trajectory compare it). */
+uint64_t cgs_trajectory_serial(const cgs_ctx* ctx);
+
+int cgs_apply_vjp_k_d(cgs_ctx* ctx, int32_t bin0, int32_t nb, const void* p_dev, const void* v_dev, void* grad_k_dev);
+int cgs_rhs_vjp_k_d(cgs_ctx* ctx, int32_t bin0, int32_t nb, const void* y_dev, const void* v_dev, void* grad_k_dev);
+
 /* Accumulation mode of the spreading (the adjoint gridding, Reco.cpp:492-504):
  * CGS_PREC_FP32 (default) plain FP32 sums in a fixed order; CGS_PREC_COMPENSATED
  * Kahan-compensated FP32 sums (the precision form).  FFT passes are FP32 and

@@ -15,7 +15,7 @@ HEADER = os.path.join(ROOT, "include", "cgsense_c.h")
 
 def declared_symbols():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"^\s*(?:int|void\s*\*|void|const char\s*\*|int64_t)\s*(cgs_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|void\s*\*|void|const char\s*\*|int64_t|uint64_t)\s*(cgs_\w+)\s*\(", text, re.M)))
 
 
 @pytest.fixture(scope="module")
