@@ -53,7 +53,7 @@ EXPORTS = [
     "cgs_fft3_noalloc", "cgs_cg_solve_plain_d", "cgs_voronoi_dcf", "cgs_cg_solve_trace_d",
     "cgs_cg_solve_fp64_d", "cgs_estimate_density_v3d", "cgs_loss_grad_d", "cgs_loss_grad_fp64_d",
     "cgs_update_trajectory_d", "cgs_set_precision", "cgs_autotune", "cgs_rhs_d", "cgs_apply_vjp_k_d",
-    "cgs_rhs_vjp_k_d", "cgs_trajectory_serial",
+    "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -158,11 +158,12 @@ def lib():
         "cgs_loss_grad_fp64_d": (C.c_int, [vp, C.c_int32, vp, vp, vp, vp, vp]),
         "cgs_update_trajectory_d": (C.c_int, [vp, vp]),
         "cgs_set_precision": (C.c_int, [vp, C.c_int32]),
-        "cgs_autotune": (C.c_int, [vp, vp, C.c_int32, vp, vp, vp]),
+        "cgs_autotune": (C.c_int, [vp, vp, C.c_int32, vp, vp, vp, vp]),
         "cgs_rhs_d": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp]),
         "cgs_apply_vjp_k_d": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp, vp]),
         "cgs_rhs_vjp_k_d": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp, vp]),
         "cgs_trajectory_serial": (C.c_uint64, [vp]),
+        "cgs_get_stream": (C.c_void_p, [vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
         "cgs_cg_solve_fp64_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
     }
@@ -451,14 +452,16 @@ class Reco:
 
     def autotune(self):
         """Picks the fastest launch shapes for this context; returns
-        {"spread_coils_per_block", "interp_coils_per_thread", "candidates_ms"}."""
+        {"spread_coils_per_block", "spread_warps_per_plane",
+         "interp_coils_per_thread", "candidates_ms"}."""
         t = np.zeros(32, np.float32)
         n = np.zeros(1, np.int32)
         sc = np.zeros(1, np.int32)
+        sw = np.zeros(1, np.int32)
         ic = np.zeros(1, np.int32)
-        self._check(self._L.cgs_autotune(self._ctx, _p(t), 32, _p(n), _p(sc), _p(ic)))
-        return {"spread_coils_per_block": int(sc[0]), "interp_coils_per_thread": int(ic[0]),
-                "candidates_ms": [float(v) for v in t[: n[0]]]}
+        self._check(self._L.cgs_autotune(self._ctx, _p(t), 32, _p(n), _p(sc), _p(sw), _p(ic)))
+        return {"spread_coils_per_block": int(sc[0]), "spread_warps_per_plane": int(sw[0]),
+                "interp_coils_per_thread": int(ic[0]), "candidates_ms": [float(v) for v in t[: n[0]]]}
 
     def set_precision(self, compensated):
         """Compensated (Kahan) spreading on or off."""

@@ -103,6 +103,7 @@ struct cgs_ctx {
     // launch shapes (cgs_autotune): coils per spreading block (0: as many as
     // fit), coils per interpolation thread
     int spread_cc = 0;
+    int spread_wpp = 1;          // warps per x plane of a spreading tile
     int interp_cc = 4;
     bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
     uint64_t traj_serial = 0;    // incremented whenever the coordinates change
@@ -527,7 +528,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
         sa.nty = c->nty;
         sa.ntz = c->ntz;
         sa.thresh = c->thresh;
-        CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->kahan, c->stream));
+        CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->kahan, c->spread_wpp, c->stream));
 
         StridedPassArgs ax{};
         ax.in = c->d_grid.as<float2>();
@@ -806,6 +807,8 @@ int cgs_set_stream(cgs_ctx* c, void* stream)
     c->stream = s;
     return CGS_OK;
 }
+
+void* cgs_get_stream(const cgs_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 int cgs_sync(cgs_ctx* c)
 {
@@ -1536,7 +1539,7 @@ int cgs_set_precision(cgs_ctx* c, int32_t mode)
 // interpolation thread).  times_ms (optional, max_times entries) receives
 // the median time of every candidate in that order.
 int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_times, int32_t* spread_cc,
-                 int32_t* interp_cc)
+                 int32_t* spread_wpp, int32_t* interp_cc)
 {
     CGS_TRY(check_ready(c, true));
     const long long Ni = c->Ni;
@@ -1565,7 +1568,8 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
         all.push_back(best);
         return CGS_OK;
     };
-    // coils per spreading block: the largest that fits, then halves, thirds
+    // coils per spreading block (the largest that fits, then halves, thirds,
+    // quarters) x warps per x plane (1, 2)
     std::vector<int> sc;
     const int mc = std::min(c->nch, spread_max_coils(c->kahan));
     for (int d = 1; d <= 4; ++d) {
@@ -1573,16 +1577,22 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
         if (std::find(sc.begin(), sc.end(), v) == sc.end()) sc.push_back(v);
     }
     float best = 1e30f;
-    int best_sc = sc[0];
-    for (int v : sc) {
-        c->spread_cc = v;
-        float ms;
-        CGS_TRY(time_apply(ms));
-        if (ms < best) {
-            best = ms;
-            best_sc = v;
+    int best_sc = sc[0], best_wpp = 1;
+    for (int wpp : {1, 2}) {
+        for (int v : sc) {
+            if (wpp == 2 && v < 2) continue;
+            c->spread_cc = v;
+            c->spread_wpp = wpp;
+            float ms;
+            CGS_TRY(time_apply(ms));
+            if (ms < best) {
+                best = ms;
+                best_sc = v;
+                best_wpp = wpp;
+            }
         }
     }
+    c->spread_wpp = best_wpp;
     c->spread_cc = best_sc;
     best = 1e30f;
     int best_ic = c->interp_cc;
@@ -1603,6 +1613,7 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
         for (int i = 0; i < (int)all.size() && i < max_times; ++i) times_ms[i] = all[i];
     if (n_times) *n_times = (int32_t)all.size();
     if (spread_cc) *spread_cc = c->spread_cc;
+    if (spread_wpp) *spread_wpp = c->spread_wpp;
     if (interp_cc) *interp_cc = c->interp_cc;
     return check_timeout(c);
 }

@@ -139,15 +139,21 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
 
 constexpr int SPREAD_BATCH = 32;   // samples staged per round
 
-// CC: compile-time upper bound of the coils per block (a.cc <= CC); the
-// coil loop is unrolled so that the shared-memory loads, FMAs and stores of
-// all coils of one grid point issue back to back.
+// WPP warps share an x plane, each owning an equal part of the block's coils
+// (so every grid value still has a single owning lane).  CCW: compile-time
+// upper bound of the coils of one warp; the coil loop is unrolled so that the
+// shared-memory loads, FMAs and stores of all its coils of one grid point
+// issue back to back.
 // KAHAN: compensated summation (the precision form): every accumulator has
 // a compensation term (the low-order part lost by its last addition), and
 // the stored value is sum - compensation.
-template <int CC, bool KAHAN>
-__global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
+constexpr int SPREAD_VAL_STRIDE = 12;   // staged values per sample (max coils per block)
+
+template <int CCW, int WPP, bool KAHAN>
+__global__ void __launch_bounds__(32 * TILE_X * WPP) k_spread(SpreadArgs a)
 {
+    constexpr int NT = 32 * TILE_X * WPP;
+    static_assert(CCW * WPP <= SPREAD_VAL_STRIDE, "staged value row");
     extern __shared__ float4 s_dyn[];
     const int bin = a.bin0 + blockIdx.z;
     const int tile = blockIdx.x;
@@ -170,7 +176,7 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
         float4* a4 = reinterpret_cast<float4*>(acc);
         float4* c4 = reinterpret_cast<float4*>(cmp);
         const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int e = tid; e < ncc * (ACC_PTS / 2); e += SPREAD_THREADS) {
+        for (int e = tid; e < ncc * (ACC_PTS / 2); e += NT) {
             a4[e] = z4;
             if (KAHAN) c4[e] = z4;
         }
@@ -181,25 +187,28 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
     const int* idx = a.tile_idx + a.tile_idx_off[bin];
     const long long sbase = a.bin_off[bin];
     const int warp = tid >> 5, lane = tid & 31;
-    const int gx = x0 + warp;
+    const int plane = warp % TILE_X, part = warp / TILE_X;
+    const int per = (ncc + WPP - 1) / WPP;
+    const int cb = part * per, nmy = min(per, ncc - cb);   // this warp's coils [cb, cb + nmy)
+    const int gx = x0 + plane;
     const int jy = lane / 5, jz = lane - 5 * (lane / 5);
-    const int2 run = a.plane_rng[((long long)bin * gridDim.x + tile) * TILE_X + warp];
+    const int2 run = a.plane_rng[((long long)bin * gridDim.x + tile) * TILE_X + plane];
 
     for (int s = beg; s < end; s += SPREAD_BATCH) {
         const int nbat = min(SPREAD_BATCH, end - s);
         __syncthreads();
-        for (int e = tid; e < nbat * 4; e += SPREAD_THREADS) {
+        for (int e = tid; e < nbat * 4; e += NT) {
             const long long si = sbase + idx[s + e / 4];
             reinterpret_cast<float4*>(s_rec)[e] = __ldg(reinterpret_cast<const float4*>(a.rec + si) + (e & 3));
         }
-        for (int e = tid; e < nbat * ncc; e += SPREAD_THREADS) {
+        for (int e = tid; e < nbat * ncc; e += NT) {
             const int j = e / ncc, c = e - j * ncc;
             const long long si = sbase + idx[s + j];
-            s_val[j * CC + c] = a.yv[si * a.nch + c0 + c];
+            s_val[j * SPREAD_VAL_STRIDE + c] = a.yv[si * a.nch + c0 + c];
         }
         __syncthreads();
         const int j0 = max(run.x - (s - beg), 0), j1 = min(run.y - (s - beg), nbat);
-        if (lane < 25) {
+        if (lane < 25 && nmy > 0) {
             for (int j = j0; j < j1; ++j) {
                 const float* w = reinterpret_cast<const float*>(&s_rec[j]);
                 int nx, ny, nz;
@@ -211,19 +220,19 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
                 const float wxv = w[jx], wyv = w[5 + jy], wzv = w[10 + jz];
                 const float wt = (wxv * wyv) * wzv;
                 if (wxv == 0.f || wyv == 0.f || wzv == 0.f || !(wt > a.thresh)) continue;
-                float2* pt = acc + (warp * TILE_Y + (gy - y0)) * TILE_ZP + (gz - z0);
-                const float2* v = s_val + j * CC;
-                float2 t[CC], vv[CC], e[CC];
+                float2* pt = acc + (size_t)cb * ACC_PTS + (plane * TILE_Y + (gy - y0)) * TILE_ZP + (gz - z0);
+                const float2* v = s_val + j * SPREAD_VAL_STRIDE + cb;
+                float2 t[CCW], vv[CCW], e[CCW];
 #pragma unroll
-                for (int c = 0; c < CC; ++c)
-                    if (c < ncc) {
+                for (int c = 0; c < CCW; ++c)
+                    if (c < nmy) {
                         t[c] = pt[c * ACC_PTS];
                         vv[c] = v[c];
                         if (KAHAN) e[c] = pt[(size_t)a.cc * ACC_PTS + c * ACC_PTS];
                     }
 #pragma unroll
-                for (int c = 0; c < CC; ++c)
-                    if (c < ncc) {
+                for (int c = 0; c < CCW; ++c)
+                    if (c < nmy) {
                         if (KAHAN) {
                             // y = v w - e;  s = t + y;  e = (s - t) - y;  t = s
                             const float yx = fmaf(vv[c].x, wt, -e[c].x), yy = fmaf(vv[c].y, wt, -e[c].y);
@@ -248,8 +257,8 @@ __global__ void __launch_bounds__(SPREAD_THREADS) k_spread(SpreadArgs a)
     static_assert(TILE_Z % 2 == 0 && (TILE_Z & (TILE_Z - 1)) == 0 && (TILE_Y & (TILE_Y - 1)) == 0,
                   "tile sides must be powers of two");
     constexpr int ZH = TILE_Z / 2;
-    constexpr int XSTEP = SPREAD_THREADS / (ZH * TILE_Y);
-    static_assert(SPREAD_THREADS % (ZH * TILE_Y) == 0 && TILE_X % XSTEP == 0, "store mapping");
+    constexpr int XSTEP = NT / (ZH * TILE_Y);
+    static_assert(NT % (ZH * TILE_Y) == 0 && TILE_X % XSTEP == 0, "store mapping");
     float2* grid = a.grid + (long long)blockIdx.z * a.grid_bs + (long long)c0 * a.coil_stride;
     const int Gx = a.G[0], Gy = a.G[1], Gz = a.G[2];
     const bool pairs = (Gz % 2 == 0) && (reinterpret_cast<uintptr_t>(a.grid) & 15) == 0 && (a.coil_stride % 2 == 0) &&

@@ -121,47 +121,58 @@ constexpr int SPREAD_CC_MAX = 12;
 
 size_t spread_smem_bytes(int cc, bool kahan)
 {
-    const int ccp = cc <= 4 ? 4 : (cc <= 8 ? 8 : SPREAD_CC_MAX);
     return (size_t)(kahan ? 2 : 1) * cc * ACC_PTS * sizeof(float2) + SPREAD_BATCH * sizeof(TapRecord) +
-           (size_t)SPREAD_BATCH * ccp * sizeof(float2);
+           (size_t)SPREAD_BATCH * SPREAD_VAL_STRIDE * sizeof(float2);
 }
 
 int spread_max_coils(bool kahan) { return kahan ? SPREAD_CC_MAX / 2 : SPREAD_CC_MAX; }
 
-template <bool K>
-static cudaError_t spread_attrs(int smax)
+template <int CCW, int WPP>
+static cudaError_t spread_attr_one(int smax_plain, int smax_kahan)
 {
-    cudaError_t e = cudaFuncSetAttribute(k_spread<4, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_spread<8, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    cudaError_t e = cudaFuncSetAttribute(k_spread<CCW, WPP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smax_plain);
     if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_spread<SPREAD_CC_MAX, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        e = cudaFuncSetAttribute(k_spread<CCW, WPP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax_kahan);
     return e;
 }
 
 cudaError_t kernels_init()
 {
-    cudaError_t e = spread_attrs<false>((int)spread_smem_bytes(SPREAD_CC_MAX, false));
-    if (e == cudaSuccess) e = spread_attrs<true>((int)spread_smem_bytes(SPREAD_CC_MAX / 2, true));
+    const int sp = (int)spread_smem_bytes(SPREAD_CC_MAX, false), sk = (int)spread_smem_bytes(SPREAD_CC_MAX / 2, true);
+    cudaError_t e = spread_attr_one<4, 1>(sp, sk);
+    if (e == cudaSuccess) e = spread_attr_one<8, 1>(sp, sk);
+    if (e == cudaSuccess) e = spread_attr_one<12, 1>(sp, sk);
+    if (e == cudaSuccess) e = spread_attr_one<2, 2>(sp, sk);
+    if (e == cudaSuccess) e = spread_attr_one<4, 2>(sp, sk);
+    if (e == cudaSuccess) e = spread_attr_one<6, 2>(sp, sk);
     if (e == cudaSuccess) e = fft_init_all();
     return e;
 }
 
 template <bool K>
-static void spread_launch(const SpreadArgs& a, dim3 grid, size_t smem, cudaStream_t s)
+static void spread_launch(const SpreadArgs& a, dim3 grid, size_t smem, int wpp, cudaStream_t s)
 {
-    if (a.cc <= 4) k_spread<4, K><<<grid, SPREAD_THREADS, smem, s>>>(a);
-    else if (a.cc <= 8) k_spread<8, K><<<grid, SPREAD_THREADS, smem, s>>>(a);
-    else k_spread<SPREAD_CC_MAX, K><<<grid, SPREAD_THREADS, smem, s>>>(a);
+    if (wpp == 2) {
+        const int ccw = (a.cc + 1) / 2;
+        if (ccw <= 2) k_spread<2, 2, K><<<grid, 32 * TILE_X * 2, smem, s>>>(a);
+        else if (ccw <= 4) k_spread<4, 2, K><<<grid, 32 * TILE_X * 2, smem, s>>>(a);
+        else k_spread<6, 2, K><<<grid, 32 * TILE_X * 2, smem, s>>>(a);
+        return;
+    }
+    if (a.cc <= 4) k_spread<4, 1, K><<<grid, 32 * TILE_X, smem, s>>>(a);
+    else if (a.cc <= 8) k_spread<8, 1, K><<<grid, 32 * TILE_X, smem, s>>>(a);
+    else k_spread<12, 1, K><<<grid, 32 * TILE_X, smem, s>>>(a);
 }
 
-cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan, cudaStream_t s)
+cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan, int wpp, cudaStream_t s)
 {
     if (ntiles == 0 || nbins == 0) return cudaSuccess;
-    if (a.cc < 1 || a.cc > spread_max_coils(kahan)) return cudaErrorInvalidValue;
+    if (a.cc < 1 || a.cc > spread_max_coils(kahan) || (wpp != 1 && wpp != 2)) return cudaErrorInvalidValue;
     const size_t smem = spread_smem_bytes(a.cc, kahan);
     dim3 grid((unsigned)ntiles, (unsigned)((a.nch + a.cc - 1) / a.cc), (unsigned)nbins);
-    if (kahan) spread_launch<true>(a, grid, smem, s);
-    else spread_launch<false>(a, grid, smem, s);
+    if (kahan) spread_launch<true>(a, grid, smem, wpp, s);
+    else spread_launch<false>(a, grid, smem, wpp, s);
     return cudaGetLastError();
 }
 

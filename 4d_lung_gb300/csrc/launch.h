@@ -30,7 +30,7 @@ cudaError_t launch_adj_z(int L, const AdjZArgs& a, int batch, cudaStream_t s);
 cudaError_t launch_tap_records(const double* k, const int* sample_idx, long long n, const KbParams& kb,
                                TapRecord* out, cudaStream_t s);
 cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, int cc, cudaStream_t s);
-cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan, cudaStream_t s);
+cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan, int wpp, cudaStream_t s);
 // packed nearest grid point of each tap record
 cudaError_t launch_record_nearest(const TapRecord* rec, long long n, unsigned* out, cudaStream_t s);
 size_t spread_smem_bytes(int cc, bool kahan);

@@ -63,6 +63,31 @@ void use_trajectory(cgs_ctx* c, const torch::Tensor& k)
     s.serial = cgs_trajectory_serial(c);
 }
 
+// Orders the library's work after PyTorch's pending work on the current
+// stream and PyTorch's later work after the library's: an event on each
+// side (the context keeps its own stream and its captured graphs).
+struct StreamJoin {
+    cudaStream_t ts = nullptr, cs = nullptr;
+    StreamJoin(cgs_ctx* c, const torch::Tensor& t)
+    {
+        ts = c10::cuda::getCurrentCUDAStream(t.device().index()).stream();
+        cs = static_cast<cudaStream_t>(cgs_get_stream(c));
+        if (cs != ts) wait(cs, ts);
+    }
+    ~StreamJoin()
+    {
+        if (cs != ts) wait(ts, cs);
+    }
+    static void wait(cudaStream_t waiter, cudaStream_t producer)
+    {
+        cudaEvent_t e;
+        TORCH_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess, "cudaEventCreate failed");
+        cudaEventRecord(e, producer);
+        cudaStreamWaitEvent(waiter, e, 0);
+        cudaEventDestroy(e);
+    }
+};
+
 struct DcLoss : public torch::autograd::Function<DcLoss> {
     static torch::Tensor forward(AutogradContext* ctx, int64_t handle, int64_t bin, const torch::Tensor& x,
                                  const torch::Tensor& k, const torch::Tensor& y)
@@ -77,8 +102,7 @@ struct DcLoss : public torch::autograd::Function<DcLoss> {
         TORCH_CHECK(y.is_cuda() && y.scalar_type() == torch::kComplexFloat && y.is_contiguous(),
                     "dc_loss: y must be a contiguous complex64 CUDA tensor [n_ch][ns]");
         const bool need_x = x.requires_grad(), need_k = k.requires_grad();
-        auto stream = c10::cuda::getCurrentCUDAStream(x.device().index());
-        check(c, cgs_set_stream(c, stream.stream()), "cgs_set_stream");
+        StreamJoin join(c, x);
         use_trajectory(c, k);
         torch::Tensor gx = need_x ? torch::empty_like(x) : torch::zeros({0}, x.options());
         torch::Tensor gk = need_k ? torch::empty({k.size(0), 3}, k.options().dtype(torch::kFloat32))
@@ -110,12 +134,6 @@ torch::Tensor dc_loss(int64_t handle, int64_t bin, const torch::Tensor& x, const
     return DcLoss::apply(handle, bin, x, k, y);
 }
 
-void set_stream(cgs_ctx* c, const torch::Tensor& t)
-{
-    auto stream = c10::cuda::getCurrentCUDAStream(t.device().index());
-    check(c, cgs_set_stream(c, stream.stream()), "cgs_set_stream");
-}
-
 void check_images(const torch::Tensor& t, const char* what)
 {
     TORCH_CHECK(t.is_cuda() && t.scalar_type() == torch::kComplexFloat && t.is_contiguous(), what,
@@ -131,7 +149,7 @@ struct ApplyA : public torch::autograd::Function<ApplyA> {
     {
         cgs_ctx* c = as_ctx(handle);
         check_images(p, "p");
-        set_stream(c, p);
+        StreamJoin join(c, p);
         use_trajectory(c, k);
         torch::Tensor q = torch::empty_like(p);
         check(c, cgs_apply_ehde_d(c, (int32_t)bin0, (int32_t)nb, reinterpret_cast<const float*>(p.data_ptr()),
@@ -151,21 +169,21 @@ struct ApplyA : public torch::autograd::Function<ApplyA> {
         cgs_ctx* c = as_ctx(ctx->saved_data["handle"].toInt());
         const int32_t bin0 = (int32_t)ctx->saved_data["bin0"].toInt(), nb = (int32_t)ctx->saved_data["nb"].toInt();
         const torch::Tensor v = g[0].contiguous();
-        set_stream(c, v);
-        use_trajectory(c, k);
         torch::Tensor gp, gk;
-        if (ctx->needs_input_grad(3)) {
-            gp = torch::empty_like(v);
-            check(c, cgs_apply_ehde_d(c, bin0, nb, reinterpret_cast<const float*>(v.data_ptr()),
-                                      reinterpret_cast<float*>(gp.data_ptr())),
-                  "cgs_apply_ehde_d");
+        // needs_input_grad counts the tensor inputs only: p is 0, k is 1
+        if (ctx->needs_input_grad(0)) gp = torch::empty_like(v);
+        if (ctx->needs_input_grad(1)) gk = torch::zeros({k.size(0), 3}, k.options().dtype(torch::kFloat32));
+        {
+            StreamJoin join(c, v);   // PyTorch's later work (the conversion below) waits for these
+            use_trajectory(c, k);
+            if (gp.defined())
+                check(c, cgs_apply_ehde_d(c, bin0, nb, reinterpret_cast<const float*>(v.data_ptr()),
+                                          reinterpret_cast<float*>(gp.data_ptr())),
+                      "cgs_apply_ehde_d");
+            if (gk.defined())
+                check(c, cgs_apply_vjp_k_d(c, bin0, nb, p.data_ptr(), v.data_ptr(), gk.data_ptr()), "cgs_apply_vjp_k_d");
         }
-        if (ctx->needs_input_grad(4)) {
-            torch::Tensor acc = torch::zeros({k.size(0), 3}, k.options().dtype(torch::kFloat32));
-            check(c, cgs_apply_vjp_k_d(c, bin0, nb, p.data_ptr(), v.data_ptr(), acc.data_ptr()), "cgs_apply_vjp_k_d");
-            gk = acc.to(torch::kFloat64);
-        }
-        return {torch::Tensor(), torch::Tensor(), torch::Tensor(), gp, gk};
+        return {torch::Tensor(), torch::Tensor(), torch::Tensor(), gp, gk.defined() ? gk.to(torch::kFloat64) : gk};
     }
 };
 
@@ -178,9 +196,9 @@ struct Rhs : public torch::autograd::Function<Rhs> {
         cgs_ctx* c = as_ctx(handle);
         TORCH_CHECK(y.is_cuda() && y.scalar_type() == torch::kComplexFloat && y.is_contiguous(),
                     "y must be a contiguous complex64 CUDA tensor [n_ch][ns]");
-        set_stream(c, y);
-        use_trajectory(c, k);
         torch::Tensor b = torch::empty({nb, nimg}, y.options());
+        StreamJoin join(c, y);
+        use_trajectory(c, k);
         check(c, cgs_rhs_d(c, (int32_t)bin0, (int32_t)nb, y.data_ptr(), b.data_ptr()), "cgs_rhs_d");
         ctx->save_for_backward({y, k});
         ctx->saved_data["handle"] = handle;
@@ -196,15 +214,15 @@ struct Rhs : public torch::autograd::Function<Rhs> {
         cgs_ctx* c = as_ctx(ctx->saved_data["handle"].toInt());
         const int32_t bin0 = (int32_t)ctx->saved_data["bin0"].toInt(), nb = (int32_t)ctx->saved_data["nb"].toInt();
         const torch::Tensor v = g[0].contiguous();
-        set_stream(c, v);
-        use_trajectory(c, k);
         torch::Tensor gk;
-        if (ctx->needs_input_grad(4)) {
-            torch::Tensor acc = torch::zeros({k.size(0), 3}, k.options().dtype(torch::kFloat32));
-            check(c, cgs_rhs_vjp_k_d(c, bin0, nb, y.data_ptr(), v.data_ptr(), acc.data_ptr()), "cgs_rhs_vjp_k_d");
-            gk = acc.to(torch::kFloat64);
+        if (ctx->needs_input_grad(1)) {   // tensor inputs: y is 0, k is 1
+            gk = torch::zeros({k.size(0), 3}, k.options().dtype(torch::kFloat32));
+            StreamJoin join(c, v);   // ends before the conversion below
+            use_trajectory(c, k);
+            check(c, cgs_rhs_vjp_k_d(c, bin0, nb, y.data_ptr(), v.data_ptr(), gk.data_ptr()), "cgs_rhs_vjp_k_d");
         }
-        return {torch::Tensor(), torch::Tensor(), torch::Tensor(), torch::Tensor(), gk, torch::Tensor()};
+        return {torch::Tensor(), torch::Tensor(), torch::Tensor(), torch::Tensor(),
+                gk.defined() ? gk.to(torch::kFloat64) : gk, torch::Tensor()};
     }
 };
 

@@ -95,6 +95,9 @@ const char* cgs_last_error(const cgs_ctx* ctx);
 /* Use an external CUDA stream (cudaStream_t); NULL returns to the context's own stream. */
 int cgs_set_stream(cgs_ctx* ctx, void* stream);
 /* Block until the context's stream is idle. */
+/* The CUDA stream the context's work is issued on (its own or the one set
+ * by cgs_set_stream). */
+void* cgs_get_stream(const cgs_ctx* ctx);
 int cgs_sync(cgs_ctx* ctx);
 
 /* WaveCaipi::calculateTraj with Trajectory::calculateKMax (Trajectory.cpp:9-184):
@@ -291,12 +294,13 @@ int cgs_set_precision(cgs_ctx* ctx, int32_t mode);
 
 /* Autotuner: times one batched E^H D E application of every bin for each
  * candidate launch shape -- coils per spreading block (all that fit, then
- * 1/2, 1/3, 1/4 of them), then coils per interpolation thread (2, 4, 6, 8)
- * -- and keeps the fastest for this context.  times_ms (may be NULL)
- * receives the median time of each candidate in that order; the chosen
- * shape is returned in *spread_cc and *interp_cc (may be NULL). */
+ * 1/2, 1/3, 1/4 of them) with one or two warps per x plane of a tile, then
+ * coils per interpolation thread (2, 4, 6, 8) -- and keeps the fastest for
+ * this context.  times_ms (may be NULL) receives the median time of each
+ * candidate in that order; the chosen shape is returned in *spread_cc,
+ * *spread_wpp and *interp_cc (each may be NULL). */
 int cgs_autotune(cgs_ctx* ctx, float* times_ms, int32_t max_times, int32_t* n_times, int32_t* spread_cc,
-                 int32_t* interp_cc);
+                 int32_t* spread_wpp, int32_t* interp_cc);
 
 /* Centred 3-D FFT (sign -1 forward, +1 backward, unscaled) that allocates no
  * device memory, for callers that cannot let a library allocate: code
