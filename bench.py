@@ -423,6 +423,82 @@ def run_diff_only(args):
     return 0
 
 
+def run_cg_grad_only(args):
+    """Combined large workload (cfg5: 256x256x176 image, 512x512x352 grid, 20
+    coils, R = 3x2 wave-CAIPI +-8 cells / 11 cycles, 1024 samples per
+    readout, 24 breathing bins): a 10-iteration CG of all bins unrolled in
+    PyTorch over the library's operators, every iteration checkpointed, and
+    the gradient of L = 1/2 sum_b |x_b(theta) - x_true,b|^2 with respect to
+    the six wave parameters.  D is the radial stand-in (per-bin Voronoi
+    weights of 7.7 M samples take minutes on the host).  One JSON line:
+    forward / backward seconds, device memory, the gradient."""
+    import torch
+    cgs = importlib.import_module("4d_lung_gb300")
+    synth = importlib.import_module("4d_lung_gb300.synth")
+    ag = importlib.import_module("4d_lung_gb300.autograd")
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    name = args.workload if args.workload != "cfg3" else "cfg5"
+    w = synth.WORKLOADS[name]
+    kb_w, kb_b = 4.0, beatty_beta(4.0)
+    lines = synth.readout_lines(w)
+    sbins = synth.bin_samples(synth.breathing_bins(len(lines), w.n_bins), w.n_read)
+    budget = int(args.workspace_gb * (1 << 30))
+    reco = cgs.Reco(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=kb_b, workspace_bytes=budget)
+    reco.set_stream(stream.cuda_stream)
+    t0 = time.perf_counter()
+    v_nom = torch.tensor([w.wave_cells, w.wave_cells, 0, 0, 0, 0], dtype=torch.float64, device=dev)
+    k_nom = ag.wave_trajectory_torch(w, v_nom, lines).contiguous()
+    k_np = k_nom.cpu().numpy()
+    reco.set_trajectory(k_np)
+    reco.set_dcf(synth.radial_dcf(k_np, w.grid))
+    reco.set_bins(sbins)
+    smaps = torch.from_numpy(synth.coil_maps(w.img, w.n_ch)).to(dev)
+    reco.set_smaps_tensor(smaps)
+    ns = k_np.shape[0]
+    y = torch.zeros((w.n_ch, ns), dtype=torch.complex64, device=dev)
+    full = torch.zeros_like(y)
+    xs = []
+    for b, idx in enumerate(sbins):
+        x_b = torch.from_numpy(synth.phantom(w.img, z_shift=w.z_shift_max * b / max(w.n_bins - 1, 1))).to(dev)
+        xs.append(x_b.reshape(-1))
+        reco.nufft_fwd_tensor((smaps * x_b[None]).contiguous(), full)
+        it = torch.from_numpy(np.asarray(idx, np.int64)).to(dev)
+        y[:, it] = full[:, it]
+    del full
+    x_true = torch.stack(xs)
+    torch.cuda.synchronize(dev)
+    t_setup = time.perf_counter() - t0
+    th = synth.perturbed_wave(w)
+    v = torch.tensor([th.amp_y, th.amp_z, th.phase_y, th.phase_z, th.delay_y, th.delay_z], dtype=torch.float64,
+                     device=dev, requires_grad=True)
+    torch.cuda.reset_peak_memory_stats(dev)
+    t0 = time.perf_counter()
+    k = ag.wave_trajectory_torch(w, v, lines).contiguous()
+    xk = ag.cg_unrolled(reco, k, y, w.cg_iters, checkpoint=True)
+    loss = 0.5 * torch.sum(torch.abs(xk.to(torch.complex128) - x_true.to(torch.complex128)) ** 2)
+    torch.cuda.synchronize(dev)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss.backward()
+    torch.cuda.synchronize(dev)
+    t_bwd = time.perf_counter() - t0
+    free, total = torch.cuda.mem_get_info(dev)
+    line = {"metric": "unrolled CG trajectory gradient (checkpointed backward)", "workload": w.name,
+            "config": {"img": list(w.img), "grid": list(w.grid), "coils": w.n_ch, "bins": len(sbins),
+                       "samples": int(ns), "cg_iters": w.cg_iters, "kb_w": kb_w, "kb_b": round(kb_b, 4),
+                       "dcf": "radial stand-in", "workspace_gb": args.workspace_gb,
+                       "checkpoint": "every CG iteration (x, r, p, rr saved; the rest recomputed)"},
+            "s_setup": t_setup, "s_forward": t_fwd, "s_backward": t_bwd, "loss": float(loss.item()),
+            "dL_dtheta": v.grad.cpu().numpy().tolist(), "params": list(synth.WAVE_PARAM_NAMES),
+            "device_gb_in_use_end": (total - free) / 2 ** 30,
+            "torch_peak_gb": torch.cuda.max_memory_allocated(dev) / 2 ** 30}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_precision_only(args):
     """Precision form of a workload (cfg2: 160x160x112, 16 coils, 20 CG
     iterations): per-iteration relative L2 error of the FP32 and the
@@ -654,6 +730,9 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiation form (cfg4)")
     ap.add_argument("--diff-only", action="store_true", help="only the differentiation form (one JSON line)")
+    ap.add_argument("--cg-grad-only", action="store_true",
+                    help="only the unrolled-CG trajectory gradient of the combined workload (cfg5)")
+    ap.add_argument("--workspace-gb", type=float, default=80.0, help="grid workspace budget (--cg-grad-only)")
     ap.add_argument("--max-bins", type=int, default=0,
                     help="keep only the first N respiratory bins (small cases for profiling)")
     ap.add_argument("--precision-only", action="store_true",
@@ -667,6 +746,8 @@ def main():
         return run_precision_only(args)
     if args.diff_only:
         return run_diff_only(args)
+    if args.cg_grad_only:
+        return run_cg_grad_only(args)
     return run_ours(args)
 
 
