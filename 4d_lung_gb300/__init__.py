@@ -53,7 +53,9 @@ EXPORTS = [
     "cgs_fft3_noalloc", "cgs_cg_solve_plain_d", "cgs_voronoi_dcf", "cgs_cg_solve_trace_d",
     "cgs_cg_solve_fp64_d", "cgs_estimate_density_v3d", "cgs_loss_grad_d", "cgs_loss_grad_fp64_d",
     "cgs_update_trajectory_d", "cgs_set_precision", "cgs_autotune", "cgs_rhs_d", "cgs_apply_vjp_k_d",
-    "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream",
+    "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream", "cgs_import_data_bin", "cgs_permute_samples_d",
+    "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
+    "cgs_reconstruct_states",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -164,6 +166,15 @@ def lib():
         "cgs_rhs_vjp_k_d": (C.c_int, [vp, C.c_int32, C.c_int32, vp, vp, vp]),
         "cgs_trajectory_serial": (C.c_uint64, [vp]),
         "cgs_get_stream": (C.c_void_p, [vp]),
+        "cgs_import_data_bin": (C.c_int, [C.c_char_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp, vp]),
+        "cgs_permute_samples_d": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, vp]),
+        "cgs_export_complex_bin": (C.c_int, [C.c_char_p, vp, i64, C.c_int32, vp]),
+        "cgs_export_float_bin": (C.c_int, [C.c_char_p, vp, i64, C.c_int32, vp]),
+        "cgs_import_smaps_bin": (C.c_int, [C.c_char_p, i64, C.c_int32, vp]),
+        "cgs_import_density_bin": (C.c_int, [C.c_char_p, i64, vp]),
+        "cgs_rss_d": (C.c_int, [vp, C.c_int32, i64, vp, vp]),
+        "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
+                                             C.c_double, C.c_int32, C.c_int32, vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
         "cgs_cg_solve_fp64_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
     }
@@ -224,6 +235,52 @@ def estimate_density_v3d(k, sX, average=False, cutoff=1.0):
     if st != CGS_OK:
         raise CGSError(st, "cgs_estimate_density_v3d failed")
     return out
+
+
+# -- file IO (IO.cpp) ---------------------------------------------------------
+
+def _io_check(st, what):
+    if st != CGS_OK:
+        raise CGSError(st, what + " failed")
+
+
+def import_smaps_bin(dirpath, n, nch):
+    """IO::importSensitivityMaps: dirpath + "map<c>.bin" -> complex64 [nch][n]."""
+    out = np.zeros((nch, n), np.complex64)
+    d = dirpath if dirpath.endswith("/") else dirpath + "/"
+    _io_check(lib().cgs_import_smaps_bin(d.encode(), n, nch, _p(out)), "cgs_import_smaps_bin")
+    return out
+
+
+def import_density_bin(path, n):
+    """IO::importDensityCorr: n float32 weights."""
+    out = np.zeros(n, np.float32)
+    _io_check(lib().cgs_import_density_bin(path.encode(), n, _p(out)), "cgs_import_density_bin")
+    return out
+
+
+def export_complex_bin(path, a):
+    """IO::exportFFTWComplexBin from a host array (complex64)."""
+    a = np.ascontiguousarray(a, dtype=np.complex64)
+    _io_check(lib().cgs_export_complex_bin(path.encode(), _p(a), a.size, 0, None), "cgs_export_complex_bin")
+
+
+def export_float_bin(path, a):
+    """IO::exportVectorBin from a host array (float32)."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    _io_check(lib().cgs_export_float_bin(path.encode(), _p(a), a.size, 0, None), "cgs_export_float_bin")
+
+
+def import_data_bin_tensor(path, sx, sy, sz, nch, out, stream=None):
+    """IO::importDataBin onto the device (out: complex64 CUDA tensor [nch][sx*sy*sz])."""
+    _io_check(lib().cgs_import_data_bin(path.encode(), sx, sy, sz, nch, C.c_void_p(out.data_ptr()),
+                                        None if stream is None else C.c_void_p(stream)), "cgs_import_data_bin")
+
+
+def rss_tensor(imgs, out, stream=None):
+    """rssq2DVecImg on the device: imgs complex64 [nch][n] -> out float32 [n]."""
+    _io_check(lib().cgs_rss_d(C.c_void_p(imgs.data_ptr()), imgs.shape[0], out.numel(), C.c_void_p(out.data_ptr()),
+                              None if stream is None else C.c_void_p(stream)), "cgs_rss_d")
 
 
 class Reco:
@@ -427,6 +484,16 @@ class Reco:
                                                 threshold, max_iter, _p(res), _p(it),
                                                 None if x_trace is None else C.c_void_p(x_trace.data_ptr())))
         return res, it
+
+    def reconstruct_states(self, files, sx, sy, sz, out_dir, threshold, max_iter=16, write_rss=True):
+        """The state loop of CGSense.cpp:200-282 (cgs_reconstruct_states);
+        returns the iteration count of every state."""
+        arr = (C.c_char_p * len(files))(*[f.encode() for f in files])
+        it = np.zeros(len(files), np.int32)
+        self._check(self._L.cgs_reconstruct_states(self._ctx, C.cast(arr, C.c_void_p), len(files), sx, sy, sz,
+                                                   out_dir.encode(), threshold, max_iter, int(bool(write_rss)),
+                                                   _p(it)))
+        return it
 
     # -- differentiation --------------------------------------------------
     def loss_grad_tensor(self, x, y, grad_x=None, grad_k=None, bin=0):

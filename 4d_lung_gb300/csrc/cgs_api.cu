@@ -8,6 +8,8 @@
 #include "launch.h"
 
 #include <algorithm>
+#include <sys/stat.h>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -1693,5 +1695,105 @@ int cgs_rhs_vjp_k_d(cgs_ctx* c, int32_t bin0, int32_t nb, const void* y, const v
 }
 
 uint64_t cgs_trajectory_serial(const cgs_ctx* c) { return c ? c->traj_serial : 0; }
+
+// The state loop of CGSense.cpp:200-282: one reconstruction per state file,
+// the next file read on a host thread while the current state runs.
+int cgs_reconstruct_states(cgs_ctx* c, const char* const* files, int32_t n_files, int32_t sx, int32_t sy, int32_t sz,
+                           const char* out_dir, double thresh, int32_t max_iter, int32_t write_rss, int32_t* iters)
+{
+    if (!c || !files || n_files < 1 || !out_dir) return CGS_ERR_ARG;
+    if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set (cgs_set_trajectory)");
+    if (!c->smaps_set) return fail(c, CGS_ERR_STATE, "no coil maps set (cgs_set_smaps)");
+    if ((long long)sx * sy * sz != c->ns) return fail(c, CGS_ERR_ARG, "sx*sy*sz differs from the trajectory's samples");
+    if (thresh == -1.0) return fail(c, CGS_ERR_NO_THRESHOLD, "no threshold set for CG SENSE (Reco.cpp:192-196)");
+    const std::string dir = std::string(out_dir) + "/";
+    mkdir(dir.c_str(), 0755);
+    mkdir((dir + "results").c_str(), 0755);
+    const long long ns = c->ns;
+    const size_t bytes = (size_t)ns * c->nch * sizeof(float2);
+    // pinned host buffers for two files, device buffers for one state
+    void* hbuf[2] = {nullptr, nullptr};
+    for (int i = 0; i < 2; ++i)
+        if (cudaMallocHost(&hbuf[i], bytes) != cudaSuccess) {
+            for (int j = 0; j < i; ++j) cudaFreeHost(hbuf[j]);
+            return fail(c, CGS_ERR_NOMEM, "pinned host buffers");
+        }
+    auto release = [&]() {
+        for (int i = 0; i < 2; ++i) cudaFreeHost(hbuf[i]);
+    };
+    auto read_file = [&](const char* path, void* h) -> int {
+        std::FILE* f = std::fopen(path, "rb");
+        if (!f) return CGS_ERR_IO;
+        const size_t got = std::fread(h, 1, bytes, f);
+        std::fclose(f);
+        return got == bytes ? CGS_OK : CGS_ERR_IO;
+    };
+    int st = read_file(files[0], hbuf[0]);
+    if (st != CGS_OK) {
+        release();
+        return fail(c, st, std::string("cannot read ") + files[0]);
+    }
+    DevBuf stage, data, img, rss, x, dglob;
+    if (stage.ensure(bytes) != cudaSuccess || data.ensure(bytes) != cudaSuccess ||
+        x.ensure((size_t)c->Ni * sizeof(float2)) != cudaSuccess) {
+        release();
+        return fail(c, CGS_ERR_NOMEM, "state buffers");
+    }
+    if (write_rss) {
+        if (img.ensure((size_t)c->nch * c->Ni * sizeof(float2)) != cudaSuccess ||
+            rss.ensure((size_t)c->Ni * sizeof(float)) != cudaSuccess) {
+            release();
+            return fail(c, CGS_ERR_NOMEM, "coil-image buffers");
+        }
+        if (c->has_dcf && (dglob.ensure((size_t)ns * sizeof(float)) != cudaSuccess ||
+                           cudaMemcpyAsync(dglob.p, c->h_dcf.data(), (size_t)ns * sizeof(float),
+                                           cudaMemcpyHostToDevice, c->stream) != cudaSuccess)) {
+            release();
+            return fail(c, CGS_ERR_CUDA, "density weights");
+        }
+    }
+    std::vector<float2> coil0(ns);
+    for (int k = 0; k < n_files && st == CGS_OK; ++k) {
+        // the next file is read while this state is reconstructed (CGSense.cpp:205-215)
+        int next_st = CGS_OK;
+        std::thread reader;
+        if (k + 1 < n_files) reader = std::thread([&, k]() { next_st = read_file(files[k + 1], hbuf[(k + 1) & 1]); });
+        auto run = [&]() -> int {
+            CGS_CUDA(c, cudaMemcpyAsync(stage.p, hbuf[k & 1], bytes, cudaMemcpyHostToDevice, c->stream));
+            CGS_TRY(cgs_permute_samples_d(stage.p, data.p, sx, sy, sz, c->nch, c->stream));
+            // excludeMissingData (Reco.cpp:681-696): samples whose channel-0 value is 0 + 0i
+            CGS_CUDA(c, cudaMemcpyAsync(coil0.data(), data.p, (size_t)ns * sizeof(float2), cudaMemcpyDeviceToHost,
+                                        c->stream));
+            CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+            std::vector<int> keep;
+            keep.reserve(ns);
+            for (long long i = 0; i < ns; ++i)
+                if (coil0[i].x != 0.f || coil0[i].y != 0.f) keep.push_back((int)i);
+            c->bins.assign(1, std::move(keep));
+            c->bins_dirty = true;
+            if (write_rss) {
+                // coil images of the density-corrected data and their root-sum-of-squares
+                // (CGSense.cpp:226-244)
+                CGS_CUDA(c, cudaMemcpyAsync(stage.p, data.p, bytes, cudaMemcpyDeviceToDevice, c->stream));
+                if (c->has_dcf)
+                    CGS_CUDA(c, launch_scale_samples(stage.as<float2>(), dglob.as<float>(), ns, c->nch, c->stream));
+                CGS_TRY(cgs_nufft_adj_d(c, stage.as<float>(), img.as<float>()));
+                CGS_TRY(cgs_rss_d(img.p, c->nch, c->Ni, rss.as<float>(), c->stream));
+                CGS_TRY(cgs_export_float_bin((dir + "resultRssq.bin").c_str(), rss.p, c->Ni, 1, c->stream));
+            }
+            int it = 0;
+            CGS_TRY(cgs_cg_solve_batched_d(c, data.as<float>(), x.as<float>(), thresh, max_iter, nullptr, &it));
+            if (iters) iters[k] = it;
+            const std::string out = dir + "results/b_state" + std::to_string(k) + ".bin";
+            CGS_TRY(cgs_export_complex_bin(out.c_str(), x.p, c->Ni, 1, c->stream));
+            return CGS_OK;
+        };
+        st = run();
+        if (reader.joinable()) reader.join();
+        if (st == CGS_OK && next_st != CGS_OK) st = fail(c, next_st, std::string("cannot read ") + files[k + 1]);
+    }
+    release();
+    return st;
+}
 
 }  // extern "C"

@@ -96,6 +96,9 @@ cudaError_t launch_interp_grad(const InterpGradArgs& a, cudaStream_t s);
 cudaError_t launch_check_finite(const double* v, long long n, int* bad, cudaStream_t s);
 cudaError_t launch_pair_grad(const PairGradArgs& a, cudaStream_t s);
 
+// File IO (io.cu)
+cudaError_t launch_scale_samples(float2* data, const float* d, long long ns, int nch, cudaStream_t s);
+
 // Full-FP64 form (fp64.cu): the precision reference on the GPU.
 struct Fp64Args {
     PlainGeom g;

@@ -454,7 +454,6 @@ def run_cg_grad_only(args):
     k_np = k_nom.cpu().numpy()
     reco.set_trajectory(k_np)
     reco.set_dcf(synth.radial_dcf(k_np, w.grid))
-    reco.set_bins(sbins)
     smaps = torch.from_numpy(synth.coil_maps(w.img, w.n_ch)).to(dev)
     reco.set_smaps_tensor(smaps)
     ns = k_np.shape[0]
@@ -468,6 +467,7 @@ def run_cg_grad_only(args):
         it = torch.from_numpy(np.asarray(idx, np.int64)).to(dev)
         y[:, it] = full[:, it]
     del full
+    reco.set_bins(sbins)
     x_true = torch.stack(xs)
     torch.cuda.synchronize(dev)
     t_setup = time.perf_counter() - t0

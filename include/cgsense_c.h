@@ -48,6 +48,7 @@ extern "C" {
 #define CGS_ERR_UNSUPPORTED 6  /* grid size without an FFT kernel */
 #define CGS_ERR_NO_THRESHOLD 7 /* cg threshold == -1 (Reco.cpp:192-196) */
 #define CGS_ERR_TIMEOUT 8      /* a kernel's bounded wait for its asynchronous copies ran out */
+#define CGS_ERR_IO 9           /* a file could not be opened, read or written (IO.cpp) */
 
 typedef struct cgs_ctx cgs_ctx;
 
@@ -317,6 +318,56 @@ int cgs_autotune(cgs_ctx* ctx, float* times_ms, int32_t max_times, int32_t* n_ti
  * calls that overlap on the GPU race and must be serialised.  stream is a
  * cudaStream_t (NULL: the default stream); the call is asynchronous. */
 int cgs_fft3_noalloc(const float* in_dev, float* out_dev, const int32_t* grid, int32_t sign, void* stream);
+
+/* --- File IO of the reconstruction (IO.cpp), context-free --------------
+ * stream: CUDA stream of the device work, NULL for the default stream. */
+
+/* IO::importDataBin (IO.cpp:55-98): reads nch * sx*sy*sz complex64 samples
+ * (interleaved float32) stored channel by channel in readout-fastest order
+ * (sample i1 + sx*i2 + sx*sy*i3) and writes them to the device in the
+ * reconstruction's z-fastest order (ch*ns + i3 + sz*i2 + sy*sz*i1).  The
+ * file is read in chunks through two pinned host buffers (the next chunk is
+ * read while the previous one is copied) and permuted by a kernel.  A
+ * missing or short file is CGS_ERR_IO. */
+int cgs_import_data_bin(const char* path, int32_t sx, int32_t sy, int32_t sz, int32_t nch, void* data_dev,
+                        void* stream);
+
+/* The permutation of cgs_import_data_bin alone, device to device. */
+int cgs_permute_samples_d(const void* file_order_dev, void* data_dev, int32_t sx, int32_t sy, int32_t sz,
+                          int32_t nch, void* stream);
+
+/* IO::exportFFTWComplexBin (IO.cpp:158-186): n complex64 values as
+ * interleaved float32; a path that cannot be opened is retried as
+ * path + "_1.bin".  src is a device pointer when src_on_device != 0. */
+int cgs_export_complex_bin(const char* path, const void* src, int64_t n, int32_t src_on_device, void* stream);
+
+/* IO::exportVectorBin (IO.cpp:12-22): n float32 values. */
+int cgs_export_float_bin(const char* path, const void* src, int64_t n, int32_t src_on_device, void* stream);
+
+/* IO::importSensitivityMaps (IO.cpp:25-51): dir + "map<c>.bin", n complex64
+ * values each, into maps_host [nch][n]. */
+int cgs_import_smaps_bin(const char* dir, int64_t n, int32_t nch, float* maps_host);
+
+/* IO::importDensityCorr (IO.cpp:129-156): n float32 weights. */
+int cgs_import_density_bin(const char* path, int64_t n, float* d_host);
+
+/* rssq2DVecImg (functions.h:290-316) on the device: out[i] =
+ * sqrt(sum_c |img_c[i]|^2), coils summed in order in float.  imgs: complex64
+ * [nch][n]; out float32 [n]. */
+int cgs_rss_d(const void* imgs_dev, int32_t nch, int64_t n, float* out_dev, void* stream);
+
+/* The state loop of CGSense.cpp:200-282 on the GPU: for every state file,
+ * IO::importDataBin (the next file is read on a host thread while the
+ * current state is reconstructed), excludeMissingData, density correction
+ * with the context's weights, the coil images and their root-sum-of-squares
+ * exported as out_dir/resultRssq.bin (float32, img voxels) when
+ * write_rss != 0, cgSenseDynamic, and the image exported as
+ * out_dir/results/b_state<k>.bin (complex64).  iters (may be NULL) receives
+ * the iteration count of every state.  Coil maps and trajectory must be set
+ * (one bin). */
+int cgs_reconstruct_states(cgs_ctx* ctx, const char* const* files, int32_t n_files, int32_t sx, int32_t sy,
+                           int32_t sz, const char* out_dir, double thresh, int32_t max_iter, int32_t write_rss,
+                           int32_t* iters);
 
 #ifdef __cplusplus
 }

@@ -92,6 +92,26 @@ def traj_fixture(name, sx, sy, sz, grid, fov_y, fov_z, **wave):
     print("wrote", name)
 
 
+def io_fixture(name, sx, sy, sz, nch, grid, seed):
+    """IO::importDataBin (readout-fastest file order -> z-fastest memory
+    order, IO.cpp:55-98), IO::importSensitivityMaps (map<c>.bin, IO.cpp:25-51)
+    and IO::exportFFTWComplexBin (IO.cpp:158-186) on seeded files."""
+    rng = np.random.default_rng(seed)
+    ns = sx * sy * sz
+    raw = crandn(rng, (nch, ns))                 # file order: channel, then i1 + sx*i2 + sx*sy*i3
+    ng = int(np.prod(grid))
+    maps = crandn(rng, (nch, ng))
+    params = dict(gx=grid[0], gy=grid[1], gz=grid[2], sx=sx, sy=sy, sz=sz, nch=nch, threads=2)
+    arrays = {"raw_file": raw}
+    arrays.update({"map%d" % c: maps[c] for c in range(nch)})
+    r = O.run_ref("io", params, arrays, {"io_data_out": (np.complex64, None), "io_maps_out": (np.complex64, None),
+                                         "io_export": (np.complex64, None)})
+    np.savez_compressed(os.path.join(HERE, name), sx=sx, sy=sy, sz=sz, nch=nch, grid=np.array(grid), raw=raw,
+                        maps=maps, data_out=r["io_data_out"].reshape(nch, ns),
+                        maps_out=r["io_maps_out"].reshape(nch, ng), export=r["io_export"])
+    print("wrote", name)
+
+
 def main():
     if not O.ref_available():
         O.build()
@@ -106,6 +126,7 @@ def main():
     traj_fixture("ref_traj_wave.npz", 112, 28, 14, (128, 128, 128), 0.5, 0.00223 * 14,
                  nosc=4, dwell=6.3e-6 * 4, grad_amp=0.006, amp_corr_y=0.998, amp_corr_z=1.01,
                  shift_y=5.6e-6, shift_z=6.5e-6)
+    io_fixture("ref_io_12x5x4.npz", 12, 5, 4, 3, (8, 6, 4), seed=21)
     traj_fixture("ref_traj_wave_b.npz", 64, 16, 8, (96, 80, 64), 0.3, 0.05,
                  nosc=7, dwell=1e-5, grad_amp=0.01, amp_corr_y=1.0, amp_corr_z=0.97,
                  shift_y=0.0, shift_z=1e-5)
