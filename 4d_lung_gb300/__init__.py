@@ -55,7 +55,7 @@ EXPORTS = [
     "cgs_update_trajectory_d", "cgs_set_precision", "cgs_autotune", "cgs_rhs_d", "cgs_apply_vjp_k_d",
     "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream", "cgs_import_data_bin", "cgs_permute_samples_d",
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
-    "cgs_reconstruct_states",
+    "cgs_reconstruct_states", "cgs_pipe_menon_dcf",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -173,6 +173,7 @@ def lib():
         "cgs_import_smaps_bin": (C.c_int, [C.c_char_p, i64, C.c_int32, vp]),
         "cgs_import_density_bin": (C.c_int, [C.c_char_p, i64, vp]),
         "cgs_rss_d": (C.c_int, [vp, C.c_int32, i64, vp, vp]),
+        "cgs_pipe_menon_dcf": (C.c_int, [vp, C.c_int32, vp, C.c_int32]),
         "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
                                              C.c_double, C.c_int32, C.c_int32, vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
@@ -484,6 +485,12 @@ class Reco:
                                                 threshold, max_iter, _p(res), _p(it),
                                                 None if x_trace is None else C.c_void_p(x_trace.data_ptr())))
         return res, it
+
+    def pipe_menon_dcf(self, iters=20):
+        """GPU iterative density weights of every bin (host array [ns])."""
+        out = np.zeros(self.ns, np.float32)
+        self._check(self._L.cgs_pipe_menon_dcf(self._ctx, int(iters), _p(out), 0))
+        return out
 
     def reconstruct_states(self, files, sx, sy, sz, out_dir, threshold, max_iter=16, write_rss=True):
         """The state loop of CGSense.cpp:200-282 (cgs_reconstruct_states);

@@ -1796,4 +1796,86 @@ int cgs_reconstruct_states(cgs_ctx* c, const char* const* files, int32_t n_files
     return st;
 }
 
+// Pipe-Menon density weights of every bin on the GPU: `iters` rounds of
+// w <- w / (C * w), C * w = interpolation (Reco.cpp:539-550 without the FFT)
+// of the spreading (Reco.cpp:492-504) of the weights on the bin's grid;
+// then each bin's weights are divided by their maximum (as
+// estimateDensityV3D normalises, functions.h:234-245).  dcf: float [ns],
+// device or host (on_device), in the reference's sample order; samples in no
+// bin get 0.
+int cgs_pipe_menon_dcf(cgs_ctx* c, int32_t iters, float* dcf, int32_t on_device)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!dcf || iters < 1 || iters > 1000) return fail(c, CGS_ERR_ARG, "bad arguments");
+    const long long n = c->total;
+    DevBuf w, v, u;
+    CGS_CUDA(c, w.ensure(std::max<long long>(n, 1) * sizeof(float)));
+    CGS_CUDA(c, v.ensure(std::max<long long>(n, 1) * sizeof(float2)));
+    CGS_CUDA(c, u.ensure(std::max<long long>(n, 1) * sizeof(float2)));
+    CGS_CUDA(c, launch_pm_init(w.as<float>(), v.as<float2>(), n, c->stream));
+    const long long grid_bs = c->Ng;   // one "coil" per bin
+    for (int it = 0; it < iters; ++it) {
+        for (int g = 0; g < c->nbins; g += c->ws_bins * c->nch) {
+            // the workspace holds ws_bins * nch grids: as many single-coil bins at once
+            const int nb = std::min(c->ws_bins * c->nch, c->nbins - g);
+            SpreadArgs sa{};
+            sa.grid = c->d_grid.as<float2>();
+            sa.coil_stride = c->Ng;
+            sa.grid_bs = grid_bs;
+            sa.rec = c->d_rec.as<TapRecord>();
+            sa.yv = v.as<float2>();
+            sa.bin_off = c->d_bin_off.as<long long>();
+            sa.tile_ptr = c->d_tile_ptr.as<int>();
+            sa.tile_ptr_off = c->d_tile_ptr_off.as<long long>();
+            sa.tile_idx_off = c->d_tile_idx_off.as<long long>();
+            sa.tile_idx = c->d_tile_idx.as<int>();
+            sa.plane_rng = c->d_plane_rng.as<int2>();
+            sa.bin0 = g;
+            sa.nch = 1;
+            sa.cc = 1;
+            for (int a = 0; a < 3; ++a) sa.G[a] = c->G[a];
+            sa.ntx = c->ntx;
+            sa.nty = c->nty;
+            sa.ntz = c->ntz;
+            sa.thresh = c->thresh;
+            CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, false, 1, c->stream));
+            InterpArgs ia{};
+            ia.grid = c->d_grid.as<float2>();
+            ia.coil_stride = c->Ng;
+            ia.grid_bs = grid_bs;
+            ia.rec = c->d_rec.as<TapRecord>();
+            ia.dcf = nullptr;
+            ia.bin_off = c->d_bin_off.as<long long>();
+            ia.bin0 = g;
+            ia.yv = u.as<float2>();
+            ia.nch = 1;
+            for (int a = 0; a < 3; ++a) ia.G[a] = c->G[a];
+            ia.thresh = c->thresh;
+            long long mx = 0;
+            for (int b = g; b < g + nb; ++b) mx = std::max(mx, c->h_bin_off[b + 1] - c->h_bin_off[b]);
+            CGS_LAUNCH(c, launch_interp(ia, mx, nb, 2, c->stream));
+        }
+        CGS_CUDA(c, launch_pm_update(w.as<float>(), v.as<float2>(), u.as<float2>(), n, c->stream));
+    }
+    // per-bin normalisation by the maximum, scatter to the reference's order
+    std::vector<float> hw(std::max<long long>(n, 1));
+    std::vector<int> hs(std::max<long long>(n, 1));
+    CGS_CUDA(c, cudaMemcpyAsync(hw.data(), w.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaMemcpyAsync(hs.data(), c->d_sorted.p, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    std::vector<float> out(c->ns, 0.f);
+    for (int b = 0; b < c->nbins; ++b) {
+        float mx = 0.f;
+        for (long long j = c->h_bin_off[b]; j < c->h_bin_off[b + 1]; ++j) mx = std::max(mx, hw[j]);
+        const float inv = mx > 0.f ? 1.f / mx : 0.f;
+        for (long long j = c->h_bin_off[b]; j < c->h_bin_off[b + 1]; ++j) out[hs[j]] = hw[j] * inv;
+    }
+    if (on_device)
+        CGS_CUDA(c, cudaMemcpyAsync(dcf, out.data(), (size_t)c->ns * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    else
+        std::copy(out.begin(), out.end(), dcf);
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return check_timeout(c);
+}
+
 }  // extern "C"

@@ -274,4 +274,39 @@ cudaError_t launch_pair_grad(const PairGradArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+// Iterative density weights (Pipe and Menon, Magn. Reson. Med. 41:179-186,
+// 1999): w <- w / (C * w) at the samples, C * w the interpolation of the
+// spread weights.  v is the spread input (w, 0) and u the interpolated sum.
+__global__ void k_pm_update(float* __restrict__ w, float2* __restrict__ v, const float2* __restrict__ u, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float c = u[i].x;
+    const float nw = c > 1e-30f ? w[i] / c : w[i];
+    w[i] = nw;
+    v[i] = make_float2(nw, 0.f);
+}
+
+cudaError_t launch_pm_update(float* w, float2* v, const float2* u, long long n, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_pm_update<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w, v, u, n);
+    return cudaGetLastError();
+}
+
+__global__ void k_pm_init(float* __restrict__ w, float2* __restrict__ v, long long n)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    w[i] = 1.f;
+    v[i] = make_float2(1.f, 0.f);
+}
+
+cudaError_t launch_pm_init(float* w, float2* v, long long n, cudaStream_t s)
+{
+    if (n == 0) return cudaSuccess;
+    k_pm_init<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(w, v, n);
+    return cudaGetLastError();
+}
+
 }  // namespace cgs

@@ -95,6 +95,8 @@ int interp_grad_blocks(long long n);
 cudaError_t launch_interp_grad(const InterpGradArgs& a, cudaStream_t s);
 cudaError_t launch_check_finite(const double* v, long long n, int* bad, cudaStream_t s);
 cudaError_t launch_pair_grad(const PairGradArgs& a, cudaStream_t s);
+cudaError_t launch_pm_init(float* w, float2* v, long long n, cudaStream_t s);
+cudaError_t launch_pm_update(float* w, float2* v, const float2* u, long long n, cudaStream_t s);
 
 // File IO (io.cu)
 cudaError_t launch_scale_samples(float2* data, const float* d, long long ns, int nch, cudaStream_t s);

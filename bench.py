@@ -147,8 +147,10 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
         dcf = np.zeros(k.shape[0], np.float32)
         for idx in sbins:
             dcf[idx] = synth.cap_dcf(cgs.voronoi_dcf(k[idx]))
-    else:
+    elif dcf_kind == "radial":
         dcf = synth.radial_dcf(k, w.grid)
+    else:
+        dcf = None   # Pipe-Menon weights on the GPU once the bins are set
     dcf_s = time.perf_counter() - t0
     reco = cgs.Reco(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=kb_b, device=device)
     reco.set_stream(stream_handle)
@@ -174,8 +176,12 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
     noise = torch.complex(torch.randn(data.shape, generator=g, device=dev),
                           torch.randn(data.shape, generator=g, device=dev)) * sigma
     data += noise
-    reco.set_dcf(dcf)
     reco.set_bins(sbins)
+    if dcf is None:
+        t0 = time.perf_counter()
+        dcf = reco.pipe_menon_dcf(20)
+        dcf_s = time.perf_counter() - t0
+    reco.set_dcf(dcf)
     reco.set_smaps_tensor(smaps_t)
     return w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s
 
@@ -689,7 +695,9 @@ def run_ours(args):
                    "bins": nb, "samples_per_bin": [min(sizes), max(sizes)], "samples_total": int(sum(sizes)),
                    "cg_iters": iters, "kb_w": kb_w, "kb_b": round(kb_b, 4),
                    "dcf": ("per-bin Voronoi volumes capped at the 99th percentile (host, %.1f s set-up)" % dcf_s)
-                   if args.dcf == "voronoi"
+                   if args.dcf == "voronoi" else
+                   ("per-bin Pipe-Menon weights, 20 iterations (GPU, %.2f s set-up)" % dcf_s)
+                   if args.dcf == "pipe-menon"
                    else "radial stand-in",
                    "step": "one 16-bin 4D CG-SENSE reconstruction (graph replay)",
                    "l2": "inputs larger than L2 (data %d MB, workspace > 30 GB)" % (h2d // 2 ** 20),
@@ -737,7 +745,7 @@ def main():
                     help="keep only the first N respiratory bins (small cases for profiling)")
     ap.add_argument("--precision-only", action="store_true",
                     help="only the precision form of --workload (one JSON line of per-iteration errors)")
-    ap.add_argument("--dcf", default="voronoi", choices=["voronoi", "radial"],
+    ap.add_argument("--dcf", default="voronoi", choices=["voronoi", "radial", "pipe-menon"],
                     help="density weights: per-bin Voronoi volumes or a radial stand-in")
     args = ap.parse_args()
     if args.impl == "reference":

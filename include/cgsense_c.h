@@ -137,6 +137,15 @@ int cgs_voronoi_dcf(const double* k, int64_t n, float* dcf);
  * average == 0 is cgs_voronoi_dcf. */
 int cgs_estimate_density_v3d(const double* k, int64_t n, int32_t sX, int32_t average, double cutoff, float* dcf);
 
+/* Iterative density weights on the GPU (Pipe and Menon 1999), the
+ * documented alternative to the Voronoi volumes: `iters` rounds of
+ * w <- w / (C * w) per bin, C * w the interpolation of the spread weights
+ * on the bin's grid (the KB gridding of Reco.cpp:492-550 without the FFT),
+ * then normalised by each bin's maximum.  dcf float [ns] in the reference's
+ * sample order (device pointer when on_device != 0); samples in no bin get
+ * 0.  Needs the trajectory and bins, not the coil maps. */
+int cgs_pipe_menon_dcf(cgs_ctx* ctx, int32_t iters, float* dcf, int32_t on_device);
+
 /* Reco::denCorr with Density::IMPORT (IO.cpp:129-156, functions.h:319-335):
  * per-sample real weights D[ns].  NULL clears (Density::NONE). */
 int cgs_set_dcf(cgs_ctx* ctx, const float* dcf);

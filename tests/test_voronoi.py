@@ -76,3 +76,31 @@ def test_density_readout_averaging(cgs, synth, cutoff):
     assert np.array_equal(cgs.estimate_density_v3d(kb, sx, average=False), cgs.voronoi_dcf(kb))
     with pytest.raises(cgs.CGSError):
         cgs.estimate_density_v3d(kb[:-1], sx, average=True)
+
+
+@pytest.mark.gpu
+def test_pipe_menon_weights_follow_density(gpu_lib, cgs):
+    """GPU Pipe-Menon weights (the documented alternative to the Voronoi
+    volumes): on a lattice twice as dense in x on one side, the interior
+    weights differ by the density ratio, and they agree with the Voronoi
+    volumes of the same samples away from the edges."""
+    grid = (48, 32, 32)
+    xs = np.concatenate([np.arange(6.0, 24.0, 1.0), np.arange(24.0, 42.0, 0.5)])
+    ys = np.arange(6.0, 26.0, 1.0)
+    zs = np.arange(6.0, 26.0, 1.0)
+    X, Y, Z = np.meshgrid(xs, ys, zs, indexing="ij")
+    cells = np.stack([X, Y, Z], -1).reshape(-1, 3)
+    k = cells / (np.array(grid) - 1)
+    r = cgs.Reco(grid, grid, 1, kb_w=4.25, kb_b=14.9086)
+    r.set_trajectory(k)
+    w = r.pipe_menon_dcf(30)
+    assert w.max() == pytest.approx(1.0) and w.min() > 0
+    interior = (np.abs(Y - 16) < 5) & (np.abs(Z - 16) < 5)
+    sparse = interior & (X > 10) & (X < 20)
+    dense = interior & (X > 28) & (X < 38)
+    ratio = np.median(w.reshape(X.shape)[sparse]) / np.median(w.reshape(X.shape)[dense])
+    assert 1.8 < ratio < 2.2, ratio
+    v = cgs.voronoi_dcf(k).reshape(X.shape)
+    wv = w.reshape(X.shape)
+    rv = np.median(v[sparse]) / np.median(v[dense])
+    assert abs(ratio / rv - 1) < 0.1, (ratio, rv)
