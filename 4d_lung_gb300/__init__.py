@@ -55,7 +55,7 @@ EXPORTS = [
     "cgs_update_trajectory_d", "cgs_set_precision", "cgs_autotune", "cgs_rhs_d", "cgs_apply_vjp_k_d",
     "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream", "cgs_import_data_bin", "cgs_permute_samples_d",
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
-    "cgs_reconstruct_states", "cgs_pipe_menon_dcf",
+    "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -174,6 +174,7 @@ def lib():
         "cgs_import_density_bin": (C.c_int, [C.c_char_p, i64, vp]),
         "cgs_rss_d": (C.c_int, [vp, C.c_int32, i64, vp, vp]),
         "cgs_pipe_menon_dcf": (C.c_int, [vp, C.c_int32, vp, C.c_int32]),
+        "cgs_set_deterministic": (C.c_int, [vp, C.c_int32]),
         "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
                                              C.c_double, C.c_int32, C.c_int32, vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
@@ -536,6 +537,11 @@ class Reco:
         self._check(self._L.cgs_autotune(self._ctx, _p(t), 32, _p(n), _p(sc), _p(sw), _p(ic)))
         return {"spread_coils_per_block": int(sc[0]), "spread_warps_per_plane": int(sw[0]),
                 "interp_coils_per_thread": int(ic[0]), "candidates_ms": [float(v) for v in t[: n[0]]]}
+
+    def set_deterministic(self, on):
+        """Fixed summation order (default); off lets the autotuner pick
+        atomic spreading."""
+        self._check(self._L.cgs_set_deterministic(self._ctx, 1 if on else 0))
 
     def set_precision(self, compensated):
         """Compensated (Kahan) spreading on or off."""

@@ -105,7 +105,8 @@ struct cgs_ctx {
     // launch shapes (cgs_autotune): coils per spreading block (0: as many as
     // fit), coils per interpolation thread
     int spread_cc = 0;
-    int spread_wpp = 1;          // warps per x plane of a spreading tile
+    int spread_wpp = 1;          // warps per x plane of a spreading tile (3: shared-memory atomics)
+    bool deterministic = true;   // fixed summation order everywhere (cgs_set_deterministic)
     int interp_cc = 4;
     bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
     uint64_t traj_serial = 0;    // incremented whenever the coordinates change
@@ -1530,6 +1531,7 @@ int cgs_set_precision(cgs_ctx* c, int32_t mode)
     const bool k = mode == CGS_PREC_COMPENSATED;
     if (k != c->kahan) {
         c->kahan = k;
+        if (k && c->spread_wpp == 3) c->spread_wpp = 1;
         drop_graphs(c);
     }
     return CGS_OK;
@@ -1580,7 +1582,8 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
     }
     float best = 1e30f;
     int best_sc = sc[0], best_wpp = 1;
-    for (int wpp : {1, 2}) {
+    for (int wpp : {1, 2, 3}) {
+        if (wpp == 3 && (c->deterministic || c->kahan)) continue;
         for (int v : sc) {
             if (wpp == 2 && v < 2) continue;
             c->spread_cc = v;
@@ -1876,6 +1879,17 @@ int cgs_pipe_menon_dcf(cgs_ctx* c, int32_t iters, float* dcf, int32_t on_device)
         std::copy(out.begin(), out.end(), dcf);
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
     return check_timeout(c);
+}
+
+int cgs_set_deterministic(cgs_ctx* c, int32_t on)
+{
+    if (!c) return CGS_ERR_ARG;
+    c->deterministic = on != 0;
+    if (c->deterministic && c->spread_wpp == 3) {
+        c->spread_wpp = 1;
+        drop_graphs(c);
+    }
+    return CGS_OK;
 }
 
 }  // extern "C"

@@ -288,4 +288,108 @@ __global__ void __launch_bounds__(32 * TILE_X * WPP) k_spread(SpreadArgs a)
     }
 }
 
+// Spreading with shared-memory atomics (no fixed summation order, so not
+// bitwise reproducible; chosen only for contexts that allow it): the warps
+// of the block take the staged samples round-robin, and the lanes of a warp
+// split the taps of one sample that fall inside the tile, so the sample's
+// set-up is paid once per tile instead of once per x plane.
+constexpr int SPREAD_ATOMIC_THREADS = 256;
+
+template <int CC>
+__global__ void __launch_bounds__(SPREAD_ATOMIC_THREADS) k_spread_atomic(SpreadArgs a)
+{
+    constexpr int NT = SPREAD_ATOMIC_THREADS, NW = NT / 32;
+    static_assert(CC <= SPREAD_VAL_STRIDE, "staged value row");
+    extern __shared__ float4 s_dyn[];
+    const int bin = a.bin0 + blockIdx.z;
+    const int tile = blockIdx.x;
+    const int c0 = blockIdx.y * a.cc;
+    const int ncc = min(a.cc, a.nch - c0);
+    const int tz = tile % a.ntz;
+    const int ty = (tile / a.ntz) % a.nty;
+    const int tx = tile / (a.ntz * a.nty);
+    const int x0 = tx * TILE_X, y0 = ty * TILE_Y, z0 = tz * TILE_Z;
+    float2* acc = reinterpret_cast<float2*>(s_dyn);
+    TapRecord* s_rec = reinterpret_cast<TapRecord*>(acc + (size_t)a.cc * ACC_PTS);
+    float2* s_val = reinterpret_cast<float2*>(s_rec + SPREAD_BATCH);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    {
+        float4* a4 = reinterpret_cast<float4*>(acc);
+        for (int e = tid; e < ncc * (ACC_PTS / 2); e += NT) a4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const long long tp = a.tile_ptr_off[bin];
+    const int beg = a.tile_ptr[tp + tile], end = a.tile_ptr[tp + tile + 1];
+    const int* idx = a.tile_idx + a.tile_idx_off[bin];
+    const long long sbase = a.bin_off[bin];
+    for (int s = beg; s < end; s += SPREAD_BATCH) {
+        const int nbat = min(SPREAD_BATCH, end - s);
+        __syncthreads();
+        for (int e = tid; e < nbat * 4; e += NT) {
+            const long long si = sbase + idx[s + e / 4];
+            reinterpret_cast<float4*>(s_rec)[e] = __ldg(reinterpret_cast<const float4*>(a.rec + si) + (e & 3));
+        }
+        for (int e = tid; e < nbat * ncc; e += NT) {
+            const int j = e / ncc, c = e - j * ncc;
+            const long long si = sbase + idx[s + j];
+            s_val[j * SPREAD_VAL_STRIDE + c] = a.yv[si * a.nch + c0 + c];
+        }
+        __syncthreads();
+        for (int j = warp; j < nbat; j += NW) {
+            const float* w = reinterpret_cast<const float*>(&s_rec[j]);
+            int nx, ny, nz;
+            unpack_nearest(__float_as_uint(w[15]), nx, ny, nz);
+            const int xl = max(nx - 2, x0), xh = min(nx + 2, x0 + TILE_X - 1);
+            const int yl = max(ny - 2, y0), yh = min(ny + 2, y0 + TILE_Y - 1);
+            const int zl = max(nz - 2, z0), zh = min(nz + 2, z0 + TILE_Z - 1);
+            if (xl > xh || yl > yh || zl > zh) continue;
+            const int cy = yh - yl + 1, cz = zh - zl + 1;
+            const int ntap = (xh - xl + 1) * cy * cz;
+            const float2* v = s_val + j * SPREAD_VAL_STRIDE;
+            for (int t = lane; t < ntap; t += 32) {
+                const int ix = t / (cy * cz), r = t - ix * (cy * cz);
+                const int iy = r / cz, iz = r - iy * cz;
+                const int gx = xl + ix, gy = yl + iy, gz = zl + iz;
+                const float wxv = w[gx - (nx - 2)], wyv = w[5 + gy - (ny - 2)], wzv = w[10 + gz - (nz - 2)];
+                const float wt = (wxv * wyv) * wzv;
+                if (wxv == 0.f || wyv == 0.f || wzv == 0.f || !(wt > a.thresh)) continue;
+                float2* pt = acc + ((gx - x0) * TILE_Y + (gy - y0)) * TILE_ZP + (gz - z0);
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+                    if (c < ncc) {
+                        const float2 vv = v[c];
+                        atomicAdd(&pt[c * ACC_PTS].x, vv.x * wt);
+                        atomicAdd(&pt[c * ACC_PTS].y, vv.y * wt);
+                    }
+            }
+        }
+    }
+    __syncthreads();
+    constexpr int ZH = TILE_Z / 2;
+    constexpr int XSTEP = NT / (ZH * TILE_Y);
+    static_assert(NT % (ZH * TILE_Y) == 0 && TILE_X % XSTEP == 0, "store mapping");
+    float2* grid = a.grid + (long long)blockIdx.z * a.grid_bs + (long long)c0 * a.coil_stride;
+    const int Gx = a.G[0], Gy = a.G[1], Gz = a.G[2];
+    const bool pairs = (Gz % 2 == 0) && (reinterpret_cast<uintptr_t>(a.grid) & 15) == 0 && (a.coil_stride % 2 == 0) &&
+                       (a.grid_bs % 2 == 0);
+    const int zq = tid % ZH, ly = (tid / ZH) % TILE_Y, lx0 = tid / (ZH * TILE_Y);
+    const int Y = y0 + ly, Z = z0 + 2 * zq;
+    if (Y < Gy && Z < Gz) {
+        for (int c = 0; c < ncc; ++c) {
+            for (int lx = lx0; lx < TILE_X; lx += XSTEP) {
+                const int X = x0 + lx;
+                if (X >= Gx) break;
+                const int q = c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + 2 * zq;
+                const float2 v0 = acc[q], v1 = acc[q + 1];
+                float2* dst = grid + (long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z;
+                if (pairs) {
+                    *reinterpret_cast<float4*>(dst) = make_float4(v0.x, v0.y, v1.x, v1.y);
+                } else {
+                    dst[0] = v0;
+                    if (Z + 1 < Gz) dst[1] = v1;
+                }
+            }
+        }
+    }
+}
+
 }  // namespace cgs

@@ -146,6 +146,11 @@ cudaError_t kernels_init()
     if (e == cudaSuccess) e = spread_attr_one<2, 2>(sp, sk);
     if (e == cudaSuccess) e = spread_attr_one<4, 2>(sp, sk);
     if (e == cudaSuccess) e = spread_attr_one<6, 2>(sp, sk);
+    for (int i = 0; i < 3 && e == cudaSuccess; ++i) {
+        const void* f = i == 0 ? (const void*)k_spread_atomic<4> : i == 1 ? (const void*)k_spread_atomic<8>
+                                                                           : (const void*)k_spread_atomic<12>;
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sp);
+    }
     if (e == cudaSuccess) e = fft_init_all();
     return e;
 }
@@ -153,6 +158,12 @@ cudaError_t kernels_init()
 template <bool K>
 static void spread_launch(const SpreadArgs& a, dim3 grid, size_t smem, int wpp, cudaStream_t s)
 {
+    if (wpp == 3 && !K) {   // shared-memory atomics (no fixed order)
+        if (a.cc <= 4) k_spread_atomic<4><<<grid, SPREAD_ATOMIC_THREADS, smem, s>>>(a);
+        else if (a.cc <= 8) k_spread_atomic<8><<<grid, SPREAD_ATOMIC_THREADS, smem, s>>>(a);
+        else k_spread_atomic<12><<<grid, SPREAD_ATOMIC_THREADS, smem, s>>>(a);
+        return;
+    }
     if (wpp == 2) {
         const int ccw = (a.cc + 1) / 2;
         if (ccw <= 2) k_spread<2, 2, K><<<grid, 32 * TILE_X * 2, smem, s>>>(a);
@@ -168,7 +179,9 @@ static void spread_launch(const SpreadArgs& a, dim3 grid, size_t smem, int wpp, 
 cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan, int wpp, cudaStream_t s)
 {
     if (ntiles == 0 || nbins == 0) return cudaSuccess;
-    if (a.cc < 1 || a.cc > spread_max_coils(kahan) || (wpp != 1 && wpp != 2)) return cudaErrorInvalidValue;
+    // wpp: 1 or 2 warps per x plane (fixed order), 3 = shared-memory atomics
+    if (a.cc < 1 || a.cc > spread_max_coils(kahan) || wpp < 1 || wpp > 3 || (wpp == 3 && kahan))
+        return cudaErrorInvalidValue;
     const size_t smem = spread_smem_bytes(a.cc, kahan);
     dim3 grid((unsigned)ntiles, (unsigned)((a.nch + a.cc - 1) / a.cc), (unsigned)nbins);
     if (kahan) spread_launch<true>(a, grid, smem, wpp, s);

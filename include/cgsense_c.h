@@ -302,6 +302,12 @@ int cgs_rhs_vjp_k_d(cgs_ctx* ctx, int32_t bin0, int32_t nb, const void* y_dev, c
 #define CGS_PREC_COMPENSATED 1
 int cgs_set_precision(cgs_ctx* ctx, int32_t mode);
 
+/* Fixed summation order (default on): every result is bitwise reproducible.
+ * Off, the autotuner may also pick spreading with shared-memory atomics
+ * (results then vary in the last bits from run to run, as the reference's
+ * OpenMP atomics do). */
+int cgs_set_deterministic(cgs_ctx* ctx, int32_t on);
+
 /* Autotuner: times one batched E^H D E application of every bin for each
  * candidate launch shape -- coils per spreading block (all that fit, then
  * 1/2, 1/3, 1/4 of them) with one or two warps per x plane of a tile, then

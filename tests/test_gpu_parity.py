@@ -211,6 +211,29 @@ def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
     assert np.array_equal(res0, res1)
 
 
+def test_atomic_spreading_matches_fixed_order(gpu_lib, cgs, oracle_mod, o64, synth):
+    """With determinism off the autotuner may pick shared-memory atomic
+    spreading; forced here, the batched solve equals the fixed-order one to
+    FP32 rounding."""
+    img, grid, nch = (32, 24, 20), (64, 48, 40), 5
+    k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 40, 48)
+    bins = synth.bin_samples([np.arange(0, 15), np.arange(15, 40)], 48)
+    smaps = synth.coil_maps(img, nch)
+    rng = np.random.default_rng(12)
+    data = (rng.standard_normal((nch, k.shape[0])) + 1j * rng.standard_normal((nch, k.shape[0]))).astype(np.complex64)
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b)
+    r.set_trajectory(k)
+    r.set_bins(bins)
+    r.set_smaps(smaps)
+    x0, res0, _ = r.cg_sense_batched(data, 0.0, 5)
+    r.set_deterministic(False)
+    tune = r.autotune()
+    assert tune["spread_warps_per_plane"] in (1, 2, 3)
+    x1, res1, _ = r.cg_sense_batched(data, 0.0, 5)
+    assert rel_l2(x1, x0) < 1e-5
+    assert np.allclose(res1, res0, rtol=1e-5)
+
+
 def test_empty_bin_and_zero_data(gpu_lib, cgs, synth):
     """A bin without samples (or all-zero data) has a zero right-hand side:
     the solve returns x = 0 after 0 iterations."""

@@ -107,7 +107,7 @@ def test_state_loop_matches_single_solves(gpu_lib, cgs, synth, tmp_path):
     exported root-sum-of-squares is that of the density-corrected coil
     images."""
     import torch
-    img = grid = (16, 16, 12)
+    img = grid = (16, 16, 16)
     nch = 3
     sx, sy, sz = 24, 8, 6
     rng = np.random.default_rng(11)
