@@ -277,12 +277,14 @@ cudaError_t launch_pair_grad(const PairGradArgs& a, cudaStream_t s)
 // Iterative density weights (Pipe and Menon, Magn. Reson. Med. 41:179-186,
 // 1999): w <- w / (C * w) at the samples, C * w the interpolation of the
 // spread weights.  v is the spread input (w, 0) and u the interpolated sum.
+// A sample without any tap in the grid (C * w = 0) gets weight 0, as a hull
+// sample's Voronoi cell does.
 __global__ void k_pm_update(float* __restrict__ w, float2* __restrict__ v, const float2* __restrict__ u, long long n)
 {
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float c = u[i].x;
-    const float nw = c > 1e-30f ? w[i] / c : w[i];
+    const float nw = c > 0.f ? w[i] / c : 0.f;
     w[i] = nw;
     v[i] = make_float2(nw, 0.f);
 }
