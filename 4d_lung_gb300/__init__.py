@@ -55,7 +55,7 @@ EXPORTS = [
     "cgs_update_trajectory_d", "cgs_set_precision", "cgs_autotune", "cgs_rhs_d", "cgs_apply_vjp_k_d",
     "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream", "cgs_import_data_bin", "cgs_permute_samples_d",
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
-    "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic",
+    "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic", "cgs_set_launch_shape",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -175,6 +175,7 @@ def lib():
         "cgs_rss_d": (C.c_int, [vp, C.c_int32, i64, vp, vp]),
         "cgs_pipe_menon_dcf": (C.c_int, [vp, C.c_int32, vp, C.c_int32]),
         "cgs_set_deterministic": (C.c_int, [vp, C.c_int32]),
+        "cgs_set_launch_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
         "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
                                              C.c_double, C.c_int32, C.c_int32, vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
@@ -537,6 +538,10 @@ class Reco:
         self._check(self._L.cgs_autotune(self._ctx, _p(t), 32, _p(n), _p(sc), _p(sw), _p(ic)))
         return {"spread_coils_per_block": int(sc[0]), "spread_warps_per_plane": int(sw[0]),
                 "interp_coils_per_thread": int(ic[0]), "candidates_ms": [float(v) for v in t[: n[0]]]}
+
+    def set_launch_shape(self, spread_cc=0, spread_variant=1, interp_cc=4):
+        """Launch shape by hand (see cgs_set_launch_shape)."""
+        self._check(self._L.cgs_set_launch_shape(self._ctx, spread_cc, spread_variant, interp_cc))
 
     def set_deterministic(self, on):
         """Fixed summation order (default); off lets the autotuner pick

@@ -105,7 +105,7 @@ struct cgs_ctx {
     // launch shapes (cgs_autotune): coils per spreading block (0: as many as
     // fit), coils per interpolation thread
     int spread_cc = 0;
-    int spread_wpp = 1;          // warps per x plane of a spreading tile (3: shared-memory atomics)
+    int spread_wpp = 1;          // spreading variant: warps per x plane 1 / 2, 3 atomics, 4 / 5 pipelined
     bool deterministic = true;   // fixed summation order everywhere (cgs_set_deterministic)
     int interp_cc = 4;
     bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
@@ -1531,7 +1531,7 @@ int cgs_set_precision(cgs_ctx* c, int32_t mode)
     const bool k = mode == CGS_PREC_COMPENSATED;
     if (k != c->kahan) {
         c->kahan = k;
-        if (k && c->spread_wpp == 3) c->spread_wpp = 1;
+        if (k && c->spread_wpp >= 3) c->spread_wpp = 1;
         drop_graphs(c);
     }
     return CGS_OK;
@@ -1582,8 +1582,9 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
     }
     float best = 1e30f;
     int best_sc = sc[0], best_wpp = 1;
-    for (int wpp : {1, 2, 3}) {
+    for (int wpp : {1, 2, 4, 5, 3}) {
         if (wpp == 3 && (c->deterministic || c->kahan)) continue;
+        if (wpp >= 4 && c->kahan) continue;
         for (int v : sc) {
             if (wpp == 2 && v < 2) continue;
             c->spread_cc = v;
@@ -1889,6 +1890,22 @@ int cgs_set_deterministic(cgs_ctx* c, int32_t on)
         c->spread_wpp = 1;
         drop_graphs(c);
     }
+    return CGS_OK;
+}
+
+int cgs_set_launch_shape(cgs_ctx* c, int32_t spread_cc, int32_t spread_variant, int32_t interp_cc)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (spread_cc < 0 || spread_cc > spread_max_coils(c->kahan)) return fail(c, CGS_ERR_ARG, "spread_cc out of range");
+    if (spread_variant < 1 || spread_variant > 5 || (spread_variant >= 3 && c->kahan) ||
+        (spread_variant == 3 && c->deterministic))
+        return fail(c, CGS_ERR_ARG, "spreading variant not allowed here");
+    if (interp_cc != 2 && interp_cc != 4 && interp_cc != 6 && interp_cc != 8)
+        return fail(c, CGS_ERR_ARG, "interp_cc must be 2, 4, 6 or 8");
+    c->spread_cc = spread_cc;
+    c->spread_wpp = spread_variant;
+    c->interp_cc = interp_cc;
+    drop_graphs(c);
     return CGS_OK;
 }
 

@@ -392,4 +392,212 @@ __global__ void __launch_bounds__(SPREAD_ATOMIC_THREADS) k_spread_atomic(SpreadA
     }
 }
 
+// Persistent, software-pipelined spreading: every block walks work items
+// (bin, coil chunk, tile) with stride gridDim.x; the loads of the next batch
+// of samples (tile list entries, tap records, values -- the same or the next
+// item) are issued into registers before the current batch is processed and
+// written to the second shared-memory buffer after it, so their latency
+// hides behind the work.  Ownership, summation order and results are those
+// of k_spread<CCW, WPP, false>.
+template <int CCW, int WPP>
+__global__ void __launch_bounds__(32 * TILE_X * WPP) k_spread_pipe(SpreadArgs a, long long nitems, int nchunk)
+{
+    constexpr int NT = 32 * TILE_X * WPP;
+    constexpr int SB = SPREAD_BATCH;
+    constexpr int NREC = (SB * 4 + NT - 1) / NT;                       // float4 record pieces per thread
+    constexpr int NVAL = (SB * SPREAD_VAL_STRIDE + NT - 1) / NT;      // values per thread
+    static_assert(CCW * WPP <= SPREAD_VAL_STRIDE, "staged value row");
+    extern __shared__ float4 s_dyn[];
+    float2* acc = reinterpret_cast<float2*>(s_dyn);
+    TapRecord* s_rec[2];
+    float2* s_val[2];
+    s_rec[0] = reinterpret_cast<TapRecord*>(acc + (size_t)a.cc * ACC_PTS);
+    s_val[0] = reinterpret_cast<float2*>(s_rec[0] + SB);
+    s_rec[1] = reinterpret_cast<TapRecord*>(s_val[0] + SB * SPREAD_VAL_STRIDE);
+    s_val[1] = reinterpret_cast<float2*>(s_rec[1] + SB);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int plane = warp % TILE_X, part = warp / TILE_X;
+    const int jy = lane / 5, jz = lane - 5 * (lane / 5);
+    const int ntiles = a.ntx * a.nty * a.ntz;
+
+    struct Item {
+        int bin, c0, ncc, tile, beg, end, x0, y0, z0;
+        long long sbase;
+        const int* idx;
+    };
+    auto item_of = [&](long long it) {
+        Item m;
+        const int tile = (int)(it % ntiles);
+        const long long r = it / ntiles;
+        const int ch = (int)(r % nchunk);
+        m.bin = a.bin0 + (int)(r / nchunk);
+        m.tile = tile;
+        m.c0 = ch * a.cc;
+        m.ncc = min(a.cc, a.nch - m.c0);
+        const long long tp = a.tile_ptr_off[m.bin];
+        m.beg = a.tile_ptr[tp + tile];
+        m.end = a.tile_ptr[tp + tile + 1];
+        m.idx = a.tile_idx + a.tile_idx_off[m.bin];
+        m.sbase = a.bin_off[m.bin];
+        const int tz = tile % a.ntz, ty = (tile / a.ntz) % a.nty, tx = tile / (a.ntz * a.nty);
+        m.x0 = tx * TILE_X;
+        m.y0 = ty * TILE_Y;
+        m.z0 = tz * TILE_Z;
+        return m;
+    };
+    // registers of one prefetched batch
+    float4 pr[NREC];
+    float2 pv[NVAL];
+    auto prefetch = [&](const Item& m, int s) {
+        const int nbat = min(SB, m.end - s);
+#pragma unroll
+        for (int q = 0; q < NREC; ++q) {
+            const int e = tid + q * NT;
+            if (e < nbat * 4) {
+                const long long si = m.sbase + m.idx[s + e / 4];
+                pr[q] = __ldg(reinterpret_cast<const float4*>(a.rec + si) + (e & 3));
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NVAL; ++q) {
+            const int e = tid + q * NT;
+            if (e < nbat * m.ncc) {
+                const int j = e / m.ncc, c = e - j * m.ncc;
+                const long long si = m.sbase + m.idx[s + j];
+                pv[q] = a.yv[si * a.nch + m.c0 + c];
+            }
+        }
+    };
+    auto commit = [&](const Item& m, int s, int buf) {
+        const int nbat = min(SB, m.end - s);
+#pragma unroll
+        for (int q = 0; q < NREC; ++q) {
+            const int e = tid + q * NT;
+            if (e < nbat * 4) reinterpret_cast<float4*>(s_rec[buf])[e] = pr[q];
+        }
+#pragma unroll
+        for (int q = 0; q < NVAL; ++q) {
+            const int e = tid + q * NT;
+            if (e < nbat * m.ncc) {
+                const int j = e / m.ncc, c = e - j * m.ncc;
+                s_val[buf][j * SPREAD_VAL_STRIDE + c] = pv[q];
+            }
+        }
+    };
+    auto zero_acc = [&](int ncc) {
+        float4* a4 = reinterpret_cast<float4*>(acc);
+        for (int e = tid; e < ncc * (ACC_PTS / 2); e += NT) a4[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    };
+
+    long long it = blockIdx.x;
+    if (it >= nitems) return;
+    Item cur = item_of(it);
+    int s = cur.beg;       // first sample of the current batch
+    int buf = 0;
+    if (s < cur.end) {
+        prefetch(cur, s);
+        commit(cur, s, buf);
+    }
+    zero_acc(cur.ncc);
+    __syncthreads();
+    while (true) {
+        // the batch after this one: the same item's next, or the next item's
+        // first (an item without samples is stored as zeros when reached)
+        long long it_n = it;
+        Item nxt = cur;
+        int s_n = s + SB;
+        bool have_next = true;
+        if (s_n >= cur.end) {
+            it_n = it + gridDim.x;
+            if (it_n >= nitems) {
+                have_next = false;
+            } else {
+                nxt = item_of(it_n);
+                s_n = nxt.beg;
+            }
+        }
+        const bool next_in_item = have_next && it_n == it;
+        const bool fetch = have_next && s_n < nxt.end;
+        if (fetch) prefetch(nxt, s_n);
+        // process the current batch
+        if (s < cur.end) {
+            const int nbat = min(SB, cur.end - s);
+            const int per = (cur.ncc + WPP - 1) / WPP;
+            const int cb = part * per, nmy = min(per, cur.ncc - cb);
+            const int2 run = a.plane_rng[((long long)cur.bin * ntiles + cur.tile) * TILE_X + plane];
+            const int j0 = max(run.x - (s - cur.beg), 0), j1 = min(run.y - (s - cur.beg), nbat);
+            const int gx = cur.x0 + plane;
+            if (lane < 25 && nmy > 0) {
+                for (int j = j0; j < j1; ++j) {
+                    const float* w = reinterpret_cast<const float*>(&s_rec[buf][j]);
+                    int nx, ny, nz;
+                    unpack_nearest(__float_as_uint(w[15]), nx, ny, nz);
+                    const int jx = gx - (nx - 2);
+                    if (jx < 0 || jx > 4) continue;
+                    const int gy = ny - 2 + jy, gz = nz - 2 + jz;
+                    if (gy < cur.y0 || gy >= cur.y0 + TILE_Y || gz < cur.z0 || gz >= cur.z0 + TILE_Z) continue;
+                    const float wxv = w[jx], wyv = w[5 + jy], wzv = w[10 + jz];
+                    const float wt = (wxv * wyv) * wzv;
+                    if (wxv == 0.f || wyv == 0.f || wzv == 0.f || !(wt > a.thresh)) continue;
+                    float2* pt = acc + (size_t)cb * ACC_PTS + (plane * TILE_Y + (gy - cur.y0)) * TILE_ZP + (gz - cur.z0);
+                    const float2* v = s_val[buf] + j * SPREAD_VAL_STRIDE + cb;
+                    float2 t[CCW], vv[CCW];
+#pragma unroll
+                    for (int c = 0; c < CCW; ++c)
+                        if (c < nmy) {
+                            t[c] = pt[c * ACC_PTS];
+                            vv[c] = v[c];
+                        }
+#pragma unroll
+                    for (int c = 0; c < CCW; ++c)
+                        if (c < nmy) {
+                            t[c].x = fmaf(vv[c].x, wt, t[c].x);
+                            t[c].y = fmaf(vv[c].y, wt, t[c].y);
+                            pt[c * ACC_PTS] = t[c];
+                        }
+                }
+            }
+        }
+        __syncthreads();   // the batch is consumed; buffer buf ^ 1 is free
+        if (fetch) commit(nxt, s_n, buf ^ 1);
+        if (!next_in_item) {
+            // store the finished tile (zeros included)
+            constexpr int ZH = TILE_Z / 2;
+            constexpr int XSTEP = NT / (ZH * TILE_Y);
+            static_assert(NT % (ZH * TILE_Y) == 0 && TILE_X % XSTEP == 0, "store mapping");
+            float2* grid = a.grid + (long long)(cur.bin - a.bin0) * a.grid_bs + (long long)cur.c0 * a.coil_stride;
+            const int Gx = a.G[0], Gy = a.G[1], Gz = a.G[2];
+            const bool pairs = (Gz % 2 == 0) && (reinterpret_cast<uintptr_t>(a.grid) & 15) == 0 &&
+                               (a.coil_stride % 2 == 0) && (a.grid_bs % 2 == 0);
+            const int zq = tid % ZH, ly = (tid / ZH) % TILE_Y, lx0 = tid / (ZH * TILE_Y);
+            const int Y = cur.y0 + ly, Z = cur.z0 + 2 * zq;
+            if (Y < Gy && Z < Gz) {
+                for (int c = 0; c < cur.ncc; ++c) {
+                    for (int lx = lx0; lx < TILE_X; lx += XSTEP) {
+                        const int X = cur.x0 + lx;
+                        if (X >= Gx) break;
+                        const int q = c * ACC_PTS + (lx * TILE_Y + ly) * TILE_ZP + 2 * zq;
+                        const float2 v0 = acc[q], v1 = acc[q + 1];
+                        float2* dst = grid + (long long)c * a.coil_stride + ((long long)X * Gy + Y) * Gz + Z;
+                        if (pairs) {
+                            *reinterpret_cast<float4*>(dst) = make_float4(v0.x, v0.y, v1.x, v1.y);
+                        } else {
+                            dst[0] = v0;
+                            if (Z + 1 < Gz) dst[1] = v1;
+                        }
+                    }
+                }
+            }
+            if (!have_next) break;
+            __syncthreads();   // the tile is read out before it is cleared
+            zero_acc(nxt.ncc);
+        }
+        __syncthreads();
+        cur = nxt;
+        it = it_n;
+        s = s_n;
+        buf ^= 1;
+    }
+}
+
 }  // namespace cgs

@@ -127,6 +127,41 @@ size_t spread_smem_bytes(int cc, bool kahan)
 
 int spread_max_coils(bool kahan) { return kahan ? SPREAD_CC_MAX / 2 : SPREAD_CC_MAX; }
 
+// the pipelined variant stages two batches
+size_t spread_pipe_smem_bytes(int cc)
+{
+    return (size_t)cc * ACC_PTS * sizeof(float2) +
+           2 * ((size_t)SPREAD_BATCH * sizeof(TapRecord) + (size_t)SPREAD_BATCH * SPREAD_VAL_STRIDE * sizeof(float2));
+}
+
+static int sm_count_misc()
+{
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int CCW, int WPP>
+static cudaError_t spread_pipe_run(const SpreadArgs& a, int ntiles, int nbins, cudaStream_t s)
+{
+    const size_t smem = spread_pipe_smem_bytes(a.cc);
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spread_pipe<CCW, WPP>, 32 * TILE_X * WPP,
+                                                                  smem);
+    if (e != cudaSuccess) return e;
+    const int nchunk = (a.nch + a.cc - 1) / a.cc;
+    const long long nitems = (long long)ntiles * nchunk * nbins;
+    long long nblk = (long long)sm_count_misc() * (per_sm > 0 ? per_sm : 1);
+    if (nblk > nitems) nblk = nitems;
+    k_spread_pipe<CCW, WPP><<<(unsigned)nblk, 32 * TILE_X * WPP, smem, s>>>(a, nitems, nchunk);
+    return cudaGetLastError();
+}
+
 template <int CCW, int WPP>
 static cudaError_t spread_attr_one(int smax_plain, int smax_kahan)
 {
@@ -151,6 +186,12 @@ cudaError_t kernels_init()
                                                                            : (const void*)k_spread_atomic<12>;
         e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, sp);
     }
+    const int spp = (int)spread_pipe_smem_bytes(SPREAD_CC_MAX);
+    const void* pipes[6] = {(const void*)k_spread_pipe<4, 1>, (const void*)k_spread_pipe<8, 1>,
+                            (const void*)k_spread_pipe<12, 1>, (const void*)k_spread_pipe<2, 2>,
+                            (const void*)k_spread_pipe<4, 2>, (const void*)k_spread_pipe<6, 2>};
+    for (int i = 0; i < 6 && e == cudaSuccess; ++i)
+        e = cudaFuncSetAttribute(pipes[i], cudaFuncAttributeMaxDynamicSharedMemorySize, spp);
     if (e == cudaSuccess) e = fft_init_all();
     return e;
 }
@@ -179,9 +220,21 @@ static void spread_launch(const SpreadArgs& a, dim3 grid, size_t smem, int wpp, 
 cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan, int wpp, cudaStream_t s)
 {
     if (ntiles == 0 || nbins == 0) return cudaSuccess;
-    // wpp: 1 or 2 warps per x plane (fixed order), 3 = shared-memory atomics
-    if (a.cc < 1 || a.cc > spread_max_coils(kahan) || wpp < 1 || wpp > 3 || (wpp == 3 && kahan))
+    // wpp: 1 or 2 warps per x plane (fixed order), 3 = shared-memory atomics,
+    // 4 / 5 = persistent and pipelined with 1 / 2 warps per x plane (fixed order)
+    if (a.cc < 1 || a.cc > spread_max_coils(kahan) || wpp < 1 || wpp > 5 || (wpp >= 3 && kahan))
         return cudaErrorInvalidValue;
+    if (wpp == 4) {
+        if (a.cc <= 4) return spread_pipe_run<4, 1>(a, ntiles, nbins, s);
+        if (a.cc <= 8) return spread_pipe_run<8, 1>(a, ntiles, nbins, s);
+        return spread_pipe_run<12, 1>(a, ntiles, nbins, s);
+    }
+    if (wpp == 5) {
+        const int ccw = (a.cc + 1) / 2;
+        if (ccw <= 2) return spread_pipe_run<2, 2>(a, ntiles, nbins, s);
+        if (ccw <= 4) return spread_pipe_run<4, 2>(a, ntiles, nbins, s);
+        return spread_pipe_run<6, 2>(a, ntiles, nbins, s);
+    }
     const size_t smem = spread_smem_bytes(a.cc, kahan);
     dim3 grid((unsigned)ntiles, (unsigned)((a.nch + a.cc - 1) / a.cc), (unsigned)nbins);
     if (kahan) spread_launch<true>(a, grid, smem, wpp, s);

@@ -181,6 +181,8 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
         t0 = time.perf_counter()
         dcf = reco.pipe_menon_dcf(20)
         dcf_s = time.perf_counter() - t0
+        for idx in sbins:   # the same per-bin cap as the Voronoi weights
+            dcf[idx] = synth.cap_dcf(dcf[idx])
     reco.set_dcf(dcf)
     reco.set_smaps_tensor(smaps_t)
     return w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s
@@ -698,7 +700,7 @@ def run_ours(args):
                    "cg_iters": iters, "kb_w": kb_w, "kb_b": round(kb_b, 4),
                    "dcf": ("per-bin Voronoi volumes capped at the 99th percentile (host, %.1f s set-up)" % dcf_s)
                    if args.dcf == "voronoi" else
-                   ("per-bin Pipe-Menon weights, 20 iterations (GPU, %.2f s set-up)" % dcf_s)
+                   ("per-bin Pipe-Menon weights, 20 iterations (GPU, %.2f s set-up), capped at the 99th percentile" % dcf_s)
                    if args.dcf == "pipe-menon"
                    else "radial stand-in",
                    "step": "one 16-bin 4D CG-SENSE reconstruction (graph replay)",

@@ -308,6 +308,14 @@ int cgs_set_precision(cgs_ctx* ctx, int32_t mode);
  * OpenMP atomics do). */
 int cgs_set_deterministic(cgs_ctx* ctx, int32_t on);
 
+/* Launch shape set by hand (what cgs_autotune picks): coils per spreading
+ * block (0: as many as fit), spreading variant (1 / 2: one / two warps per x
+ * plane of a tile; 3: shared-memory atomics, only with determinism off;
+ * 4 / 5: persistent and software-pipelined with one / two warps per plane),
+ * coils per interpolation thread (2, 4, 6, 8).  Variants 1, 2, 4, 5 give
+ * bitwise-identical results. */
+int cgs_set_launch_shape(cgs_ctx* ctx, int32_t spread_cc, int32_t spread_variant, int32_t interp_cc);
+
 /* Autotuner: times one batched E^H D E application of every bin for each
  * candidate launch shape -- coils per spreading block (all that fit, then
  * 1/2, 1/3, 1/4 of them) with one or two warps per x plane of a tile, then

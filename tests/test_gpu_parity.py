@@ -211,6 +211,30 @@ def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
     assert np.array_equal(res0, res1)
 
 
+@pytest.mark.parametrize("img,grid,nch", [((32, 24, 20), (64, 48, 40), 7), ((48, 40, 24), (96, 80, 48), 12)])
+def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid, nch):
+    """The fixed-order spreading variants (one / two warps per x plane,
+    plain or persistent and pipelined) and every coil chunk size give
+    bitwise-identical solves: each grid value is summed in the same order."""
+    k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 48)
+    bins = synth.bin_samples([np.arange(0, 7), np.arange(7, 41), np.arange(41, 60)], 48)
+    smaps = synth.coil_maps(img, nch)
+    rng = np.random.default_rng(13)
+    data = (rng.standard_normal((nch, k.shape[0])) + 1j * rng.standard_normal((nch, k.shape[0]))).astype(np.complex64)
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b)
+    r.set_trajectory(k)
+    r.set_bins(bins)
+    r.set_smaps(smaps)
+    r.set_launch_shape(0, 1, 4)
+    x0, res0, _ = r.cg_sense_batched(data, 0.0, 4)
+    for cc in (0, 3, 5):
+        for variant in (1, 2, 4, 5):
+            r.set_launch_shape(cc, variant, 2)
+            x1, res1, _ = r.cg_sense_batched(data, 0.0, 4)
+            assert np.array_equal(x1, x0), (cc, variant)
+            assert np.array_equal(res1, res0), (cc, variant)
+
+
 def test_atomic_spreading_matches_fixed_order(gpu_lib, cgs, oracle_mod, o64, synth):
     """With determinism off the autotuner may pick shared-memory atomic
     spreading; forced here, the batched solve equals the fixed-order one to
