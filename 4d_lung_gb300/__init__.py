@@ -56,6 +56,7 @@ EXPORTS = [
     "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream", "cgs_import_data_bin", "cgs_permute_samples_d",
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
     "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic", "cgs_set_launch_shape",
+    "cgs_set_support_pruning", "cgs_support_stats",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -176,6 +177,8 @@ def lib():
         "cgs_pipe_menon_dcf": (C.c_int, [vp, C.c_int32, vp, C.c_int32]),
         "cgs_set_deterministic": (C.c_int, [vp, C.c_int32]),
         "cgs_set_launch_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
+        "cgs_set_support_pruning": (C.c_int, [vp, C.c_int32]),
+        "cgs_support_stats": (C.c_int, [vp, vp, vp]),
         "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
                                              C.c_double, C.c_int32, C.c_int32, vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
@@ -542,6 +545,20 @@ class Reco:
     def set_launch_shape(self, spread_cc=0, spread_variant=1, interp_cc=4):
         """Launch shape by hand (see cgs_set_launch_shape)."""
         self._check(self._L.cgs_set_launch_shape(self._ctx, spread_cc, spread_variant, interp_cc))
+
+    def set_support_pruning(self, on):
+        """Transform only the grid columns the samples' supports reach (default on;
+        see cgs_set_support_pruning)."""
+        self._check(self._L.cgs_set_support_pruning(self._ctx, 1 if on else 0))
+
+    def support_stats(self):
+        """Per bin: grid (y, z) columns the x passes transform and spreading
+        tiles stored (see cgs_support_stats)."""
+        nb = self.num_bins()
+        cols = np.zeros(nb, np.int64)
+        live = np.zeros(nb, np.int64)
+        self._check(self._L.cgs_support_stats(self._ctx, _p(cols), _p(live)))
+        return cols, live
 
     def set_deterministic(self, on):
         """Fixed summation order (default); off lets the autotuner pick

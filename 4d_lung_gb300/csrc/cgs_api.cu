@@ -112,6 +112,19 @@ struct cgs_ctx {
     uint64_t traj_serial = 0;    // incremented whenever the coordinates change
     bool tiles_stale = false;    // spreading lists built from older coordinates
     int ntx = 0, nty = 0, ntz = 0, ntiles = 0;
+    // sample-support pruning of the x FFT passes and the spreading
+    // (cgs_set_support_pruning)
+    bool sup_prune = true;
+    bool sup_built = false;
+    std::vector<long long> h_sup_off;        // per bin: first entry in d_sup_tiles
+    std::vector<long long> h_live_off;       // per bin: first entry in d_live (spreading tiles)
+    DevBuf d_sup_tiles, d_live, d_live_off;
+    // The adjoint x pass writes its own y buffer (d_ybuf_adj), and with
+    // pruning only the supported columns of the slot's bin; the rest of the
+    // slot must hold zeros.  adj_slot[j]: the bin whose supported columns
+    // bound the non-zeros of workspace slot j, -1 when unknown.
+    DevBuf d_ybuf_adj;
+    std::vector<int> adj_slot;
     // coil maps
     DevBuf d_smaps;
     bool smaps_set = false;
@@ -122,6 +135,8 @@ struct cgs_ctx {
     DevBuf d_b, d_x, d_r, d_pv, d_q, d_state, d_partials, d_partials2, d_res;
     std::map<GraphKey, cudaGraphExec_t> graphs;
     std::map<GraphKey, long long> graph_launches;
+    // adjoint y-buffer slot records at the start and at the end of each graph
+    std::map<GraphKey, std::pair<std::vector<int>, std::vector<int>>> graph_slots;
     long long launches = 0;
     // plain per-bin form (cgs_cg_solve_plain_d)
     cufftHandle plain_plan = 0;
@@ -215,6 +230,8 @@ struct BinPrep {
     std::vector<int> tile_ptr;
     std::vector<int> tile_idx;
     std::vector<int> plane_rng;   // [ntiles][TILE_X][2]
+    std::vector<int> sup_cols;        // first column of each x-pass tile the samples touch
+    std::vector<int> live;            // spreading tiles holding a supported column
 };
 
 void nearest_point(const double* kk, const int* G, int* nr)
@@ -310,6 +327,55 @@ void tile_lists(const cgs_ctx* c, const unsigned* nearest, long long n, BinPrep&
     }
 }
 
+// Sample-support lists of one bin.  The interpolation reads, and the
+// spreading writes, grid points within +-2 cells of each sample's nearest
+// point (clipped to the grid).  A (y, z) column of the grid that no sample's
+// support reaches is never read after the forward x pass, and the adjoint x
+// pass transforms zeros there.  The x passes work on tiles of tb consecutive
+// columns of the flattened [Gy][Gz] plane: the tiles holding a supported
+// column are listed (sup_cols); the spreading stores the grid tiles whose
+// (y, z) extent meets a listed column (live).
+void support_lists(const cgs_ctx* c, const unsigned* nearest, long long n, int tb, BinPrep& out)
+{
+    const int Gy = c->G[1], Gz = c->G[2];
+    const long long ncol = (long long)Gy * Gz;
+    std::vector<unsigned char> col(ncol, 0);
+    for (long long j = 0; j < n; ++j) {
+        const int ny = (int)((nearest[j] >> 11) & 2047u), nz = (int)(nearest[j] >> 22);
+        const int y0 = std::max(ny - 2, 0), y1 = std::min(ny + 2, Gy - 1);
+        const int z0 = std::max(nz - 2, 0), z1 = std::min(nz + 2, Gz - 1);
+        for (int y = y0; y <= y1; ++y)
+            for (int z = z0; z <= z1; ++z) col[(long long)y * Gz + z] = 1;
+    }
+    std::vector<unsigned char> listed(ncol, 0);   // column lies in a listed tile
+    out.sup_cols.clear();
+    for (long long b0 = 0; b0 < ncol; b0 += tb) {
+        const long long b1 = std::min(ncol, b0 + tb);
+        bool any = false;
+        for (long long b = b0; b < b1 && !any; ++b) any = col[b] != 0;
+        if (!any) continue;
+        out.sup_cols.push_back((int)b0);
+        for (long long b = b0; b < b1; ++b) listed[b] = 1;
+    }
+    // spreading tiles whose (y, z) extent holds a masked column: the adjoint
+    // x pass reads those columns at every x, so these tiles are stored (with
+    // zeros where no sample reaches); no other grid point is ever read
+    std::vector<unsigned char> tcol((size_t)c->nty * c->ntz, 0);
+    for (int ty = 0; ty < c->nty; ++ty)
+        for (int tz = 0; tz < c->ntz; ++tz) {
+            bool any = false;
+            for (int y = ty * TILE_Y; y < std::min((ty + 1) * TILE_Y, Gy) && !any; ++y)
+                for (int z = tz * TILE_Z; z < std::min((tz + 1) * TILE_Z, Gz) && !any; ++z) {
+                    any = listed[(long long)y * Gz + z] != 0;
+                }
+            tcol[(size_t)ty * c->ntz + tz] = any;
+        }
+    out.live.clear();
+    for (int tx = 0; tx < c->ntx; ++tx)
+        for (int j = 0; j < c->nty * c->ntz; ++j)
+            if (tcol[j]) out.live.push_back(tx * c->nty * c->ntz + j);
+}
+
 int upload(cgs_ctx* c, DevBuf& b, const void* h, size_t bytes)
 {
     CGS_CUDA(c, b.ensure(bytes));
@@ -322,6 +388,7 @@ void drop_graphs(cgs_ctx* c)
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
     c->graphs.clear();
     c->graph_launches.clear();
+    c->graph_slots.clear();
 }
 
 KbParams kb_params(const cgs_ctx* c)
@@ -376,9 +443,30 @@ int rebuild_bins(cgs_ctx* c)
                                     c->stream));
         CGS_CUDA(c, cudaStreamSynchronize(c->stream));
     }
+    const int tbx = fft_strided_cols(c->G[0]);
 #pragma omp parallel for schedule(dynamic, 1)
-    for (int b = 0; b < c->nbins; ++b)
+    for (int b = 0; b < c->nbins; ++b) {
         tile_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], prep[b]);
+        if (tbx > 0)
+            support_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], tbx, prep[b]);
+    }
+    c->sup_built = false;
+    c->h_sup_off.assign(c->nbins + 1, 0);
+    if (tbx > 0) {
+        std::vector<int2> tiles;
+        std::vector<int> live;
+        c->h_live_off.assign(c->nbins + 1, 0);
+        for (int b = 0; b < c->nbins; ++b) {
+            for (int b0 : prep[b].sup_cols) tiles.push_back(make_int2(b, b0));
+            c->h_sup_off[b + 1] = (long long)tiles.size();
+            live.insert(live.end(), prep[b].live.begin(), prep[b].live.end());
+            c->h_live_off[b + 1] = (long long)live.size();
+        }
+        CGS_TRY(upload(c, c->d_sup_tiles, tiles.data(), std::max<size_t>(tiles.size(), 1) * sizeof(int2)));
+        CGS_TRY(upload(c, c->d_live, live.data(), std::max<size_t>(live.size(), 1) * sizeof(int)));
+        CGS_TRY(upload(c, c->d_live_off, c->h_live_off.data(), c->h_live_off.size() * sizeof(long long)));
+        c->sup_built = true;
+    }
     std::vector<int> tile_ptr;
     std::vector<int> tile_idx;
     std::vector<int> plane_rng;
@@ -402,7 +490,7 @@ int rebuild_bins(cgs_ctx* c)
     }
     CGS_CUDA(c, c->d_yv.ensure(std::max<long long>(c->total, 1) * c->nch * sizeof(float2)));
     // workspace for a group of bins
-    const long long per_bin = (long long)c->nch * (c->Nl * c->G[2] + (long long)c->I[0] * c->G[1] * c->G[2] + c->Ng) *
+    const long long per_bin = (long long)c->nch * (c->Nl * c->G[2] + 2LL * c->I[0] * c->G[1] * c->G[2] + c->Ng) *
                               (long long)sizeof(float2);
     long long budget = c->p.workspace_bytes > 0 ? c->p.workspace_bytes : (64LL << 30);
     int wsb = (int)std::max<long long>(1, std::min<long long>(c->nbins, budget / std::max<long long>(per_bin, 1)));
@@ -410,6 +498,8 @@ int rebuild_bins(cgs_ctx* c)
     const long long wsn = (long long)c->ws_bins * c->nch;
     CGS_CUDA(c, c->d_zbuf.ensure(wsn * c->Nl * c->G[2] * sizeof(float2)));
     CGS_CUDA(c, c->d_ybuf.ensure(wsn * (long long)c->I[0] * c->G[1] * c->G[2] * sizeof(float2)));
+    CGS_CUDA(c, c->d_ybuf_adj.ensure(wsn * (long long)c->I[0] * c->G[1] * c->G[2] * sizeof(float2)));
+    c->adj_slot.assign(c->ws_bins, -1);
     CGS_CUDA(c, c->d_grid.ensure(wsn * c->Ng * sizeof(float2)));
     c->bins_dirty = false;
     return CGS_OK;
@@ -418,6 +508,38 @@ int rebuild_bins(cgs_ctx* c)
 // ---------------------------------------------------------------------------
 // chains
 // ---------------------------------------------------------------------------
+
+// The support lists describe the current tap records (not after
+// cgs_update_trajectory_d until the lists are rebuilt).
+bool support_pruned(const cgs_ctx* c) { return c->sup_prune && !c->tiles_stale && c->sup_built; }
+
+// Zero the adjoint y-buffer slots [0, nb) that held other bins' columns
+// before bins [b0, b0 + nb) are written there with pruning (the adjoint y
+// pass reads whole planes).  During graph capture the clears become graph
+// nodes; the host's slot record then describes the state after the graph.
+int prepare_adj_slots(cgs_ctx* c, int b0, int nb, bool pruned)
+{
+    const long long slot = (long long)c->nch * c->I[0] * c->G[1] * c->G[2];
+    for (int j = 0; j < nb; ++j) {
+        if (!pruned) {
+            c->adj_slot[j] = -1;   // every column written
+        } else if (c->adj_slot[j] != b0 + j) {
+            CGS_CUDA(c, cudaMemsetAsync(c->d_ybuf_adj.as<float2>() + j * slot, 0, (size_t)slot * sizeof(float2),
+                                        c->stream));
+            c->adj_slot[j] = b0 + j;
+        }
+    }
+    return CGS_OK;
+}
+
+// x pass over bins [b0, b0 + nb): only the listed tiles
+void set_support_tiles(const cgs_ctx* c, StridedPassArgs& a, int b0, int nb)
+{
+    a.sup_tiles = c->d_sup_tiles.as<int2>() + c->h_sup_off[b0];
+    a.sup_ntiles = c->h_sup_off[b0 + nb] - c->h_sup_off[b0];
+    a.sup_bin0 = b0;
+    a.sup_nsub = c->nch;
+}
 
 // Forward half for bins [b0, b0+nb) (nb <= ws_bins): image(s) -> grid -> samples (yv).
 // x: per bin [Ni] (x_bs) shared by the coils, or per coil (x_cs) without coil maps.
@@ -462,6 +584,8 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fy.out_off = 0;
     fy.err = c->d_err.as<int>();
     fy.tw = c->tw[1].as<float2>();
+    // every row is stored: the forward x pass reads only the listed tiles
+    const bool sup = support_pruned(c);
     CGS_LAUNCH(c, launch_strided(Gy, -1, fy, Ix, nb * c->nch, c->stream));
 
     StridedPassArgs fx{};
@@ -478,6 +602,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fx.out_off = 0;
     fx.err = c->d_err.as<int>();
     fx.tw = c->tw[0].as<float2>();
+    if (sup) set_support_tiles(c, fx, b0, nb);
     CGS_LAUNCH(c, launch_strided(Gx, -1, fx, 1, nb * c->nch, c->stream));
 
     InterpArgs ia{};
@@ -508,6 +633,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
     const int Ix = c->I[0], Iy = c->I[1], Iz = c->I[2];
     const int Gx = c->G[0], Gy = c->G[1], Gz = c->G[2];
     const long long zb = c->Nl * Gz, yb = (long long)Ix * Gy * Gz;
+    const bool sup = support_pruned(c);
     {
         SpreadArgs sa{};
         sa.grid = c->d_grid.as<float2>();
@@ -531,11 +657,18 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
         sa.nty = c->nty;
         sa.ntz = c->ntz;
         sa.thresh = c->thresh;
+        if (sup) {
+            sa.live = c->d_live.as<int>();
+            sa.live_off = c->d_live_off.as<long long>();
+            for (int b = b0; b < b0 + nb; ++b)
+                sa.live_max = (int)std::max<long long>(sa.live_max, c->h_live_off[b + 1] - c->h_live_off[b]);
+        }
         CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->kahan, c->spread_wpp, c->stream));
 
+        CGS_TRY(prepare_adj_slots(c, b0, nb, sup));
         StridedPassArgs ax{};
         ax.in = c->d_grid.as<float2>();
-        ax.out = c->d_ybuf.as<float2>();
+        ax.out = c->d_ybuf_adj.as<float2>();
         ax.in_bs = c->Ng;
         ax.out_bs = yb;
         ax.B = Gy * Gz;
@@ -545,11 +678,12 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
         ax.out_off = c->lo[0];
         ax.err = c->d_err.as<int>();
         ax.tw = c->tw[0].as<float2>();
+        if (sup) set_support_tiles(c, ax, b0, nb);
         CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
     }
 
     StridedPassArgs ay{};
-    ay.in = c->d_ybuf.as<float2>();
+    ay.in = c->d_ybuf_adj.as<float2>();
     ay.out = c->d_zbuf.as<float2>();
     ay.in_bs = yb;
     ay.out_bs = zb;
@@ -1108,11 +1242,13 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
     cudaGraphExec_t exec = nullptr;
     if (it == c->graphs.end()) {
         c->launches = 0;
+        const std::vector<int> entry = c->adj_slot;
         CGS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         int st = record_solve(c, reinterpret_cast<const float2*>(data), reinterpret_cast<float2*>(x), thresh, max_iter,
                               rhs_from_images, reinterpret_cast<float2*>(x_trace));
         cudaGraph_t graph = nullptr;
         cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
+        if (st != CGS_OK || ee != cudaSuccess) c->adj_slot = entry;   // nothing of the capture ran
         if (st != CGS_OK) {
             if (graph) cudaGraphDestroy(graph);
             return st;
@@ -1120,11 +1256,22 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
         CGS_CUDA(c, ee);
         cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) c->adj_slot = entry;
         CGS_CUDA(c, ei);
         c->graphs[key] = exec;
         c->graph_launches[key] = c->launches;
+        c->graph_slots[key] = {entry, c->adj_slot};
     } else {
         exec = it->second;
+        // the graph's clears assume the slot records it was captured with: a
+        // slot recorded differently now is cleared (zeros suit any record)
+        const auto& gs = c->graph_slots[key];
+        const long long slot = (long long)c->nch * c->I[0] * c->G[1] * c->G[2];
+        for (size_t j = 0; j < gs.first.size() && j < c->adj_slot.size(); ++j)
+            if (c->adj_slot[j] != gs.first[j])
+                CGS_CUDA(c, cudaMemsetAsync(c->d_ybuf_adj.as<float2>() + (long long)j * slot, 0,
+                                            (size_t)slot * sizeof(float2), c->stream));
+        c->adj_slot = gs.second;
     }
     c->launches = c->graph_launches[key];
     CGS_CUDA(c, cudaGraphLaunch(exec, c->stream));
@@ -1889,6 +2036,28 @@ int cgs_set_deterministic(cgs_ctx* c, int32_t on)
     if (c->deterministic && c->spread_wpp == 3) {
         c->spread_wpp = 1;
         drop_graphs(c);
+    }
+    return CGS_OK;
+}
+
+int cgs_set_support_pruning(cgs_ctx* c, int32_t on)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (c->sup_prune != (on != 0)) drop_graphs(c);
+    c->sup_prune = on != 0;
+    return CGS_OK;
+}
+
+int cgs_support_stats(cgs_ctx* c, int64_t* listed_cols, int64_t* live_tiles)
+{
+    CGS_TRY(check_ready(c, false));
+    const bool sup = support_pruned(c);
+    const long long ncol = (long long)c->G[1] * c->G[2];
+    const int tbx = fft_strided_cols(c->G[0]);
+    for (int b = 0; b < c->nbins; ++b) {
+        if (listed_cols)
+            listed_cols[b] = sup ? std::min(ncol, (c->h_sup_off[b + 1] - c->h_sup_off[b]) * (long long)tbx) : ncol;
+        if (live_tiles) live_tiles[b] = sup ? c->h_live_off[b + 1] - c->h_live_off[b] : c->ntiles;
     }
     return CGS_OK;
 }

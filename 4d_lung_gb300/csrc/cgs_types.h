@@ -41,6 +41,14 @@ struct StridedPassArgs {
     int Lin, in_off, Lout, out_off;
     const float2* tw;          // L twiddles
     int* err;                  // error flag of the pipelined pass (null: plain loads)
+    // Sample-support pruning (pipelined pass only; the plain pass ignores it
+    // and computes every tile, which is also correct): the pass visits only
+    // the listed tiles {bin, first column} (outer index 0), each for every
+    // sub-item (coil), sup_ntiles * sup_nsub tiles; batch item
+    // (bin - sup_bin0) * sup_nsub + sub.
+    const int2* sup_tiles;
+    long long sup_ntiles;
+    int sup_bin0, sup_nsub;
 };
 
 struct ContigPassArgs {
@@ -131,6 +139,11 @@ struct SpreadArgs {
     int G[3];
     int ntx, nty, ntz;         // tiles per axis
     float thresh;
+    // tiles to store (null: all): per bin the ascending tile indices
+    // live[live_off[bin] ..< live_off[bin + 1]]; live_max = the longest list
+    const int* live;
+    const long long* live_off;
+    int live_max;
 };
 
 // Loss gradient pass (grad.cu): one bin's samples [s0, s0 + n) in sorted order.

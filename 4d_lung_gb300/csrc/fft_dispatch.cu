@@ -82,6 +82,16 @@ bool fft_supported(int L)
     return false;
 }
 
+int fft_strided_cols(int L)
+{
+    switch (L) {
+#define CGS_CASE(L_, R1_, R2_, G_) case L_: return fft_strided_tile_cols(R1_, R2_);
+        CGS_FFT_SIZES(CGS_CASE)
+#undef CGS_CASE
+    }
+    return 0;
+}
+
 const int* fft_supported_list(int* n)
 {
     *n = (int)(sizeof(kSizes) / sizeof(kSizes[0]));

@@ -23,7 +23,7 @@ static int sm_count()
 }
 
 constexpr int rmax2(int a, int b) { return a > b ? a : b; }
-constexpr int strided_tb(int r1, int r2) { return rmax2(r1, r2) > 16 ? 8 : 16; }
+constexpr int strided_tb(int r1, int r2) { return fft_strided_tile_cols(r1, r2); }
 constexpr int contig_lpb(int r1, int r2) { return rmax2(r1, r2) > 16 ? 8 : (rmax2(r1, r2) > 8 ? 16 : 32); }
 
 template <int R1, int R2>
@@ -86,7 +86,8 @@ struct SizeImpl {
             &per_sm, k_fft_strided_tma<R1, R2, SIGN, TB, NSTAGE, MODE>, Pipe::NT, smem);
         if (e != cudaSuccess) return e;
         const long long tiles_per_item = (long long)A * a.ntb;
-        const long long ntiles = tiles_per_item * batch;
+        const long long ntiles = a.sup_tiles ? a.sup_ntiles * a.sup_nsub : tiles_per_item * batch;
+        if (ntiles <= 0) return cudaSuccess;   // no listed tile: nothing to transform
         long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
         if (nblk > ntiles) nblk = ntiles;
         k_fft_strided_tma<R1, R2, SIGN, TB, NSTAGE, MODE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(

@@ -179,18 +179,35 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
     __syncthreads();
     const long long my_n = ntiles > (long long)blockIdx.x ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
 
+    // tile t -> (batch item, outer index, first column)
+    auto decode = [&](long long t, long long& item, int& ai, int& b0) {
+        if (a.sup_tiles) {
+            const long long j = t / a.sup_nsub;
+            const int sub = (int)(t - j * a.sup_nsub);
+            const int2 e = a.sup_tiles[j];
+            item = (long long)(e.x - a.sup_bin0) * a.sup_nsub + sub;
+            ai = 0;
+            b0 = e.y;
+        } else {
+            item = t / tiles_per_item;
+            const int rem = (int)(t - item * tiles_per_item);
+            ai = rem / a.ntb;
+            b0 = (rem - ai * a.ntb) * TB;
+        }
+    };
+
     auto issue = [&](long long k) {   // thread 0 only
         const long long t = blockIdx.x + k * gridDim.x;
-        const int item = (int)(t / tiles_per_item);
-        const int rem = (int)(t - (long long)item * tiles_per_item);
-        const int ai = rem / a.ntb;
-        const int b0 = (rem - ai * a.ntb) * TB;
+        long long item;
+        int ai, b0;
+        decode(t, item, ai, b0);
         const int s = (int)(k % NSTAGE);
         mbar_arrive_expect_tx(&s_bar[s], (uint32_t)(stage_elems * sizeof(float2)));
         float2* dst = s_in + (size_t)s * stage_elems;
         for (int r0 = 0; r0 < a.Lin; r0 += box_rows)
-            tma_load_4d(dst + (size_t)r0 * TB, &tmap, b0, r0, ai, item, &s_bar[s]);
+            tma_load_4d(dst + (size_t)r0 * TB, &tmap, b0, r0, ai, (int)item, &s_bar[s]);
     };
+
 
     if (tid == 0)
         for (long long k = 0; k < NSTAGE - 1 && k < my_n; ++k) issue(k);
@@ -208,10 +225,9 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
             return;
         }
         const long long t = blockIdx.x + k * gridDim.x;
-        const long long item = t / tiles_per_item;
-        const int rem = (int)(t - item * tiles_per_item);
-        const int ai = rem / a.ntb;
-        const int b0 = (rem - ai * a.ntb) * TB;
+        long long item;
+        int ai, b0;
+        decode(t, item, ai, b0);
         const int bi = tid % TB;
         const int b = b0 + bi;
         const bool bok = b < a.B;

@@ -9,3 +9,6 @@
     X(256, 16, 16, 2) X(320, 16, 20, 3) X(352, 32, 11, 4) X(384, 16, 24, 5)           \
     X(448, 16, 28, 0) X(512, 16, 32, 1)
 #define CGS_FFT_NGROUPS 6
+
+// columns per tile of the strided passes of a line length L = R1 * R2
+constexpr int fft_strided_tile_cols(int r1, int r2) { return (r1 > r2 ? r1 : r2) > 16 ? 8 : 16; }

@@ -156,7 +156,12 @@ __global__ void __launch_bounds__(32 * TILE_X * WPP) k_spread(SpreadArgs a)
     static_assert(CCW * WPP <= SPREAD_VAL_STRIDE, "staged value row");
     extern __shared__ float4 s_dyn[];
     const int bin = a.bin0 + blockIdx.z;
-    const int tile = blockIdx.x;
+    int tile = blockIdx.x;
+    if (a.live) {   // only the listed tiles are stored; the rest of the grid is never read
+        const long long o = a.live_off[bin];
+        if ((long long)blockIdx.x >= a.live_off[bin + 1] - o) return;
+        tile = a.live[o + blockIdx.x];
+    }
     const int c0 = blockIdx.y * a.cc;
     const int ncc = min(a.cc, a.nch - c0);
     const int tz = tile % a.ntz;
@@ -192,7 +197,8 @@ __global__ void __launch_bounds__(32 * TILE_X * WPP) k_spread(SpreadArgs a)
     const int cb = part * per, nmy = min(per, ncc - cb);   // this warp's coils [cb, cb + nmy)
     const int gx = x0 + plane;
     const int jy = lane / 5, jz = lane - 5 * (lane / 5);
-    const int2 run = a.plane_rng[((long long)bin * gridDim.x + tile) * TILE_X + plane];
+    const long long ntiles = (long long)a.ntx * a.nty * a.ntz;
+    const int2 run = a.plane_rng[((long long)bin * ntiles + tile) * TILE_X + plane];
 
     for (int s = beg; s < end; s += SPREAD_BATCH) {
         const int nbat = min(SPREAD_BATCH, end - s);
@@ -302,7 +308,12 @@ __global__ void __launch_bounds__(SPREAD_ATOMIC_THREADS) k_spread_atomic(SpreadA
     static_assert(CC <= SPREAD_VAL_STRIDE, "staged value row");
     extern __shared__ float4 s_dyn[];
     const int bin = a.bin0 + blockIdx.z;
-    const int tile = blockIdx.x;
+    int tile = blockIdx.x;
+    if (a.live) {   // only the listed tiles are stored; the rest of the grid is never read
+        const long long o = a.live_off[bin];
+        if ((long long)blockIdx.x >= a.live_off[bin + 1] - o) return;
+        tile = a.live[o + blockIdx.x];
+    }
     const int c0 = blockIdx.y * a.cc;
     const int ncc = min(a.cc, a.nch - c0);
     const int tz = tile % a.ntz;

@@ -224,6 +224,12 @@ cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan
     // 4 / 5 = persistent and pipelined with 1 / 2 warps per x plane (fixed order)
     if (a.cc < 1 || a.cc > spread_max_coils(kahan) || wpp < 1 || wpp > 5 || (wpp >= 3 && kahan))
         return cudaErrorInvalidValue;
+    if (wpp >= 4 && a.live) {   // the persistent variants store every tile
+        SpreadArgs b = a;
+        b.live = nullptr;
+        b.live_off = nullptr;
+        return launch_spread(b, ntiles, nbins, kahan, wpp, s);
+    }
     if (wpp == 4) {
         if (a.cc <= 4) return spread_pipe_run<4, 1>(a, ntiles, nbins, s);
         if (a.cc <= 8) return spread_pipe_run<8, 1>(a, ntiles, nbins, s);
@@ -236,7 +242,9 @@ cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan
         return spread_pipe_run<6, 2>(a, ntiles, nbins, s);
     }
     const size_t smem = spread_smem_bytes(a.cc, kahan);
-    dim3 grid((unsigned)ntiles, (unsigned)((a.nch + a.cc - 1) / a.cc), (unsigned)nbins);
+    const int nx = a.live ? a.live_max : ntiles;
+    if (nx <= 0) return cudaSuccess;
+    dim3 grid((unsigned)nx, (unsigned)((a.nch + a.cc - 1) / a.cc), (unsigned)nbins);
     if (kahan) spread_launch<true>(a, grid, smem, wpp, s);
     else spread_launch<false>(a, grid, smem, wpp, s);
     return cudaGetLastError();

@@ -16,6 +16,8 @@ cudaError_t fft_init_all();
 // TB x box_rows box; false when the buffer or strides are not 16-byte aligned
 bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int batch, int TB, int* box_rows);
 const int* fft_supported_list(int* n);
+// columns per tile of the strided passes of line length L (0: unsupported)
+int fft_strided_cols(int L);
 
 // One launch per pass; `batch` items along blockIdx.y.
 cudaError_t launch_strided(int L, int sign, const StridedPassArgs& a, int A, int batch, cudaStream_t s);

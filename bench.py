@@ -188,33 +188,41 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
     return w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s
 
 
-def stage_bytes(w, sizes):
+def stage_bytes(w, sizes, support=None):
     """Algorithmic bytes of each stage of one E^H D E application over all
-    bins: every stage reads its input and writes its output once."""
+    bins: every stage reads its input and writes its output once.
+    support = (listed columns, stored spreading tiles) per bin, from
+    Reco.support_stats(): with sample-support pruning the x passes move only
+    the listed (y, z) columns, the interpolation reads within them and the
+    spreading stores only the listed tiles.  None: the full grid."""
     Ix, Iy, Iz = w.img
     Gx, Gy, Gz = w.grid
     Ni, Ng, Nl = Ix * Iy * Iz, Gx * Gy * Gz, Ix * Iy
     C8 = 8 * w.n_ch
     nb = len(sizes)
     M = int(sum(sizes))
+    if support is None:
+        cols = [Gy * Gz] * nb
+        tiles = [Ng // 512] * nb
+    else:
+        cols, tiles = [int(v) for v in support[0]], [int(v) for v in support[1]]
+    scol, stile = sum(cols), sum(tiles)
     return {
         "fwd_z": nb * (8 * Ni + C8 * Ni + C8 * Nl * Gz),
         "fwd_y": nb * C8 * (Nl * Gz + Ix * Gy * Gz),
-        "fwd_x": nb * C8 * (Ix * Gy * Gz + Ng),
-        "interp": nb * C8 * Ng + M * (64 + 4 + C8),
-        "spread": nb * C8 * Ng + M * (64 + C8),
-        "adj_x": nb * C8 * (Ng + Ix * Gy * Gz),
+        "fwd_x": C8 * scol * (Ix + Gx),
+        "interp": C8 * scol * Gx + M * (64 + 4 + C8),
+        "spread": C8 * stile * 512 + M * (64 + C8),   # 4 x 8 x 16 points per tile
+        "adj_x": C8 * scol * (Gx + Ix),
         "adj_y": nb * C8 * (Ix * Gy * Gz + Nl * Gz),
         "adj_z": nb * (C8 * Nl * Gz + C8 * Ni + 8 * Ni),
     }
 
 
-def apply_bytes(w, sizes):
-    """B_apply = Nc (48 Ni + 56 Ng + 44 M) + 56 Ni per bin (the operator's
-    algorithmic traffic: coil/apod/pad, FFT, interpolation + D, spreading,
-    adjoint FFT, crop/apod/conj-coil accumulate, CG update)."""
-    Ni, Ng = int(np.prod(w.img)), int(np.prod(w.grid))
-    return sum(w.n_ch * (48 * Ni + 56 * Ng + 44 * int(m)) + 56 * Ni for m in sizes)
+def apply_bytes(w, sizes, support=None):
+    """Algorithmic bytes of one application: the stages plus the CG vector
+    update (x, r, p, q and their reductions, 56 bytes per voxel and bin)."""
+    return sum(stage_bytes(w, sizes, support).values()) + 56 * int(np.prod(w.img)) * len(sizes)
 
 
 # ---------------------------------------------------------------------------
@@ -666,7 +674,8 @@ def run_ours(args):
     st = np.median(np.stack(reps), axis=0)
     groups = len(st) // 8
     stage_ms = {s: float(sum(st[g * 8 + i] for g in range(groups))) for i, s in enumerate(STAGES)}
-    sb = stage_bytes(w, sizes)
+    support = reco.support_stats()
+    sb = stage_bytes(w, sizes, support)
     apply_ms = float(sum(stage_ms.values()))
     # kernel families: the four x/y passes are one kernel template
     fam = {k: [s for s in STAGES if FAMILY[s] == k] for k in dict.fromkeys(FAMILY.values())}
@@ -675,7 +684,8 @@ def run_ours(args):
     dom_bytes = sum(sb[s] for s in fam[dom])
     peak, peak_kind = measured_peaks()
     achieved = dom_bytes / (fam_ms[dom] / 1e3) / 1e9
-    tr = traffic_record().get(args.workload, {}).get(dom)
+    tkey = args.workload + ("_%dbin" % args.max_bins if args.max_bins > 0 else "")
+    tr = traffic_record().get(tkey, {}).get(dom)
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
@@ -688,7 +698,10 @@ def run_ours(args):
         "stage_ms": stage_ms,
         "stage_frac_of_peak": {s: sb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
         "apply_ms": apply_ms,
-        "apply_achieved_gbs": apply_bytes(w, sizes) / (apply_ms / 1e3) / 1e9,
+        "apply_achieved_gbs": apply_bytes(w, sizes, support) / (apply_ms / 1e3) / 1e9,
+        "apply_bytes": apply_bytes(w, sizes, support),
+        "support": {"listed_column_fraction": float(sum(support[0])) / (nb * w.grid[1] * w.grid[2]),
+                    "stored_tile_fraction": float(sum(support[1])) / (nb * int(np.prod(w.grid)) // 512)},
     }
 
     line = {

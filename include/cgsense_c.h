@@ -316,6 +316,21 @@ int cgs_set_deterministic(cgs_ctx* ctx, int32_t on);
  * bitwise-identical results. */
 int cgs_set_launch_shape(cgs_ctx* ctx, int32_t spread_cc, int32_t spread_variant, int32_t interp_cc);
 
+/* Sample-support pruning of the oversampled FFT (default on): the x passes
+ * transform only the tiles of grid columns that some sample's kernel support
+ * reaches, the forward y pass stores only those columns and the adjoint y
+ * pass reads the others as zero.  Results are unchanged (a column no sample
+ * reaches is never read by the interpolation, and is all zero after the
+ * spreading); off, every column is transformed (the reference's full FFT,
+ * Fourier.cpp:19-42). */
+int cgs_set_support_pruning(cgs_ctx* ctx, int32_t on);
+
+/* Per bin (arrays of cgs_num_bins entries, either may be NULL): the (y, z)
+ * grid columns the x passes transform (whole column tiles of the pass) and
+ * the spreading tiles stored, as the current pruning setting uses them
+ * (without pruning: every column, every tile). */
+int cgs_support_stats(cgs_ctx* ctx, int64_t* listed_cols, int64_t* live_tiles);
+
 /* Autotuner: times one batched E^H D E application of every bin for each
  * candidate launch shape -- coils per spreading block (all that fit, then
  * 1/2, 1/3, 1/4 of them) with one or two warps per x plane of a tile, then

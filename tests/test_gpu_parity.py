@@ -235,6 +235,51 @@ def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, g
             assert np.array_equal(res1, res0), (cc, variant)
 
 
+@pytest.mark.parametrize("img,grid,nch", [((32, 24, 20), (64, 48, 40), 5),
+                                          # x passes with 8-column tiles (L = 320), Gz % 16 != 0
+                                          ((160, 16, 12), (320, 32, 24), 3),
+                                          ((48, 40, 24), (96, 80, 48), 4)])
+def test_support_pruning_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid, nch):
+    """Sample-support pruning (x passes over the supported column tiles only,
+    masked y passes, spreading tiles of supported columns only) leaves every
+    result unchanged: the forward and adjoint NUFFT and the batched solve of
+    sparse bins are bitwise equal with and without it."""
+    k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 48)
+    bins = synth.bin_samples([np.arange(0, 3), np.arange(3, 11), np.arange(11, 60)], 48)
+    smaps = synth.coil_maps(img, nch)
+    rng = np.random.default_rng(21)
+    data = (rng.standard_normal((nch, k.shape[0])) + 1j * rng.standard_normal((nch, k.shape[0]))).astype(np.complex64)
+    x = (rng.standard_normal((nch,) + img) + 1j * rng.standard_normal((nch,) + img)).astype(np.complex64)
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b)
+    r.set_trajectory(k)
+    r.set_smaps(smaps)
+    f0, a0 = r.nufft_fwd(x), r.nufft_adj(data)
+    r.set_support_pruning(False)
+    f1, a1 = r.nufft_fwd(x), r.nufft_adj(data)
+    assert np.array_equal(f0, f1) and np.array_equal(a0, a1)
+    r.set_bins(bins)
+    out = {}
+    for on in (True, False):
+        r.set_support_pruning(on)
+        for variant in (1, 2, 4):
+            r.set_launch_shape(0, variant, 2)
+            out[on, variant] = r.cg_sense_batched(data, 0.0, 4)[:2]
+    ref = out[False, 1]
+    for key, (xv, res) in out.items():
+        assert np.array_equal(xv, ref[0]), key
+        assert np.array_equal(res, ref[1]), key
+    # per-bin applications reuse workspace slot 0 for other bins between
+    # replays of the batched solve's graph
+    img1 = x[0]
+    q_off = [r.apply_ehde(img1, bin=b) for b in range(3)]
+    r.set_support_pruning(True)
+    r.set_launch_shape(0, 1, 2)
+    for b in (2, 0, 1, 2):
+        assert np.array_equal(r.apply_ehde(img1, bin=b), q_off[b]), b
+        xv, res = r.cg_sense_batched(data, 0.0, 4)[:2]
+        assert np.array_equal(xv, ref[0]) and np.array_equal(res, ref[1]), b
+
+
 def test_atomic_spreading_matches_fixed_order(gpu_lib, cgs, oracle_mod, o64, synth):
     """With determinism off the autotuner may pick shared-memory atomic
     spreading; forced here, the batched solve equals the fixed-order one to
