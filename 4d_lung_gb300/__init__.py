@@ -531,7 +531,8 @@ class Reco:
 
     def autotune(self):
         """Picks the fastest launch shapes for this context; returns
-        {"spread_coils_per_block", "spread_warps_per_plane",
+        {"spread_coils_per_block", "spread_variant" (see cgs_set_launch_shape;
+         also under its older name "spread_warps_per_plane"),
          "interp_coils_per_thread", "candidates_ms"}."""
         t = np.zeros(32, np.float32)
         n = np.zeros(1, np.int32)
@@ -539,7 +540,8 @@ class Reco:
         sw = np.zeros(1, np.int32)
         ic = np.zeros(1, np.int32)
         self._check(self._L.cgs_autotune(self._ctx, _p(t), 32, _p(n), _p(sc), _p(sw), _p(ic)))
-        return {"spread_coils_per_block": int(sc[0]), "spread_warps_per_plane": int(sw[0]),
+        return {"spread_coils_per_block": int(sc[0]), "spread_variant": int(sw[0]),
+                "spread_warps_per_plane": int(sw[0]),
                 "interp_coils_per_thread": int(ic[0]), "candidates_ms": [float(v) for v in t[: n[0]]]}
 
     def set_launch_shape(self, spread_cc=0, spread_variant=1, interp_cc=4):

@@ -105,7 +105,8 @@ struct cgs_ctx {
     // launch shapes (cgs_autotune): coils per spreading block (0: as many as
     // fit), coils per interpolation thread
     int spread_cc = 0;
-    int spread_wpp = 1;          // spreading variant: warps per x plane 1 / 2, 3 atomics, 4 / 5 pipelined
+    int spread_wpp = 6;          // spreading variant: warps per x plane 1 / 2, 3 atomics, 4 / 5 pipelined,
+                                 // 6 gather over the transposed tap matrix (2 when it is not built)
     bool deterministic = true;   // fixed summation order everywhere (cgs_set_deterministic)
     int interp_cc = 4;
     bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
@@ -117,6 +118,12 @@ struct cgs_ctx {
     bool sup_prune = true;
     bool sup_built = false;
     std::vector<long long> h_sup_off;        // per bin: first entry in d_sup_tiles
+    std::vector<int2> h_sup_tiles;           // listed tiles {bin, first column}, all bins
+    // transposed tap matrix of the listed tiles' points (spreading variant 6)
+    bool csr_valid = false;
+    long long csr_pts = 0;
+    unsigned long long csr_entries = 0;
+    DevBuf d_col_tile, d_csr_cnt, d_csr_ptr, d_csr_ent, d_csr_tmp;
     std::vector<long long> h_live_off;       // per bin: first entry in d_live (spreading tiles)
     DevBuf d_sup_tiles, d_live, d_live_off;
     // The adjoint x pass writes its own y buffer (d_ybuf_adj), and with
@@ -383,6 +390,60 @@ int upload(cgs_ctx* c, DevBuf& b, const void* h, size_t bytes)
     return CGS_OK;
 }
 
+// The transposed tap matrix over the points of the listed x-pass tiles
+// (spreading variant 6), from the current tap records and support lists.
+// Skipped (variant 6 then falls back to the tiled kernel) when the counts
+// could overflow 32-bit offsets.
+int build_csr(cgs_ctx* c)
+{
+    c->csr_valid = false;
+    c->csr_entries = 0;
+    if (!c->sup_built || c->total == 0) return CGS_OK;
+    const int tbx = fft_strided_cols(c->G[0]);
+    const long long ncol = (long long)c->G[1] * c->G[2];
+    const long long ntl = c->h_sup_off[c->nbins];
+    const long long npts = ntl * c->G[0] * tbx;
+    if (npts <= 0 || (unsigned long long)c->total * 125ull >= 0xffffffffull || npts + 1 >= 0x7fffffffLL) return CGS_OK;
+    std::vector<int> ct((size_t)c->nbins * ncol, -1);
+    for (int b = 0; b < c->nbins; ++b)
+        for (long long J = c->h_sup_off[b]; J < c->h_sup_off[b + 1]; ++J)
+            for (int k = 0; k < tbx && c->h_sup_tiles[J].y + k < ncol; ++k)
+                ct[(size_t)b * ncol + c->h_sup_tiles[J].y + k] = (int)J;
+    CGS_TRY(upload(c, c->d_col_tile, ct.data(), ct.size() * sizeof(int)));
+    const size_t tmp = csr_scan_tmp_elems(npts + 1);
+    CGS_CUDA(c, c->d_csr_cnt.ensure((size_t)(npts + 1) * sizeof(unsigned)));
+    CGS_CUDA(c, c->d_csr_ptr.ensure((size_t)(npts + 1) * sizeof(unsigned)));
+    CGS_CUDA(c, c->d_csr_tmp.ensure(tmp * sizeof(unsigned)));
+    CGS_CUDA(c, c->d_flag.ensure(sizeof(int)));
+    CGS_CUDA(c, cudaMemsetAsync(c->d_flag.p, 0, sizeof(int), c->stream));
+    CsrBuildArgs a{};
+    a.rec = c->d_rec.as<TapRecord>();
+    a.total = c->total;
+    a.bin_off = c->d_bin_off.as<long long>();
+    a.nbins = c->nbins;
+    a.col_tile = c->d_col_tile.as<int>();
+    for (int i = 0; i < 3; ++i) a.G[i] = c->G[i];
+    a.tb = tbx;
+    a.thresh = c->thresh;
+    a.cnt = c->d_csr_cnt.as<unsigned>();
+    a.ptr = c->d_csr_ptr.as<unsigned>();
+    a.err = c->d_flag.as<int>();
+    unsigned long long ne = 0;
+    CGS_CUDA(c, csr_count_and_scan(a, npts, c->d_csr_ptr.as<unsigned>(), c->d_csr_tmp.as<unsigned>(), tmp, &ne,
+                                   c->stream));
+    CGS_CUDA(c, c->d_csr_ent.ensure(std::max<unsigned long long>(ne, 1) * sizeof(int2)));
+    a.ent = c->d_csr_ent.as<int2>();
+    CGS_CUDA(c, csr_fill_and_order(a, npts, c->stream));
+    int bad = 0;
+    CGS_CUDA(c, cudaMemcpyAsync(&bad, c->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (bad) return CGS_OK;   // a tap outside the lists: keep the tiled kernel
+    c->csr_pts = npts;
+    c->csr_entries = ne;
+    c->csr_valid = true;
+    return CGS_OK;
+}
+
 void drop_graphs(cgs_ctx* c)
 {
     for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second);
@@ -463,10 +524,12 @@ int rebuild_bins(cgs_ctx* c)
             c->h_live_off[b + 1] = (long long)live.size();
         }
         CGS_TRY(upload(c, c->d_sup_tiles, tiles.data(), std::max<size_t>(tiles.size(), 1) * sizeof(int2)));
+        c->h_sup_tiles = tiles;
         CGS_TRY(upload(c, c->d_live, live.data(), std::max<size_t>(live.size(), 1) * sizeof(int)));
         CGS_TRY(upload(c, c->d_live_off, c->h_live_off.data(), c->h_live_off.size() * sizeof(long long)));
         c->sup_built = true;
     }
+    CGS_TRY(build_csr(c));
     std::vector<int> tile_ptr;
     std::vector<int> tile_idx;
     std::vector<int> plane_rng;
@@ -663,7 +726,32 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
             for (int b = b0; b < b0 + nb; ++b)
                 sa.live_max = (int)std::max<long long>(sa.live_max, c->h_live_off[b + 1] - c->h_live_off[b]);
         }
-        CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->kahan, c->spread_wpp, c->stream));
+        if (sup && c->spread_wpp == 6 && c->csr_valid) {
+            // gather over the transposed tap matrix: stores the listed tiles' points
+            CsrSpreadArgs ca{};
+            ca.grid = c->d_grid.as<float2>();
+            ca.coil_stride = c->Ng;
+            ca.grid_bs = (long long)c->nch * c->Ng;
+            ca.ptr = c->d_csr_ptr.as<unsigned>();
+            ca.ent = c->d_csr_ent.as<int2>();
+            ca.yv = c->d_yv.as<float2>();
+            ca.tiles = c->d_sup_tiles.as<int2>();
+            ca.j0 = c->h_sup_off[b0];
+            ca.nj = c->h_sup_off[b0 + nb] - c->h_sup_off[b0];
+            ca.bin0 = b0;
+            ca.nch = c->nch;
+            ca.Gx = Gx;
+            ca.B = (long long)Gy * Gz;
+            ca.tb = fft_strided_cols(Gx);
+            ca.cc = c->spread_cc;   // coils per thread of the gather (0: by the coil count)
+            if (ca.cc != 2 && ca.cc != 4 && ca.cc != 6 && ca.cc != 8) ca.cc = 0;
+            CGS_LAUNCH(c, launch_spread_csr(ca, c->kahan, c->stream));
+        } else {
+            // variant 6 without its matrix: the two-warps-per-plane tiled kernel
+            const int wpp = c->spread_wpp == 6 ? 2 : c->spread_wpp;
+            if (wpp == 2 && sa.cc < 2) sa.cc = std::min(2, c->nch);
+            CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->kahan, wpp, c->stream));
+        }
 
         CGS_TRY(prepare_adj_slots(c, b0, nb, sup));
         StridedPassArgs ax{};
@@ -1678,7 +1766,7 @@ int cgs_set_precision(cgs_ctx* c, int32_t mode)
     const bool k = mode == CGS_PREC_COMPENSATED;
     if (k != c->kahan) {
         c->kahan = k;
-        if (k && c->spread_wpp >= 3) c->spread_wpp = 1;
+        if (k && c->spread_wpp >= 3 && c->spread_wpp <= 5) c->spread_wpp = 1;
         drop_graphs(c);
     }
     return CGS_OK;
@@ -1729,10 +1817,13 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
     }
     float best = 1e30f;
     int best_sc = sc[0], best_wpp = 1;
-    for (int wpp : {1, 2, 4, 5, 3}) {
+    for (int wpp : {1, 2, 4, 5, 3, 6}) {
         if (wpp == 3 && (c->deterministic || c->kahan)) continue;
-        if (wpp >= 4 && c->kahan) continue;
-        for (int v : sc) {
+        if ((wpp == 4 || wpp == 5) && c->kahan) continue;
+        if (wpp == 6 && !(c->csr_valid && support_pruned(c))) continue;
+        // the gather's shape parameter is its coils per thread
+        const std::vector<int> cand = wpp == 6 ? std::vector<int>{4, 6, 8} : sc;
+        for (int v : cand) {
             if (wpp == 2 && v < 2) continue;
             c->spread_cc = v;
             c->spread_wpp = wpp;
@@ -2066,7 +2157,7 @@ int cgs_set_launch_shape(cgs_ctx* c, int32_t spread_cc, int32_t spread_variant, 
 {
     if (!c) return CGS_ERR_ARG;
     if (spread_cc < 0 || spread_cc > spread_max_coils(c->kahan)) return fail(c, CGS_ERR_ARG, "spread_cc out of range");
-    if (spread_variant < 1 || spread_variant > 5 || (spread_variant >= 3 && c->kahan) ||
+    if (spread_variant < 1 || spread_variant > 6 || (spread_variant >= 3 && spread_variant <= 5 && c->kahan) ||
         (spread_variant == 3 && c->deterministic))
         return fail(c, CGS_ERR_ARG, "spreading variant not allowed here");
     if (interp_cc != 2 && interp_cc != 4 && interp_cc != 6 && interp_cc != 8)

@@ -44,7 +44,8 @@ struct StridedPassArgs {
     // Sample-support pruning (pipelined pass only; the plain pass ignores it
     // and computes every tile, which is also correct): the pass visits only
     // the listed tiles {bin, first column} (outer index 0), each for every
-    // sub-item (coil), sup_ntiles * sup_nsub tiles; batch item
+    // sub-item (coil), sup_ntiles * sup_nsub tiles (tile t: sub-item
+    // t / sup_ntiles, list entry t % sup_ntiles); batch item
     // (bin - sup_bin0) * sup_nsub + sub.
     const int2* sup_tiles;
     long long sup_ntiles;
@@ -144,6 +145,44 @@ struct SpreadArgs {
     const int* live;
     const long long* live_off;
     int live_max;
+};
+
+// Spreading as a gather over the transposed tap matrix (spread_csr.cu).
+// Grid points of the listed x-pass column tiles are numbered
+//   p = (J * Gx + x) * tb + k,
+// J the global index of a listed tile {bin, first column b0} (all bins'
+// lists concatenated), x the grid row, k < tb the column within the tile
+// (flattened (y, z) column b0 + k).  Row p of the matrix lists the
+// (sorted sample, weight) pairs of the taps landing on point p.
+struct CsrBuildArgs {
+    const TapRecord* rec;      // sorted tap records (all bins)
+    long long total;           // sorted samples
+    const long long* bin_off;  // [nbins + 1]
+    int nbins;
+    const int* col_tile;       // [nbins][Gy * Gz]: listed tile J of a column, -1 if unlisted
+    int G[3];
+    int tb;                    // columns per listed tile
+    float thresh;
+    unsigned* cnt;             // [P] tap counts, then fill cursors
+    const unsigned* ptr;       // [P + 1] row offsets (fill pass)
+    int2* ent;                 // {sorted sample, weight bits} (fill pass)
+    int* err;                  // set when a tap lands outside the listed columns
+};
+
+struct CsrSpreadArgs {
+    float2* grid;              // coil c of bin slot s at grid + s * grid_bs + c * coil_stride
+    long long coil_stride, grid_bs;
+    const unsigned* ptr;       // [P + 1]
+    const int2* ent;
+    const float2* yv;          // [total samples][nch]
+    const int2* tiles;         // listed tiles {bin, first column}, global index
+    long long j0, nj;          // the tiles of this launch: [j0, j0 + nj)
+    int bin0;                  // bin of workspace slot 0
+    int nch;
+    int Gx;
+    long long B;               // Gy * Gz
+    int tb;
+    int cc;                    // coils per thread (2, 4, 6, 8; 0: by the coil count)
 };
 
 // Loss gradient pass (grad.cu): one bin's samples [s0, s0 + n) in sorted order.

@@ -181,9 +181,9 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
 
     // tile t -> (batch item, outer index, first column)
     auto decode = [&](long long t, long long& item, int& ai, int& b0) {
-        if (a.sup_tiles) {
-            const long long j = t / a.sup_nsub;
-            const int sub = (int)(t - j * a.sup_nsub);
+        if (a.sup_tiles) {   // sub-item outer: blocks in flight share a coil plane
+            const int sub = (int)(t / a.sup_ntiles);
+            const long long j = t - (long long)sub * a.sup_ntiles;
             const int2 e = a.sup_tiles[j];
             item = (long long)(e.x - a.sup_bin0) * a.sup_nsub + sub;
             ai = 0;

@@ -91,6 +91,11 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
     for (int c = 0; c < CC; ++c) acc[c] = make_float2(0.f, 0.f);
     const int Gy = a.G[1], Gz = a.G[2];
     const int ncc = min(CC, a.nch - c0);
+    // Rows of 5 z taps away from the z edges are read as three aligned
+    // 16-byte loads (6 points from the even index at or below the row's
+    // first); grids and coil planes start on 16-byte boundaries (Ng even).
+    const bool vec = nz >= 3 && nz + 3 <= Gz - 1 && (a.coil_stride & 1) == 0 &&
+                     (reinterpret_cast<uintptr_t>(a.grid) & 15) == 0 && (a.grid_bs & 1) == 0;
 #pragma unroll
     for (int jx = 0; jx < 5; ++jx) {
         const float wx = w[jx];
@@ -101,6 +106,29 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
             const float wxy = wx * w[5 + jy];
             if (wxy == 0.f) continue;
             const long long row = ((long long)gx * Gy + (ny - 2 + jy)) * Gz + (nz - 2);
+            if (vec) {
+                const int odd = (int)(row & 1);
+                const float4* r4 = reinterpret_cast<const float4*>(grid + (row - odd));
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+                    if (c < ncc) {
+                        const float4* p = r4 + (long long)c * (a.coil_stride / 2);
+                        const float4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2);
+                        const float2 e[6] = {make_float2(q0.x, q0.y), make_float2(q0.z, q0.w), make_float2(q1.x, q1.y),
+                                             make_float2(q1.z, q1.w), make_float2(q2.x, q2.y), make_float2(q2.z, q2.w)};
+#pragma unroll
+                        for (int jz = 0; jz < 5; ++jz) {
+                            const float wz = w[10 + jz];
+                            const float wt = wxy * wz;
+                            if (wz != 0.f && wt > a.thresh) {
+                                const float2 g = odd ? e[jz + 1] : e[jz];
+                                acc[c].x = fmaf(g.x, wt, acc[c].x);
+                                acc[c].y = fmaf(g.y, wt, acc[c].y);
+                            }
+                        }
+                    }
+                continue;
+            }
 #pragma unroll
             for (int jz = 0; jz < 5; ++jz) {
                 const float wz = w[10 + jz];

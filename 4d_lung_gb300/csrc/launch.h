@@ -40,6 +40,15 @@ size_t spread_smem_bytes(int cc, bool kahan);
 cudaError_t kernels_init();
 int spread_max_coils(bool kahan);
 
+// Transposed tap matrix (spread_csr.cu).  csr_build runs the count pass,
+// the scan, the fill pass and the per-row ordering; ent must hold
+// *entries pairs (csr_count_and_scan returns that number).
+cudaError_t csr_count_and_scan(const CsrBuildArgs& a, long long npts, unsigned* ptr, unsigned* scan_tmp,
+                               size_t scan_tmp_elems, unsigned long long* entries, cudaStream_t s);
+cudaError_t csr_fill_and_order(const CsrBuildArgs& a, long long npts, cudaStream_t s);
+size_t csr_scan_tmp_elems(long long n);
+cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, cudaStream_t s);
+
 // samples: reference order [nch][ns] <-> sorted, coil-interleaved [total][nch]
 cudaError_t launch_gather_samples(const float2* data, long long ns, const int* sorted, long long total, int nch,
                                   const float* dcf_sorted, float2* yv, cudaStream_t s);

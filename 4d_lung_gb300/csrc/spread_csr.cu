@@ -1,0 +1,344 @@
+// spread_csr.cu -- spreading (Reco.cpp:492-504) as a gather over the
+// transposed tap matrix.
+//
+// The tap set of a trajectory is fixed, so its transpose is built once per
+// set of tap records: for every grid point of the listed x-pass column tiles
+// (the only points the adjoint x pass reads), the (sample, weight) pairs of
+// the taps that land on it.  Rows are ordered by (nearest x, sorted sample
+// position) -- the order in which the tiled spreading kernels add the
+// samples to a grid point -- so the gather sums every point in the same
+// order with the same fused multiply-adds and gives bitwise the same grid.
+// One thread owns a grid point and a chunk of coils, sums in registers and
+// stores once: no shared-memory read-modify-write chains, no barriers, and
+// every point of the listed tiles is stored (zeros where no tap lands).
+#include "launch.h"
+#include "gridding_common.cuh"
+
+namespace cgs {
+
+// Taps of sorted sample i: the same products and tests as the tiled
+// spreading (weight (wx wy) wz, every factor non-zero, above the threshold).
+template <bool FILL>
+__global__ void __launch_bounds__(128) k_csr_taps(CsrBuildArgs a)
+{
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.total) return;
+    int lo = 0, hi = a.nbins;   // bin: bin_off[bin] <= i < bin_off[bin + 1]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) / 2;
+        if (a.bin_off[mid] <= i) lo = mid;
+        else hi = mid;
+    }
+    const int bin = lo;
+    float w[15];
+    int nx, ny, nz;
+    load_record(a.rec, i, w, nx, ny, nz);
+    const int Gx = a.G[0], Gz = a.G[2];
+    const long long ncol = (long long)a.G[1] * Gz;
+    const int* ct = a.col_tile + (long long)bin * ncol;
+#pragma unroll
+    for (int jx = 0; jx < 5; ++jx) {
+        const float wx = w[jx];
+        if (wx == 0.f) continue;
+        const int x = nx - 2 + jx;
+#pragma unroll
+        for (int jy = 0; jy < 5; ++jy) {
+            const float wy = w[5 + jy];
+            if (wy == 0.f) continue;
+            const int y = ny - 2 + jy;
+#pragma unroll
+            for (int jz = 0; jz < 5; ++jz) {
+                const float wz = w[10 + jz];
+                const float wt = (wx * wy) * wz;
+                if (wz == 0.f || !(wt > a.thresh)) continue;
+                const long long f = (long long)y * Gz + (nz - 2 + jz);
+                const int J = ct[f];
+                if (J < 0 || x < 0 || x >= Gx) {   // cannot happen: the lists hold every support column
+                    atomicExch(a.err, 1);
+                    continue;
+                }
+                const long long p = ((long long)J * Gx + x) * a.tb + (int)(f % a.tb);
+                if (FILL) {
+                    const unsigned slot = atomicAdd(a.cnt + p, 1u);
+                    a.ent[a.ptr[p] + slot] = make_int2((int)i, __float_as_int(wt));
+                } else {
+                    atomicAdd(a.cnt + p, 1u);
+                }
+            }
+        }
+    }
+}
+
+// Order each row by (nearest x, sorted position): insertion sort (rows hold
+// a few to a few tens of taps).
+__global__ void k_csr_order(CsrBuildArgs a, long long npts)
+{
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npts) return;
+    const unsigned e0 = a.ptr[p], e1 = a.ptr[p + 1];
+    auto key = [&](int2 e) {
+        const unsigned nr = __float_as_uint(__ldg(&a.rec[e.x].q[3].w));
+        return ((unsigned long long)(nr & 2047u) << 32) | (unsigned)e.x;
+    };
+    for (unsigned q = e0 + 1; q < e1; ++q) {
+        const int2 v = a.ent[q];
+        const unsigned long long kv = key(v);
+        unsigned r = q;
+        while (r > e0 && key(a.ent[r - 1]) > kv) {
+            a.ent[r] = a.ent[r - 1];
+            --r;
+        }
+        a.ent[r] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan of unsigned counts (three-level block scan)
+// ---------------------------------------------------------------------------
+constexpr int SCAN_T = 512, SCAN_PER = 4, SCAN_CHUNK = SCAN_T * SCAN_PER;
+
+// out[j] = sum of in[0..j) within each chunk; sums[chunk] = chunk total
+__global__ void __launch_bounds__(SCAN_T) k_scan_chunk(const unsigned* __restrict__ in, long long n,
+                                                       unsigned* __restrict__ out, unsigned* __restrict__ sums)
+{
+    __shared__ unsigned s_w[SCAN_T / 32];
+    const long long base = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_PER;
+    unsigned v[SCAN_PER], t = 0;
+#pragma unroll
+    for (int q = 0; q < SCAN_PER; ++q) {
+        v[q] = base + q < n ? in[base + q] : 0u;
+        t += v[q];
+    }
+    // inclusive scan of the thread totals
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned inc = t;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned o = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += o;
+    }
+    if (lane == 31) s_w[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned ws = lane < SCAN_T / 32 ? s_w[lane] : 0u;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned o = __shfl_up_sync(0xffffffffu, ws, d);
+            if (lane >= d) ws += o;
+        }
+        if (lane < SCAN_T / 32) s_w[lane] = ws;
+    }
+    __syncthreads();
+    unsigned run = inc - t + (warp > 0 ? s_w[warp - 1] : 0u);
+#pragma unroll
+    for (int q = 0; q < SCAN_PER; ++q) {
+        if (base + q < n) out[base + q] = run;
+        run += v[q];
+    }
+    if (threadIdx.x == SCAN_T - 1) sums[blockIdx.x] = run;
+}
+
+__global__ void k_scan_add(unsigned* __restrict__ out, long long n, const unsigned* __restrict__ offs)
+{
+    const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) out[j] += offs[j / SCAN_CHUNK];
+}
+
+size_t csr_scan_tmp_elems(long long n)
+{
+    size_t e = 0;
+    for (long long m = (n + SCAN_CHUNK - 1) / SCAN_CHUNK; m > 1; m = (m + SCAN_CHUNK - 1) / SCAN_CHUNK) e += 2 * (size_t)m;
+    return e + 2;
+}
+
+// out[j] = sum in[0..j) for j < n; tmp holds the per-level chunk sums
+static cudaError_t scan_exclusive(const unsigned* in, long long n, unsigned* out, unsigned* tmp, cudaStream_t s)
+{
+    const long long nchunk = (n + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    unsigned* sums = tmp;
+    unsigned* sums_scan = tmp + nchunk;
+    k_scan_chunk<<<(unsigned)nchunk, SCAN_T, 0, s>>>(in, n, out, sums);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || nchunk == 1) return e;
+    e = scan_exclusive(sums, nchunk, sums_scan, tmp + 2 * nchunk, s);
+    if (e != cudaSuccess) return e;
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(out, n, sums_scan);
+    return cudaGetLastError();
+}
+
+cudaError_t csr_count_and_scan(const CsrBuildArgs& a, long long npts, unsigned* ptr, unsigned* scan_tmp,
+                               size_t scan_tmp_elems, unsigned long long* entries, cudaStream_t s)
+{
+    if (scan_tmp_elems < csr_scan_tmp_elems(npts + 1)) return cudaErrorInvalidValue;
+    cudaError_t e = cudaMemsetAsync(a.cnt, 0, (size_t)(npts + 1) * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    if (a.total > 0) {
+        k_csr_taps<false><<<(unsigned)((a.total + 127) / 128), 128, 0, s>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    // ptr[p] = taps before point p; ptr[npts] = all taps (cnt[npts] is 0)
+    if ((e = scan_exclusive(a.cnt, npts + 1, ptr, scan_tmp, s)) != cudaSuccess) return e;
+    unsigned tot = 0;
+    if ((e = cudaMemcpyAsync(&tot, ptr + npts, sizeof(unsigned), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    *entries = tot;
+    return cudaSuccess;
+}
+
+cudaError_t csr_fill_and_order(const CsrBuildArgs& a, long long npts, cudaStream_t s)
+{
+    cudaError_t e = cudaMemsetAsync(a.cnt, 0, (size_t)npts * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    if (a.total > 0) {
+        k_csr_taps<true><<<(unsigned)((a.total + 127) / 128), 128, 0, s>>>(a);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if (npts > 0) {
+        k_csr_order<<<(unsigned)((npts + 255) / 256), 256, 0, s>>>(a, npts);
+        e = cudaGetLastError();
+    }
+    return e;
+}
+
+// ---------------------------------------------------------------------------
+// the gather: block-persistent over the listed tiles.  Thread (column k,
+// coil chunk ch, row offset xo) owns points (x, k) for x = xo, xo + xs, ...
+// and coils [ch CC, ch CC + CC): the coil chunks of a point run on
+// neighbouring threads, the columns of a tile on consecutive threads
+// (coalesced stores, one 16 x 8-byte row segment per coil).  The row
+// offsets of the next point are loaded before the current point's taps,
+// and the taps two at a time (their sample values in flight together); the
+// sums keep the row order.
+// ---------------------------------------------------------------------------
+template <int CC, bool KAHAN>
+__global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(CsrSpreadArgs a)
+{
+    const int nchunk = (a.nch + CC - 1) / CC;
+    const int tid = threadIdx.x;
+    const int k = tid % a.tb;
+    const int ch = (tid / a.tb) % nchunk;
+    const int xo = tid / (a.tb * nchunk), xs = blockDim.x / (a.tb * nchunk);
+    const int c0 = ch * CC;
+    const int ncc = min(CC, a.nch - c0);
+    const bool pairs = (a.nch % 2) == 0 && (reinterpret_cast<uintptr_t>(a.yv) & 15) == 0 && ncc == CC;
+    auto load_v = [&](int i, float2 (&vv)[CC]) {
+        const float2* v = a.yv + (long long)i * a.nch + c0;
+        if (pairs) {
+#pragma unroll
+            for (int c = 0; c < CC; c += 2) {
+                const float4 f = __ldg(reinterpret_cast<const float4*>(v + c));
+                vv[c] = make_float2(f.x, f.y);
+                vv[c + 1] = make_float2(f.z, f.w);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < CC; ++c) vv[c] = c < ncc ? __ldg(v + c) : make_float2(0.f, 0.f);
+        }
+    };
+    float2 acc[CC], cmp[CC];
+    auto add = [&](const float2 (&vv)[CC], float w) {
+#pragma unroll
+        for (int c = 0; c < CC; ++c) {
+            if (KAHAN) {
+                // y = v w - e;  s = t + y;  e = (s - t) - y;  t = s
+                const float yx = fmaf(vv[c].x, w, -cmp[c].x), yy = fmaf(vv[c].y, w, -cmp[c].y);
+                const float sx = __fadd_rn(acc[c].x, yx), sy = __fadd_rn(acc[c].y, yy);
+                cmp[c].x = __fsub_rn(__fsub_rn(sx, acc[c].x), yx);
+                cmp[c].y = __fsub_rn(__fsub_rn(sy, acc[c].y), yy);
+                acc[c] = make_float2(sx, sy);
+            } else {
+                acc[c].x = fmaf(vv[c].x, w, acc[c].x);
+                acc[c].y = fmaf(vv[c].y, w, acc[c].y);
+            }
+        }
+    };
+    if (xo >= a.Gx || ch >= nchunk) return;
+    for (long long J = a.j0 + blockIdx.x; J < a.j0 + a.nj; J += gridDim.x) {
+        const int2 t = a.tiles[J];
+        float2* g = a.grid + (long long)(t.x - a.bin0) * a.grid_bs + (long long)c0 * a.coil_stride;
+        const bool col_ok = (long long)t.y + k < a.B;
+        const long long pbase = J * a.Gx * a.tb + k;
+        unsigned n0 = __ldg(a.ptr + pbase + (long long)xo * a.tb), n1 = __ldg(a.ptr + pbase + (long long)xo * a.tb + 1);
+        for (int x = xo; x < a.Gx; x += xs) {
+            const unsigned e0 = n0, e1 = n1;
+            if (x + xs < a.Gx) {   // the next point's row
+                const long long pn = pbase + (long long)(x + xs) * a.tb;
+                n0 = __ldg(a.ptr + pn);
+                n1 = __ldg(a.ptr + pn + 1);
+            }
+#pragma unroll
+            for (int c = 0; c < CC; ++c) acc[c] = cmp[c] = make_float2(0.f, 0.f);
+            unsigned q = e0;
+            for (; q + 1 < e1; q += 2) {
+                const int2 u = __ldg(a.ent + q), v = __ldg(a.ent + q + 1);
+                float2 vu[CC], vv[CC];
+                load_v(u.x, vu);
+                load_v(v.x, vv);
+                add(vu, __int_as_float(u.y));
+                add(vv, __int_as_float(v.y));
+            }
+            if (q < e1) {
+                const int2 u = __ldg(a.ent + q);
+                float2 vu[CC];
+                load_v(u.x, vu);
+                add(vu, __int_as_float(u.y));
+            }
+            if (col_ok) {
+                const long long go = (long long)x * a.B + t.y + k;
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+                    if (c < ncc) {
+                        float2 o = acc[c];
+                        if (KAHAN) o = make_float2(__fsub_rn(o.x, cmp[c].x), __fsub_rn(o.y, cmp[c].y));
+                        g[(long long)c * a.coil_stride + go] = o;
+                    }
+            }
+        }
+    }
+}
+
+static int sm_count_csr()
+{
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int CC, bool KAHAN>
+static cudaError_t spread_csr_run(const CsrSpreadArgs& a, cudaStream_t s)
+{
+    const int nchunk = (a.nch + CC - 1) / CC;
+    const int per = a.tb * nchunk;
+    if (per > 256) return cudaErrorInvalidValue;
+    const int nt = (256 / per) * per;
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spread_csr<CC, KAHAN>, nt, 0);
+    if (e != cudaSuccess) return e;
+    const long long nblk = std::min<long long>(a.nj, (long long)sm_count_csr() * std::max(per_sm, 1));
+    k_spread_csr<CC, KAHAN><<<(unsigned)nblk, nt, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+// coils per thread: a.cc (2, 4, 6, 8) or, with 0, 2 / 4 for up to 2 / 4
+// coils, else 6 (12 coils: two threads per point)
+cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, cudaStream_t s)
+{
+    if (a.nj <= 0) return cudaSuccess;
+    if (a.tb < 1 || a.tb > 32 || a.nch < 1) return cudaErrorInvalidValue;
+    int cc = a.cc;
+    if (cc == 0) cc = a.nch <= 2 ? 2 : a.nch <= 4 ? 4 : 6;
+    switch (cc) {
+    case 2: return kahan ? spread_csr_run<2, true>(a, s) : spread_csr_run<2, false>(a, s);
+    case 4: return kahan ? spread_csr_run<4, true>(a, s) : spread_csr_run<4, false>(a, s);
+    case 6: return kahan ? spread_csr_run<6, true>(a, s) : spread_csr_run<6, false>(a, s);
+    case 8: return kahan ? spread_csr_run<8, true>(a, s) : spread_csr_run<8, false>(a, s);
+    }
+    return cudaErrorInvalidValue;
+}
+
+}  // namespace cgs

@@ -311,8 +311,11 @@ int cgs_set_deterministic(cgs_ctx* ctx, int32_t on);
 /* Launch shape set by hand (what cgs_autotune picks): coils per spreading
  * block (0: as many as fit), spreading variant (1 / 2: one / two warps per x
  * plane of a tile; 3: shared-memory atomics, only with determinism off;
- * 4 / 5: persistent and software-pipelined with one / two warps per plane),
- * coils per interpolation thread (2, 4, 6, 8).  Variants 1, 2, 4, 5 give
+ * 4 / 5: persistent and software-pipelined with one / two warps per plane;
+ * 6 (default): a gather over the transposed tap matrix, built with the bins
+ * when sample-support pruning is on -- without it variant 2 runs; its
+ * spread_cc is the coils per thread, 2, 4, 6 or 8, 0 by the coil count),
+ * coils per interpolation thread (2, 4, 6, 8).  Variants 1, 2, 4, 5, 6 give
  * bitwise-identical results. */
 int cgs_set_launch_shape(cgs_ctx* ctx, int32_t spread_cc, int32_t spread_variant, int32_t interp_cc);
 

@@ -202,10 +202,13 @@ def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
     r.set_smaps(smaps)
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 5)
     tune = r.autotune()
-    assert tune["spread_coils_per_block"] in range(1, nch + 1)
-    assert tune["spread_warps_per_plane"] in (1, 2)
+    assert tune["spread_variant"] in (1, 2, 4, 5, 6)
+    if tune["spread_variant"] == 6:   # the gather's parameter: coils per thread
+        assert tune["spread_coils_per_block"] in (4, 6, 8)
+    else:
+        assert tune["spread_coils_per_block"] in range(1, nch + 1)
     assert tune["interp_coils_per_thread"] in (2, 4, 6, 8)
-    assert len(tune["candidates_ms"]) >= 5 and all(t > 0 for t in tune["candidates_ms"])
+    assert len(tune["candidates_ms"]) >= 6 and all(t > 0 for t in tune["candidates_ms"])
     x1, res1, _ = r.cg_sense_batched(data, 0.0, 5)
     assert np.array_equal(x0, x1)
     assert np.array_equal(res0, res1)
@@ -214,8 +217,9 @@ def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
 @pytest.mark.parametrize("img,grid,nch", [((32, 24, 20), (64, 48, 40), 7), ((48, 40, 24), (96, 80, 48), 12)])
 def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid, nch):
     """The fixed-order spreading variants (one / two warps per x plane,
-    plain or persistent and pipelined) and every coil chunk size give
-    bitwise-identical solves: each grid value is summed in the same order."""
+    plain or persistent and pipelined, the gather over the transposed tap
+    matrix) and every coil chunk size give bitwise-identical solves: each
+    grid value is summed in the same order."""
     k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 48)
     bins = synth.bin_samples([np.arange(0, 7), np.arange(7, 41), np.arange(41, 60)], 48)
     smaps = synth.coil_maps(img, nch)
@@ -228,11 +232,18 @@ def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, g
     r.set_launch_shape(0, 1, 4)
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 4)
     for cc in (0, 3, 5):
-        for variant in (1, 2, 4, 5):
+        for variant in (1, 2, 4, 5, 6):
             r.set_launch_shape(cc, variant, 2)
             x1, res1, _ = r.cg_sense_batched(data, 0.0, 4)
             assert np.array_equal(x1, x0), (cc, variant)
             assert np.array_equal(res1, res0), (cc, variant)
+    # compensated sums: the tiled kernel and the transposed-matrix gather agree bitwise
+    r.set_precision("compensated")
+    r.set_launch_shape(0, 1, 2)
+    xk, rk, _ = r.cg_sense_batched(data, 0.0, 4)
+    r.set_launch_shape(0, 6, 2)
+    xk6, rk6, _ = r.cg_sense_batched(data, 0.0, 4)
+    assert np.array_equal(xk, xk6) and np.array_equal(rk, rk6)
 
 
 @pytest.mark.parametrize("img,grid,nch", [((32, 24, 20), (64, 48, 40), 5),
@@ -261,7 +272,7 @@ def test_support_pruning_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid
     out = {}
     for on in (True, False):
         r.set_support_pruning(on)
-        for variant in (1, 2, 4):
+        for variant in (1, 2, 4, 6):
             r.set_launch_shape(0, variant, 2)
             out[on, variant] = r.cg_sense_batched(data, 0.0, 4)[:2]
     ref = out[False, 1]
@@ -297,7 +308,7 @@ def test_atomic_spreading_matches_fixed_order(gpu_lib, cgs, oracle_mod, o64, syn
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 5)
     r.set_deterministic(False)
     tune = r.autotune()
-    assert tune["spread_warps_per_plane"] in (1, 2, 3)
+    assert tune["spread_variant"] in (1, 2, 3, 4, 5, 6)
     x1, res1, _ = r.cg_sense_batched(data, 0.0, 5)
     assert rel_l2(x1, x0) < 1e-5
     assert np.allclose(res1, res0, rtol=1e-5)
