@@ -77,13 +77,34 @@ k_cg_init(const float2* __restrict__ b, float2* r, float2* p, float2* x, long lo
     }
 }
 
-// Sum the partials of <b, b> and arm the state: rr, active.
+// Sum of a bin's nblk (re, im) partials by one warp: lane l adds the
+// partials l, l + 32, ... in order, then a butterfly of shuffles (a fixed
+// order; every lane ends with the same sums).
+CGS_D void warp_partials(const double* partials, long long base, int nblk, double& re, double& im)
+{
+    const int lane = threadIdx.x & 31;
+    double a = 0.0, b = 0.0;
+    for (int i = lane; i < nblk; i += 32) {
+        a += partials[2 * (base + i)];
+        b += partials[2 * (base + i) + 1];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    re = a;
+    im = b;
+}
+
+// Sum the partials of <b, b> and arm the state: rr, active.  One warp per bin.
 __global__ void k_cg_arm(CgState* st, const double* partials, int nblk, int nbins, double thresh, int max_iter)
 {
-    const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    const int bin = blockIdx.x;
     if (bin >= nbins) return;
-    double s = 0.0;
-    for (int i = 0; i < nblk; ++i) s += partials[2 * ((long long)bin * nblk + i)];
+    double s, unused;
+    warp_partials(partials, (long long)bin * nblk, nblk, s, unused);
+    if (threadIdx.x != 0) return;
     CgState& S = st[bin];
     S.rr[0] = s;
     S.rr[1] = 0.0;
@@ -104,15 +125,13 @@ __global__ void k_cg_arm(CgState* st, const double* partials, int nblk, int nbin
 __global__ void k_cg_alpha(CgState* st, const double* partials, int nblk, int nbins, const float2* q0,
                            long long bs)
 {
-    const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    const int bin = blockIdx.x;   // one warp per bin
     if (bin >= nbins) return;
     CgState& S = st[bin];
     if (!S.active) return;
-    double pr = 0.0, pim = 0.0;
-    for (int i = 0; i < nblk; ++i) {
-        pr += partials[2 * ((long long)bin * nblk + i)];
-        pim += partials[2 * ((long long)bin * nblk + i) + 1];
-    }
+    double pr, pim;
+    warp_partials(partials, (long long)bin * nblk, nblk, pr, pim);
+    if (threadIdx.x != 0) return;
     S.pq[0] = pr;
     S.pq[1] = pim;
     const float2 qv = q0[(long long)bin * bs];
@@ -169,12 +188,13 @@ k_cg_update_xr(float2* x, float2* r, const float2* __restrict__ p, const float2*
 __global__ void k_cg_beta(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
                           int res_stride)
 {
-    const int bin = blockIdx.x * blockDim.x + threadIdx.x;
+    const int bin = blockIdx.x;   // one warp per bin
     if (bin >= nbins) return;
     CgState& S = st[bin];
     if (!S.active) return;
-    double s = 0.0;
-    for (int i = 0; i < nblk; ++i) s += partials[2 * ((long long)bin * nblk + i)];
+    double s, unused;
+    warp_partials(partials, (long long)bin * nblk, nblk, s, unused);
+    if (threadIdx.x != 0) return;
     S.res = sqrt(s);
     if (residuals) residuals[(long long)bin * res_stride + S.iter] = S.res;
     // beta = rr_new / rr_old with rr_new real

@@ -273,14 +273,14 @@ cudaError_t launch_cg_init(const float2* b, float2* r, float2* p, float2* x, lon
 cudaError_t launch_cg_arm(CgState* st, const double* partials, int nblk, int nbins, double thresh, int max_iter,
                           cudaStream_t s)
 {
-    k_cg_arm<<<(nbins + 63) / 64, 64, 0, s>>>(st, partials, nblk, nbins, thresh, max_iter);
+    k_cg_arm<<<nbins, 32, 0, s>>>(st, partials, nblk, nbins, thresh, max_iter);
     return cudaGetLastError();
 }
 
 cudaError_t launch_cg_alpha(CgState* st, const double* partials, int nblk, int nbins, const float2* q0,
                             long long bs, cudaStream_t s)
 {
-    k_cg_alpha<<<(nbins + 63) / 64, 64, 0, s>>>(st, partials, nblk, nbins, q0, bs);
+    k_cg_alpha<<<nbins, 32, 0, s>>>(st, partials, nblk, nbins, q0, bs);
     return cudaGetLastError();
 }
 
@@ -295,7 +295,7 @@ cudaError_t launch_cg_update_xr(float2* x, float2* r, const float2* p, const flo
 cudaError_t launch_cg_beta(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
                            int res_stride, cudaStream_t s)
 {
-    k_cg_beta<<<(nbins + 63) / 64, 64, 0, s>>>(st, partials, nblk, nbins, residuals, res_stride);
+    k_cg_beta<<<nbins, 32, 0, s>>>(st, partials, nblk, nbins, residuals, res_stride);
     return cudaGetLastError();
 }
 
