@@ -2153,6 +2153,14 @@ int cgs_support_stats(cgs_ctx* c, int64_t* listed_cols, int64_t* live_tiles)
     return CGS_OK;
 }
 
+int cgs_spread_matrix_stats(cgs_ctx* c, int64_t* taps, int64_t* points)
+{
+    CGS_TRY(check_ready(c, false));
+    if (taps) *taps = c->csr_valid ? (int64_t)c->csr_entries : 0;
+    if (points) *points = c->csr_valid ? (int64_t)c->csr_pts : 0;
+    return CGS_OK;
+}
+
 int cgs_set_launch_shape(cgs_ctx* c, int32_t spread_cc, int32_t spread_variant, int32_t interp_cc)
 {
     if (!c) return CGS_ERR_ARG;

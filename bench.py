@@ -188,13 +188,17 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
     return w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s
 
 
-def stage_bytes(w, sizes, support=None):
+def stage_bytes(w, sizes, support=None, matrix=None):
     """Algorithmic bytes of each stage of one E^H D E application over all
     bins: every stage reads its input and writes its output once.
     support = (listed columns, stored spreading tiles) per bin, from
     Reco.support_stats(): with sample-support pruning the x passes move only
     the listed (y, z) columns, the interpolation reads within them and the
-    spreading stores only the listed tiles.  None: the full grid."""
+    spreading stores only the listed tiles.  None: the full grid.
+    matrix = (taps, points) of the transposed tap matrix when the spreading
+    is its gather: it stores every point of the listed columns and reads the
+    row offsets (4 bytes per point), the taps (8 bytes each) and the coil
+    values of the samples."""
     Ix, Iy, Iz = w.img
     Gx, Gy, Gz = w.grid
     Ni, Ng, Nl = Ix * Iy * Iz, Gx * Gy * Gz, Ix * Iy
@@ -212,17 +216,18 @@ def stage_bytes(w, sizes, support=None):
         "fwd_y": nb * C8 * (Nl * Gz + Ix * Gy * Gz),
         "fwd_x": C8 * scol * (Ix + Gx),
         "interp": C8 * scol * Gx + M * (64 + 4 + C8),
-        "spread": C8 * stile * 512 + M * (64 + C8),   # 4 x 8 x 16 points per tile
+        "spread": (C8 * scol * Gx + 4 * matrix[1] + 8 * matrix[0] + M * C8) if matrix
+        else C8 * stile * 512 + M * (64 + C8),   # tiled kernels: 4 x 8 x 16 points per tile
         "adj_x": C8 * scol * (Gx + Ix),
         "adj_y": nb * C8 * (Ix * Gy * Gz + Nl * Gz),
         "adj_z": nb * (C8 * Nl * Gz + C8 * Ni + 8 * Ni),
     }
 
 
-def apply_bytes(w, sizes, support=None):
+def apply_bytes(w, sizes, support=None, matrix=None):
     """Algorithmic bytes of one application: the stages plus the CG vector
     update (x, r, p, q and their reductions, 56 bytes per voxel and bin)."""
-    return sum(stage_bytes(w, sizes, support).values()) + 56 * int(np.prod(w.img)) * len(sizes)
+    return sum(stage_bytes(w, sizes, support, matrix).values()) + 56 * int(np.prod(w.img)) * len(sizes)
 
 
 # ---------------------------------------------------------------------------
@@ -675,10 +680,15 @@ def run_ours(args):
     groups = len(st) // 8
     stage_ms = {s: float(sum(st[g * 8 + i] for g in range(groups))) for i, s in enumerate(STAGES)}
     support = reco.support_stats()
-    sb = stage_bytes(w, sizes, support)
+    taps, points = reco.spread_matrix_stats()
+    variant = tune.get("spread_variant") if tune else 6   # the library's default is the gather
+    gather = variant == 6 and taps > 0
+    matrix = (taps, points) if gather else None
+    sb = stage_bytes(w, sizes, support, matrix)
     apply_ms = float(sum(stage_ms.values()))
     # kernel families: the four x/y passes are one kernel template
-    fam = {k: [s for s in STAGES if FAMILY[s] == k] for k in dict.fromkeys(FAMILY.values())}
+    family = dict(FAMILY, spread="k_spread_csr" if gather else "k_spread")
+    fam = {k: [s for s in STAGES if family[s] == k] for k in dict.fromkeys(family.values())}
     fam_ms = {k: sum(stage_ms[s] for s in v) for k, v in fam.items()}
     dom = max(fam_ms, key=fam_ms.get)
     dom_bytes = sum(sb[s] for s in fam[dom])
@@ -698,8 +708,8 @@ def run_ours(args):
         "stage_ms": stage_ms,
         "stage_frac_of_peak": {s: sb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
         "apply_ms": apply_ms,
-        "apply_achieved_gbs": apply_bytes(w, sizes, support) / (apply_ms / 1e3) / 1e9,
-        "apply_bytes": apply_bytes(w, sizes, support),
+        "apply_achieved_gbs": apply_bytes(w, sizes, support, matrix) / (apply_ms / 1e3) / 1e9,
+        "apply_bytes": apply_bytes(w, sizes, support, matrix),
         "support": {"listed_column_fraction": float(sum(support[0])) / (nb * w.grid[1] * w.grid[2]),
                     "stored_tile_fraction": float(sum(support[1])) / (nb * int(np.prod(w.grid)) // 512)},
     }

@@ -334,6 +334,10 @@ int cgs_set_support_pruning(cgs_ctx* ctx, int32_t on);
  * (without pruning: every column, every tile). */
 int cgs_support_stats(cgs_ctx* ctx, int64_t* listed_cols, int64_t* live_tiles);
 
+/* The transposed tap matrix of spreading variant 6 (all bins): its taps
+ * (entries) and grid points (rows); both 0 when it is not built. */
+int cgs_spread_matrix_stats(cgs_ctx* ctx, int64_t* taps, int64_t* points);
+
 /* Autotuner: times one batched E^H D E application of every bin for each
  * candidate launch shape -- coils per spreading block (all that fit, then
  * 1/2, 1/3, 1/4 of them) with one or two warps per x plane of a tile, then
