@@ -56,7 +56,7 @@ EXPORTS = [
     "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream", "cgs_import_data_bin", "cgs_permute_samples_d",
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
     "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic", "cgs_set_launch_shape",
-    "cgs_set_support_pruning", "cgs_support_stats", "cgs_spread_matrix_stats",
+    "cgs_set_support_pruning", "cgs_support_stats", "cgs_spread_matrix_stats", "cgs_estimate_smaps_d",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -180,6 +180,7 @@ def lib():
         "cgs_set_support_pruning": (C.c_int, [vp, C.c_int32]),
         "cgs_support_stats": (C.c_int, [vp, vp, vp]),
         "cgs_spread_matrix_stats": (C.c_int, [vp, vp, vp]),
+        "cgs_estimate_smaps_d": (C.c_int, [vp, vp, C.c_double, C.c_double, vp]),
         "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
                                              C.c_double, C.c_int32, C.c_int32, vp]),
         "cgs_cg_solve_trace_d": (C.c_int, [vp, vp, vp, dbl, i32, vp, vp, vp]),
@@ -562,6 +563,12 @@ class Reco:
         live = np.zeros(nb, np.int64)
         self._check(self._L.cgs_support_stats(self._ctx, _p(cols), _p(live)))
         return cols, live
+
+    def estimate_smaps_tensor(self, data, maps, radius, eps=0.05):
+        """Coil maps from low-resolution coil images (see cgs_estimate_smaps_d):
+        data complex64 [n_ch][ns], maps complex64 [n_ch][img], device tensors."""
+        self._check(self._L.cgs_estimate_smaps_d(self._ctx, C.c_void_p(data.data_ptr()), float(radius), float(eps),
+                                                 C.c_void_p(maps.data_ptr())))
 
     def spread_matrix_stats(self):
         """(taps, grid points) of the transposed tap matrix (0, 0 when not built)."""

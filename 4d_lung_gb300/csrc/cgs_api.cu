@@ -1208,6 +1208,29 @@ int cgs_nufft_adj_d(cgs_ctx* c, const float* data, float* img)
     return CGS_OK;
 }
 
+int cgs_estimate_smaps_d(cgs_ctx* c, const void* data, double radius, double eps, void* maps)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!data || !maps) return fail(c, CGS_ERR_ARG, "null pointer");
+    if (c->nbins != 1) return fail(c, CGS_ERR_STATE, "coil maps are estimated from a single bin (mask)");
+    if (!(radius > 0.0) || !(eps >= 0.0) || !(eps < 1.0)) return fail(c, CGS_ERR_ARG, "radius > 0, 0 <= eps < 1");
+    c->launches = 0;
+    DevBuf w, rss, mx;
+    CGS_CUDA(c, w.ensure(std::max<long long>(c->total, 1) * sizeof(float)));
+    CGS_CUDA(c, rss.ensure((size_t)c->Ni * sizeof(float)));
+    CGS_CUDA(c, mx.ensure(sizeof(unsigned)));
+    CGS_LAUNCH(c, launch_lowpass_weights(c->d_k.as<double>(), c->d_sorted.as<int>(), c->total, c->G, radius,
+                                         c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr, w.as<float>(), c->stream));
+    CGS_LAUNCH(c, launch_gather_samples(reinterpret_cast<const float2*>(data), c->ns, c->d_sorted.as<int>(), c->total,
+                                        c->nch, w.as<float>(), c->d_yv.as<float2>(), c->stream));
+    // per-coil images (no coil maps): the adjoint chain of bin 0
+    CGS_TRY(adj_chain(c, 0, 1, reinterpret_cast<float2*>(maps), 0, false, nullptr, nullptr));
+    CGS_LAUNCH(c, launch_smaps_from_images(reinterpret_cast<float2*>(maps), c->nch, c->Ni, (float)eps, rss.as<float>(),
+                                           mx.as<unsigned>(), c->stream));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    return check_timeout(c);
+}
+
 int cgs_nufft_fwd(cgs_ctx* c, const float* img, float* data)
 {
     CGS_TRY(check_ready(c, false));

@@ -109,6 +109,13 @@ cudaError_t launch_pair_grad(const PairGradArgs& a, cudaStream_t s);
 cudaError_t launch_pm_init(float* w, float2* v, long long n, cudaStream_t s);
 cudaError_t launch_pm_update(float* w, float2* v, const float2* u, long long n, cudaStream_t s);
 
+// Coil maps from low-resolution coil images (smaps.cu)
+cudaError_t launch_lowpass_weights(const double* k, const int* sorted, long long n, const int* G, double radius,
+                                   const float* dcf_sorted, float* w, cudaStream_t s);
+// imgs [nch][n] coil images -> maps in place; rss_tmp [n], max_tmp one word
+cudaError_t launch_smaps_from_images(float2* imgs, int nch, long long n, float eps, float* rss_tmp,
+                                     unsigned* max_tmp, cudaStream_t s);
+
 // File IO (io.cu)
 cudaError_t launch_scale_samples(float2* data, const float* d, long long ns, int nch, cudaStream_t s);
 

@@ -328,6 +328,17 @@ int cgs_set_launch_shape(cgs_ctx* ctx, int32_t spread_cc, int32_t spread_variant
  * Fourier.cpp:19-42). */
 int cgs_set_support_pruning(cgs_ctx* ctx, int32_t on);
 
+/* Coil sensitivity maps from the measured data of a single-bin context
+ * (device pointers; data [n_ch][ns] in the reference's order, maps
+ * [n_ch][img]): the adjoint NUFFT of each coil's samples weighted by a Hann
+ * window of `radius` grid cells around the k-space centre (times the
+ * density weights when set), divided by the coils' root-sum-of-squares
+ * where that exceeds eps times its maximum, 0 elsewhere.  A low-resolution
+ * estimate for the SENSE solve when no map files exist (the reference reads
+ * maps, IO.cpp:25-51, and exports the root-sum-of-squares,
+ * functions.h:290-316, for external estimation). */
+int cgs_estimate_smaps_d(cgs_ctx* ctx, const void* data, double radius, double eps, void* maps);
+
 /* Per bin (arrays of cgs_num_bins entries, either may be NULL): the (y, z)
  * grid columns the x passes transform (whole column tiles of the pass) and
  * the spreading tiles stored, as the current pruning setting uses them
