@@ -119,6 +119,10 @@ struct cgs_ctx {
     bool sup_built = false;
     std::vector<long long> h_sup_off;        // per bin: first entry in d_sup_tiles
     std::vector<int2> h_sup_tiles;           // listed tiles {bin, first column}, all bins
+    // rows of each forward-y-pass tile that the x pass reads (per bin, z tile, Gy / 32 words);
+    // built when the x and y passes' column tiles coincide
+    DevBuf d_sup_rowmask;
+    long long sup_rowmask_bs = 0;            // words per bin (0: not built)
     // transposed tap matrix of the listed tiles' points (spreading variant 6)
     bool csr_valid = false;
     long long csr_pts = 0;
@@ -528,6 +532,22 @@ int rebuild_bins(cgs_ctx* c)
         CGS_TRY(upload(c, c->d_live, live.data(), std::max<size_t>(live.size(), 1) * sizeof(int)));
         CGS_TRY(upload(c, c->d_live_off, c->h_live_off.data(), c->h_live_off.size() * sizeof(long long)));
         c->sup_built = true;
+        // row masks of the forward y pass: its tile (z tile zs, all y) stores row y only
+        // when the x pass lists the column tile starting at y * Gz + zs * tb
+        c->sup_rowmask_bs = 0;
+        const int tby = fft_strided_cols(c->G[1]);
+        if (tby == tbx && c->G[2] % tby == 0 && c->G[1] % 32 == 0) {
+            const int nzs = c->G[2] / tby, wpr = c->G[1] / 32;
+            const long long bs = (long long)nzs * wpr;
+            std::vector<unsigned> rm((size_t)c->nbins * bs, 0u);
+            for (int b = 0; b < c->nbins; ++b)
+                for (long long J = c->h_sup_off[b]; J < c->h_sup_off[b + 1]; ++J) {
+                    const int f = tiles[J].y, y = f / c->G[2], zs = (f % c->G[2]) / tby;
+                    rm[(size_t)b * bs + (size_t)zs * wpr + y / 32] |= 1u << (y % 32);
+                }
+            CGS_TRY(upload(c, c->d_sup_rowmask, rm.data(), rm.size() * sizeof(unsigned)));
+            c->sup_rowmask_bs = bs;
+        }
     }
     CGS_TRY(build_csr(c));
     std::vector<int> tile_ptr;
@@ -647,8 +667,13 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fy.out_off = 0;
     fy.err = c->d_err.as<int>();
     fy.tw = c->tw[1].as<float2>();
-    // every row is stored: the forward x pass reads only the listed tiles
+    // only the rows of the tiles the forward x pass lists are stored
     const bool sup = support_pruned(c);
+    if (sup && c->sup_rowmask_bs > 0) {
+        fy.sup_rowmask = c->d_sup_rowmask.as<unsigned>() + (long long)b0 * c->sup_rowmask_bs;
+        fy.sup_rowmask_bs = c->sup_rowmask_bs;
+        fy.sup_nsub = c->nch;
+    }
     CGS_LAUNCH(c, launch_strided(Gy, -1, fy, Ix, nb * c->nch, c->stream));
 
     StridedPassArgs fx{};

@@ -287,11 +287,34 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
                             o[(k2 - R2 / 4) * step] = FOLD ? u[k2] : parity(u[k2], k1 + R1 * k2);
                     }
                 } else {
+                    // with a row mask (forward y pass): only the rows the x pass reads.  Row
+                    // l = k1 + R1 k2 is bit (R1 k2 + k1) & 31 of word (R1 k2) / 32 when R1 is a
+                    // power of two up to 32 (k1 < R1): compile-time words in registers
+                    constexpr bool RM = (R1 & (R1 - 1)) == 0 && R1 <= 32 && L % 32 == 0;
+                    bool done = false;
+                    if constexpr (RM) {
+                        if (a.sup_rowmask && a.out_off == 0 && a.Lout == L) {
+                            const unsigned* mw = a.sup_rowmask + (item / a.sup_nsub) * a.sup_rowmask_bs +
+                                                 (long long)(b0 / TB) * (L / 32);
+                            unsigned rm[L / 32];
 #pragma unroll
-                    for (int k2 = 0; k2 < R2; ++k2) {
-                        const int l = k1 + R1 * k2;
-                        const int lo = l - a.out_off;
-                        if (bok && lo >= 0 && lo < a.Lout) out[(long long)lo * a.B] = FOLD ? u[k2] : parity(u[k2], l);
+                            for (int q = 0; q < L / 32; ++q) rm[q] = __ldg(mw + q);
+#pragma unroll
+                            for (int k2 = 0; k2 < R2; ++k2) {
+                                const int l = k1 + R1 * k2;
+                                if (bok && ((rm[(R1 * k2) / 32] >> (((R1 * k2) & 31) + k1)) & 1u))
+                                    out[(long long)l * a.B] = FOLD ? u[k2] : parity(u[k2], l);
+                            }
+                            done = true;
+                        }
+                    }
+                    if (!done) {
+#pragma unroll
+                        for (int k2 = 0; k2 < R2; ++k2) {
+                            const int l = k1 + R1 * k2;
+                            const int lo = l - a.out_off;
+                            if (bok && lo >= 0 && lo < a.Lout) out[(long long)lo * a.B] = FOLD ? u[k2] : parity(u[k2], l);
+                        }
                     }
                 }
             }
