@@ -1377,6 +1377,10 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
     auto it = c->graphs.find(key);
     cudaGraphExec_t exec = nullptr;
     if (it == c->graphs.end()) {
+        // one group of bins: clear stale adjoint y-buffer slots now, so that the
+        // graph holds no clears (with several groups the clears between them are
+        // part of the graph)
+        if (c->ws_bins >= nb) CGS_TRY(prepare_adj_slots(c, 0, nb, support_pruned(c)));
         c->launches = 0;
         const std::vector<int> entry = c->adj_slot;
         CGS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
