@@ -39,7 +39,7 @@ struct SizeImpl {
     using Pipe = PipeLayout<R1, R2, TB, NSTAGE>;
 
     // pipelined z passes: coil tiles in flight ahead of the FFT
-    static constexpr int ZNST_F = 3, ZNST_A = 2;
+    static constexpr int ZNST_F = 2, ZNST_A = 2;
     using ZF = ZPipeLayout<R1, R2, LPB, ZNST_F>;
     using ZA = ZPipeLayout<R1, R2, LPB, ZNST_A>;
 

@@ -626,14 +626,17 @@ struct ZPipeLayout {
     static constexpr int NT = LPB * Lay::RMAX;
     // elements of one stage: S tile (+ z-buffer tile for the adjoint)
     __host__ __device__ static size_t stage_elems(int Iz, bool adj) { return (size_t)LPB * Iz + (adj ? (size_t)LPB * L : 0); }
+    // forward: the block's x * apod lines stay in shared memory across the coils
     static size_t smem_bytes(int Iz, bool adj)
     {
-        return (NST * stage_elems(Iz, adj) + L + (size_t)LPB * Lay::LINE) * sizeof(float2) + 16 * NST;
+        return (NST * stage_elems(Iz, adj) + L + (size_t)LPB * Lay::LINE + (adj ? 0 : (size_t)LPB * Iz)) *
+                   sizeof(float2) +
+               16 * NST;
     }
 };
 
 template <int R1, int R2, int LPB, int NST>
-__global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX)
+__global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX, (R1 > 16 || R2 > 16) ? 2 : 3)
 k_fwd_z_pipe(FwdZArgs a)
 {
     using Lay = ContigLayout<R1, R2>;
@@ -645,7 +648,8 @@ k_fwd_z_pipe(FwdZArgs a)
     float2* s_stage = reinterpret_cast<float2*>(s_dyn);
     float2* s_tw = s_stage + NST * se;
     float2* s_y = s_tw + L;
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_y + LPB * Lay::LINE);
+    float2* s_xa = s_y + LPB * Lay::LINE;   // x * apod * parity of the block's lines, [LPB][Iz]
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_xa + (size_t)LPB * a.Iz);
     const int tid = threadIdx.x;
     for (int m = tid; m < L; m += ZL::NT) s_tw[m] = a.tw[m];
     const long long line0 = (long long)blockIdx.x * LPB;
@@ -670,7 +674,7 @@ k_fwd_z_pipe(FwdZArgs a)
     const int ln1 = tid / R2, n2 = tid % R2;
     const long long line1 = line0 + ln1;
     const bool act1 = ln1 < LPB && line1 < a.nl;
-    float2 xa[R1];
+    float2* xa = s_xa + (size_t)ln1 * a.Iz;   // written and read by this thread only
     if (act1) {
         const int ix = (int)(line1 / a.Iy), iy = (int)(line1 - (long long)ix * a.Iy);
         const float axy = a.apx[ix] * a.apy[iy];
@@ -679,9 +683,7 @@ k_fwd_z_pipe(FwdZArgs a)
         for (int n1 = 0; n1 < R1; ++n1) {
             const int l = R2 * n1 + n2;
             const int zi = l - a.lo_z;
-            float2 v = make_float2(0.f, 0.f);
-            if (zi >= 0 && zi < a.Iz) v = parity(cscale(xl[zi], axy * a.apz[zi]), l);
-            xa[n1] = v;
+            if (zi >= 0 && zi < a.Iz) xa[zi] = parity(cscale(xl[zi], axy * a.apz[zi]), l);
         }
     }
     const int ln2 = tid / R1, k1 = tid % R1;
@@ -708,7 +710,7 @@ k_fwd_z_pipe(FwdZArgs a)
 #pragma unroll
             for (int n1 = 0; n1 < R1; ++n1) {
                 const int zi = R2 * n1 + n2 - a.lo_z;
-                v[n1] = (zi >= 0 && zi < a.Iz) ? cmul(xa[n1], S[zi]) : make_float2(0.f, 0.f);
+                v[n1] = (zi >= 0 && zi < a.Iz) ? cmul(xa[zi], S[zi]) : make_float2(0.f, 0.f);
             }
             Dft<R1, SIGN>::run(v);
 #pragma unroll
