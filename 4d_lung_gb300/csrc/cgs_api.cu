@@ -441,6 +441,7 @@ int build_csr(cgs_ctx* c)
     int bad = 0;
     CGS_CUDA(c, cudaMemcpyAsync(&bad, c->d_flag.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->d_csr_cnt.release();   // the counts / fill cursors are not needed after the build
     if (bad) return CGS_OK;   // a tap outside the lists: keep the tiled kernel
     c->csr_pts = npts;
     c->csr_entries = ne;

@@ -350,12 +350,13 @@ int cgs_support_stats(cgs_ctx* ctx, int64_t* listed_cols, int64_t* live_tiles);
 int cgs_spread_matrix_stats(cgs_ctx* ctx, int64_t* taps, int64_t* points);
 
 /* Autotuner: times one batched E^H D E application of every bin for each
- * candidate launch shape -- coils per spreading block (all that fit, then
- * 1/2, 1/3, 1/4 of them) with one or two warps per x plane of a tile, then
+ * candidate launch shape -- the spreading variants of cgs_set_launch_shape
+ * (tiled kernels with coils per block all that fit, then 1/2, 1/3, 1/4 of
+ * them; the transposed-matrix gather with 4, 6 or 8 coils per thread), then
  * coils per interpolation thread (2, 4, 6, 8) -- and keeps the fastest for
  * this context.  times_ms (may be NULL) receives the median time of each
  * candidate in that order; the chosen shape is returned in *spread_cc,
- * *spread_wpp and *interp_cc (each may be NULL). */
+ * *spread_wpp (the spreading variant) and *interp_cc (each may be NULL). */
 int cgs_autotune(cgs_ctx* ctx, float* times_ms, int32_t max_times, int32_t* n_times, int32_t* spread_cc,
                  int32_t* spread_wpp, int32_t* interp_cc);
 
