@@ -607,6 +607,38 @@ def run_ours(args):
     res, its = reco.cg_sense_batched_tensor(data, x, 0.0, iters, want_stats=True)
     assert np.all(its == iters) and np.all(np.isfinite(res))
 
+    # end to end through the host-buffer C ABI call (pinned host memory),
+    # right after the device-timed solves (before the comparison forms run)
+    h_data = torch.empty(data.shape, dtype=torch.complex64, pin_memory=True)
+    h_data.copy_(data.cpu())
+    h_x = torch.empty(x.shape, dtype=torch.complex64, pin_memory=True)
+    h_res = np.zeros((nb, iters), np.float64)
+    h_it = np.zeros(nb, np.int32)
+    import ctypes as C
+    L = cgs.lib()
+
+    def host_call():
+        st = L.cgs_cg_solve_batched(reco.ctx, C.c_void_p(h_data.data_ptr()), C.c_void_p(h_x.data_ptr()),
+                                    0.0, iters, h_res.ctypes.data_as(C.c_void_p),
+                                    h_it.ctypes.data_as(C.c_void_p))
+        if st != 0:
+            raise RuntimeError(L.cgs_last_error(reco.ctx).decode())
+
+    for _ in range(max(1, args.warmup)):
+        host_call()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_call()
+    e2e_s = time.perf_counter() - t0
+    te = torch.tensor([e2e_s], device=dev)
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * applies_per_step * args.steps / float(te.item())
+    h2d = data.numel() * 8
+    d2h = x.numel() * 8 + h_res.nbytes + h_it.nbytes
+
     # the plain per-bin GPU form (frozen comparison point): same solve
     plain = None
     if not args.no_plain:
@@ -639,36 +671,6 @@ def run_ours(args):
     if not args.no_diff:
         diff = differentiation_report(cgs, synth, torch, dev, stream.cuda_stream)
 
-    # end to end through the host-buffer C ABI call (pinned host memory)
-    h_data = torch.empty(data.shape, dtype=torch.complex64, pin_memory=True)
-    h_data.copy_(data.cpu())
-    h_x = torch.empty(x.shape, dtype=torch.complex64, pin_memory=True)
-    h_res = np.zeros((nb, iters), np.float64)
-    h_it = np.zeros(nb, np.int32)
-    import ctypes as C
-    L = cgs.lib()
-
-    def host_call():
-        st = L.cgs_cg_solve_batched(reco.ctx, C.c_void_p(h_data.data_ptr()), C.c_void_p(h_x.data_ptr()),
-                                    0.0, iters, h_res.ctypes.data_as(C.c_void_p),
-                                    h_it.ctypes.data_as(C.c_void_p))
-        if st != 0:
-            raise RuntimeError(L.cgs_last_error(reco.ctx).decode())
-
-    for _ in range(max(1, args.warmup)):
-        host_call()
-    if world > 1:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        host_call()
-    e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], device=dev)
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * applies_per_step * args.steps / float(te.item())
-    h2d = data.numel() * 8
-    d2h = x.numel() * 8 + h_res.nbytes + h_it.nbytes
 
     # per-stage kernel times of one batched application (roofline)
     xa = torch.from_numpy(np.stack([synth.phantom(w.img)] * nb)).to(dev)
