@@ -57,6 +57,7 @@ EXPORTS = [
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
     "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic", "cgs_set_launch_shape",
     "cgs_set_support_pruning", "cgs_support_stats", "cgs_spread_matrix_stats", "cgs_estimate_smaps_d",
+    "cgs_forward_y_listed_rows",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -180,6 +181,7 @@ def lib():
         "cgs_set_support_pruning": (C.c_int, [vp, C.c_int32]),
         "cgs_support_stats": (C.c_int, [vp, vp, vp]),
         "cgs_spread_matrix_stats": (C.c_int, [vp, vp, vp]),
+        "cgs_forward_y_listed_rows": (C.c_int, [vp, vp]),
         "cgs_estimate_smaps_d": (C.c_int, [vp, vp, C.c_double, C.c_double, vp]),
         "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
                                              C.c_double, C.c_int32, C.c_int32, vp]),
@@ -569,6 +571,12 @@ class Reco:
         data complex64 [n_ch][ns], maps complex64 [n_ch][img], device tensors."""
         self._check(self._L.cgs_estimate_smaps_d(self._ctx, C.c_void_p(data.data_ptr()), float(radius), float(eps),
                                                  C.c_void_p(maps.data_ptr())))
+
+    def forward_y_listed_rows(self):
+        """True when the forward y pass stores only the x pass's listed rows."""
+        v = np.zeros(1, np.int32)
+        self._check(self._L.cgs_forward_y_listed_rows(self._ctx, _p(v)))
+        return bool(v[0])
 
     def spread_matrix_stats(self):
         """(taps, grid points) of the transposed tap matrix (0, 0 when not built)."""

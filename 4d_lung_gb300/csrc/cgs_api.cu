@@ -2206,6 +2206,14 @@ int cgs_support_stats(cgs_ctx* c, int64_t* listed_cols, int64_t* live_tiles)
     return CGS_OK;
 }
 
+int cgs_forward_y_listed_rows(cgs_ctx* c, int32_t* listed)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!listed) return fail(c, CGS_ERR_ARG, "null pointer");
+    *listed = (support_pruned(c) && c->sup_rowmask_bs > 0) ? 1 : 0;
+    return CGS_OK;
+}
+
 int cgs_spread_matrix_stats(cgs_ctx* c, int64_t* taps, int64_t* points)
 {
     CGS_TRY(check_ready(c, false));

@@ -188,7 +188,7 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
     return w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s
 
 
-def stage_bytes(w, sizes, support=None, matrix=None):
+def stage_bytes(w, sizes, support=None, matrix=None, y_listed=False):
     """Algorithmic bytes of each stage of one E^H D E application over all
     bins: every stage reads its input and writes its output once.
     support = (listed columns, stored spreading tiles) per bin, from
@@ -198,7 +198,8 @@ def stage_bytes(w, sizes, support=None, matrix=None):
     matrix = (taps, points) of the transposed tap matrix when the spreading
     is its gather: it stores every point of the listed columns and reads the
     row offsets (4 bytes per point), the taps (8 bytes each) and the coil
-    values of the samples."""
+    values of the samples.  y_listed: the forward y pass stores only the
+    listed columns' rows (8 bytes x Ix per listed column)."""
     Ix, Iy, Iz = w.img
     Gx, Gy, Gz = w.grid
     Ni, Ng, Nl = Ix * Iy * Iz, Gx * Gy * Gz, Ix * Iy
@@ -213,7 +214,7 @@ def stage_bytes(w, sizes, support=None, matrix=None):
     scol, stile = sum(cols), sum(tiles)
     return {
         "fwd_z": nb * (8 * Ni + C8 * Ni + C8 * Nl * Gz),
-        "fwd_y": nb * C8 * (Nl * Gz + Ix * Gy * Gz),
+        "fwd_y": C8 * (nb * Nl * Gz + Ix * scol) if y_listed else nb * C8 * (Nl * Gz + Ix * Gy * Gz),
         "fwd_x": C8 * scol * (Ix + Gx),
         "interp": C8 * scol * Gx + M * (64 + 4 + C8),
         "spread": (C8 * scol * Gx + 4 * matrix[1] + 8 * matrix[0] + M * C8) if matrix
@@ -224,10 +225,10 @@ def stage_bytes(w, sizes, support=None, matrix=None):
     }
 
 
-def apply_bytes(w, sizes, support=None, matrix=None):
+def apply_bytes(w, sizes, support=None, matrix=None, y_listed=False):
     """Algorithmic bytes of one application: the stages plus the CG vector
     update (x, r, p, q and their reductions, 56 bytes per voxel and bin)."""
-    return sum(stage_bytes(w, sizes, support, matrix).values()) + 56 * int(np.prod(w.img)) * len(sizes)
+    return sum(stage_bytes(w, sizes, support, matrix, y_listed).values()) + 56 * int(np.prod(w.img)) * len(sizes)
 
 
 # ---------------------------------------------------------------------------
@@ -686,7 +687,8 @@ def run_ours(args):
     variant = tune.get("spread_variant") if tune else 6   # the library's default is the gather
     gather = variant == 6 and taps > 0
     matrix = (taps, points) if gather else None
-    sb = stage_bytes(w, sizes, support, matrix)
+    y_listed = reco.forward_y_listed_rows()
+    sb = stage_bytes(w, sizes, support, matrix, y_listed)
     apply_ms = float(sum(stage_ms.values()))
     # kernel families: the four x/y passes are one kernel template
     family = dict(FAMILY, spread="k_spread_csr" if gather else "k_spread")
@@ -710,8 +712,8 @@ def run_ours(args):
         "stage_ms": stage_ms,
         "stage_frac_of_peak": {s: sb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
         "apply_ms": apply_ms,
-        "apply_achieved_gbs": apply_bytes(w, sizes, support, matrix) / (apply_ms / 1e3) / 1e9,
-        "apply_bytes": apply_bytes(w, sizes, support, matrix),
+        "apply_achieved_gbs": apply_bytes(w, sizes, support, matrix, y_listed) / (apply_ms / 1e3) / 1e9,
+        "apply_bytes": apply_bytes(w, sizes, support, matrix, y_listed),
         "support": {"listed_column_fraction": float(sum(support[0])) / (nb * w.grid[1] * w.grid[2]),
                     "stored_tile_fraction": float(sum(support[1])) / (nb * int(np.prod(w.grid)) // 512)},
     }

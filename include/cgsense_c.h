@@ -345,6 +345,11 @@ int cgs_estimate_smaps_d(cgs_ctx* ctx, const void* data, double radius, double e
  * (without pruning: every column, every tile). */
 int cgs_support_stats(cgs_ctx* ctx, int64_t* listed_cols, int64_t* live_tiles);
 
+/* 1 when the forward y pass stores only the rows of the x pass's listed
+ * tiles (sample-support pruning on and the passes' column tiles coincide),
+ * else 0. */
+int cgs_forward_y_listed_rows(cgs_ctx* ctx, int32_t* listed);
+
 /* The transposed tap matrix of spreading variant 6 (all bins): its taps
  * (entries) and grid points (rows); both 0 when it is not built. */
 int cgs_spread_matrix_stats(cgs_ctx* ctx, int64_t* taps, int64_t* points);
