@@ -28,7 +28,7 @@ def _units():
     units = []
     for g in range(FFT_GROUPS):
         units.append(("fft_inst.cu", "fft_inst_%d.o" % g, ["-DCGS_FFT_GROUP=%d" % g]))
-    for src in ("fft_dispatch.cu", "kernels_misc.cu", "cgs_api.cu", "fft_noalloc.cu", "plain.cu", "fp64.cu", "grad.cu", "io.cu", "spread_csr.cu", "smaps.cu"):
+    for src in ("fft_dispatch.cu", "kernels_misc.cu", "cgs_api.cu", "fft_noalloc.cu", "plain.cu", "fp64.cu", "grad.cu", "io.cu", "spread_csr.cu", "smaps.cu", "toeplitz.cu"):
         units.append((src, src.replace(".cu", ".o"), ["-Xcompiler", "-fopenmp"] if src == "cgs_api.cu" else []))
     units.append(("wave_caipi.cpp", "wave_caipi.o", []))
     units.append(("reco_shim.cpp", "reco_shim.o", []))
@@ -94,7 +94,7 @@ def build(verbose=False, jobs=None):
                     raise RuntimeError("compilation failed: %s" % cmd[-3])
     if _stale(LIB, objs):
         cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + [
-            "-cudart", "static", "-lcufft", "-lgomp", "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
+            "-cudart", "static", "-lcufft", "-lgomp", "-ldl", "-Xlinker", "-rpath,/usr/local/cuda/lib64"]
         r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
         if r.returncode != 0:
             sys.stderr.write(r.stdout)

@@ -136,6 +136,14 @@ struct cgs_ctx {
     // bound the non-zeros of workspace slot j, -1 when unknown.
     DevBuf d_ybuf_adj;
     std::vector<int> adj_slot;
+    // Toeplitz embedding of E^H D E (cgs_set_toeplitz): 0 off, 1 on (fused x
+    // stage where it applies), 2 on with the unfused x stage; per bin the real
+    // spectrum P [Gx][Gy * Gz] of the point-spread function
+    int toep_mode = 0;
+    bool toep_valid = false;
+    uint64_t toep_serial = 0;    // traj_serial the spectra were built from
+    double toep_build_ms = 0.0;
+    DevBuf d_toep, d_ones;
     // coil maps
     DevBuf d_smaps;
     bool smaps_set = false;
@@ -585,6 +593,7 @@ int rebuild_bins(cgs_ctx* c)
     CGS_CUDA(c, c->d_ybuf_adj.ensure(wsn * (long long)c->I[0] * c->G[1] * c->G[2] * sizeof(float2)));
     c->adj_slot.assign(c->ws_bins, -1);
     CGS_CUDA(c, c->d_grid.ensure(wsn * c->Ng * sizeof(float2)));
+    c->toep_valid = false;
     c->bins_dirty = false;
     return CGS_OK;
 }
@@ -838,6 +847,193 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
     return CGS_OK;
 }
 
+// Toeplitz embedding: per bin the spectrum P of the point-spread function
+// of its samples (current coordinates and density weights), scaled so that
+// F_c^H P F_c between the unscaled passes is the gridded operator's
+// adjoint scale times the exact E^H D E.
+int build_toeplitz(cgs_ctx* c)
+{
+    for (int a = 0; a < 3; ++a)
+        if (c->G[a] < 2 * c->I[a] - 1)
+            return fail(c, CGS_ERR_ARG, "the Toeplitz embedding needs grid >= 2 x image - 1 on every axis");
+    const long long Ng = c->Ng;
+    CGS_CUDA(c, c->d_toep.ensure((size_t)std::max(c->nbins, 1) * Ng * sizeof(float)));
+    const int gmax = std::max(c->G[0], std::max(c->G[1], c->G[2]));
+    if (c->d_ones.bytes < (size_t)gmax * sizeof(float)) {
+        std::vector<float> one(gmax, 1.f);
+        CGS_TRY(upload(c, c->d_ones, one.data(), one.size() * sizeof(float)));
+    }
+    // work: a chunk of samples' Dirichlet tables and their (y, z) products (W
+    // of at most 2^28 floats, the whole bin when it fits)
+    const long long yz = (long long)c->G[1] * c->G[2];
+    const long long per = yz + c->G[0] + c->G[1] + c->G[2];
+    const long long chunk = std::max<long long>(1, std::min<long long>(std::max<long long>(c->max_bin, 1),
+                                                                     std::max<long long>(64, (1LL << 28) / yz)));
+    DevBuf work;
+    CGS_CUDA(c, work.ensure((size_t)(chunk * per) * sizeof(float)));
+    cudaEvent_t e0, e1;
+    CGS_CUDA(c, cudaEventCreate(&e0));
+    CGS_CUDA(c, cudaEventCreate(&e1));
+    CGS_CUDA(c, cudaEventRecord(e0, c->stream));
+    int st = CGS_OK;
+    for (int b = 0; b < c->nbins && st == CGS_OK; ++b) {
+        ToepBuildArgs a{};
+        a.k = c->d_k.as<double>();
+        a.sorted = c->d_sorted.as<int>();
+        a.dcf = c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr;
+        a.s0 = c->h_bin_off[b];
+        a.n = c->h_bin_off[b + 1] - c->h_bin_off[b];
+        for (int ax = 0; ax < 3; ++ax) {
+            a.G[ax] = c->G[ax];
+            a.I[ax] = c->I[ax];
+        }
+        a.scale = c->adj_scale_total / (double)Ng;
+        a.P = c->d_toep.as<float>() + (long long)b * Ng;
+        std::string e;
+        if (toeplitz_build(a, work.as<float>(), chunk * per, c->stream, &e) != 0)
+            st = fail(c, CGS_ERR_CUDA, "Toeplitz spectrum of bin " + std::to_string(b) + ": " + e);
+    }
+    cudaEventRecord(e1, c->stream);
+    const cudaError_t es = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (es == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != CGS_OK) return st;
+    CGS_CUDA(c, es);
+    c->toep_build_ms = ms;
+    c->toep_valid = true;
+    c->toep_serial = c->traj_serial;
+    return CGS_OK;
+}
+
+// q = c sum_c conj(S_c) crop F_c^H P F_c pad (S_c x) for bins [b0, b0 + nb)
+// (nb <= ws_bins): the forward z and y passes without deapodisation, the x
+// stage (forward x transform, P, adjoint x transform) in place on the y
+// buffer, the adjoint y and z passes.
+int toep_chain(cgs_ctx* c, int b0, int nb, const float2* x, float2* q, const float2* pdot, double* partials)
+{
+    const int Ix = c->I[0], Iy = c->I[1], Iz = c->I[2];
+    const int Gx = c->G[0], Gy = c->G[1], Gz = c->G[2];
+    const long long zb = c->Nl * Gz, yb = (long long)Ix * Gy * Gz;
+    const float* one = c->d_ones.as<float>();
+    FwdZArgs fz{};
+    fz.x = x;
+    fz.x_cs = 0;
+    fz.smaps = c->d_smaps.as<float2>();
+    fz.apx = one;
+    fz.apy = one;
+    fz.apz = one;
+    fz.out = c->d_zbuf.as<float2>();
+    fz.nl = c->Nl;
+    fz.Iy = Iy;
+    fz.Iz = Iz;
+    fz.lo_z = c->lo[2];
+    fz.nch = c->nch;
+    fz.x_bs = c->Ni;
+    fz.out_bs = (long long)c->nch * zb;
+    fz.err = c->d_err.as<int>();
+    fz.coil_in = c->Ni;
+    fz.coil_out = zb;
+    fz.tw = c->tw[2].as<float2>();
+    CGS_LAUNCH(c, launch_fwd_z(Gz, fz, nb, c->stream));
+
+    StridedPassArgs fy{};
+    fy.in = c->d_zbuf.as<float2>();
+    fy.out = c->d_ybuf.as<float2>();
+    fy.in_bs = zb;
+    fy.out_bs = yb;
+    fy.in_as = (long long)Iy * Gz;
+    fy.out_as = (long long)Gy * Gz;
+    fy.B = Gz;
+    fy.Lin = Iy;
+    fy.in_off = c->lo[1];
+    fy.Lout = Gy;
+    fy.out_off = 0;
+    fy.err = c->d_err.as<int>();
+    fy.tw = c->tw[1].as<float2>();
+    CGS_LAUNCH(c, launch_strided(Gy, -1, fy, Ix, nb * c->nch, c->stream));
+
+    const float* P = c->d_toep.as<float>() + (long long)b0 * c->Ng;
+    StridedPassArgs tx{};
+    tx.in = c->d_ybuf.as<float2>();
+    tx.out = c->d_ybuf.as<float2>();
+    tx.in_bs = yb;
+    tx.out_bs = yb;
+    tx.B = Gy * Gz;
+    tx.Lin = Ix;
+    tx.in_off = c->lo[0];
+    tx.Lout = Ix;
+    tx.out_off = c->lo[0];
+    tx.err = c->d_err.as<int>();
+    tx.tw = c->tw[0].as<float2>();
+    cudaError_t ex = cudaErrorNotSupported;
+    if (c->toep_mode == 1) ex = launch_toep_x(Gx, tx, P, c->Ng, c->nch, nb * c->nch, c->stream);
+    if (ex == cudaSuccess) {
+        ++c->launches;
+        if (c->prof_ev) CGS_CUDA(c, cudaEventRecord(c->prof_ev[c->prof_n++], c->stream));
+    } else if (ex == cudaErrorNotSupported) {
+        cudaGetLastError();
+        // unfused: forward x pass onto the grid, P, adjoint x pass back
+        StridedPassArgs fx = tx;
+        fx.out = c->d_grid.as<float2>();
+        fx.out_bs = c->Ng;
+        fx.Lout = Gx;
+        fx.out_off = 0;
+        CGS_LAUNCH(c, launch_strided(Gx, -1, fx, 1, nb * c->nch, c->stream));
+        CGS_LAUNCH(c, launch_toep_mul(c->d_grid.as<float2>(), P, c->Ng, c->nch, nb * c->nch, c->stream));
+        StridedPassArgs ax = tx;
+        ax.in = c->d_grid.as<float2>();
+        ax.in_bs = c->Ng;
+        ax.Lin = Gx;
+        ax.in_off = 0;
+        CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
+    } else {
+        CGS_CUDA(c, ex);
+    }
+
+    StridedPassArgs ay{};
+    ay.in = c->d_ybuf.as<float2>();
+    ay.out = c->d_zbuf.as<float2>();
+    ay.in_bs = yb;
+    ay.out_bs = zb;
+    ay.in_as = (long long)Gy * Gz;
+    ay.out_as = (long long)Iy * Gz;
+    ay.B = Gz;
+    ay.Lin = Gy;
+    ay.in_off = 0;
+    ay.Lout = Iy;
+    ay.out_off = c->lo[1];
+    ay.err = c->d_err.as<int>();
+    ay.tw = c->tw[1].as<float2>();
+    CGS_LAUNCH(c, launch_strided(Gy, +1, ay, Ix, nb * c->nch, c->stream));
+
+    AdjZArgs az{};
+    az.in = c->d_zbuf.as<float2>();
+    az.smaps = c->d_smaps.as<float2>();
+    az.apx = one;
+    az.apy = one;
+    az.apz = one;
+    az.scale = 1.f;
+    az.q = q;
+    az.p = pdot;
+    az.partials = partials;
+    az.nl = c->Nl;
+    az.Iy = Iy;
+    az.Iz = Iz;
+    az.lo_z = c->lo[2];
+    az.nch = c->nch;
+    az.in_bs = (long long)c->nch * zb;
+    az.q_bs = c->Ni;
+    az.coil_in = zb;
+    az.coil_s = c->Ni;
+    az.q_cs = c->Ni;
+    az.tw = c->tw[2].as<float2>();
+    az.err = c->d_err.as<int>();
+    CGS_LAUNCH(c, launch_adj_z(Gz, az, nb, c->stream));
+    return CGS_OK;
+}
+
 // q = A x for bins [b0, b0+nb) (all groups).  pdot/partials: fused <p, q>.
 int apply_bins(cgs_ctx* c, int b0, int nb, const float2* x, float2* q, const float2* pdot, double* partials,
                int nblk)
@@ -845,6 +1041,11 @@ int apply_bins(cgs_ctx* c, int b0, int nb, const float2* x, float2* q, const flo
     for (int g = b0; g < b0 + nb; g += c->ws_bins) {
         const int n = std::min(c->ws_bins, b0 + nb - g);
         const long long off = (long long)(g - b0) * c->Ni;
+        if (c->toep_mode) {
+            CGS_TRY(toep_chain(c, g, n, x + off, q + off, pdot ? pdot + off : nullptr,
+                               partials ? partials + 2LL * (g - b0) * nblk : nullptr));
+            continue;
+        }
         CGS_TRY(fwd_chain(c, g, n, x + off, c->Ni, 0, true, true));
         CGS_TRY(adj_chain(c, g, n, q + off, c->Ni, true, pdot ? pdot + off : nullptr,
                           partials ? partials + 2LL * (g - b0) * nblk : nullptr));
@@ -875,6 +1076,7 @@ int check_ready(cgs_ctx* c, bool need_smaps, bool need_tiles = true)
     if (need_smaps && !c->smaps_set) return fail(c, CGS_ERR_STATE, "no coil maps set (cgs_set_smaps)");
     if (need_tiles && c->tiles_stale) c->bins_dirty = true;
     CGS_TRY(rebuild_bins(c));
+    if (c->toep_mode && (!c->toep_valid || c->toep_serial != c->traj_serial)) CGS_TRY(build_toeplitz(c));
     return CGS_OK;
 }
 
@@ -1834,6 +2036,14 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
                  int32_t* spread_wpp, int32_t* interp_cc)
 {
     CGS_TRY(check_ready(c, true));
+    // the candidates are shapes of the gridded operator's kernels: timed with
+    // the Toeplitz embedding off
+    struct ModeGuard {
+        cgs_ctx* c;
+        int mode;
+        ~ModeGuard() { c->toep_mode = mode; }
+    } guard{c, c->toep_mode};
+    c->toep_mode = 0;
     const long long Ni = c->Ni;
     const int nb = c->nbins;
     DevBuf xb, qb;
@@ -2181,6 +2391,29 @@ int cgs_set_deterministic(cgs_ctx* c, int32_t on)
         c->spread_wpp = 1;
         drop_graphs(c);
     }
+    return CGS_OK;
+}
+
+int cgs_set_toeplitz(cgs_ctx* c, int32_t mode)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (mode < 0 || mode > 2) return fail(c, CGS_ERR_ARG, "Toeplitz mode must be 0, 1 or 2");
+    if (mode)
+        for (int a = 0; a < 3; ++a)
+            if (c->G[a] < 2 * c->I[a] - 1)
+                return fail(c, CGS_ERR_ARG, "the Toeplitz embedding needs grid >= 2 x image - 1 on every axis");
+    if (c->toep_mode != mode) drop_graphs(c);
+    c->toep_mode = mode;
+    // with a trajectory and bins the spectra are built now, else at first use
+    if (mode && c->ns > 0 && !c->bins.empty()) return check_ready(c, false, false);
+    return CGS_OK;
+}
+
+int cgs_toeplitz_stats(cgs_ctx* c, double* build_ms, int64_t* bytes)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (build_ms) *build_ms = c->toep_valid ? c->toep_build_ms : 0.0;
+    if (bytes) *bytes = c->toep_valid ? (int64_t)c->nbins * c->Ng * (int64_t)sizeof(float) : 0;
     return CGS_OK;
 }
 

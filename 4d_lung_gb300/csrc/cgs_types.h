@@ -190,6 +190,18 @@ struct CsrSpreadArgs {
     int cc;                    // coils per thread (2, 4, 6, 8; 0: by the coil count)
 };
 
+// Toeplitz embedding (toeplitz.cu): the spectrum P of one bin's point-spread
+// function, from sorted samples [s0, s0 + n).
+struct ToepBuildArgs {
+    const double* k;           // coordinates [ns][3] (global index)
+    const int* sorted;         // sorted position -> global sample index
+    const float* dcf;          // sorted density weights, or null
+    long long s0, n;
+    int G[3], I[3];
+    double scale;              // adjoint scale / Ng
+    float* P;                  // out: [Gx][Gy * Gz]
+};
+
 // Loss gradient pass (grad.cu): one bin's samples [s0, s0 + n) in sorted order.
 struct InterpGradArgs {
     const float2* grid;        // coil c at grid + c * coil_stride (one bin)

@@ -11,7 +11,9 @@ namespace cgs {
     cudaError_t fft_fwd_z_##L_(const FwdZArgs& a, int batch, cudaStream_t s);                          \
     cudaError_t fft_adj_z_##L_(const AdjZArgs& a, int batch, cudaStream_t s);                          \
     int fft_adj_blocks_##L_(long long nl);                                                             \
-    cudaError_t fft_init_##L_();
+    cudaError_t fft_init_##L_();                                                                       \
+    cudaError_t fft_toep_x_##L_(const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch, \
+                                cudaStream_t s);
 CGS_FFT_SIZES(CGS_DECLARE)
 
 static const int kSizes[] = {
@@ -146,6 +148,17 @@ cudaError_t launch_adj_z(int L, const AdjZArgs& a, int batch, cudaStream_t s)
 #undef CGS_CASE
     }
     return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_toep_x(int L, const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch,
+                          cudaStream_t s)
+{
+    switch (L) {
+#define CGS_CASE(L_, R1_, R2_, G_) case L_: return fft_toep_x_##L_(a, P, p_bs, nsub, batch, s);
+        CGS_FFT_SIZES(CGS_CASE)
+#undef CGS_CASE
+    }
+    return cudaErrorNotSupported;
 }
 
 }  // namespace cgs

@@ -63,6 +63,10 @@ struct SizeImpl {
             if (e == cudaSuccess) e = tma_attr<-1, PRUNE_IN>(smem);
         if constexpr (HAS_OUT)
             if (e == cudaSuccess) e = tma_attr<+1, PRUNE_OUT>(smem);
+        if constexpr (HAS_IN)
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(k_toep_x_tma<R1, R2, TB, NSTAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         smem);
         // the z extent of an image never exceeds the grid's: size for Iz = L
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_fwd_z_pipe<R1, R2, LPB, ZNST_F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -117,6 +121,33 @@ struct SizeImpl {
         else k_fft_strided<R1, R2, +1, TB><<<grid, NT_S, 0, s>>>(a);
         return cudaGetLastError();
     }
+    // Toeplitz x stage (in place, rows L/4 .. 3L/4 in and out)
+    static cudaError_t toep_x(StridedPassArgs a, const float* P, long long p_bs, int nsub, int batch, cudaStream_t s)
+    {
+        if constexpr (!HAS_IN) {
+            return cudaErrorNotSupported;
+        } else {
+            a.ntb = (a.B + TB - 1) / TB;
+            if (4 * a.in_off != L || 2 * a.Lin != L || 4 * a.out_off != L || 2 * a.Lout != L || !a.err || nsub < 1 ||
+                batch % nsub != 0)
+                return cudaErrorNotSupported;
+            CUtensorMap map;
+            int box_rows = 0;
+            if (!encode_strided_map(&map, a, 1, batch, TB, &box_rows)) return cudaErrorNotSupported;
+            const size_t smem = Pipe::smem_bytes(a.Lin);
+            int per_sm = 0;
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_toep_x_tma<R1, R2, TB, NSTAGE>,
+                                                                          Pipe::NT, smem);
+            if (e != cudaSuccess) return e;
+            const long long ntiles = (long long)a.ntb * batch;
+            if (ntiles <= 0) return cudaSuccess;
+            long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
+            if (nblk > ntiles) nblk = ntiles;
+            k_toep_x_tma<R1, R2, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, P, p_bs, nsub, map, ntiles,
+                                                                                   box_rows);
+            return cudaGetLastError();
+        }
+    }
     static cudaError_t contig(int sign, const ContigPassArgs& a, int batch, cudaStream_t s)
     {
         dim3 grid((unsigned)((a.nl + LPB - 1) / LPB), (unsigned)batch);
@@ -157,6 +188,8 @@ struct SizeImpl {
     cudaError_t fft_adj_z_##L_(const AdjZArgs& a, int batch, cudaStream_t s);                          \
     int fft_adj_blocks_##L_(long long nl);                                                             \
     cudaError_t fft_init_##L_();                                                                       \
+    cudaError_t fft_toep_x_##L_(const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch, \
+                                cudaStream_t s);                                                       \
     CGS_DEFINE_IF_##G_(L_, R1_, R2_)
 
 #define CGS_BODY(L_, R1_, R2_)                                                                      \
@@ -169,7 +202,10 @@ struct SizeImpl {
     cudaError_t fft_adj_z_##L_(const AdjZArgs& a, int batch, cudaStream_t s)                           \
     { return SizeImpl<R1_, R2_>::adj_z(a, batch, s); }                                              \
     int fft_adj_blocks_##L_(long long nl) { return SizeImpl<R1_, R2_>::adj_blocks(nl); }               \
-    cudaError_t fft_init_##L_() { return SizeImpl<R1_, R2_>::init(); }
+    cudaError_t fft_init_##L_() { return SizeImpl<R1_, R2_>::init(); }                                 \
+    cudaError_t fft_toep_x_##L_(const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch, \
+                                cudaStream_t s)                                                        \
+    { return SizeImpl<R1_, R2_>::toep_x(a, P, p_bs, nsub, batch, s); }
 
 #if CGS_FFT_GROUP == 0
 #define CGS_DEFINE_IF_0(L, R1, R2) CGS_BODY(L, R1, R2)

@@ -324,6 +324,156 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
 }
 
 // ---------------------------------------------------------------------------
+// Toeplitz x stage, in place on the [items][Lin][B] buffer of the forward y
+// pass: the forward x transform of a tile's L/2 stored rows (rows L/4 ..
+// 3L/4 of the line), the product with the real spectrum P of the tile's bin,
+// and the adjoint x transform of which the same L/2 rows are stored back.
+//   stage 1: thread n2: R1-point DFT over n1 (rows R2 n1 + n2), W^(-n2 k1)
+//            -> Y[k1][n2]
+//   stage 2: thread k1: R2-point DFT over n2 -> X[k1 + R1 k2]; X *= P; the
+//            R2-point inverse DFT over k2 -> Z[n2]; W^(+n2 k1) -> Y'[n2][k1]
+//   stage 3: thread n2: R1-point inverse DFT over k1 -> row n2 + R2 n1
+// The centring sign (-1)^k of the forward output and that of the adjoint
+// input cancel; the rows keep theirs.  Tiles t -> (sub-item t % nsub,
+// column strip, bin): the nsub tiles of one strip run back to back, so that
+// the strip of P they share comes from DRAM once.  Pipeline, bounded waits
+// and the timeout exit are those of k_fft_strided_tma.
+// ---------------------------------------------------------------------------
+template <int R1, int R2, int TB, int NSTAGE>
+__global__ void __launch_bounds__(PipeLayout<R1, R2, TB, NSTAGE>::NT, 2)
+k_toep_x_tma(StridedPassArgs a, const float* __restrict__ P, long long p_bs, int nsub,
+             const __grid_constant__ CUtensorMap tmap, long long ntiles, int box_rows)
+{
+    constexpr int L = R1 * R2;
+    constexpr int NT = PipeLayout<R1, R2, TB, NSTAGE>::NT;
+    static_assert(R1 % 4 == 0, "the stored rows L/4 .. 3L/4 need R1 % 4 == 0");
+    extern __shared__ float4 s_pipe[];
+    const uintptr_t base = (reinterpret_cast<uintptr_t>(s_pipe) + 1023) & ~(uintptr_t)1023;
+    const int stage_elems = a.Lin * TB;
+    float2* s_in = reinterpret_cast<float2*>(base);
+    float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
+    float2* s_tw = s_y + L * TB;
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + 2 * L);
+    const int tid = threadIdx.x;
+    for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
+    if (tid == 0) {
+        for (int s = 0; s < NSTAGE; ++s) mbar_init(&s_bar[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const long long my_n = ntiles > (long long)blockIdx.x ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+
+    auto decode = [&](long long t, long long& item, long long& bin, int& b0) {
+        const long long strip = t / nsub;
+        const int sub = (int)(t - strip * nsub);
+        bin = strip / a.ntb;
+        b0 = (int)(strip - bin * a.ntb) * TB;
+        item = bin * nsub + sub;
+    };
+    auto issue = [&](long long k) {   // thread 0 only
+        const long long t = blockIdx.x + k * gridDim.x;
+        long long item, bin;
+        int b0;
+        decode(t, item, bin, b0);
+        const int s = (int)(k % NSTAGE);
+        mbar_arrive_expect_tx(&s_bar[s], (uint32_t)(stage_elems * sizeof(float2)));
+        float2* dst = s_in + (size_t)s * stage_elems;
+        for (int r0 = 0; r0 < a.Lin; r0 += box_rows)
+            tma_load_4d(dst + (size_t)r0 * TB, &tmap, b0, r0, 0, (int)item, &s_bar[s]);
+    };
+
+    if (tid == 0)
+        for (long long k = 0; k < NSTAGE - 1 && k < my_n; ++k) issue(k);
+    for (long long k = 0; k < my_n; ++k) {
+        const int s = (int)(k % NSTAGE);
+        if (tid == 0 && k + NSTAGE - 1 < my_n) issue(k + NSTAGE - 1);
+        const long long t = blockIdx.x + k * gridDim.x;
+        long long item, bin;
+        int b0;
+        decode(t, item, bin, b0);
+        const int bi = tid % TB;
+        const int b = b0 + bi;
+        const bool bok = b < a.B;
+        // the tile's column strip of P (rows k1 + R1 k2), requested before the wait
+        const int k1 = tid / TB;
+        float pv[R2];
+        {
+            const float* pr = P + bin * p_bs + (long long)k1 * a.B + b;
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) pv[k2] = (k1 < R1 && bok) ? __ldg(pr + (long long)R1 * k2 * a.B) : 0.f;
+        }
+        const bool ok = mbar_wait_bounded(&s_bar[s], (uint32_t)((k / NSTAGE) & 1), PIPE_WAIT_NS);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicExch(a.err, 1);
+                for (long long j = k; j < my_n && j < k + NSTAGE; ++j)
+                    mbar_wait_bounded(&s_bar[j % NSTAGE], (uint32_t)((j / NSTAGE) & 1), PIPE_WAIT_NS);
+            }
+            return;
+        }
+        const float2* sin_s = s_in + (size_t)s * stage_elems;
+        {
+            const int n2 = tid / TB;
+            if (n2 < R2) {
+                float2 v[R1];
+                const float2* src = sin_s + n2 * TB + bi;
+#pragma unroll
+                for (int n1 = 0; n1 < R1; ++n1) {
+                    if (n1 >= R1 / 4 && n1 < 3 * R1 / 4)
+                        v[n1] = parity(src[(R2 * (n1 - R1 / 4)) * TB], R2 * n1 + n2);
+                    else
+                        v[n1] = make_float2(0.f, 0.f);
+                }
+                Dft<R1, -1>::run(v);
+#pragma unroll
+                for (int q = 0; q < R1; ++q) {
+                    float2 tv = v[q];
+                    if (q > 0) tv = table_twiddle<-1>(tv, s_tw[n2 * q]);
+                    s_y[(q * R2 + n2) * TB + bi] = tv;
+                }
+            }
+        }
+        __syncthreads();
+        float2 u[R2];
+        if (k1 < R1) {
+#pragma unroll
+            for (int n2 = 0; n2 < R2; ++n2) u[n2] = s_y[(k1 * R2 + n2) * TB + bi];
+            Dft<R2, -1>::run(u);
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) {
+                u[k2].x *= pv[k2];
+                u[k2].y *= pv[k2];
+            }
+            Dft<R2, +1>::run(u);
+#pragma unroll
+            for (int n2 = 1; n2 < R2; ++n2) u[n2] = table_twiddle<+1>(u[n2], s_tw[n2 * k1]);
+        }
+        __syncthreads();
+        if (k1 < R1) {
+#pragma unroll
+            for (int n2 = 0; n2 < R2; ++n2) s_y[(n2 * R1 + k1) * TB + bi] = u[n2];
+        }
+        __syncthreads();
+        {
+            const int n2 = tid / TB;
+            if (n2 < R2) {
+                float2 w[R1];
+#pragma unroll
+                for (int q = 0; q < R1; ++q) w[q] = s_y[(n2 * R1 + q) * TB + bi];
+                Dft<R1, +1>::run(w);
+                if (bok) {
+                    float2* out = a.out + item * a.out_bs + b;
+#pragma unroll
+                    for (int n1 = R1 / 4; n1 < 3 * R1 / 4; ++n1)
+                        out[(long long)(n2 + R2 * (n1 - R1 / 4)) * a.B] = parity(w[n1], n2 + R2 * n1);
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Contiguous passes (z axis): LPB whole lines per block.
 // Shared layout per line: Y[n2][k1] with an odd row pitch (conflict-free).
 // ---------------------------------------------------------------------------

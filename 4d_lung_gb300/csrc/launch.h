@@ -4,6 +4,7 @@
 #include "cgs_types.h"
 #include <cufft.h>
 #include <cuda.h>
+#include <string>
 
 namespace cgs {
 
@@ -115,6 +116,20 @@ cudaError_t launch_lowpass_weights(const double* k, const int* sorted, long long
 // imgs [nch][n] coil images -> maps in place; rss_tmp [n], max_tmp one word
 cudaError_t launch_smaps_from_images(float2* imgs, int nch, long long n, float eps, float* rss_tmp,
                                      unsigned* max_tmp, cudaStream_t s);
+
+// Toeplitz embedding of E^H D E (toeplitz.cu, fft_inst.cu).  toeplitz_build
+// accumulates one bin's P with cuBLAS over chunks of toeplitz_chunk samples
+// (work: work_elems floats); returns 0 on success, else sets *err.
+long long toeplitz_chunk(const int G[3], long long work_elems);
+int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, cudaStream_t s, std::string* err);
+// grid[item][j] *= P[item / nch][j] over items grids of Ng points
+cudaError_t launch_toep_mul(float2* grid, const float* P, long long Ng, int nch, int items, cudaStream_t s);
+// Fused x stage in place: forward x transform of the Lin = L/2 stored rows,
+// multiply by P (bin of item = item / nsub, bin stride p_bs), adjoint x
+// transform, the L/2 kept rows stored over the input.  cudaErrorNotSupported
+// when the pass does not apply (line length, pruning, alignment).
+cudaError_t launch_toep_x(int L, const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch,
+                          cudaStream_t s);
 
 // File IO (io.cu)
 cudaError_t launch_scale_samples(float2* data, const float* d, long long ns, int nch, cudaStream_t s);

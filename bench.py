@@ -431,6 +431,61 @@ def differentiation_report(cgs, synth, torch, dev, stream_handle, steps=50):
     }
 
 
+def toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, steps, w, sizes):
+    """The same batched solve with the Toeplitz embedding of E^H D E
+    (cgs_set_toeplitz): the spectra's build time, the timed reconstruction,
+    the per-stage times of one application and its images against the
+    gridded solve's (the operators differ by the gridding error).  The
+    library is left on the gridded operator."""
+    nb = len(sizes)
+    reco.set_toeplitz(1)
+    try:
+        build_ms, pbytes = reco.toeplitz_stats()
+        xt = torch.zeros_like(x)
+        for _ in range(3):
+            reco.cg_sense_batched_tensor(data, xt, 0.0, iters, want_stats=False)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            reco.cg_sense_batched_tensor(data, xt, 0.0, iters, want_stats=False)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        res, its = reco.cg_sense_batched_tensor(data, xt, 0.0, iters, want_stats=True)
+        launches = reco.launch_count()
+        rel = float(torch.linalg.vector_norm(xt - x) / torch.linalg.vector_norm(x))
+        xa = torch.from_numpy(np.stack([synth.phantom(w.img)] * nb)).to(dev)
+        qa = torch.empty_like(xa)
+        reps = [reco.profile_apply_tensor(xa, qa, 0, nb) for _ in range(5)]
+        st = np.median(np.stack(reps), axis=0)
+        names = ["fwd_z", "fwd_y", "toep_x", "adj_y", "adj_z"]
+        groups = len(st) // len(names)
+        stage_ms = {s: float(sum(st[g * len(names) + i] for g in range(groups))) for i, s in enumerate(names)}
+        sb = stage_bytes(w, sizes)
+        Ix, Gy, Gz = w.img[0], w.grid[1], w.grid[2]
+        ng = int(np.prod(w.grid))
+        tb = {"fwd_z": sb["fwd_z"], "fwd_y": sb["fwd_y"], "adj_y": sb["adj_y"], "adj_z": sb["adj_z"],
+              "toep_x": nb * (2 * 8 * w.n_ch * Ix * Gy * Gz + 4 * ng)}
+        peak, _ = measured_peaks()
+        apply_ms = float(sum(stage_ms.values()))
+        return {
+            "operator": "Toeplitz embedding: crop F_c^H (P_b . F_c pad(S_c x)), P_b the real spectrum of bin b's "
+                        "point-spread function (exact normal operator; no gridding inside CG)",
+            "spectra_build_s": build_ms / 1e3, "spectra_bytes": pbytes,
+            "s_per_4d_recon": ms / 1e3, "applies_per_s": nb * iters / (ms / 1e3),
+            "launches_per_recon": launches,
+            "iters": [int(v) for v in its], "final_residual_rel": [float(r[-1] / r[0]) for r in res],
+            "rel_l2_vs_gridded_solve": rel,
+            "apply_ms": apply_ms, "stage_ms": stage_ms,
+            "stage_frac_of_peak": {s: tb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
+            "apply_achieved_gbs": (sum(tb.values()) + 56 * int(np.prod(w.img)) * nb) / (apply_ms / 1e3) / 1e9,
+        }
+    finally:
+        reco.set_toeplitz(0)
+
+
 def run_diff_only(args):
     """The differentiation form alone (cfg4), one JSON line."""
     import torch
@@ -673,6 +728,12 @@ def run_ours(args):
         diff = differentiation_report(cgs, synth, torch, dev, stream.cuda_stream)
 
 
+    # the Toeplitz-embedded operator on the same solve (an alternative
+    # operator for fixed trajectories; not the headline form)
+    toep = None
+    if not args.no_toeplitz:
+        toep = toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, max(1, args.steps), w, sizes)
+
     # per-stage kernel times of one batched application (roofline)
     xa = torch.from_numpy(np.stack([synth.phantom(w.img)] * nb)).to(dev)
     qa = torch.empty_like(xa)
@@ -743,6 +804,7 @@ def run_ours(args):
         "autotune": tune,
         "differentiation": diff,
         "plain": plain,
+        "toeplitz": toep,
     }
     if rank == 0 and not args.no_cpu:
         cb = cpu_apply_sample(synth, args.workload)
@@ -770,6 +832,7 @@ def main():
     ap.add_argument("--nondeterministic", action="store_true",
                     help="let the autotuner pick atomic spreading (results not bitwise reproducible)")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiation form (cfg4)")
+    ap.add_argument("--no-toeplitz", action="store_true", help="skip the Toeplitz-embedded solve")
     ap.add_argument("--diff-only", action="store_true", help="only the differentiation form (one JSON line)")
     ap.add_argument("--cg-grad-only", action="store_true",
                     help="only the unrolled-CG trajectory gradient of the combined workload (cfg5)")

@@ -328,6 +328,27 @@ int cgs_set_launch_shape(cgs_ctx* ctx, int32_t spread_cc, int32_t spread_variant
  * Fourier.cpp:19-42). */
 int cgs_set_support_pruning(cgs_ctx* ctx, int32_t on);
 
+/* Toeplitz embedding of E^H D E (fixed trajectory): mode 1 replaces the
+ * gridded normal operator inside cgs_apply_ehde* and the CG solvers by
+ *   q = s sum_c conj(S_c) crop F_c^H (P_b . F_c pad(S_c x)),
+ * P_b the real spectrum of bin b's point-spread function
+ *   h(d) = sum_i D_i exp(2 pi i nu_i . d),  nu_ia = (k_ia (G_a - 1) - G_a / 2) / G_a,
+ * on the oversampled grid (needs G_a >= 2 I_a - 1), s the adjoint scale:
+ * the exact non-uniform DFT's normal operator, with no gridding inside the
+ * CG loop.  It differs from the gridded operator by the gridding error
+ * (about 1e-3 relative at kernel width 4 and 2x oversampling).  The
+ * right-hand side stays the gridded adjoint of the data; the trajectory
+ * derivatives keep the gridded operator.  The spectra (4 bytes per grid
+ * point and bin) are built from the current coordinates, bins and density
+ * weights (one FP32 matrix product per chunk of samples, cuBLAS opened at
+ * run time) and rebuilt after any of them changes.  Mode 2: the same
+ * operator with the x stage unfused (forward x pass, multiply, adjoint x
+ * pass; for comparison).  Mode 0 (default): the gridded operator. */
+int cgs_set_toeplitz(cgs_ctx* ctx, int32_t mode);
+/* Time of the last spectrum build (ms) and the bytes the spectra hold (0
+ * while not built). */
+int cgs_toeplitz_stats(cgs_ctx* ctx, double* build_ms, int64_t* bytes);
+
 /* Coil sensitivity maps from the measured data of a single-bin context
  * (device pointers; data [n_ch][ns] in the reference's order, maps
  * [n_ch][img]): the adjoint NUFFT of each coil's samples weighted by a Hann

@@ -217,6 +217,86 @@ class Oracle:
 
 
 # ---------------------------------------------------------------------------
+# Exact normal operator (numpy, FP64): the operator that the Toeplitz
+# embedding computes and that the gridded operator approximates.  Small
+# problems only (a dense samples x voxels matrix).
+# ---------------------------------------------------------------------------
+
+def sample_frequencies(k, grid):
+    """nu = (k (G - 1) - G/2) / G per axis: the cycles per grid cell of each
+    sample in the exact non-uniform DFT that the gridded forward operator
+    approximates, exp(-2 pi i nu . (r + lo - G/2)) (k in [0, 1] maps to grid
+    coordinate k (G - 1), Reco.cpp:698-806; the FFT centre is G/2,
+    Fourier.cpp:19-42)."""
+    G = np.asarray(grid, np.float64)
+    return (np.asarray(k, np.float64) * (G - 1) - G / 2) / G
+
+
+def exact_normal(k, img, grid, smaps, dcf, x, adj_scale=ADJ_SCALE):
+    """q = s sum_c conj(S_c) E^H D E (S_c x) with E the exact non-uniform DFT
+    and s = adj_scale / sqrt(N_grid), the adjoint scale of the gridded
+    operator (Reco.cpp:482, Fourier.cpp:34)."""
+    nu = sample_frequencies(k, grid)
+    r = np.stack(np.meshgrid(*[np.arange(n) for n in img], indexing="ij"), -1).reshape(-1, 3)
+    E = np.exp(-2j * np.pi * (nu @ r.T))
+    d = np.ones(nu.shape[0]) if dcf is None else np.asarray(dcf, np.float64)
+    s = adj_scale / np.sqrt(np.prod(grid))
+    q = np.zeros(tuple(img), np.complex128)
+    for c in range(smaps.shape[0]):
+        v = (smaps[c] * x).ravel()
+        q += np.conj(smaps[c]) * (s * (E.conj().T @ (d * (E @ v)))).reshape(img)
+    return q
+
+
+def toeplitz_spectrum(k, img, grid, dcf, adj_scale=ADJ_SCALE):
+    """Real spectrum P on the grid such that crop F_c^H (P . F_c pad(.)) is
+    s E^H D E, F_c the centred unscaled transform: per axis the Dirichlet
+    kernel K(psi) = sum_{|d| < I} exp(2 pi i psi d) at psi = nu - k/G + 1/2,
+    P = s / N_grid sum_i D_i Kx Ky Kz."""
+    nu = sample_frequencies(k, grid)
+    d = np.ones(nu.shape[0]) if dcf is None else np.asarray(dcf, np.float64)
+    K = []
+    for a in range(3):
+        e = nu[:, a:a + 1] - np.arange(grid[a])[None, :] / grid[a] + 0.5
+        e = e - np.floor(e + 0.5)
+        m = 2 * img[a] - 1
+        with np.errstate(invalid="ignore", divide="ignore"):
+            v = np.sin(m * np.pi * e) / np.sin(np.pi * e)
+        v[e == 0.0] = m
+        K.append(v)
+    s = adj_scale / np.sqrt(np.prod(grid))
+    return np.einsum("i,ia,ib,ic->abc", d, K[0], K[1], K[2]) * (s / np.prod(grid))
+
+
+def centred_fft_np(a, sign):
+    """Fourier::transformFWD (sign -1) / transformBWD (+1) without scaling:
+    (-1)^n before and (-1)^k after an unnormalised transform on each axis."""
+    out = np.asarray(a, np.complex128)
+    for ax in range(out.ndim):
+        n = out.shape[ax]
+        shp = [1] * out.ndim
+        shp[ax] = n
+        sg = ((-1.0) ** np.arange(n)).reshape(shp)
+        out = out * sg
+        out = np.fft.fft(out, axis=ax) if sign < 0 else np.fft.ifft(out, axis=ax) * n
+        out = out * sg
+    return out
+
+
+def toeplitz_apply(P, img, grid, smaps, x):
+    """q = sum_c conj(S_c) crop F_c^H (P . F_c pad(S_c x)), the image centred
+    in the grid at lo = (G - I) / 2."""
+    lo = [(g - i) // 2 for g, i in zip(grid, img)]
+    box = tuple(slice(l, l + i) for l, i in zip(lo, img))
+    q = np.zeros(tuple(img), np.complex128)
+    for c in range(smaps.shape[0]):
+        pad = np.zeros(tuple(grid), np.complex128)
+        pad[box] = smaps[c] * x
+        q += np.conj(smaps[c]) * centred_fft_np(P * centred_fft_np(pad, -1), +1)[box]
+    return q
+
+
+# ---------------------------------------------------------------------------
 # Reference driver runner (only where the reference sources were compiled)
 # ---------------------------------------------------------------------------
 

@@ -82,3 +82,38 @@ def test_nudft_known_answer(oracle_mod, o64, kb_w, kb_b, tol):
     assert abs(scale.imag) < 1e-3
     assert abs(scale.real - 1.0) < 5e-2
     assert rel_l2(e, scale.real * exact) < tol
+
+
+@pytest.mark.parametrize("img,grid", [((16, 12, 8), (32, 24, 16)), ((10, 8, 6), (20, 16, 12))])
+def test_toeplitz_embedding_is_exact(oracle_mod, img, grid):
+    """The Toeplitz form crop F_c^H (P . F_c pad(.)) with the Dirichlet-kernel
+    spectrum equals the exact normal operator s E^H D E (FP64 rounding)."""
+    rng = np.random.default_rng(11)
+    ns, nch = 300, 2
+    k = rng.uniform(0.05, 0.95, (ns, 3))
+    dcf = rng.uniform(0.5, 1.5, ns)
+    smaps = rng.standard_normal((nch,) + img) + 1j * rng.standard_normal((nch,) + img)
+    x = rng.standard_normal(img) + 1j * rng.standard_normal(img)
+    P = oracle_mod.toeplitz_spectrum(k, img, grid, dcf)
+    q_t = oracle_mod.toeplitz_apply(P, img, grid, smaps, x)
+    q_e = oracle_mod.exact_normal(k, img, grid, smaps, dcf, x)
+    assert rel_l2(q_t, q_e) < 1e-12
+
+
+def test_gridded_normal_operator_vs_exact(oracle_mod, o64):
+    """The gridded E^H D E (KB width 4, 2x oversampling, the Beatty shape)
+    approximates the exact normal operator to its gridding error."""
+    img, grid = (16, 12, 8), (32, 24, 16)
+    rng = np.random.default_rng(5)
+    ns, nch = 500, 2
+    k = rng.uniform(0.1, 0.9, (ns, 3))
+    w = 4.0
+    p = oracle_mod.make_params(img, grid, nch, kb_w=w, kb_b=np.pi * np.sqrt(w ** 2 / 4 * 1.5 ** 2 - 0.8))
+    taps = o64.taps(p, k)
+    smaps = rng.standard_normal((nch,) + img) + 1j * rng.standard_normal((nch,) + img)
+    dcf = rng.uniform(0.5, 1.5, ns).astype(np.float32)
+    x = rng.standard_normal(img) + 1j * rng.standard_normal(img)
+    q_g = o64.apply_ehde(p, taps, o64.kernel_ft(p), smaps, dcf, x)
+    q_e = oracle_mod.exact_normal(k, img, grid, smaps, dcf.astype(np.float64), x)
+    err = rel_l2(q_g, q_e)
+    assert 1e-5 < err < 5e-3
