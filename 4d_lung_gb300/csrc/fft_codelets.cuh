@@ -129,4 +129,63 @@ struct Dft {
     }
 };
 
+// Dft<N, SIGN> of a vector whose entries outside [N/4, 3N/4) are zero (the
+// zero-padded half of a 2x oversampled line), N a multiple of 4.  With the
+// radix-4 first level n = q n1 + n2 (q = N/4) the non-zero inputs are
+// n1 = 1, 2, and each 4-point DFT of (0, a, b, 0),
+//   X_0 = a + b,  X_1 = SIGN i a - b,  X_2 = b - a,  X_3 = -SIGN i a - b,
+// takes four complex additions instead of eight (an addition of a zero is
+// not removed by the compiler, as x + 0 differs from x for x = -0).  The
+// results equal Dft<N, SIGN>'s up to the sign of zeros.
+template <int SIGN>
+CGS_D void dft4_mid(float2 a, float2 b, float2 (&o)[4])
+{
+    const float2 ia = (SIGN < 0) ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);   // SIGN i a
+    o[0] = cadd(a, b);
+    o[1] = csub(ia, b);
+    o[2] = csub(b, a);
+    o[3] = make_float2(-ia.x - b.x, -ia.y - b.y);
+}
+
+template <int N, int SIGN>
+struct DftMid {
+    static_assert(N % 4 == 0, "the zero pattern needs N % 4 == 0");
+    static CGS_D void run(float2 (&v)[N])
+    {
+        constexpr int q = N / 4;
+        if constexpr (q == 1) {
+            float2 o[4];
+            dft4_mid<SIGN>(v[1], v[2], o);
+            static_for<0, 4>([&](auto k_) {
+                constexpr int k = decltype(k_)::value;
+                v[k] = o[k];
+            });
+        } else {
+            float2 t[N];
+            static_for<0, q>([&](auto n2_) {
+                constexpr int n2 = decltype(n2_)::value;
+                float2 a[4];
+                dft4_mid<SIGN>(v[q + n2], v[2 * q + n2], a);
+                static_for<0, 4>([&](auto k1_) {
+                    constexpr int k1 = decltype(k1_)::value;
+                    t[n2 * 4 + k1] = twiddle_const<SIGN, n2 * k1, N>(a[k1]);
+                });
+            });
+            static_for<0, 4>([&](auto k1_) {
+                constexpr int k1 = decltype(k1_)::value;
+                float2 b[q];
+                static_for<0, q>([&](auto n2_) {
+                    constexpr int n2 = decltype(n2_)::value;
+                    b[n2] = t[n2 * 4 + k1];
+                });
+                Dft<q, SIGN>::run(b);
+                static_for<0, q>([&](auto k2_) {
+                    constexpr int k2 = decltype(k2_)::value;
+                    v[k1 + 4 * k2] = b[k2];
+                });
+            });
+        }
+    }
+};
+
 }  // namespace cgs

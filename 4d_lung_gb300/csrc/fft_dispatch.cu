@@ -77,6 +77,28 @@ bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int b
     return true;
 }
 
+bool encode_spectrum_map(CUtensorMap* map, const float* P, long long B, int L, int nbins, int TB, int* box_rows)
+{
+    // rows of 4-byte elements: base and row pitch on 16-byte boundaries
+    if ((reinterpret_cast<uintptr_t>(P) & 15) || (B & 3) || nbins < 1) return false;
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    int br = L;
+    if (br > 256)
+        for (br = 256; br > 1 && L % br != 0; --br) {
+        }
+    const cuuint64_t dims[3] = {(cuuint64_t)B, (cuuint64_t)L, (cuuint64_t)nbins};
+    const cuuint64_t strides[2] = {(cuuint64_t)B * 4, (cuuint64_t)B * L * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)TB, (cuuint32_t)br, 1};
+    const cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(P), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return false;
+    *box_rows = br;
+    return true;
+}
+
 bool fft_supported(int L)
 {
     for (int s : kSizes)

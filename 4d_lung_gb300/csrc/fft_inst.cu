@@ -66,7 +66,7 @@ struct SizeImpl {
         if constexpr (HAS_IN)
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(k_toep_x_tma<R1, R2, TB, NSTAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         smem);
+                                         (int)ToepLayout<R1, R2, TB, NSTAGE>::smem_bytes(L / 2));
         // the z extent of an image never exceeds the grid's: size for Iz = L
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_fwd_z_pipe<R1, R2, LPB, ZNST_F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -127,24 +127,26 @@ struct SizeImpl {
         if constexpr (!HAS_IN) {
             return cudaErrorNotSupported;
         } else {
+            using Lay = ToepLayout<R1, R2, TB, NSTAGE>;
             a.ntb = (a.B + TB - 1) / TB;
             if (4 * a.in_off != L || 2 * a.Lin != L || 4 * a.out_off != L || 2 * a.Lout != L || !a.err || nsub < 1 ||
-                batch % nsub != 0)
+                batch % nsub != 0 || p_bs != (long long)L * a.B)
                 return cudaErrorNotSupported;
-            CUtensorMap map;
-            int box_rows = 0;
+            CUtensorMap map, pmap;
+            int box_rows = 0, pbox_rows = 0;
             if (!encode_strided_map(&map, a, 1, batch, TB, &box_rows)) return cudaErrorNotSupported;
-            const size_t smem = Pipe::smem_bytes(a.Lin);
+            if (!encode_spectrum_map(&pmap, P, a.B, L, batch / nsub, TB, &pbox_rows)) return cudaErrorNotSupported;
+            const size_t smem = Lay::smem_bytes(a.Lin);
             int per_sm = 0;
             cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_toep_x_tma<R1, R2, TB, NSTAGE>,
-                                                                          Pipe::NT, smem);
+                                                                          Lay::NT, smem);
             if (e != cudaSuccess) return e;
             const long long ntiles = (long long)a.ntb * batch;
             if (ntiles <= 0) return cudaSuccess;
             long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
             if (nblk > ntiles) nblk = ntiles;
-            k_toep_x_tma<R1, R2, TB, NSTAGE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(a, P, p_bs, nsub, map, ntiles,
-                                                                                   box_rows);
+            k_toep_x_tma<R1, R2, TB, NSTAGE><<<(unsigned)nblk, Lay::NT, smem, s>>>(a, nsub, map, pmap, ntiles, box_rows,
+                                                                                  pbox_rows);
             return cudaGetLastError();
         }
     }

@@ -248,6 +248,7 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
                             v[n1] = make_float2(0.f, 0.f);
                         }
                     }
+                    DftMid<R1, SIGN>::run(v);
                 } else {
 #pragma unroll
                     for (int n1 = 0; n1 < R1; ++n1) {
@@ -257,8 +258,8 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
                         if (li >= 0 && li < a.Lin) x = sin_s[li * TB + bi];
                         v[n1] = FOLD ? x : parity(x, l);
                     }
+                    Dft<R1, SIGN>::run(v);
                 }
-                Dft<R1, SIGN>::run(v);
 #pragma unroll
                 for (int k1 = 0; k1 < R1; ++k1) {
                     float2 tv = v[k1];
@@ -334,26 +335,41 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
 //            R2-point inverse DFT over k2 -> Z[n2]; W^(+n2 k1) -> Y'[n2][k1]
 //   stage 3: thread n2: R1-point inverse DFT over k1 -> row n2 + R2 n1
 // The centring sign (-1)^k of the forward output and that of the adjoint
-// input cancel; the rows keep theirs.  Tiles t -> (sub-item t % nsub,
-// column strip, bin): the nsub tiles of one strip run back to back, so that
-// the strip of P they share comes from DRAM once.  Pipeline, bounded waits
-// and the timeout exit are those of k_fft_strided_tma.
+// input cancel; the rows keep theirs.  A pipeline stage holds the tile's
+// rows (4-D map over the buffer) and its strip of P (3-D map [bins][L][B],
+// 4-byte elements), both fetched by the TMA unit NSTAGE - 1 tiles ahead on
+// one mbarrier.  Tiles t -> (sub-item t % nsub, column strip, bin): the nsub
+// tiles of one strip run back to back, so that the strip of P they share
+// comes from DRAM once.  Bounded waits and the timeout exit are those of
+// k_fft_strided_tma.
 // ---------------------------------------------------------------------------
 template <int R1, int R2, int TB, int NSTAGE>
-__global__ void __launch_bounds__(PipeLayout<R1, R2, TB, NSTAGE>::NT, 2)
-k_toep_x_tma(StridedPassArgs a, const float* __restrict__ P, long long p_bs, int nsub,
-             const __grid_constant__ CUtensorMap tmap, long long ntiles, int box_rows)
+struct ToepLayout {
+    static constexpr int L = R1 * R2;
+    static constexpr int NT = TB * (R1 > R2 ? R1 : R2);
+    static size_t smem_bytes(int Lin)
+    {
+        return 1024 + (size_t)NSTAGE * Lin * TB * sizeof(float2) + (size_t)NSTAGE * L * TB * sizeof(float) +
+               (size_t)L * TB * sizeof(float2) + (size_t)L * sizeof(float2) + NSTAGE * sizeof(uint64_t);
+    }
+};
+
+template <int R1, int R2, int TB, int NSTAGE>
+__global__ void __launch_bounds__(ToepLayout<R1, R2, TB, NSTAGE>::NT, 2)
+k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tmap,
+             const __grid_constant__ CUtensorMap pmap, long long ntiles, int box_rows, int pbox_rows)
 {
     constexpr int L = R1 * R2;
-    constexpr int NT = PipeLayout<R1, R2, TB, NSTAGE>::NT;
+    constexpr int NT = ToepLayout<R1, R2, TB, NSTAGE>::NT;
     static_assert(R1 % 4 == 0, "the stored rows L/4 .. 3L/4 need R1 % 4 == 0");
     extern __shared__ float4 s_pipe[];
     const uintptr_t base = (reinterpret_cast<uintptr_t>(s_pipe) + 1023) & ~(uintptr_t)1023;
     const int stage_elems = a.Lin * TB;
     float2* s_in = reinterpret_cast<float2*>(base);
-    float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
+    float* s_p = reinterpret_cast<float*>(s_in + (size_t)NSTAGE * stage_elems);
+    float2* s_y = reinterpret_cast<float2*>(s_p + (size_t)NSTAGE * L * TB);
     float2* s_tw = s_y + L * TB;
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + 2 * L);
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
     const int tid = threadIdx.x;
     for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
     if (tid == 0) {
@@ -376,10 +392,12 @@ k_toep_x_tma(StridedPassArgs a, const float* __restrict__ P, long long p_bs, int
         int b0;
         decode(t, item, bin, b0);
         const int s = (int)(k % NSTAGE);
-        mbar_arrive_expect_tx(&s_bar[s], (uint32_t)(stage_elems * sizeof(float2)));
+        mbar_arrive_expect_tx(&s_bar[s], (uint32_t)(stage_elems * sizeof(float2) + L * TB * sizeof(float)));
         float2* dst = s_in + (size_t)s * stage_elems;
         for (int r0 = 0; r0 < a.Lin; r0 += box_rows)
             tma_load_4d(dst + (size_t)r0 * TB, &tmap, b0, r0, 0, (int)item, &s_bar[s]);
+        float* pdst = s_p + (size_t)s * L * TB;
+        for (int r0 = 0; r0 < L; r0 += pbox_rows) tma_load_3d(pdst + (size_t)r0 * TB, &pmap, b0, r0, (int)bin, &s_bar[s]);
     };
 
     if (tid == 0)
@@ -387,21 +405,6 @@ k_toep_x_tma(StridedPassArgs a, const float* __restrict__ P, long long p_bs, int
     for (long long k = 0; k < my_n; ++k) {
         const int s = (int)(k % NSTAGE);
         if (tid == 0 && k + NSTAGE - 1 < my_n) issue(k + NSTAGE - 1);
-        const long long t = blockIdx.x + k * gridDim.x;
-        long long item, bin;
-        int b0;
-        decode(t, item, bin, b0);
-        const int bi = tid % TB;
-        const int b = b0 + bi;
-        const bool bok = b < a.B;
-        // the tile's column strip of P (rows k1 + R1 k2), requested before the wait
-        const int k1 = tid / TB;
-        float pv[R2];
-        {
-            const float* pr = P + bin * p_bs + (long long)k1 * a.B + b;
-#pragma unroll
-            for (int k2 = 0; k2 < R2; ++k2) pv[k2] = (k1 < R1 && bok) ? __ldg(pr + (long long)R1 * k2 * a.B) : 0.f;
-        }
         const bool ok = mbar_wait_bounded(&s_bar[s], (uint32_t)((k / NSTAGE) & 1), PIPE_WAIT_NS);
         if (__syncthreads_or(!ok)) {
             if (tid == 0) {
@@ -411,7 +414,15 @@ k_toep_x_tma(StridedPassArgs a, const float* __restrict__ P, long long p_bs, int
             }
             return;
         }
+        const long long t = blockIdx.x + k * gridDim.x;
+        long long item, bin;
+        int b0;
+        decode(t, item, bin, b0);
+        const int bi = tid % TB;
+        const int b = b0 + bi;
+        const bool bok = b < a.B;
         const float2* sin_s = s_in + (size_t)s * stage_elems;
+        const float* sp = s_p + (size_t)s * L * TB;
         {
             const int n2 = tid / TB;
             if (n2 < R2) {
@@ -424,7 +435,7 @@ k_toep_x_tma(StridedPassArgs a, const float* __restrict__ P, long long p_bs, int
                     else
                         v[n1] = make_float2(0.f, 0.f);
                 }
-                Dft<R1, -1>::run(v);
+                DftMid<R1, -1>::run(v);
 #pragma unroll
                 for (int q = 0; q < R1; ++q) {
                     float2 tv = v[q];
@@ -434,6 +445,7 @@ k_toep_x_tma(StridedPassArgs a, const float* __restrict__ P, long long p_bs, int
             }
         }
         __syncthreads();
+        const int k1 = tid / TB;
         float2 u[R2];
         if (k1 < R1) {
 #pragma unroll
@@ -441,8 +453,9 @@ k_toep_x_tma(StridedPassArgs a, const float* __restrict__ P, long long p_bs, int
             Dft<R2, -1>::run(u);
 #pragma unroll
             for (int k2 = 0; k2 < R2; ++k2) {
-                u[k2].x *= pv[k2];
-                u[k2].y *= pv[k2];
+                const float pv = sp[(k1 + R1 * k2) * TB + bi];
+                u[k2].x *= pv;
+                u[k2].y *= pv;
             }
             Dft<R2, +1>::run(u);
 #pragma unroll

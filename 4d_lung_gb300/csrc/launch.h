@@ -16,6 +16,9 @@ cudaError_t fft_init_all();
 // 4-D tensor map [batch][A][Lin][B] of a strided pass's input with a
 // TB x box_rows box; false when the buffer or strides are not 16-byte aligned
 bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int batch, int TB, int* box_rows);
+// 3-D tensor map [nbins][L][B] of 4-byte spectrum values with a TB x
+// box_rows box; false when the buffer or pitch is not 16-byte aligned
+bool encode_spectrum_map(CUtensorMap* map, const float* P, long long B, int L, int nbins, int TB, int* box_rows);
 const int* fft_supported_list(int* n);
 // columns per tile of the strided passes of line length L (0: unsupported)
 int fft_strided_cols(int L);

@@ -1,5 +1,6 @@
 // ptx_async.cuh -- inline-PTX wrappers for the asynchronous copy engine
-// (cp.async.bulk global -> shared with mbarrier completion) used by the
+// (cp.async.bulk / cp.async.bulk.tensor between global and shared memory,
+// mbarrier completion for loads, bulk async-groups for stores) used by the
 // pipelined FFT passes on sm_103a.
 #pragma once
 #include <stdint.h>
@@ -74,5 +75,34 @@ CGS_D void tma_load_4d(void* dst_smem, const void* tmap, int c0, int c1, int c2,
         "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
         : "memory");
 }
+
+// 3-D tensor-map tile load (TMA) into shared memory, completion on `bar`.
+CGS_D void tma_load_3d(void* dst_smem, const void* tmap, int c0, int c1, int c2, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+            smem_addr(dst_smem)),
+        "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// 4-D tensor-map tile store (TMA) from shared memory, tracked by the
+// thread's bulk async-group (commit with bulk_commit, wait with
+// bulk_wait_read / bulk_wait_all).  The shared-memory writes it reads must be
+// made visible to the async proxy first (fence_proxy_async_smem).
+CGS_D void tma_store_4d(const void* tmap, int c0, int c1, int c2, int c3, const void* src_smem)
+{
+    asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(
+                     tmap),
+                 "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(src_smem))
+                 : "memory");
+}
+
+CGS_D void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the shared-memory sources of all committed bulk stores have been read
+CGS_D void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// all committed bulk stores have completed
+CGS_D void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+CGS_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 }  // namespace cgs
