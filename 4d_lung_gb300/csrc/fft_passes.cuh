@@ -320,6 +320,9 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
                 }
             }
         }
+        // (the __syncthreads_or of the next wait would order the next stage 1
+        // after this stage 2 as well; without this barrier the forward passes
+        // measured 4-6 % slower)
         __syncthreads();
     }
 }
@@ -332,7 +335,8 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
 //   stage 1: thread n2: R1-point DFT over n1 (rows R2 n1 + n2), W^(-n2 k1)
 //            -> Y[k1][n2]
 //   stage 2: thread k1: R2-point DFT over n2 -> X[k1 + R1 k2]; X *= P; the
-//            R2-point inverse DFT over k2 -> Z[n2]; W^(+n2 k1) -> Y'[n2][k1]
+//            R2-point inverse DFT over k2 -> Z[n2]; W^(+n2 k1) -> Y[k1][n2]
+//            (the row it read)
 //   stage 3: thread n2: R1-point inverse DFT over k1 -> row n2 + R2 n1
 // The centring sign (-1)^k of the forward output and that of the adjoint
 // input cancel; the rows keep theirs.  A pipeline stage holds the tile's
@@ -355,7 +359,7 @@ struct ToepLayout {
 };
 
 template <int R1, int R2, int TB, int NSTAGE>
-__global__ void __launch_bounds__(ToepLayout<R1, R2, TB, NSTAGE>::NT, 2)
+__global__ void __launch_bounds__(ToepLayout<R1, R2, TB, NSTAGE>::NT, ToepLayout<R1, R2, TB, NSTAGE>::NT <= 128 ? 4 : 2)
 k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tmap,
              const __grid_constant__ CUtensorMap pmap, long long ntiles, int box_rows, int pbox_rows)
 {
@@ -458,13 +462,11 @@ k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tm
                 u[k2].y *= pv;
             }
             Dft<R2, +1>::run(u);
+            // back into the positions this thread read (row k1): no other
+            // thread touches them before the barrier
 #pragma unroll
-            for (int n2 = 1; n2 < R2; ++n2) u[n2] = table_twiddle<+1>(u[n2], s_tw[n2 * k1]);
-        }
-        __syncthreads();
-        if (k1 < R1) {
-#pragma unroll
-            for (int n2 = 0; n2 < R2; ++n2) s_y[(n2 * R1 + k1) * TB + bi] = u[n2];
+            for (int n2 = 0; n2 < R2; ++n2)
+                s_y[(k1 * R2 + n2) * TB + bi] = n2 > 0 ? table_twiddle<+1>(u[n2], s_tw[n2 * k1]) : u[n2];
         }
         __syncthreads();
         {
@@ -472,7 +474,7 @@ k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tm
             if (n2 < R2) {
                 float2 w[R1];
 #pragma unroll
-                for (int q = 0; q < R1; ++q) w[q] = s_y[(n2 * R1 + q) * TB + bi];
+                for (int q = 0; q < R1; ++q) w[q] = s_y[(q * R2 + n2) * TB + bi];
                 Dft<R1, +1>::run(w);
                 if (bok) {
                     float2* out = a.out + item * a.out_bs + b;
@@ -482,7 +484,9 @@ k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tm
                 }
             }
         }
-        __syncthreads();
+        // no barrier here: stage 3 of thread (n2, bi) read exactly the s_y
+        // positions that its own stage 1 of the next tile writes, and the
+        // stage refilled next was last read before the barrier above
     }
 }
 
