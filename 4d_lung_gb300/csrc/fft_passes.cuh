@@ -156,9 +156,11 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
     static_assert(MODE != PRUNE_IN || R1 % 4 == 0, "input pruning needs R1 % 4 == 0");
     static_assert(MODE != PRUNE_OUT || R2 % 4 == 0, "output pruning needs R2 % 4 == 0");
     extern __shared__ float4 s_pipe[];
-    const uintptr_t base = (reinterpret_cast<uintptr_t>(s_pipe) + 1023) & ~(uintptr_t)1023;
+    // 1 KiB-aligned start, derived from the shared array itself so that the
+    // compiler keeps shared-memory (not generic) loads and stores
+    const uint32_t pad = (1024u - (smem_addr(s_pipe) & 1023u)) & 1023u;
     const int stage_elems = a.Lin * TB;
-    float2* s_in = reinterpret_cast<float2*>(base);
+    float2* s_in = reinterpret_cast<float2*>(reinterpret_cast<char*>(s_pipe) + pad);
     float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
     float2* s_tw = s_y + L * TB;        // W^m, or the signed table [n2][k1] when FOLD
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + 2 * L);
@@ -367,9 +369,9 @@ k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tm
     constexpr int NT = ToepLayout<R1, R2, TB, NSTAGE>::NT;
     static_assert(R1 % 4 == 0, "the stored rows L/4 .. 3L/4 need R1 % 4 == 0");
     extern __shared__ float4 s_pipe[];
-    const uintptr_t base = (reinterpret_cast<uintptr_t>(s_pipe) + 1023) & ~(uintptr_t)1023;
+    const uint32_t pad = (1024u - (smem_addr(s_pipe) & 1023u)) & 1023u;   // as in k_fft_strided_tma
     const int stage_elems = a.Lin * TB;
-    float2* s_in = reinterpret_cast<float2*>(base);
+    float2* s_in = reinterpret_cast<float2*>(reinterpret_cast<char*>(s_pipe) + pad);
     float* s_p = reinterpret_cast<float*>(s_in + (size_t)NSTAGE * stage_elems);
     float2* s_y = reinterpret_cast<float2*>(s_p + (size_t)NSTAGE * L * TB);
     float2* s_tw = s_y + L * TB;
