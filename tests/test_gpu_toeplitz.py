@@ -72,6 +72,35 @@ def test_toeplitz_matches_exact_normal_operator(gpu_lib, cgs, oracle_mod, img, g
         assert 1e-5 < rel_l2(qg[b], ref) < 5e-3
 
 
+def test_toeplitz_unfused_fallback_and_workspace_groups(gpu_lib, cgs, oracle_mod):
+    """A grid oversampled by 2.5 along x (the fused x stage needs exactly 2x)
+    falls back to the unfused x stage; a workspace of one bin runs the bins
+    as separate groups, each with its own spectrum."""
+    img, grid, nch = (16, 12, 8), (40, 24, 16), 2
+    k, dcf, S, bins, x = random_case(img, nch, 600, 2, seed=13)
+    r = make_reco(cgs, img, grid, nch, k, dcf, S, bins)
+    r.set_toeplitz(1)
+    q, n = apply(r, x)
+    assert n == 7
+    img2, grid2 = (16, 12, 8), (32, 24, 16)
+    per_bin = nch * (img2[0] * img2[1] * grid2[2] + 2 * img2[0] * grid2[1] * grid2[2] + int(np.prod(grid2))) * 8
+    r2 = cgs.Reco(img2, grid2, nch, kb_w=KB_W, kb_b=KB_B, workspace_bytes=per_bin)
+    r2.set_trajectory(k)
+    r2.set_bins(bins)
+    r2.set_dcf(dcf)
+    r2.set_smaps(S)
+    r2.set_toeplitz(1)
+    q2, n2 = apply(r2, x)
+    assert n2 == 10   # two groups of five launches
+    Sd = S.astype(np.complex128)
+    for b in range(2):
+        d = dcf[bins[b]].astype(np.float64)
+        ref = oracle_mod.exact_normal(k[bins[b]], img, grid, Sd, d, x[b].astype(np.complex128))
+        assert rel_l2(q[b], ref) < 2e-5
+        ref2 = oracle_mod.exact_normal(k[bins[b]], img2, grid2, Sd, d, x[b].astype(np.complex128))
+        assert rel_l2(q2[b], ref2) < 2e-5
+
+
 def test_toeplitz_without_density_and_after_changes(gpu_lib, cgs, oracle_mod):
     """The spectra follow the density weights, the bins and the coordinates."""
     img, grid, nch = (16, 12, 8), (32, 24, 16), 2
