@@ -2143,6 +2143,9 @@ int cgs_rhs_d(cgs_ctx* c, int32_t bin0, int32_t nb, const void* y, void* b)
 
 int cgs_apply_vjp_k_d(cgs_ctx* c, int32_t bin0, int32_t nb, const void* p, const void* v, void* grad_k)
 {
+    if (c && c->toep_mode)
+        return fail(c, CGS_ERR_STATE, "the operator's trajectory derivative is that of the gridded operator: "
+                                      "turn the Toeplitz embedding off (cgs_set_toeplitz 0)");
     CGS_TRY(check_ready(c, true, false));
     if (!p || !v || !grad_k) return fail(c, CGS_ERR_ARG, "null pointer");
     if (bin0 < 0 || nb < 1 || bin0 + nb > c->nbins) return fail(c, CGS_ERR_ARG, "bin range out of bounds");
@@ -2404,6 +2407,10 @@ int cgs_set_toeplitz(cgs_ctx* c, int32_t mode)
                 return fail(c, CGS_ERR_ARG, "the Toeplitz embedding needs grid >= 2 x image - 1 on every axis");
     if (c->toep_mode != mode) drop_graphs(c);
     c->toep_mode = mode;
+    if (!mode) {   // the spectra are rebuilt when the embedding is turned on again
+        c->d_toep.release();
+        c->toep_valid = false;
+    }
     // with a trajectory and bins the spectra are built now, else at first use
     if (mode && c->ns > 0 && !c->bins.empty()) return check_ready(c, false, false);
     return CGS_OK;

@@ -343,7 +343,9 @@ int cgs_set_support_pruning(cgs_ctx* ctx, int32_t on);
  * weights (one FP32 matrix product per chunk of samples, cuBLAS opened at
  * run time) and rebuilt after any of them changes.  Mode 2: the same
  * operator with the x stage unfused (forward x pass, multiply, adjoint x
- * pass; for comparison).  Mode 0 (default): the gridded operator. */
+ * pass; for comparison).  Mode 0 (default): the gridded operator; the
+ * spectra are released.  cgs_apply_vjp_k_d (the derivative of the gridded
+ * operator) fails with CGS_ERR_STATE while the embedding is on. */
 int cgs_set_toeplitz(cgs_ctx* ctx, int32_t mode);
 /* Time of the last spectrum build (ms) and the bytes the spectra hold (0
  * while not built). */

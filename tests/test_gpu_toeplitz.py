@@ -147,6 +147,28 @@ def test_toeplitz_needs_room_for_the_embedding(gpu_lib, cgs):
     apply(r, x)   # the gridded operator still works
 
 
+def test_toeplitz_refuses_the_gridded_trajectory_derivative(gpu_lib, cgs):
+    """The operator's trajectory derivative belongs to the gridded operator:
+    it is refused while the embedding is on, and works again once it is off."""
+    import torch
+    img, grid, nch = (16, 12, 8), (32, 24, 16), 2
+    k, dcf, S, bins, x = random_case(img, nch, 300, 1, seed=17)
+    r = make_reco(cgs, img, grid, nch, k, dcf, S, bins)
+    p = torch.from_numpy(x).cuda()
+    g = torch.zeros((300, 3), dtype=torch.float32, device="cuda")
+    L = gpu_lib
+    import ctypes as C
+    r.set_toeplitz(1)
+    st = L.cgs_apply_vjp_k_d(r.ctx, 0, 1, C.c_void_p(p.data_ptr()), C.c_void_p(p.data_ptr()), C.c_void_p(g.data_ptr()))
+    assert st == cgs.CGS_ERR_STATE
+    assert b"Toeplitz" in L.cgs_last_error(r.ctx)
+    r.set_toeplitz(0)
+    assert r.toeplitz_stats() == (0.0, 0)
+    st = L.cgs_apply_vjp_k_d(r.ctx, 0, 1, C.c_void_p(p.data_ptr()), C.c_void_p(p.data_ptr()), C.c_void_p(g.data_ptr()))
+    torch.cuda.synchronize()
+    assert st == 0 and bool(torch.isfinite(g).all())
+
+
 def test_toeplitz_cg_matches_exact_cg(gpu_lib, cgs, oracle_mod):
     """CG-SENSE from coil images with the Toeplitz operator against the same
     CG (Reco.cpp:175-321) in FP64 numpy on the exact normal operator."""
