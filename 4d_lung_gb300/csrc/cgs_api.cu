@@ -144,6 +144,7 @@ struct cgs_ctx {
     uint64_t toep_serial = 0;    // traj_serial the spectra were built from
     double toep_build_ms = 0.0;
     DevBuf d_toep, d_ones;
+    void* blas = nullptr;        // cuBLAS handle of the spectrum builds
     // coil maps
     DevBuf d_smaps;
     bool smaps_set = false;
@@ -890,7 +891,7 @@ int build_toeplitz(cgs_ctx* c)
         a.scale = c->adj_scale_total / (double)Ng;
         a.P = c->d_toep.as<float>() + (long long)b * Ng;
         std::string e;
-        if (toeplitz_build(a, work.as<float>(), chunk * per, c->stream, &e) != 0)
+        if (toeplitz_build(a, work.as<float>(), chunk * per, &c->blas, c->stream, &e) != 0)
             st = fail(c, CGS_ERR_CUDA, "Toeplitz spectrum of bin " + std::to_string(b) + ": " + e);
     }
     cudaEventRecord(e1, c->stream);
@@ -1248,6 +1249,7 @@ void cgs_destroy(cgs_ctx* c)
     drop_graphs(c);
     if (c->plain_plan_ok) cufftDestroy(c->plain_plan);
     if (c->z_plan_ok) cufftDestroy(c->z_plan);
+    if (c->blas) toeplitz_release(c->blas);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }

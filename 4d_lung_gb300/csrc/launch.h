@@ -122,9 +122,13 @@ cudaError_t launch_smaps_from_images(float2* imgs, int nch, long long n, float e
 
 // Toeplitz embedding of E^H D E (toeplitz.cu, fft_inst.cu).  toeplitz_build
 // accumulates one bin's P with cuBLAS over chunks of toeplitz_chunk samples
-// (work: work_elems floats); returns 0 on success, else sets *err.
+// (work: work_elems floats; *handle: the caller's cuBLAS handle, created at
+// the first call, released with toeplitz_release); returns 0 on success,
+// else sets *err.
 long long toeplitz_chunk(const int G[3], long long work_elems);
-int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, cudaStream_t s, std::string* err);
+int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, void** handle, cudaStream_t s,
+                   std::string* err);
+void toeplitz_release(void* handle);
 // grid[item][j] *= P[item / nch][j] over items grids of Ng points
 cudaError_t launch_toep_mul(float2* grid, const float* P, long long Ng, int nch, int items, cudaStream_t s);
 // Fused x stage in place: forward x transform of the Lin = L/2 stored rows,

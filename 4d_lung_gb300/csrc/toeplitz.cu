@@ -147,7 +147,14 @@ long long toeplitz_chunk(const int G[3], long long work_elems)
     return std::min(n, 65535LL);
 }
 
-int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, cudaStream_t s, std::string* err)
+void toeplitz_release(void* handle)
+{
+    Blas& b = blas();
+    if (handle && b.destroy) b.destroy(static_cast<cublasHandle_t>(handle));
+}
+
+int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, void** handle, cudaStream_t s,
+                   std::string* err)
 {
     Blas& b = blas();
     if (!b.lib || !b.create || !b.destroy || !b.set_stream || !b.sgemm) {
@@ -166,11 +173,16 @@ int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, cu
         if (err) *err = "Toeplitz work buffer too small";
         return 1;
     }
-    cublasHandle_t h = nullptr;
-    if (b.create(&h) != CUBLAS_STATUS_SUCCESS) {
-        if (err) *err = "cublasCreate failed";
-        return 1;
+    // one handle per context, created at its first build
+    if (!*handle) {
+        cublasHandle_t hn = nullptr;
+        if (b.create(&hn) != CUBLAS_STATUS_SUCCESS) {
+            if (err) *err = "cublasCreate failed";
+            return 1;
+        }
+        *handle = hn;
     }
+    cublasHandle_t h = static_cast<cublasHandle_t>(*handle);
     int rc = 0;
     if (b.set_stream(h, s) != CUBLAS_STATUS_SUCCESS) rc = 1;
     for (long long c0 = 0; rc == 0 && c0 < a.n; c0 += chunk) {
@@ -194,7 +206,6 @@ int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, cu
                     (int)yz) != CUBLAS_STATUS_SUCCESS)
             rc = 1;
     }
-    b.destroy(h);
     if (rc && err) *err = rc == 2 ? "Toeplitz table kernels failed to launch" : "cublasSgemm failed";
     return rc;
 }
