@@ -14,6 +14,12 @@ second (bins x iterations per step / time per step), summed over ranks.
 With torchrun (N > 1) every rank reconstructs its own 16-bin scan on its
 GPU (replicas, weak scaling, no collective on the data path).
 
+Beside the headline the line carries the plain per-bin GPU form, the
+per-iteration precision against the FP64 form, the differentiation form,
+and the same solve with the Toeplitz-embedded operator ("toeplitz": the
+exact normal operator, not the reference's gridded one; skip with
+--no-toeplitz).
+
 --impl reference times the reference's CPU implementation of the same
 operator on the host cores: the oracle port (oracle/cgs_oracle.c, FP32,
 OpenMP over coils like Reco.cpp:470,523), one E^H D E application of bin 0
