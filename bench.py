@@ -745,7 +745,10 @@ def run_ours(args):
     # operator for fixed trajectories; not the headline form)
     toep = None
     if not args.no_toeplitz:
-        toep = toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, max(1, args.steps), w, sizes)
+        try:
+            toep = toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, max(1, args.steps), w, sizes)
+        except cgs.CGSError as e:   # e.g. no cuBLAS on the host: the headline stands without it
+            toep = {"unavailable": str(e)}
 
     # per-stage kernel times of one batched application (roofline)
     xa = torch.from_numpy(np.stack([synth.phantom(w.img)] * nb)).to(dev)
