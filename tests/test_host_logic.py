@@ -95,3 +95,33 @@ def test_partition_two_ranks_gloo():
         assert p.exitcode == 0
     assert counts == [1] * 16
     assert abs(loads[0] - loads[1]) <= max(sizes)
+
+
+def test_roofline_byte_model(synth):
+    """bench.stage_bytes: each stage reads its input and writes its output
+    once; with sample-support pruning the x passes count only the listed
+    columns, the forward y pass (listed rows) only their rows, and the
+    spreading gather its stores, row offsets, taps and sample values."""
+    import importlib
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    bench = importlib.import_module("bench")
+    w = synth.scaled(synth.WORKLOADS["cfg1"], (8, 8, 4), (16, 16, 8), n_ch=2, read_os=2)
+    Ix, Iy, Iz = w.img
+    Gx, Gy, Gz = w.grid
+    Ni, Nl, C8 = Ix * Iy * Iz, Ix * Iy, 8 * w.n_ch
+    sizes = [10, 30]
+    full = bench.stage_bytes(w, sizes)
+    assert full["fwd_z"] == 2 * (8 * Ni + C8 * Ni + C8 * Nl * Gz)
+    assert full["fwd_y"] == 2 * C8 * (Nl * Gz + Ix * Gy * Gz)
+    assert full["fwd_x"] == C8 * 2 * Gy * Gz * (Ix + Gx)
+    assert full["adj_x"] == full["fwd_x"] and full["adj_y"] == full["fwd_y"] and full["adj_z"] == full["fwd_z"]
+    cols, tiles = [40, 60], [3, 5]
+    pruned = bench.stage_bytes(w, sizes, (cols, tiles), matrix=(500, 100 * Gx), y_listed=True)
+    assert pruned["fwd_x"] == C8 * 100 * (Ix + Gx)
+    assert pruned["fwd_y"] == C8 * (2 * Nl * Gz + Ix * 100)
+    assert pruned["spread"] == C8 * 100 * Gx + 4 * 100 * Gx + 8 * 500 + 40 * C8
+    assert pruned["interp"] == C8 * 100 * Gx + 40 * (64 + 4 + C8)
+    assert bench.apply_bytes(w, sizes) == sum(full.values()) + 56 * Ni * 2
