@@ -482,7 +482,8 @@ def toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, steps, w, s
             "spectra_build_s": build_ms / 1e3, "spectra_bytes": pbytes,
             "s_per_4d_recon": ms / 1e3, "applies_per_s": nb * iters / (ms / 1e3),
             "launches_per_recon": launches,
-            "iters": [int(v) for v in its], "final_residual_rel": [float(r[-1] / r[0]) for r in res],
+            "iters": [int(v) for v in its],
+            "final_residual_rel": [float(r[-1] / r[0]) if r[0] > 0 else 0.0 for r in res],
             "rel_l2_vs_gridded_solve": rel,
             "apply_ms": apply_ms, "stage_ms": stage_ms,
             "stage_frac_of_peak": {s: tb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
