@@ -15,8 +15,15 @@
 // GPU that loads the library holds them (4 MiB + 12 KiB) until the process
 // exits.  Device code could name the arrays directly; host code only has a
 // host-side stand-in for each symbol, so their device addresses are looked
-// up once per device with cudaGetSymbolAddress (on that device's first call,
-// with the device current) and passed to the kernels.
+// up with cudaGetSymbolAddress on the first call in each CUDA context (the
+// device current, the module loaded there) and passed to the kernels.  The
+// addresses are cached per device and context: a caller that switches
+// between several contexts of one device gets each context's own copy of
+// the arrays.
+//
+// in and out are read and written as float2, so both must be 8-byte
+// aligned; a misaligned pointer is rejected before anything is launched (a
+// misaligned access would end the caller's CUDA context).
 //
 // All calls share the same arrays and the arrays keep the last call's
 // contents.  Nothing here relies on them starting at zero: the z pass writes
@@ -44,6 +51,7 @@ static __device__ __align__(256) float2 g_noalloc_twiddles[3 * CGS_FFT_NOALLOC_M
 namespace {
 
 struct NoallocSymbols {
+    void* ctx = nullptr;        // the CUDA context the addresses belong to
     float2* scratch = nullptr;
     float2* twiddles = nullptr;
 };
@@ -51,6 +59,24 @@ struct NoallocSymbols {
 constexpr int kMaxDevices = 64;
 std::mutex g_symbols_mutex;
 NoallocSymbols g_symbols[kMaxDevices];
+
+// cuCtxGetCurrent from the driver (no link-time dependency on libcuda)
+typedef int (*CtxGetCurrentFn)(void**);
+
+void* current_context()
+{
+    static CtxGetCurrentFn fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<CtxGetCurrentFn>(p);
+    }();
+    void* ctx = nullptr;
+    if (fn && fn(&ctx) != 0) ctx = nullptr;
+    return ctx;
+}
 // There is no context to hold a message: errors go to stderr with the code.
 int noalloc_fail(int code, const std::string& msg)
 {
@@ -73,6 +99,8 @@ __global__ void k_noalloc_twiddles(float2* tw, int L)
 extern "C" int cgs_fft3_noalloc(const float* in, float* out, const int32_t* grid, int32_t sign, void* stream)
 {
     if (!in || !out || !grid) return noalloc_fail(CGS_ERR_ARG, "null pointer");
+    if ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 7)
+        return noalloc_fail(CGS_ERR_ARG, "in and out must be 8-byte aligned (complex float values)");
     if (sign != -1 && sign != 1) return noalloc_fail(CGS_ERR_ARG, "sign must be -1 or +1");
     long long n = 1;
     for (int a = 0; a < 3; ++a) {
@@ -87,18 +115,21 @@ extern "C" int cgs_fft3_noalloc(const float* in, float* out, const int32_t* grid
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return noalloc_fail(CGS_ERR_CUDA, "no current CUDA device");
+    void* ctx = current_context();   // null before the runtime has made a context current
     NoallocSymbols sym;
     {
         std::lock_guard<std::mutex> lock(g_symbols_mutex);
-        if (!g_symbols[dev].scratch) {
-            // once per device, with that device current: device addresses of
-            // the file-scope arrays (the host names are only stand-ins)
+        if (!g_symbols[dev].scratch || g_symbols[dev].ctx != ctx) {
+            // once per device and context, with that device current: device
+            // addresses of the file-scope arrays (the host names are only
+            // stand-ins)
             void* s = nullptr;
             void* t = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&s, g_noalloc_scratch);
             if (e != cudaSuccess) return noalloc_fail(CGS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
             e = cudaGetSymbolAddress(&t, g_noalloc_twiddles);
             if (e != cudaSuccess) return noalloc_fail(CGS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            g_symbols[dev].ctx = current_context();   // the lookup made the primary context current
             g_symbols[dev].scratch = reinterpret_cast<float2*>(s);
             g_symbols[dev].twiddles = reinterpret_cast<float2*>(t);
         }

@@ -159,7 +159,14 @@ void Reco::setTrajectory(WaveCaipi* t)
 
 bool Reco::createLogFile(const std::string&) { return true; }
 bool Reco::importParameters(const std::string&) { return true; }
-bool Reco::setDataInputPaths() { return true; }
+// Reco.cpp:63-71: one state file per batch entry,
+// root + file name + index + extension
+bool Reco::setDataInputPaths()
+{
+    for (int i = 0; i < batch; i++)
+        batchFiles.push_back(dataPathRoot + dataPathFileName + std::to_string(i) + dataPathFileExtension);
+    return true;
+}
 
 void Reco::check()
 {

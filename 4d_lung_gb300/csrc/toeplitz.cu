@@ -105,9 +105,9 @@ __global__ void k_toep_mul(float2* __restrict__ grid, const float* __restrict__ 
     }
 }
 
-// cuBLAS entry points, resolved once
+// cuBLAS entry points, resolved once (thread-safe: a function-local static
+// is initialised by exactly one thread, the others wait for it)
 struct Blas {
-    bool tried = false;
     void* lib = nullptr;
     cublasStatus_t (*create)(cublasHandle_t*) = nullptr;
     cublasStatus_t (*destroy)(cublasHandle_t) = nullptr;
@@ -116,22 +116,25 @@ struct Blas {
                             const float*, int, const float*, int, const float*, float*, int) = nullptr;
 };
 
-Blas& blas()
+Blas open_blas()
 {
-    static Blas b;
-    if (!b.tried) {
-        b.tried = true;
-        for (const char* name : {"libcublas.so.13", "libcublas.so"}) {
-            b.lib = dlopen(name, RTLD_NOW | RTLD_LOCAL);
-            if (b.lib) break;
-        }
-        if (b.lib) {
-            b.create = reinterpret_cast<decltype(b.create)>(dlsym(b.lib, "cublasCreate_v2"));
-            b.destroy = reinterpret_cast<decltype(b.destroy)>(dlsym(b.lib, "cublasDestroy_v2"));
-            b.set_stream = reinterpret_cast<decltype(b.set_stream)>(dlsym(b.lib, "cublasSetStream_v2"));
-            b.sgemm = reinterpret_cast<decltype(b.sgemm)>(dlsym(b.lib, "cublasSgemm_v2"));
-        }
+    Blas b;
+    for (const char* name : {"libcublas.so.13", "libcublas.so"}) {
+        b.lib = dlopen(name, RTLD_NOW | RTLD_LOCAL);
+        if (b.lib) break;
     }
+    if (b.lib) {
+        b.create = reinterpret_cast<decltype(b.create)>(dlsym(b.lib, "cublasCreate_v2"));
+        b.destroy = reinterpret_cast<decltype(b.destroy)>(dlsym(b.lib, "cublasDestroy_v2"));
+        b.set_stream = reinterpret_cast<decltype(b.set_stream)>(dlsym(b.lib, "cublasSetStream_v2"));
+        b.sgemm = reinterpret_cast<decltype(b.sgemm)>(dlsym(b.lib, "cublasSgemm_v2"));
+    }
+    return b;
+}
+
+const Blas& blas()
+{
+    static const Blas b = open_blas();
     return b;
 }
 
@@ -149,14 +152,14 @@ long long toeplitz_chunk(const int G[3], long long work_elems)
 
 void toeplitz_release(void* handle)
 {
-    Blas& b = blas();
+    const Blas& b = blas();
     if (handle && b.destroy) b.destroy(static_cast<cublasHandle_t>(handle));
 }
 
 int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, void** handle, cudaStream_t s,
                    std::string* err)
 {
-    Blas& b = blas();
+    const Blas& b = blas();
     if (!b.lib || !b.create || !b.destroy || !b.set_stream || !b.sgemm) {
         if (err) *err = "cuBLAS could not be opened (libcublas.so.13)";
         return 1;

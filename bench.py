@@ -483,7 +483,9 @@ def toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, steps, w, s
             "s_per_4d_recon": ms / 1e3, "applies_per_s": nb * iters / (ms / 1e3),
             "launches_per_recon": launches,
             "iters": [int(v) for v in its],
-            "final_residual_rel": [float(r[-1] / r[0]) if r[0] > 0 else 0.0 for r in res],
+            # None for a bin whose initial residual is zero (an empty bin), so
+            # that it cannot pass for a solve that converged
+            "final_residual_rel": [float(r[-1] / r[0]) if r[0] > 0 else None for r in res],
             "rel_l2_vs_gridded_solve": rel,
             "apply_ms": apply_ms, "stage_ms": stage_ms,
             "stage_frac_of_peak": {s: tb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},

@@ -247,6 +247,10 @@ private:
     std::string outputParentDir;
     std::string densityCorrPath;
     std::vector<std::string> batchFiles;
+    // file name parts of setDataInputPaths (Reco.h:207-209, Reco.cpp:15)
+    std::string dataPathRoot;
+    std::string dataPathFileName;
+    std::string dataPathFileExtension = ".bin";
     cgs_ctx* ctx = nullptr;
     fftwf_complex* imgBlock = nullptr;
     fftwf_complex* mapBlock = nullptr;

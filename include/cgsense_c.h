@@ -394,14 +394,18 @@ int cgs_autotune(cgs_ctx* ctx, float* times_ms, int32_t max_times, int32_t* n_ti
  * own allocator, or a latency-critical loop that must not pay for
  * cudaMalloc/cudaFree.  No counterpart in the reference.  in and out are
  * device arrays of grid[0]*grid[1]*grid[2] complex values (they may be the
- * same array); no context is needed.  The intermediate grid lives in a fixed
- * file-scope device array of 2^19 complex values (4 MiB, held by every GPU
- * that loads the library); larger grids are rejected with CGS_ERR_ARG, sizes
- * without an FFT kernel with CGS_ERR_UNSUPPORTED (messages go to stderr).
- * The first call on a device looks up that array's device address, so make
- * that first call before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race and must be serialised.  stream is a
- * cudaStream_t (NULL: the default stream); the call is asynchronous. */
+ * same array), each 8-byte aligned (a misaligned pointer is CGS_ERR_ARG,
+ * checked before any launch); no context is needed.  The intermediate grid
+ * lives in a fixed file-scope device array of 2^19 complex values (4 MiB,
+ * held by every GPU that loads the library); larger grids are rejected with
+ * CGS_ERR_ARG, sizes without an FFT kernel with CGS_ERR_UNSUPPORTED
+ * (messages go to stderr).  The first call in each CUDA context looks up
+ * that array's device address there (cached per device and context), so
+ * make that first call before any stream capture; cudaDeviceReset between
+ * calls is not supported (the driver may hand the new context the old
+ * handle, and the cached address would be stale).  All calls share the
+ * array: calls that overlap on the GPU race and must be serialised.  stream
+ * is a cudaStream_t (NULL: the default stream); the call is asynchronous. */
 int cgs_fft3_noalloc(const float* in_dev, float* out_dev, const int32_t* grid, int32_t sign, void* stream);
 
 /* --- File IO of the reconstruction (IO.cpp), context-free --------------

@@ -33,8 +33,7 @@ def build():
     """Compile liboracle{64,32}.so (and the reference driver when the
     reference sources are present)."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if os.path.isdir("/root/reference/CGSense"):
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)   # skipped without the reference sources
 
 
 class Params(C.Structure):

@@ -17,11 +17,15 @@ from __future__ import annotations
 import os
 import sys
 
+import importlib
+
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-sys.path.insert(0, os.path.join(ROOT, "oracle"))
+for _p in (ROOT, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
 import oracle_py as O  # noqa: E402
 
 
@@ -112,6 +116,79 @@ def io_fixture(name, sx, sy, sz, nch, grid, seed):
     print("wrote", name)
 
 
+# The mid-size CG fixture: the reference's own parameters (grid == image,
+# KB w = 4.25, b = 14.9086, the 11^3 tap neighbourhood, 16 CG iterations) on
+# a 64x64x48 grid with 4 coils and a wave-CAIPI trajectory of 33 k samples.
+# Its inputs are not stored: wave_cg_inputs() regenerates them from seeds
+# (numpy's PCG64 streams and the FP64 oracle's forward operator), and the
+# fixture keeps fingerprints of them so that a test can tell when the
+# regenerated inputs drift.
+WAVE_CG_NAME = "ref_cg_64x64x48_wave.npz"
+
+
+def wave_cg_inputs():
+    """(workload, k, smaps, x, dcf, data) of the mid-size CG fixture: a
+    wave-CAIPI trajectory (R = 3x2, CAIPI shift 1, 64 samples per readout,
+    +-3 cells over 5 cycles; readouts near the grid's faces leave it and lose
+    taps there), Gaussian coil maps, the ellipsoid phantom, the radial
+    density stand-in, and k-space = the FP64 oracle's nufftFWD of the coil
+    images plus complex noise at SNR 30, rounded to complex64."""
+    synth = importlib.import_module("4d_lung_gb300.synth")
+    w = synth.Workload("ref_cg_64x64x48_wave", (64, 64, 48), (64, 64, 48), 4, (3, 2), 1, 1, 3.0, 5, 1, 16)
+    k = synth.wave_trajectory(w)
+    smaps = synth.coil_maps(w.img, w.n_ch)
+    x = synth.phantom(w.img)
+    dcf = synth.radial_dcf(k, w.grid)
+    o = O.Oracle(64)
+    p = O.make_params(w.img, w.grid, w.n_ch)
+    taps = o.taps(p, k)
+    y = o.nufft_fwd(p, taps, o.kernel_ft(p), smaps.astype(np.complex128) * x[None]).astype(np.complex64)
+    y += synth.complex_noise(y.shape, 30.0, float(np.sqrt(np.mean(np.abs(y) ** 2))))
+    return w, k, smaps, x, dcf, y
+
+
+def input_fingerprint(k, data):
+    """Sums that identify the regenerated inputs (FP64)."""
+    d = data.astype(np.complex128)
+    return np.array([k.sum(), (k * k).sum(), np.abs(d).sum(), (d.real * np.arange(d.size).reshape(d.shape)).sum()])
+
+
+def wave_cg_fixture(threads=8):
+    """Runs the reference's calculateWeights, nufftFWD, nufftBWD and
+    cgSenseDynamic (Reco.cpp:175-321,468-553,698-806) on the mid-size inputs
+    and stores subsampled outputs: per-sample tap counts and weight sums, the
+    forward samples of every 8th sample, the adjoint image of coil 0 and the
+    CG image on every second voxel per axis, the residual sequence and the
+    iteration count."""
+    w, k, smaps, x, dcf, y = wave_cg_inputs()
+    grid, nch, ns = w.grid, w.n_ch, k.shape[0]
+    params = dict(gx=grid[0], gy=grid[1], gz=grid[2], sx=ns, sy=1, sz=1, nch=nch, threads=threads)
+    r = O.run_ref("taps", params, {"traj": k},
+                  {"tap_count_out": (np.int32, None), "tap_idx_out": (np.int32, None),
+                   "tap_w_out": (np.float32, None)})
+    cnt = r["tap_count_out"]
+    seg = np.repeat(np.arange(ns), cnt)
+    wsum = np.bincount(seg, weights=r["tap_w_out"].astype(np.float64), minlength=ns)
+    imgs = (smaps * x[None]).astype(np.complex64)
+    r = O.run_ref("fwd", params, {"traj": k, "img": imgs}, {"data_out": (np.complex64, None)})
+    fwd = r["data_out"].reshape(nch, ns)
+    r = O.run_ref("bwd", params, {"traj": k, "data": y, "dcf": dcf}, {"img_out": (np.complex64, None)})
+    bwd0 = r["img_out"].reshape((nch,) + grid)[0]
+    r = O.run_ref("cg", dict(params, cg_threshold=0.0), {"traj": k, "data": y, "smaps": smaps, "dcf": dcf},
+                  {"x_out": (np.complex64, None), "residuals_out": (np.float64, None),
+                   "iters_out": (np.int32, None), "cg_seconds_out": (np.float64, None)})
+    xr = r["x_out"].reshape(grid)
+    np.savez_compressed(os.path.join(HERE, WAVE_CG_NAME), grid=np.array(grid), nch=nch, ns=ns,
+                        fingerprint=input_fingerprint(k, y),
+                        tap_count=cnt.astype(np.uint8), tap_wsum=wsum,
+                        fwd_every8=fwd[:, ::8], bwd_coil0_sub2=bwd0[::2, ::2, ::2],
+                        cg_x_sub2=xr[::2, ::2, ::2], cg_x_norm=np.linalg.norm(xr.astype(np.complex128)),
+                        cg_residuals=r["residuals_out"], cg_iters=r["iters_out"],
+                        ref_cg_seconds=r["cg_seconds_out"], ref_threads=threads)
+    print("wrote", WAVE_CG_NAME, "samples", ns, "taps", int(cnt.sum()), "cg iters", int(r["iters_out"][0]),
+          "ref cg %.1f s" % float(r["cg_seconds_out"][0]))
+
+
 def main():
     if not O.ref_available():
         O.build()
@@ -130,7 +207,11 @@ def main():
     traj_fixture("ref_traj_wave_b.npz", 64, 16, 8, (96, 80, 64), 0.3, 0.05,
                  nosc=7, dwell=1e-5, grad_amp=0.01, amp_corr_y=1.0, amp_corr_z=0.97,
                  shift_y=0.0, shift_z=1e-5)
+    wave_cg_fixture()
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["wave_cg"]:
+        wave_cg_fixture()
+    else:
+        main()

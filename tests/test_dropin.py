@@ -53,3 +53,23 @@ def test_dropin_matches_reference(gpu_lib, dropin_exe, name):
     assert np.allclose(res, z["cg_residuals"], rtol=2e-4, atol=0)
     assert rel_l2(x, z["cg_x"]) < 2e-4
     assert rel_l2(kft, z["kernelft"]) < 1e-5
+
+
+def test_dropin_data_input_paths(cgs, tmp_path):
+    """Reco::setDataInputPaths (Reco.cpp:63-71): one state file per batch
+    entry, root + file name + index + ".bin" (root and file name are empty
+    in the reference, which has no setters for them).  Host only."""
+    if not os.path.exists(cgs.LIB_PATH):
+        cgs.build()
+    src = tmp_path / "paths.cpp"
+    src.write_text('#include "cgsense/Reco.h"\n#include <cstdio>\n'
+                   'int main() { Reco r; r.setBatch(3); r.setDataInputPaths();\n'
+                   '  for (const auto& f : r.getBatchFiles()) std::printf("%s\\n", f.c_str());\n'
+                   '  return r.getBatchSize() == 3 ? 0 : 1; }\n')
+    exe = str(tmp_path / "paths")
+    libdir = os.path.dirname(cgs.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe,
+                    "-L", libdir, "-l:libcgsense.so", "-Wl,-rpath," + libdir], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert r.stdout.split() == ["0.bin", "1.bin", "2.bin"]

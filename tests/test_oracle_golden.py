@@ -1,10 +1,16 @@
 """Pins the CPU oracle to the reference: the golden vectors in tests/golden/
 were produced by the reference's own Reco.cpp / Fourier.cpp /
 Trajectory.cpp compiled unmodified (tests/golden/make_golden.py)."""
+import os
+import sys
+
 import numpy as np
 import pytest
 
-from conftest import golden, rel_l2
+from conftest import GOLDEN, golden, rel_l2
+
+if GOLDEN not in sys.path:
+    sys.path.insert(0, GOLDEN)
 
 OPS = ["ref_ops_24x20x16.npz", "ref_ops_32x24x16_mask.npz", "ref_ops_40x20x16_stop.npz"]
 
@@ -78,3 +84,48 @@ def test_wave_caipi(o64, name):
                        amp_corr_z=wave["amp_corr_z"], shift_y=wave["shift_y"],
                        shift_z=wave["shift_z"], dwell=wave["dwell"])
     assert np.max(np.abs(k - z["traj"])) < 1e-12
+
+
+@pytest.fixture(scope="module")
+def wave_cg():
+    """The mid-size fixture (64x64x48 grid == image, 4 coils, 32 768
+    wave-CAIPI samples, the reference's KB w = 4.25 / b = 14.9086) and its
+    regenerated inputs (tests/golden/make_golden.py: wave_cg_inputs)."""
+    import make_golden as mg
+    z = golden(mg.WAVE_CG_NAME)
+    w, k, smaps, x, dcf, y = mg.wave_cg_inputs()
+    fp = mg.input_fingerprint(k, y)
+    assert np.allclose(fp, z["fingerprint"], rtol=1e-6, atol=0), "regenerated inputs drifted"
+    return z, w, k, smaps, x, dcf, y
+
+
+def test_wave_cg_taps(oracle_mod, o64, wave_cg):
+    """calculateWeights at a realistic size: the 11^3 neighbourhood, the
+    float distance arithmetic and the grid faces (readouts leave the grid):
+    per-sample tap counts exact, per-sample weight sums to float rounding."""
+    z, w, k, smaps, x, dcf, y = wave_cg
+    p = oracle_mod.make_params(w.img, w.grid, w.n_ch)
+    taps = o64.taps(p, k)
+    cnt = np.diff(taps.ptr)
+    assert np.array_equal(cnt, z["tap_count"].astype(np.int64))
+    ws = np.add.reduceat(taps.w.astype(np.float64), taps.ptr[:-1]) * (cnt > 0)
+    assert np.allclose(ws, z["tap_wsum"], rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_wave_cg_operators_and_solve(oracle_mod, o64, o32, wave_cg, prec):
+    """nufftFWD, nufftBWD and cgSenseDynamic of the mid-size fixture: the
+    FP64 oracle and the FP32 port against the reference's own outputs."""
+    o = o64 if prec == 64 else o32
+    z, w, k, smaps, x, dcf, y = wave_cg
+    p = oracle_mod.make_params(w.img, w.grid, w.n_ch)
+    taps = o.taps(p, k)
+    kft = o.kernel_ft(p)
+    fwd = o.nufft_fwd(p, taps, kft, (smaps * x[None]).astype(np.complex64))
+    assert rel_l2(fwd[:, ::8], z["fwd_every8"]) < 1e-5
+    bwd = o.nufft_adj(p, taps, kft, y * dcf[None])
+    assert rel_l2(bwd[0][::2, ::2, ::2], z["bwd_coil0_sub2"]) < 1e-5
+    st, xo, res, it = o.cg_sense(p, taps, kft, smaps, dcf, y, 0.0, 16)
+    assert st == 0 and it == int(z["cg_iters"][0]) == 16
+    assert np.allclose(res, z["cg_residuals"], rtol=1e-4, atol=0)
+    assert rel_l2(xo[::2, ::2, ::2], z["cg_x_sub2"]) < 1e-4
