@@ -106,7 +106,8 @@ struct cgs_ctx {
     // fit), coils per interpolation thread
     int spread_cc = 0;
     int spread_wpp = 6;          // spreading variant: warps per x plane 1 / 2, 3 atomics, 4 / 5 pipelined,
-                                 // 6 gather over the transposed tap matrix (2 when it is not built)
+                                 // 6 / 7 gather over the transposed tap matrix, staged in shared memory /
+                                 // read from global memory (2 when it is not built)
     bool deterministic = true;   // fixed summation order everywhere (cgs_set_deterministic)
     int interp_cc = 4;
     bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
@@ -425,7 +426,8 @@ int build_csr(cgs_ctx* c)
     CGS_TRY(upload(c, c->d_col_tile, ct.data(), ct.size() * sizeof(int)));
     const size_t tmp = csr_scan_tmp_elems(npts + 1);
     CGS_CUDA(c, c->d_csr_cnt.ensure((size_t)(npts + 1) * sizeof(unsigned)));
-    CGS_CUDA(c, c->d_csr_ptr.ensure((size_t)(npts + 1) * sizeof(unsigned)));
+    // padding: the staged gather copies whole 16-byte words past a slab's last offset and tap
+    CGS_CUDA(c, c->d_csr_ptr.ensure((size_t)(npts + 8) * sizeof(unsigned)));
     CGS_CUDA(c, c->d_csr_tmp.ensure(tmp * sizeof(unsigned)));
     CGS_CUDA(c, c->d_flag.ensure(sizeof(int)));
     CGS_CUDA(c, cudaMemsetAsync(c->d_flag.p, 0, sizeof(int), c->stream));
@@ -444,7 +446,7 @@ int build_csr(cgs_ctx* c)
     unsigned long long ne = 0;
     CGS_CUDA(c, csr_count_and_scan(a, npts, c->d_csr_ptr.as<unsigned>(), c->d_csr_tmp.as<unsigned>(), tmp, &ne,
                                    c->stream));
-    CGS_CUDA(c, c->d_csr_ent.ensure(std::max<unsigned long long>(ne, 1) * sizeof(int2)));
+    CGS_CUDA(c, c->d_csr_ent.ensure((ne + 2) * sizeof(int2)));
     a.ent = c->d_csr_ent.as<int2>();
     CGS_CUDA(c, csr_fill_and_order(a, npts, c->stream));
     int bad = 0;
@@ -762,7 +764,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
             for (int b = b0; b < b0 + nb; ++b)
                 sa.live_max = (int)std::max<long long>(sa.live_max, c->h_live_off[b + 1] - c->h_live_off[b]);
         }
-        if (sup && c->spread_wpp == 6 && c->csr_valid) {
+        if (sup && (c->spread_wpp == 6 || c->spread_wpp == 7) && c->csr_valid) {
             // gather over the transposed tap matrix: stores the listed tiles' points
             CsrSpreadArgs ca{};
             ca.grid = c->d_grid.as<float2>();
@@ -781,10 +783,12 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
             ca.tb = fft_strided_cols(Gx);
             ca.cc = c->spread_cc;   // coils per thread of the gather (0: by the coil count)
             if (ca.cc != 2 && ca.cc != 4 && ca.cc != 6 && ca.cc != 8) ca.cc = 0;
-            CGS_LAUNCH(c, launch_spread_csr(ca, c->kahan, c->stream));
+            ca.err = c->d_err.as<int>();
+            // variant 6: the matrix staged in shared memory; 7: read from global memory
+            CGS_LAUNCH(c, launch_spread_csr(ca, c->kahan, c->spread_wpp == 6, c->stream));
         } else {
-            // variant 6 without its matrix: the two-warps-per-plane tiled kernel
-            const int wpp = c->spread_wpp == 6 ? 2 : c->spread_wpp;
+            // variants 6 / 7 without their matrix: the two-warps-per-plane tiled kernel
+            const int wpp = c->spread_wpp >= 6 ? 2 : c->spread_wpp;
             if (wpp == 2 && sa.cc < 2) sa.cc = std::min(2, c->nch);
             CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->kahan, wpp, c->stream));
         }
@@ -2082,12 +2086,12 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
     }
     float best = 1e30f;
     int best_sc = sc[0], best_wpp = 1;
-    for (int wpp : {1, 2, 4, 5, 3, 6}) {
+    for (int wpp : {1, 2, 4, 5, 3, 7, 6}) {
         if (wpp == 3 && (c->deterministic || c->kahan)) continue;
         if ((wpp == 4 || wpp == 5) && c->kahan) continue;
-        if (wpp == 6 && !(c->csr_valid && support_pruned(c))) continue;
+        if (wpp >= 6 && !(c->csr_valid && support_pruned(c))) continue;
         // the gather's shape parameter is its coils per thread
-        const std::vector<int> cand = wpp == 6 ? std::vector<int>{4, 6, 8} : sc;
+        const std::vector<int> cand = wpp >= 6 ? std::vector<int>{4, 6, 8} : sc;
         for (int v : cand) {
             if (wpp == 2 && v < 2) continue;
             c->spread_cc = v;
@@ -2468,7 +2472,7 @@ int cgs_set_launch_shape(cgs_ctx* c, int32_t spread_cc, int32_t spread_variant, 
 {
     if (!c) return CGS_ERR_ARG;
     if (spread_cc < 0 || spread_cc > spread_max_coils(c->kahan)) return fail(c, CGS_ERR_ARG, "spread_cc out of range");
-    if (spread_variant < 1 || spread_variant > 6 || (spread_variant >= 3 && spread_variant <= 5 && c->kahan) ||
+    if (spread_variant < 1 || spread_variant > 7 || (spread_variant >= 3 && spread_variant <= 5 && c->kahan) ||
         (spread_variant == 3 && c->deterministic))
         return fail(c, CGS_ERR_ARG, "spreading variant not allowed here");
     if (interp_cc != 2 && interp_cc != 4 && interp_cc != 6 && interp_cc != 8)

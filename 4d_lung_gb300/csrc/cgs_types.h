@@ -188,6 +188,7 @@ struct CsrSpreadArgs {
     long long B;               // Gy * Gz
     int tb;
     int cc;                    // coils per thread (2, 4, 6, 8; 0: by the coil count)
+    int* err;                  // error flag (a bounded wait of the staged form ran out)
 };
 
 // Toeplitz embedding (toeplitz.cu): the spectrum P of one bin's point-spread

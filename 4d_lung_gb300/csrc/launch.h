@@ -51,7 +51,7 @@ cudaError_t csr_count_and_scan(const CsrBuildArgs& a, long long npts, unsigned* 
                                size_t scan_tmp_elems, unsigned long long* entries, cudaStream_t s);
 cudaError_t csr_fill_and_order(const CsrBuildArgs& a, long long npts, cudaStream_t s);
 size_t csr_scan_tmp_elems(long long n);
-cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, cudaStream_t s);
+cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, bool staged, cudaStream_t s);
 
 // samples: reference order [nch][ns] <-> sorted, coil-interleaved [total][nch]
 cudaError_t launch_gather_samples(const float2* data, long long ns, const int* sorted, long long total, int nch,

@@ -13,6 +13,7 @@
 // every point of the listed tiles is stored (zeros where no tap lands).
 #include "launch.h"
 #include "gridding_common.cuh"
+#include "ptx_async.cuh"
 
 namespace cgs {
 
@@ -297,6 +298,168 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
     }
 }
 
+// ---------------------------------------------------------------------------
+// The same gather with the matrix staged in shared memory.  Work unit: a
+// slab of CSR_SX consecutive x rows of one listed tile (CSR_SX * tb points,
+// consecutive in the matrix, so their row offsets and their taps are two
+// contiguous ranges).  One thread per block issues both ranges of the unit
+// CSR_NST - 1 ahead as bulk copies (cp.async.bulk, completion on an
+// mbarrier); the threads then read row offsets and taps from shared memory
+// and only the sample values (L2-resident) from global memory, which takes
+// the matrix's DRAM latency out of every point's dependent-load chain.  A
+// slab with more than CSR_CAP taps reads its taps from global memory as
+// the unstaged kernel does.  Sums, their order and the stores are those of
+// k_spread_csr: the grids are bitwise equal.
+// Every wait is bounded: on a timeout the block sets the error flag, lets
+// its issued copies land and leaves.
+// ---------------------------------------------------------------------------
+constexpr int CSR_SX = 32;            // x rows per unit
+constexpr int CSR_CAP = 2048;         // staged taps per unit
+constexpr int CSR_NST = 2;            // pipeline stages
+constexpr unsigned long long CSR_WAIT_NS = 2000000000ull;
+
+__host__ __device__ inline int csr_ptr_stride(int tb) { return ((CSR_SX * tb + 1) + 3) & ~3; }
+
+static size_t csr_staged_smem(int tb)
+{
+    return (size_t)CSR_NST * ((size_t)csr_ptr_stride(tb) * sizeof(unsigned) + (size_t)CSR_CAP * sizeof(int2)) +
+           CSR_NST * sizeof(uint64_t);
+}
+
+template <int CC, bool KAHAN>
+__global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_staged(CsrSpreadArgs a, long long nunits)
+{
+    extern __shared__ float4 s_csr[];
+    const int PS = csr_ptr_stride(a.tb);
+    int2* s_ent = reinterpret_cast<int2*>(s_csr);                       // [CSR_NST][CSR_CAP]
+    unsigned* s_ptr = reinterpret_cast<unsigned*>(s_ent + CSR_NST * CSR_CAP);   // [CSR_NST][PS]
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_ptr + CSR_NST * PS);
+    const int nchunk = (a.nch + CC - 1) / CC;
+    const int tid = threadIdx.x;
+    const int k = tid % a.tb;
+    const int ch = (tid / a.tb) % nchunk;
+    const int xo = tid / (a.tb * nchunk), xs = blockDim.x / (a.tb * nchunk);
+    const int c0 = ch * CC;
+    const int ncc = min(CC, a.nch - c0);
+    const int nslab = (a.Gx + CSR_SX - 1) / CSR_SX;
+    const bool pairs = (a.nch % 2) == 0 && (reinterpret_cast<uintptr_t>(a.yv) & 15) == 0 && ncc == CC;
+    auto load_v = [&](int i, float2 (&vv)[CC]) {
+        const float2* v = a.yv + (long long)i * a.nch + c0;
+        if (pairs) {
+#pragma unroll
+            for (int c = 0; c < CC; c += 2) {
+                const float4 f = __ldg(reinterpret_cast<const float4*>(v + c));
+                vv[c] = make_float2(f.x, f.y);
+                vv[c + 1] = make_float2(f.z, f.w);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < CC; ++c) vv[c] = c < ncc ? __ldg(v + c) : make_float2(0.f, 0.f);
+        }
+    };
+    float2 acc[CC], cmp[CC];
+    auto add = [&](const float2 (&vv)[CC], float w) {
+#pragma unroll
+        for (int c = 0; c < CC; ++c) {
+            if (KAHAN) {
+                const float yx = fmaf(vv[c].x, w, -cmp[c].x), yy = fmaf(vv[c].y, w, -cmp[c].y);
+                const float sx = __fadd_rn(acc[c].x, yx), sy = __fadd_rn(acc[c].y, yy);
+                cmp[c].x = __fsub_rn(__fsub_rn(sx, acc[c].x), yx);
+                cmp[c].y = __fsub_rn(__fsub_rn(sy, acc[c].y), yy);
+                acc[c] = make_float2(sx, sy);
+            } else {
+                acc[c].x = fmaf(vv[c].x, w, acc[c].x);
+                acc[c].y = fmaf(vv[c].y, w, acc[c].y);
+            }
+        }
+    };
+    // unit u: slab u % nslab of tile j0 + u / nslab
+    auto unit = [&](long long u, long long& J, int& xa, int& nx) {
+        J = a.j0 + u / nslab;
+        xa = (int)(u % nslab) * CSR_SX;
+        nx = min(CSR_SX, a.Gx - xa);
+    };
+    auto issue = [&](long long kk) {   // thread 0 only
+        long long J;
+        int xa, nx;
+        unit(blockIdx.x + kk * gridDim.x, J, xa, nx);
+        const long long p0 = (J * a.Gx + xa) * a.tb;
+        const int np = nx * a.tb;
+        const unsigned e0a = __ldg(a.ptr + p0) & ~1u, e1 = __ldg(a.ptr + p0 + np);
+        const unsigned ne = e1 - e0a;
+        const uint32_t pb = ((uint32_t)(np + 1) * 4u + 15u) & ~15u;
+        const uint32_t eb = ne <= (unsigned)CSR_CAP ? ((ne * 8u + 15u) & ~15u) : 0u;
+        const int st = (int)(kk % CSR_NST);
+        mbar_arrive_expect_tx(&s_bar[st], pb + eb);
+        bulk_load(s_ptr + st * PS, a.ptr + p0, pb, &s_bar[st]);
+        if (eb) bulk_load(s_ent + st * CSR_CAP, a.ent + e0a, eb, &s_bar[st]);
+    };
+    if (tid == 0) {
+        for (int st = 0; st < CSR_NST; ++st) mbar_init(&s_bar[st], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const long long my_n = nunits > (long long)blockIdx.x ? (nunits - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    if (tid == 0)
+        for (long long kk = 0; kk < CSR_NST - 1 && kk < my_n; ++kk) issue(kk);
+    for (long long kk = 0; kk < my_n; ++kk) {
+        const int st = (int)(kk % CSR_NST);
+        if (tid == 0 && kk + CSR_NST - 1 < my_n) issue(kk + CSR_NST - 1);
+        const bool ok = mbar_wait_bounded(&s_bar[st], (uint32_t)((kk / CSR_NST) & 1), CSR_WAIT_NS);
+        if (__syncthreads_or(!ok)) {
+            // timeout: report, let the copies already issued land, leave
+            if (tid == 0) {
+                atomicExch(a.err, 1);
+                for (long long j = kk; j < my_n && j < kk + CSR_NST; ++j)
+                    mbar_wait_bounded(&s_bar[j % CSR_NST], (uint32_t)((j / CSR_NST) & 1), CSR_WAIT_NS);
+            }
+            return;
+        }
+        long long J;
+        int xa, nx;
+        unit(blockIdx.x + kk * gridDim.x, J, xa, nx);
+        const unsigned* sp = s_ptr + st * PS;
+        const int2* se = s_ent + st * CSR_CAP;
+        const unsigned e0a = sp[0] & ~1u;
+        const bool staged = sp[nx * a.tb] - e0a <= (unsigned)CSR_CAP;
+        auto entry = [&](unsigned q) { return staged ? se[q - e0a] : __ldg(a.ent + q); };
+        const int2 t = a.tiles[J];
+        float2* g = a.grid + (long long)(t.x - a.bin0) * a.grid_bs + (long long)c0 * a.coil_stride;
+        const bool col_ok = (long long)t.y + k < a.B;
+        for (int x = xo; x < nx; x += xs) {
+            const unsigned e0 = sp[x * a.tb + k], e1 = sp[x * a.tb + k + 1];
+#pragma unroll
+            for (int c = 0; c < CC; ++c) acc[c] = cmp[c] = make_float2(0.f, 0.f);
+            unsigned q = e0;
+            for (; q + 1 < e1; q += 2) {
+                const int2 u = entry(q), v = entry(q + 1);
+                float2 vu[CC], vv[CC];
+                load_v(u.x, vu);
+                load_v(v.x, vv);
+                add(vu, __int_as_float(u.y));
+                add(vv, __int_as_float(v.y));
+            }
+            if (q < e1) {
+                const int2 u = entry(q);
+                float2 vu[CC];
+                load_v(u.x, vu);
+                add(vu, __int_as_float(u.y));
+            }
+            if (col_ok) {
+                const long long go = (long long)(xa + x) * a.B + t.y + k;
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+                    if (c < ncc) {
+                        float2 o = acc[c];
+                        if (KAHAN) o = make_float2(__fsub_rn(o.x, cmp[c].x), __fsub_rn(o.y, cmp[c].y));
+                        g[(long long)c * a.coil_stride + go] = o;
+                    }
+            }
+        }
+        __syncthreads();   // the stage is free for the copy issued next
+    }
+}
+
 static int sm_count_csr()
 {
     static int n = 0;
@@ -324,14 +487,51 @@ static cudaError_t spread_csr_run(const CsrSpreadArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+template <int CC, bool KAHAN>
+static cudaError_t spread_csr_staged_run(const CsrSpreadArgs& a, cudaStream_t s)
+{
+    const int nchunk = (a.nch + CC - 1) / CC;
+    const int per = a.tb * nchunk;
+    if (per > 256) return cudaErrorInvalidValue;
+    const int nt = (256 / per) * per;
+    const size_t smem = csr_staged_smem(a.tb);
+    static bool attr = false;   // above 48 KiB only with the opt-in (set once per template)
+    if (!attr && smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(k_spread_csr_staged<CC, KAHAN>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spread_csr_staged<CC, KAHAN>, nt, smem);
+    if (e != cudaSuccess) return e;
+    const long long nunits = a.nj * ((a.Gx + CSR_SX - 1) / CSR_SX);
+    const long long nblk = std::min<long long>(nunits, (long long)sm_count_csr() * std::max(per_sm, 1));
+    k_spread_csr_staged<CC, KAHAN><<<(unsigned)nblk, nt, smem, s>>>(a, nunits);
+    return cudaGetLastError();
+}
+
 // coils per thread: a.cc (2, 4, 6, 8) or, with 0, 2 / 4 for up to 2 / 4
-// coils, else 6 (12 coils: two threads per point)
-cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, cudaStream_t s)
+// coils, else 6 (12 coils: two threads per point).  staged: the
+// shared-memory staged form (needs the error flag and 16-byte aligned row
+// offsets of every slab: tb a multiple of 4, 16-byte aligned arrays).
+cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, bool staged, cudaStream_t s)
 {
     if (a.nj <= 0) return cudaSuccess;
     if (a.tb < 1 || a.tb > 32 || a.nch < 1) return cudaErrorInvalidValue;
     int cc = a.cc;
     if (cc == 0) cc = a.nch <= 2 ? 2 : a.nch <= 4 ? 4 : 6;
+    staged = staged && a.err && (a.tb % 4) == 0 && (reinterpret_cast<uintptr_t>(a.ptr) & 15) == 0 &&
+             (reinterpret_cast<uintptr_t>(a.ent) & 15) == 0;
+    if (staged) {
+        switch (cc) {
+        case 2: return kahan ? spread_csr_staged_run<2, true>(a, s) : spread_csr_staged_run<2, false>(a, s);
+        case 4: return kahan ? spread_csr_staged_run<4, true>(a, s) : spread_csr_staged_run<4, false>(a, s);
+        case 6: return kahan ? spread_csr_staged_run<6, true>(a, s) : spread_csr_staged_run<6, false>(a, s);
+        case 8: return kahan ? spread_csr_staged_run<8, true>(a, s) : spread_csr_staged_run<8, false>(a, s);
+        }
+        return cudaErrorInvalidValue;
+    }
     switch (cc) {
     case 2: return kahan ? spread_csr_run<2, true>(a, s) : spread_csr_run<2, false>(a, s);
     case 4: return kahan ? spread_csr_run<4, true>(a, s) : spread_csr_run<4, false>(a, s);

@@ -765,7 +765,7 @@ def run_ours(args):
     support = reco.support_stats()
     taps, points = reco.spread_matrix_stats()
     variant = tune.get("spread_variant") if tune else 6   # the library's default is the gather
-    gather = variant == 6 and taps > 0
+    gather = variant in (6, 7) and taps > 0
     matrix = (taps, points) if gather else None
     y_listed = reco.forward_y_listed_rows()
     sb = stage_bytes(w, sizes, support, matrix, y_listed)

@@ -313,9 +313,11 @@ int cgs_set_deterministic(cgs_ctx* ctx, int32_t on);
  * plane of a tile; 3: shared-memory atomics, only with determinism off;
  * 4 / 5: persistent and software-pipelined with one / two warps per plane;
  * 6 (default): a gather over the transposed tap matrix, built with the bins
- * when sample-support pruning is on -- without it variant 2 runs; its
- * spread_cc is the coils per thread, 2, 4, 6 or 8, 0 by the coil count),
- * coils per interpolation thread (2, 4, 6, 8).  Variants 1, 2, 4, 5, 6 give
+ * when sample-support pruning is on -- without it variant 2 runs -- whose
+ * row offsets and taps are staged in shared memory by bulk copies; 7: the
+ * same gather reading the matrix from global memory; for 6 and 7 spread_cc
+ * is the coils per thread, 2, 4, 6 or 8, 0 by the coil count), coils per
+ * interpolation thread (2, 4, 6, 8).  Variants 1, 2, 4, 5, 6, 7 give
  * bitwise-identical results. */
 int cgs_set_launch_shape(cgs_ctx* ctx, int32_t spread_cc, int32_t spread_variant, int32_t interp_cc);
 

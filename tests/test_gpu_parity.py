@@ -202,8 +202,8 @@ def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
     r.set_smaps(smaps)
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 5)
     tune = r.autotune()
-    assert tune["spread_variant"] in (1, 2, 4, 5, 6)
-    if tune["spread_variant"] == 6:   # the gather's parameter: coils per thread
+    assert tune["spread_variant"] in (1, 2, 4, 5, 6, 7)
+    if tune["spread_variant"] in (6, 7):   # the gather's parameter: coils per thread
         assert tune["spread_coils_per_block"] in (4, 6, 8)
     else:
         assert tune["spread_coils_per_block"] in range(1, nch + 1)
@@ -218,8 +218,9 @@ def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
 def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid, nch):
     """The fixed-order spreading variants (one / two warps per x plane,
     plain or persistent and pipelined, the gather over the transposed tap
-    matrix) and every coil chunk size give bitwise-identical solves: each
-    grid value is summed in the same order."""
+    matrix with and without its shared-memory staging) and every coil chunk
+    size give bitwise-identical solves: each grid value is summed in the
+    same order."""
     k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 48)
     bins = synth.bin_samples([np.arange(0, 7), np.arange(7, 41), np.arange(41, 60)], 48)
     smaps = synth.coil_maps(img, nch)
@@ -232,7 +233,7 @@ def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, g
     r.set_launch_shape(0, 1, 4)
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 4)
     for cc in (0, 3, 5):
-        for variant in (1, 2, 4, 5, 6):
+        for variant in (1, 2, 4, 5, 6, 7):
             r.set_launch_shape(cc, variant, 2)
             x1, res1, _ = r.cg_sense_batched(data, 0.0, 4)
             assert np.array_equal(x1, x0), (cc, variant)
@@ -244,6 +245,9 @@ def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, g
     r.set_launch_shape(0, 6, 2)
     xk6, rk6, _ = r.cg_sense_batched(data, 0.0, 4)
     assert np.array_equal(xk, xk6) and np.array_equal(rk, rk6)
+    r.set_launch_shape(0, 7, 2)
+    xk7, rk7, _ = r.cg_sense_batched(data, 0.0, 4)
+    assert np.array_equal(xk, xk7) and np.array_equal(rk, rk7)
 
 
 @pytest.mark.parametrize("img,grid,nch", [((32, 24, 20), (64, 48, 40), 5),
@@ -274,7 +278,7 @@ def test_support_pruning_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid
     out = {}
     for on in (True, False):
         r.set_support_pruning(on)
-        for variant in (1, 2, 4, 6):
+        for variant in (1, 2, 4, 6, 7):
             r.set_launch_shape(0, variant, 2)
             out[on, variant] = r.cg_sense_batched(data, 0.0, 4)[:2]
     ref = out[False, 1]
@@ -310,7 +314,7 @@ def test_atomic_spreading_matches_fixed_order(gpu_lib, cgs, oracle_mod, o64, syn
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 5)
     r.set_deterministic(False)
     tune = r.autotune()
-    assert tune["spread_variant"] in (1, 2, 3, 4, 5, 6)
+    assert tune["spread_variant"] in (1, 2, 3, 4, 5, 6, 7)
     x1, res1, _ = r.cg_sense_batched(data, 0.0, 5)
     assert rel_l2(x1, x0) < 1e-5
     assert np.allclose(res1, res0, rtol=1e-5)
