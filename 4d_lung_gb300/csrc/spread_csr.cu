@@ -299,64 +299,66 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
 }
 
 // ---------------------------------------------------------------------------
-// The same gather with the matrix staged in shared memory.  Work unit: a
-// slab of CSR_SX consecutive x rows of one listed tile (CSR_SX * tb points,
-// consecutive in the matrix, so their row offsets and their taps are two
-// contiguous ranges).  One thread per block issues both ranges of the unit
-// CSR_NST - 1 ahead as bulk copies (cp.async.bulk, completion on an
-// mbarrier); the threads then read row offsets and taps from shared memory
-// and only the sample values (L2-resident) from global memory, which takes
-// the matrix's DRAM latency out of every point's dependent-load chain.  A
-// slab with more than CSR_CAP taps reads its taps from global memory as
-// the unstaged kernel does.  Sums, their order and the stores are those of
-// k_spread_csr: the grids are bitwise equal.
-// Every wait is bounded: on a timeout the block sets the error flag, lets
-// its issued copies land and leaves.
+// The same gather in two phases per work unit, with everything it reads
+// staged in shared memory.  Work unit: a slab of CSR_SX consecutive x rows
+// of one listed tile (CSR_SX * tb points, consecutive in the matrix, so
+// their row offsets and their taps are two contiguous ranges).
+//   * One thread per block issues both ranges of the unit CSR_NST - 1 units
+//     ahead as bulk copies (cp.async.bulk, completion on an mbarrier).
+//   * Phase 1: the block gathers the sample values of the unit's taps
+//     (every coil, 16-byte cp.async copies, all independent: many loads in
+//     flight per thread and no registers held) into shared memory.
+//   * Phase 2: every thread sums its points' taps from shared memory in row
+//     order and stores the points once, as k_spread_csr does.
+// A unit whose taps exceed the staged values' capacity is done in several
+// sub-passes of consecutive points (a point with more taps than the
+// capacity reads the rest from global memory); a unit with more taps than
+// the matrix stage holds reads the matrix from global memory.  Sums, their
+// order and the stores are those of k_spread_csr: the grids are bitwise
+// equal.  Every wait is bounded: on a timeout the block sets the error flag,
+// lets its issued copies land and leaves.
 // ---------------------------------------------------------------------------
-constexpr int CSR_SX = 32;            // x rows per unit
-constexpr int CSR_CAP = 2048;         // staged taps per unit
-constexpr int CSR_NST = 2;            // pipeline stages
+constexpr int CSR_SX = 16;            // x rows per unit
+constexpr int CSR_CAP = 1024;         // staged taps per unit (matrix stage)
+constexpr int CSR_NST = 2;            // pipeline stages of the matrix
+constexpr int CSR_VAL_BYTES = 48 * 1024;   // staged sample values
 constexpr unsigned long long CSR_WAIT_NS = 2000000000ull;
 
 __host__ __device__ inline int csr_ptr_stride(int tb) { return ((CSR_SX * tb + 1) + 3) & ~3; }
 
 static size_t csr_staged_smem(int tb)
 {
-    return (size_t)CSR_NST * ((size_t)csr_ptr_stride(tb) * sizeof(unsigned) + (size_t)CSR_CAP * sizeof(int2)) +
+    return (size_t)CSR_VAL_BYTES +
+           (size_t)CSR_NST * ((size_t)csr_ptr_stride(tb) * sizeof(unsigned) + (size_t)CSR_CAP * sizeof(int2)) +
            CSR_NST * sizeof(uint64_t);
 }
 
+CGS_D void cp_async16(void* dst_smem, const void* src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst_smem)), "l"(src) : "memory");
+}
+CGS_D void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 template <int CC, bool KAHAN>
-__global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_staged(CsrSpreadArgs a, long long nunits)
+__global__ void __launch_bounds__(256, 3) k_spread_csr_staged(CsrSpreadArgs a, long long nunits)
 {
     extern __shared__ float4 s_csr[];
     const int PS = csr_ptr_stride(a.tb);
-    int2* s_ent = reinterpret_cast<int2*>(s_csr);                       // [CSR_NST][CSR_CAP]
-    unsigned* s_ptr = reinterpret_cast<unsigned*>(s_ent + CSR_NST * CSR_CAP);   // [CSR_NST][PS]
+    float2* s_val = reinterpret_cast<float2*>(s_csr);                                        // [capv][nch]
+    int2* s_ent = reinterpret_cast<int2*>(reinterpret_cast<char*>(s_csr) + CSR_VAL_BYTES);  // [CSR_NST][CSR_CAP]
+    unsigned* s_ptr = reinterpret_cast<unsigned*>(s_ent + CSR_NST * CSR_CAP);               // [CSR_NST][PS]
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_ptr + CSR_NST * PS);
-    const int nchunk = (a.nch + CC - 1) / CC;
-    const int tid = threadIdx.x;
+    const int nch = a.nch;
+    const int capv = CSR_VAL_BYTES / (nch * (int)sizeof(float2));
+    const int nchunk = (nch + CC - 1) / CC;
+    const int tid = threadIdx.x, nt = blockDim.x;
     const int k = tid % a.tb;
     const int ch = (tid / a.tb) % nchunk;
-    const int xo = tid / (a.tb * nchunk), xs = blockDim.x / (a.tb * nchunk);
+    const int xo = tid / (a.tb * nchunk), xs = nt / (a.tb * nchunk);
     const int c0 = ch * CC;
-    const int ncc = min(CC, a.nch - c0);
+    const int ncc = min(CC, nch - c0);
     const int nslab = (a.Gx + CSR_SX - 1) / CSR_SX;
-    const bool pairs = (a.nch % 2) == 0 && (reinterpret_cast<uintptr_t>(a.yv) & 15) == 0 && ncc == CC;
-    auto load_v = [&](int i, float2 (&vv)[CC]) {
-        const float2* v = a.yv + (long long)i * a.nch + c0;
-        if (pairs) {
-#pragma unroll
-            for (int c = 0; c < CC; c += 2) {
-                const float4 f = __ldg(reinterpret_cast<const float4*>(v + c));
-                vv[c] = make_float2(f.x, f.y);
-                vv[c + 1] = make_float2(f.z, f.w);
-            }
-        } else {
-#pragma unroll
-            for (int c = 0; c < CC; ++c) vv[c] = c < ncc ? __ldg(v + c) : make_float2(0.f, 0.f);
-        }
-    };
+    const int v4 = nch / 2;   // 16-byte copies per sample (nch even)
     float2 acc[CC], cmp[CC];
     auto add = [&](const float2 (&vv)[CC], float w) {
 #pragma unroll
@@ -418,45 +420,81 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_s
         long long J;
         int xa, nx;
         unit(blockIdx.x + kk * gridDim.x, J, xa, nx);
+        const int np = nx * a.tb;
         const unsigned* sp = s_ptr + st * PS;
         const int2* se = s_ent + st * CSR_CAP;
         const unsigned e0a = sp[0] & ~1u;
-        const bool staged = sp[nx * a.tb] - e0a <= (unsigned)CSR_CAP;
+        const bool staged = sp[np] - e0a <= (unsigned)CSR_CAP;
         auto entry = [&](unsigned q) { return staged ? se[q - e0a] : __ldg(a.ent + q); };
         const int2 t = a.tiles[J];
         float2* g = a.grid + (long long)(t.x - a.bin0) * a.grid_bs + (long long)c0 * a.coil_stride;
         const bool col_ok = (long long)t.y + k < a.B;
-        for (int x = xo; x < nx; x += xs) {
-            const unsigned e0 = sp[x * a.tb + k], e1 = sp[x * a.tb + k + 1];
-#pragma unroll
-            for (int c = 0; c < CC; ++c) acc[c] = cmp[c] = make_float2(0.f, 0.f);
-            unsigned q = e0;
-            for (; q + 1 < e1; q += 2) {
-                const int2 u = entry(q), v = entry(q + 1);
-                float2 vu[CC], vv[CC];
-                load_v(u.x, vu);
-                load_v(v.x, vv);
-                add(vu, __int_as_float(u.y));
-                add(vv, __int_as_float(v.y));
+        // sub-passes over consecutive points whose taps fit the staged values
+        for (int ps = 0; ps < np;) {
+            const unsigned qs = sp[ps];
+            int pe = np;
+            if (sp[np] - qs > (unsigned)capv) {   // largest pe with sp[pe] - qs <= capv (same in every thread)
+                int lo = ps, hi = np;
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (sp[mid] - qs <= (unsigned)capv) lo = mid;
+                    else hi = mid;
+                }
+                pe = lo > ps ? lo : ps + 1;   // a point heavier than the capacity reads its rest globally
             }
-            if (q < e1) {
-                const int2 u = entry(q);
-                float2 vu[CC];
-                load_v(u.x, vu);
-                add(vu, __int_as_float(u.y));
+            const unsigned nv = min(sp[pe] - qs, (unsigned)capv);
+            // phase 1: values of taps [qs, qs + nv), every coil
+            for (unsigned j = tid; j < nv * (unsigned)v4; j += nt) {
+                const unsigned e = j / v4, c2 = j - e * v4;
+                const int smp = entry(qs + e).x;
+                cp_async16(s_val + (size_t)e * nch + 2 * c2, a.yv + (long long)smp * nch + 2 * c2);
             }
-            if (col_ok) {
-                const long long go = (long long)(xa + x) * a.B + t.y + k;
+            cp_async_wait_all();
+            __syncthreads();
+            // phase 2: the points of [ps, pe) in row order
+            for (int x = xo; x < nx; x += xs) {
+                const int pl = x * a.tb + k;
+                if (pl < ps || pl >= pe) continue;
+                const unsigned e0 = sp[pl], e1 = sp[pl + 1];
 #pragma unroll
-                for (int c = 0; c < CC; ++c)
-                    if (c < ncc) {
-                        float2 o = acc[c];
-                        if (KAHAN) o = make_float2(__fsub_rn(o.x, cmp[c].x), __fsub_rn(o.y, cmp[c].y));
-                        g[(long long)c * a.coil_stride + go] = o;
+                for (int c = 0; c < CC; ++c) acc[c] = cmp[c] = make_float2(0.f, 0.f);
+                for (unsigned q = e0; q < e1; ++q) {
+                    const int2 u = entry(q);
+                    float2 vv[CC];
+                    const unsigned j = q - qs;
+                    if (j < nv) {
+                        const float2* v = s_val + (size_t)j * nch + c0;
+#pragma unroll
+                        for (int c = 0; c < CC; c += 2) {
+                            if (c < ncc) {
+                                const float4 f = *reinterpret_cast<const float4*>(v + c);
+                                vv[c] = make_float2(f.x, f.y);
+                                vv[c + 1] = make_float2(f.z, f.w);
+                            } else {
+                                vv[c] = vv[c + 1] = make_float2(0.f, 0.f);
+                            }
+                        }
+                    } else {
+                        const float2* v = a.yv + (long long)u.x * nch + c0;
+#pragma unroll
+                        for (int c = 0; c < CC; ++c) vv[c] = c < ncc ? __ldg(v + c) : make_float2(0.f, 0.f);
                     }
+                    add(vv, __int_as_float(u.y));
+                }
+                if (col_ok) {
+                    const long long go = (long long)(xa + x) * a.B + t.y + k;
+#pragma unroll
+                    for (int c = 0; c < CC; ++c)
+                        if (c < ncc) {
+                            float2 o = acc[c];
+                            if (KAHAN) o = make_float2(__fsub_rn(o.x, cmp[c].x), __fsub_rn(o.y, cmp[c].y));
+                            g[(long long)c * a.coil_stride + go] = o;
+                        }
+                }
             }
+            __syncthreads();   // the values (and, after the last sub-pass, the stage) are free
+            ps = pe;
         }
-        __syncthreads();   // the stage is free for the copy issued next
     }
 }
 
@@ -521,8 +559,12 @@ cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, bool staged, c
     if (a.tb < 1 || a.tb > 32 || a.nch < 1) return cudaErrorInvalidValue;
     int cc = a.cc;
     if (cc == 0) cc = a.nch <= 2 ? 2 : a.nch <= 4 ? 4 : 6;
+    // the staged form: an error flag, 16-byte aligned row offsets of every
+    // slab (tb a multiple of 4), 16-byte sample values (an even coil count,
+    // coils per thread even) and room for at least one sample's values
     staged = staged && a.err && (a.tb % 4) == 0 && (reinterpret_cast<uintptr_t>(a.ptr) & 15) == 0 &&
-             (reinterpret_cast<uintptr_t>(a.ent) & 15) == 0;
+             (reinterpret_cast<uintptr_t>(a.ent) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.yv) & 15) == 0 &&
+             (a.nch % 2) == 0 && (cc % 2) == 0 && a.nch * (int)sizeof(float2) <= CSR_VAL_BYTES;
     if (staged) {
         switch (cc) {
         case 2: return kahan ? spread_csr_staged_run<2, true>(a, s) : spread_csr_staged_run<2, false>(a, s);
