@@ -8,6 +8,7 @@
 #include "launch.h"
 
 #include <algorithm>
+#include <chrono>
 #include <sys/stat.h>
 #include <thread>
 #include <cmath>
@@ -144,6 +145,10 @@ struct cgs_ctx {
     bool toep_valid = false;
     uint64_t toep_serial = 0;    // traj_serial the spectra were built from
     double toep_build_ms = 0.0;
+    // set-up cost of the last rebuild of the bins and of the last graph
+    // capture (host clock, ms): sort, tap records, tile and support lists,
+    // transposed tap matrix, workspaces, graph capture + instantiation
+    double setup_ms[6] = {0, 0, 0, 0, 0, 0};
     DevBuf d_toep, d_ones;
     void* blas = nullptr;        // cuBLAS handle of the spectrum builds
     // coil maps
@@ -489,6 +494,9 @@ int rebuild_bins(cgs_ctx* c)
     }
     if (c->ns == 0) return fail(c, CGS_ERR_STATE, "no trajectory set");
     drop_graphs(c);
+    using clk = std::chrono::steady_clock;
+    auto ms_since = [](clk::time_point t0) { return std::chrono::duration<double, std::milli>(clk::now() - t0).count(); };
+    auto t0 = clk::now();
     c->nbins = (int)c->bins.size();
     std::vector<BinPrep> prep(c->nbins);
     c->h_bin_off.assign(c->nbins + 1, 0);
@@ -504,6 +512,8 @@ int rebuild_bins(cgs_ctx* c)
     for (int b = 0; b < c->nbins; ++b) sorted.insert(sorted.end(), prep[b].sorted.begin(), prep[b].sorted.end());
     CGS_TRY(upload(c, c->d_sorted, sorted.data(), std::max<size_t>(sorted.size(), 1) * sizeof(int)));
     CGS_TRY(upload(c, c->d_bin_off, c->h_bin_off.data(), c->h_bin_off.size() * sizeof(long long)));
+    c->setup_ms[0] = ms_since(t0);
+    t0 = clk::now();
     // tap records (the device's nearest points decide the tile lists)
     CGS_CUDA(c, c->d_rec.ensure(std::max<long long>(c->total, 1) * sizeof(TapRecord)));
     const KbParams kb = kb_params(c);
@@ -520,6 +530,8 @@ int rebuild_bins(cgs_ctx* c)
                                     c->stream));
         CGS_CUDA(c, cudaStreamSynchronize(c->stream));
     }
+    c->setup_ms[1] = ms_since(t0);
+    t0 = clk::now();
     const int tbx = fft_strided_cols(c->G[0]);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int b = 0; b < c->nbins; ++b) {
@@ -561,7 +573,12 @@ int rebuild_bins(cgs_ctx* c)
             c->sup_rowmask_bs = bs;
         }
     }
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->setup_ms[2] = ms_since(t0);
+    t0 = clk::now();
     CGS_TRY(build_csr(c));
+    c->setup_ms[3] = ms_since(t0);
+    t0 = clk::now();
     std::vector<int> tile_ptr;
     std::vector<int> tile_idx;
     std::vector<int> plane_rng;
@@ -596,6 +613,8 @@ int rebuild_bins(cgs_ctx* c)
     CGS_CUDA(c, c->d_ybuf_adj.ensure(wsn * (long long)c->I[0] * c->G[1] * c->G[2] * sizeof(float2)));
     c->adj_slot.assign(c->ws_bins, -1);
     CGS_CUDA(c, c->d_grid.ensure(wsn * c->Ng * sizeof(float2)));
+    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->setup_ms[4] = ms_since(t0);   // the remaining lists' uploads and the workspaces
     c->toep_valid = false;
     c->bins_dirty = false;
     return CGS_OK;
@@ -1592,6 +1611,7 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
         if (c->ws_bins >= nb) CGS_TRY(prepare_adj_slots(c, 0, nb, support_pruned(c)));
         c->launches = 0;
         const std::vector<int> entry = c->adj_slot;
+        const auto tc0 = std::chrono::steady_clock::now();
         CGS_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         int st = record_solve(c, reinterpret_cast<const float2*>(data), reinterpret_cast<float2*>(x), thresh, max_iter,
                               rhs_from_images, reinterpret_cast<float2*>(x_trace));
@@ -1608,6 +1628,7 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
         if (ei != cudaSuccess) c->adj_slot = entry;
         CGS_CUDA(c, ei);
         c->graphs[key] = exec;
+        c->setup_ms[5] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tc0).count();
         c->graph_launches[key] = c->launches;
         c->graph_slots[key] = {entry, c->adj_slot};
     } else {
@@ -2465,6 +2486,13 @@ int cgs_spread_matrix_stats(cgs_ctx* c, int64_t* taps, int64_t* points)
     CGS_TRY(check_ready(c, false));
     if (taps) *taps = c->csr_valid ? (int64_t)c->csr_entries : 0;
     if (points) *points = c->csr_valid ? (int64_t)c->csr_pts : 0;
+    return CGS_OK;
+}
+
+int cgs_setup_stats(cgs_ctx* c, double* ms, int32_t n)
+{
+    if (!c || (!ms && n > 0) || n < 0) return CGS_ERR_ARG;
+    for (int i = 0; i < n && i < 6; ++i) ms[i] = c->setup_ms[i];
     return CGS_OK;
 }
 

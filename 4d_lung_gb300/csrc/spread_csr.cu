@@ -299,203 +299,188 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
 }
 
 // ---------------------------------------------------------------------------
-// The same gather in two phases per work unit, with everything it reads
-// staged in shared memory.  Work unit: a slab of CSR_SX consecutive x rows
-// of one listed tile (CSR_SX * tb points, consecutive in the matrix, so
-// their row offsets and their taps are two contiguous ranges).
-//   * One thread per block issues both ranges of the unit CSR_NST - 1 units
-//     ahead as bulk copies (cp.async.bulk, completion on an mbarrier).
-//   * Phase 1: the block gathers the sample values of the unit's taps
-//     (every coil, 16-byte cp.async copies, all independent: many loads in
-//     flight per thread and no registers held) into shared memory.
-//   * Phase 2: every thread sums its points' taps from shared memory in row
-//     order and stores the points once, as k_spread_csr does.
-// A unit whose taps exceed the staged values' capacity is done in several
-// sub-passes of consecutive points (a point with more taps than the
-// capacity reads the rest from global memory); a unit with more taps than
-// the matrix stage holds reads the matrix from global memory.  Sums, their
-// order and the stores are those of k_spread_csr: the grids are bitwise
-// equal.  Every wait is bounded: on a timeout the block sets the error flag,
-// lets its issued copies land and leaves.
+// The same gather with the matrix staged in shared memory.  Work unit: a
+// slab of CSR_SX consecutive x rows of one listed tile (CSR_SX * tb points,
+// consecutive in the matrix, so their row offsets and their taps are two
+// contiguous ranges).  One thread per block issues both ranges of the unit
+// CSR_NST - 1 ahead as bulk copies (cp.async.bulk, completion on an
+// mbarrier); the threads then read row offsets and taps from shared memory
+// and only the sample values (L2-resident) from global memory, which takes
+// the matrix's DRAM latency out of every point's dependent-load chain.  A
+// slab with more than CSR_CAP taps reads its taps from global memory as
+// the unstaged kernel does.  Sums, their order and the stores are those of
+// k_spread_csr: the grids are bitwise equal.
+// Every wait is bounded: on a timeout the block sets the error flag, lets
+// its issued copies land and leaves.
 // ---------------------------------------------------------------------------
-constexpr int CSR_SX = 16;            // x rows per unit
-constexpr int CSR_CAP = 1024;         // staged taps per unit (matrix stage)
-constexpr int CSR_NST = 2;            // pipeline stages of the matrix
-constexpr int CSR_VAL_BYTES = 48 * 1024;   // staged sample values
+constexpr int CSR_SX = 32;            // x rows per unit
+constexpr int CSR_CAP = 2048;         // staged taps per unit
+constexpr int CSR_NST = 3;            // pipeline stages
 constexpr unsigned long long CSR_WAIT_NS = 2000000000ull;
 
 __host__ __device__ inline int csr_ptr_stride(int tb) { return ((CSR_SX * tb + 1) + 3) & ~3; }
 
 static size_t csr_staged_smem(int tb)
 {
-    return (size_t)CSR_VAL_BYTES +
-           (size_t)CSR_NST * ((size_t)csr_ptr_stride(tb) * sizeof(unsigned) + (size_t)CSR_CAP * sizeof(int2)) +
-           CSR_NST * sizeof(uint64_t);
+    return (size_t)CSR_NST * ((size_t)csr_ptr_stride(tb) * sizeof(unsigned) + (size_t)CSR_CAP * sizeof(int2)) +
+           2 * CSR_NST * sizeof(uint64_t);
 }
 
-CGS_D void cp_async16(void* dst_smem, const void* src)
+CGS_D void mbar_arrive(uint64_t* bar)
 {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst_smem)), "l"(src) : "memory");
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
-CGS_D void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 template <int CC, bool KAHAN>
-__global__ void __launch_bounds__(256, 3) k_spread_csr_staged(CsrSpreadArgs a, long long nunits)
+__global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_staged(CsrSpreadArgs a, int nunits)
 {
+    static_assert(CC % 2 == 0, "sample values are read as coil pairs");
     extern __shared__ float4 s_csr[];
     const int PS = csr_ptr_stride(a.tb);
-    float2* s_val = reinterpret_cast<float2*>(s_csr);                                        // [capv][nch]
-    int2* s_ent = reinterpret_cast<int2*>(reinterpret_cast<char*>(s_csr) + CSR_VAL_BYTES);  // [CSR_NST][CSR_CAP]
-    unsigned* s_ptr = reinterpret_cast<unsigned*>(s_ent + CSR_NST * CSR_CAP);               // [CSR_NST][PS]
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_ptr + CSR_NST * PS);
-    const int nch = a.nch;
-    const int capv = CSR_VAL_BYTES / (nch * (int)sizeof(float2));
-    const int nchunk = (nch + CC - 1) / CC;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    const int k = tid % a.tb;
-    const int ch = (tid / a.tb) % nchunk;
-    const int xo = tid / (a.tb * nchunk), xs = nt / (a.tb * nchunk);
-    const int c0 = ch * CC;
-    const int ncc = min(CC, nch - c0);
-    const int nslab = (a.Gx + CSR_SX - 1) / CSR_SX;
-    const int v4 = nch / 2;   // 16-byte copies per sample (nch even)
+    int2* s_ent = reinterpret_cast<int2*>(s_csr);                                // [CSR_NST][CSR_CAP]
+    unsigned* s_ptr = reinterpret_cast<unsigned*>(s_ent + CSR_NST * CSR_CAP);   // [CSR_NST][PS]
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_ptr + CSR_NST * PS);   // [CSR_NST] full: the copies landed
+    uint64_t* s_free = s_bar + CSR_NST;                                       // [CSR_NST] empty: every warp is done
+    const int tb = a.tb;
+    const int nchunk = a.nch / CC;     // the launcher guarantees nch % CC == 0
+    const int tid = threadIdx.x;
+    const int k = tid % tb;
+    const int ch = (tid / tb) % nchunk;
+    const int xo = tid / (tb * nchunk), xs = blockDim.x / (tb * nchunk);
+    const unsigned nslab = (unsigned)((a.Gx + CSR_SX - 1) / CSR_SX);
+    const float4* yv4 = reinterpret_cast<const float4*>(a.yv) + ch * (CC / 2);
+    const int yv4_stride = a.nch / 2;
+    const long long cs = a.coil_stride;
     float2 acc[CC], cmp[CC];
-    auto add = [&](const float2 (&vv)[CC], float w) {
+    auto add = [&](const float4 (&v)[CC / 2], float w) {
 #pragma unroll
         for (int c = 0; c < CC; ++c) {
+            const float vx = (c & 1) ? v[c / 2].z : v[c / 2].x;
+            const float vy = (c & 1) ? v[c / 2].w : v[c / 2].y;
             if (KAHAN) {
-                const float yx = fmaf(vv[c].x, w, -cmp[c].x), yy = fmaf(vv[c].y, w, -cmp[c].y);
+                const float yx = fmaf(vx, w, -cmp[c].x), yy = fmaf(vy, w, -cmp[c].y);
                 const float sx = __fadd_rn(acc[c].x, yx), sy = __fadd_rn(acc[c].y, yy);
                 cmp[c].x = __fsub_rn(__fsub_rn(sx, acc[c].x), yx);
                 cmp[c].y = __fsub_rn(__fsub_rn(sy, acc[c].y), yy);
                 acc[c] = make_float2(sx, sy);
             } else {
-                acc[c].x = fmaf(vv[c].x, w, acc[c].x);
-                acc[c].y = fmaf(vv[c].y, w, acc[c].y);
+                acc[c].x = fmaf(vx, w, acc[c].x);
+                acc[c].y = fmaf(vy, w, acc[c].y);
             }
         }
     };
-    // unit u: slab u % nslab of tile j0 + u / nslab
-    auto unit = [&](long long u, long long& J, int& xa, int& nx) {
-        J = a.j0 + u / nslab;
-        xa = (int)(u % nslab) * CSR_SX;
-        nx = min(CSR_SX, a.Gx - xa);
+    auto load_v = [&](int i, float4 (&v)[CC / 2]) {
+        const float4* p = yv4 + (long long)i * yv4_stride;
+#pragma unroll
+        for (int c = 0; c < CC / 2; ++c) v[c] = __ldg(p + c);
     };
-    auto issue = [&](long long kk) {   // thread 0 only
-        long long J;
-        int xa, nx;
-        unit(blockIdx.x + kk * gridDim.x, J, xa, nx);
-        const long long p0 = (J * a.Gx + xa) * a.tb;
-        const int np = nx * a.tb;
+    // the points of a unit: row offsets sp (local), taps from ENT(q)
+    auto points = [&](const unsigned* sp, int nx, float2* gp, long long gstep, auto ent) {
+        for (int x = xo; x < nx; x += xs, gp += gstep) {
+            const unsigned e0 = sp[x * tb + k], e1 = sp[x * tb + k + 1];
+#pragma unroll
+            for (int c = 0; c < CC; ++c) acc[c] = cmp[c] = make_float2(0.f, 0.f);
+            unsigned q = e0;
+            for (; q + 1 < e1; q += 2) {
+                const int2 u = ent(q), v = ent(q + 1);
+                float4 vu[CC / 2], vv[CC / 2];
+                load_v(u.x, vu);
+                load_v(v.x, vv);
+                add(vu, __int_as_float(u.y));
+                add(vv, __int_as_float(v.y));
+            }
+            if (q < e1) {
+                const int2 u = ent(q);
+                float4 vu[CC / 2];
+                load_v(u.x, vu);
+                add(vu, __int_as_float(u.y));
+            }
+            if (gp) {
+#pragma unroll
+                for (int c = 0; c < CC; ++c) {
+                    float2 o = acc[c];
+                    if (KAHAN) o = make_float2(__fsub_rn(o.x, cmp[c].x), __fsub_rn(o.y, cmp[c].y));
+                    gp[c * cs] = o;
+                }
+            }
+        }
+    };
+    auto issue = [&](int kk) {   // thread 0 only
+        const unsigned u = blockIdx.x + (unsigned)kk * gridDim.x;
+        const unsigned jt = u / nslab;
+        const int xa = (int)(u - jt * nslab) * CSR_SX;
+        const int nx = min(CSR_SX, a.Gx - xa);
+        const long long p0 = ((a.j0 + jt) * a.Gx + xa) * tb;
+        const int np = nx * tb;
         const unsigned e0a = __ldg(a.ptr + p0) & ~1u, e1 = __ldg(a.ptr + p0 + np);
         const unsigned ne = e1 - e0a;
         const uint32_t pb = ((uint32_t)(np + 1) * 4u + 15u) & ~15u;
         const uint32_t eb = ne <= (unsigned)CSR_CAP ? ((ne * 8u + 15u) & ~15u) : 0u;
-        const int st = (int)(kk % CSR_NST);
+        const int st = kk % CSR_NST;
         mbar_arrive_expect_tx(&s_bar[st], pb + eb);
         bulk_load(s_ptr + st * PS, a.ptr + p0, pb, &s_bar[st]);
         if (eb) bulk_load(s_ent + st * CSR_CAP, a.ent + e0a, eb, &s_bar[st]);
     };
+    const int nwarps = (int)(blockDim.x + 31) / 32;
     if (tid == 0) {
-        for (int st = 0; st < CSR_NST; ++st) mbar_init(&s_bar[st], 1);
+        for (int st = 0; st < CSR_NST; ++st) {
+            mbar_init(&s_bar[st], 1);
+            mbar_init(&s_free[st], nwarps);
+        }
         fence_mbar_init();
     }
     __syncthreads();
-    const long long my_n = nunits > (long long)blockIdx.x ? (nunits - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    // No block-wide barrier per unit: a stage is refilled once every warp has
+    // arrived on its empty barrier, so fast warps run up to CSR_NST - 1 units
+    // ahead of slow ones.  Thread 0 issues unit kk + CSR_NST - 1 into the
+    // stage that unit kk - 1 used.  A wait that runs out sets the error flag
+    // and ends the warp's loop; thread 0 then lets its issued copies land.
+    const int my_n = nunits > (int)blockIdx.x ? (nunits - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    int issued = 0;
     if (tid == 0)
-        for (long long kk = 0; kk < CSR_NST - 1 && kk < my_n; ++kk) issue(kk);
-    for (long long kk = 0; kk < my_n; ++kk) {
-        const int st = (int)(kk % CSR_NST);
-        if (tid == 0 && kk + CSR_NST - 1 < my_n) issue(kk + CSR_NST - 1);
-        const bool ok = mbar_wait_bounded(&s_bar[st], (uint32_t)((kk / CSR_NST) & 1), CSR_WAIT_NS);
-        if (__syncthreads_or(!ok)) {
-            // timeout: report, let the copies already issued land, leave
-            if (tid == 0) {
+        for (; issued < CSR_NST - 1 && issued < my_n; ++issued) issue(issued);
+    bool failed = false;
+    for (int kk = 0; kk < my_n && !failed; ++kk) {
+        const int st = kk % CSR_NST;
+        if (tid == 0 && issued < my_n && issued == kk + CSR_NST - 1) {
+            if (kk > 0 && !mbar_wait_bounded(&s_free[(kk - 1) % CSR_NST], (uint32_t)(((kk - 1) / CSR_NST) & 1),
+                                             CSR_WAIT_NS)) {
                 atomicExch(a.err, 1);
-                for (long long j = kk; j < my_n && j < kk + CSR_NST; ++j)
-                    mbar_wait_bounded(&s_bar[j % CSR_NST], (uint32_t)((j / CSR_NST) & 1), CSR_WAIT_NS);
+                failed = true;
+                break;
             }
-            return;
+            issue(issued++);
         }
-        long long J;
-        int xa, nx;
-        unit(blockIdx.x + kk * gridDim.x, J, xa, nx);
-        const int np = nx * a.tb;
+        if (!mbar_wait_bounded(&s_bar[st], (uint32_t)((kk / CSR_NST) & 1), CSR_WAIT_NS)) {
+            atomicExch(a.err, 1);
+            failed = true;
+            break;
+        }
+        const unsigned u = blockIdx.x + (unsigned)kk * gridDim.x;
+        const unsigned jt = u / nslab;
+        const int xa = (int)(u - jt * nslab) * CSR_SX;
+        const int nx = min(CSR_SX, a.Gx - xa);
         const unsigned* sp = s_ptr + st * PS;
-        const int2* se = s_ent + st * CSR_CAP;
+        const int2 t = a.tiles[a.j0 + jt];
+        // store pointer of (x = xa + xo, column t.y + k, first coil of the chunk); null: no column
+        float2* gp = (long long)t.y + k < a.B
+                         ? a.grid + (long long)(t.x - a.bin0) * a.grid_bs + (long long)(ch * CC) * cs +
+                               (long long)(xa + xo) * a.B + t.y + k
+                         : nullptr;
+        const long long gstep = gp ? (long long)xs * a.B : 0;
         const unsigned e0a = sp[0] & ~1u;
-        const bool staged = sp[np] - e0a <= (unsigned)CSR_CAP;
-        auto entry = [&](unsigned q) { return staged ? se[q - e0a] : __ldg(a.ent + q); };
-        const int2 t = a.tiles[J];
-        float2* g = a.grid + (long long)(t.x - a.bin0) * a.grid_bs + (long long)c0 * a.coil_stride;
-        const bool col_ok = (long long)t.y + k < a.B;
-        // sub-passes over consecutive points whose taps fit the staged values
-        for (int ps = 0; ps < np;) {
-            const unsigned qs = sp[ps];
-            int pe = np;
-            if (sp[np] - qs > (unsigned)capv) {   // largest pe with sp[pe] - qs <= capv (same in every thread)
-                int lo = ps, hi = np;
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (sp[mid] - qs <= (unsigned)capv) lo = mid;
-                    else hi = mid;
-                }
-                pe = lo > ps ? lo : ps + 1;   // a point heavier than the capacity reads its rest globally
-            }
-            const unsigned nv = min(sp[pe] - qs, (unsigned)capv);
-            // phase 1: values of taps [qs, qs + nv), every coil
-            for (unsigned j = tid; j < nv * (unsigned)v4; j += nt) {
-                const unsigned e = j / v4, c2 = j - e * v4;
-                const int smp = entry(qs + e).x;
-                cp_async16(s_val + (size_t)e * nch + 2 * c2, a.yv + (long long)smp * nch + 2 * c2);
-            }
-            cp_async_wait_all();
-            __syncthreads();
-            // phase 2: the points of [ps, pe) in row order
-            for (int x = xo; x < nx; x += xs) {
-                const int pl = x * a.tb + k;
-                if (pl < ps || pl >= pe) continue;
-                const unsigned e0 = sp[pl], e1 = sp[pl + 1];
-#pragma unroll
-                for (int c = 0; c < CC; ++c) acc[c] = cmp[c] = make_float2(0.f, 0.f);
-                for (unsigned q = e0; q < e1; ++q) {
-                    const int2 u = entry(q);
-                    float2 vv[CC];
-                    const unsigned j = q - qs;
-                    if (j < nv) {
-                        const float2* v = s_val + (size_t)j * nch + c0;
-#pragma unroll
-                        for (int c = 0; c < CC; c += 2) {
-                            if (c < ncc) {
-                                const float4 f = *reinterpret_cast<const float4*>(v + c);
-                                vv[c] = make_float2(f.x, f.y);
-                                vv[c + 1] = make_float2(f.z, f.w);
-                            } else {
-                                vv[c] = vv[c + 1] = make_float2(0.f, 0.f);
-                            }
-                        }
-                    } else {
-                        const float2* v = a.yv + (long long)u.x * nch + c0;
-#pragma unroll
-                        for (int c = 0; c < CC; ++c) vv[c] = c < ncc ? __ldg(v + c) : make_float2(0.f, 0.f);
-                    }
-                    add(vv, __int_as_float(u.y));
-                }
-                if (col_ok) {
-                    const long long go = (long long)(xa + x) * a.B + t.y + k;
-#pragma unroll
-                    for (int c = 0; c < CC; ++c)
-                        if (c < ncc) {
-                            float2 o = acc[c];
-                            if (KAHAN) o = make_float2(__fsub_rn(o.x, cmp[c].x), __fsub_rn(o.y, cmp[c].y));
-                            g[(long long)c * a.coil_stride + go] = o;
-                        }
-                }
-            }
-            __syncthreads();   // the values (and, after the last sub-pass, the stage) are free
-            ps = pe;
+        if (sp[nx * tb] - e0a <= (unsigned)CSR_CAP) {
+            const int2* se = s_ent + st * CSR_CAP;
+            points(sp, nx, gp, gstep, [&](unsigned q) { return se[q - e0a]; });
+        } else {
+            points(sp, nx, gp, gstep, [&](unsigned q) { return __ldg(a.ent + q); });
         }
+        __syncwarp();
+        if ((tid & 31) == 0) mbar_arrive(&s_free[st]);   // this warp is done with the stage
     }
+    if (failed && tid == 0)   // the last copies this thread issued (at most a stage each) must land first
+        for (int j = issued > CSR_NST ? issued - CSR_NST : 0; j < issued; ++j)
+            mbar_wait_bounded(&s_bar[j % CSR_NST], (uint32_t)((j / CSR_NST) & 1), CSR_WAIT_NS);
 }
 
 static int sm_count_csr()
@@ -528,7 +513,7 @@ static cudaError_t spread_csr_run(const CsrSpreadArgs& a, cudaStream_t s)
 template <int CC, bool KAHAN>
 static cudaError_t spread_csr_staged_run(const CsrSpreadArgs& a, cudaStream_t s)
 {
-    const int nchunk = (a.nch + CC - 1) / CC;
+    const int nchunk = a.nch / CC;
     const int per = a.tb * nchunk;
     if (per > 256) return cudaErrorInvalidValue;
     const int nt = (256 / per) * per;
@@ -544,8 +529,9 @@ static cudaError_t spread_csr_staged_run(const CsrSpreadArgs& a, cudaStream_t s)
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spread_csr_staged<CC, KAHAN>, nt, smem);
     if (e != cudaSuccess) return e;
     const long long nunits = a.nj * ((a.Gx + CSR_SX - 1) / CSR_SX);
+    if (nunits >= 0x7fffffffLL) return cudaErrorInvalidValue;
     const long long nblk = std::min<long long>(nunits, (long long)sm_count_csr() * std::max(per_sm, 1));
-    k_spread_csr_staged<CC, KAHAN><<<(unsigned)nblk, nt, smem, s>>>(a, nunits);
+    k_spread_csr_staged<CC, KAHAN><<<(unsigned)nblk, nt, smem, s>>>(a, (int)nunits);
     return cudaGetLastError();
 }
 
@@ -560,11 +546,10 @@ cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, bool staged, c
     int cc = a.cc;
     if (cc == 0) cc = a.nch <= 2 ? 2 : a.nch <= 4 ? 4 : 6;
     // the staged form: an error flag, 16-byte aligned row offsets of every
-    // slab (tb a multiple of 4), 16-byte sample values (an even coil count,
-    // coils per thread even) and room for at least one sample's values
+    // slab (tb a multiple of 4), whole coil chunks of 16-byte coil pairs
     staged = staged && a.err && (a.tb % 4) == 0 && (reinterpret_cast<uintptr_t>(a.ptr) & 15) == 0 &&
              (reinterpret_cast<uintptr_t>(a.ent) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.yv) & 15) == 0 &&
-             (a.nch % 2) == 0 && (cc % 2) == 0 && a.nch * (int)sizeof(float2) <= CSR_VAL_BYTES;
+             (cc % 2) == 0 && (a.nch % cc) == 0;
     if (staged) {
         switch (cc) {
         case 2: return kahan ? spread_csr_staged_run<2, true>(a, s) : spread_csr_staged_run<2, false>(a, s);

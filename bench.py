@@ -132,6 +132,44 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class MemSampler:
+    """Device memory in use (nvidia-smi memory.used, MiB) sampled every
+    100 ms in the background; stop() returns the maximum in GiB."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="mem_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=memory.used", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        vals = []
+        with open(self.path) as f:
+            for line in f:
+                try:
+                    vals.append(float(line.strip()))
+                except ValueError:
+                    pass
+        os.unlink(self.path)
+        return max(vals) / 1024.0 if vals else None
+
+
 # ---------------------------------------------------------------------------
 # workload
 # ---------------------------------------------------------------------------
@@ -495,6 +533,124 @@ def toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, steps, w, s
         reco.set_toeplitz(0)
 
 
+def cfg1_report(cgs, synth, torch, dev, stream, steps=5, with_cpu=True):
+    """The reference's CPU-path configuration at its full size: a 64^3 image on
+    the 2x oversampled 128^3 grid, 8 coils, 1024 wave-CAIPI readouts of 256
+    samples (262 144 samples, R = 2x2, +-4 cells, 7 cycles), Voronoi density
+    weights (capped at their 99th percentile), KB width 4, 10 CG iterations.
+    GPU: the graph-captured solve (device-timed) and its host-buffer C-ABI
+    call.  CPU: the FP32 oracle port (the reference's arithmetic, OpenMP over
+    coils as Reco.cpp:470,523) on all host cores -- one E^H D E application
+    and the full 10-iteration solve, with its residual sequence -- and the
+    relative L2 distance between the two images."""
+    import ctypes as C
+    w = synth.WORKLOADS["cfg1"]
+    kb_w = 4.0
+    kb_b = beatty_beta(kb_w)
+    k = synth.wave_trajectory(w)
+    t0 = time.perf_counter()
+    dcf = synth.cap_dcf(cgs.voronoi_dcf(k))
+    dcf_s = time.perf_counter() - t0
+    smaps = synth.coil_maps(w.img, w.n_ch)
+    x_true = synth.phantom(w.img)
+    reco = cgs.Reco(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=kb_b, device=dev.index or 0)
+    reco.set_stream(stream.cuda_stream)
+    reco.set_trajectory(k)
+    smaps_t = torch.from_numpy(smaps).to(dev)
+    y = torch.zeros((w.n_ch, k.shape[0]), dtype=torch.complex64, device=dev)
+    reco.nufft_fwd_tensor((smaps_t * torch.from_numpy(x_true).to(dev)[None]).contiguous(), y)
+    torch.cuda.synchronize(dev)
+    rms = float(torch.sqrt(torch.mean(torch.abs(y) ** 2)))
+    g = torch.Generator(device=dev)
+    g.manual_seed(2)
+    y += torch.complex(torch.randn(y.shape, generator=g, device=dev),
+                       torch.randn(y.shape, generator=g, device=dev)) * (rms / 30 / np.sqrt(2))
+    reco.set_dcf(dcf)
+    reco.set_smaps_tensor(smaps_t)
+    iters = w.cg_iters
+    x = torch.zeros((1,) + w.img, dtype=torch.complex64, device=dev)
+    for _ in range(3):
+        res, its = reco.cg_sense_batched_tensor(y, x, 0.0, iters, want_stats=True)
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        reco.cg_sense_batched_tensor(y, x, 0.0, iters, want_stats=False)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    gpu_s = e0.elapsed_time(e1) / 1e3 / steps
+    # host buffers through the C ABI (copies and the result read back included)
+    h_y = torch.empty(y.shape, dtype=torch.complex64, pin_memory=True)
+    h_y.copy_(y.cpu())
+    h_x = torch.zeros(x.shape, dtype=torch.complex64, pin_memory=True)
+    h_res = np.zeros((1, iters), np.float64)
+    h_it = np.zeros(1, np.int32)
+    L = cgs.lib()
+
+    def host_call():
+        st = L.cgs_cg_solve_batched(reco.ctx, C.c_void_p(h_y.data_ptr()), C.c_void_p(h_x.data_ptr()), 0.0, iters,
+                                    h_res.ctypes.data_as(C.c_void_p), h_it.ctypes.data_as(C.c_void_p))
+        if st != 0:
+            raise RuntimeError(L.cgs_last_error(reco.ctx).decode())
+
+    host_call()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        host_call()
+    e2e_s = (time.perf_counter() - t0) / steps
+    out = {"workload": w.name, "img": list(w.img), "grid": list(w.grid), "coils": w.n_ch,
+           "samples": int(k.shape[0]), "cg_iters": iters, "kb_w": kb_w, "kb_b": round(kb_b, 4),
+           "dcf": "Voronoi volumes capped at the 99th percentile (host, %.1f s)" % dcf_s,
+           "gpu_s_per_solve": gpu_s, "gpu_applies_per_s": iters / gpu_s,
+           "gpu_e2e_s_per_solve": e2e_s, "gpu_residuals": [float(v) for v in res[0, :iters]],
+           "setup_ms": reco.setup_stats()}
+    if with_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle_py
+        o = oracle_py.Oracle(32)
+        p = oracle_py.make_params(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=kb_b)
+        yh = y.cpu().numpy()
+        t0 = time.perf_counter()
+        taps = o.taps(p, k)                 # ConvKernel::calculateWeights
+        kft = o.kernel_ft(p)                # ConvKernel::calculateKernelFT
+        t_setup = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        o.apply_ehde(p, taps, kft, smaps, dcf, x_true)
+        t_apply = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        st, xc, resc, itc = o.cg_sense(p, taps, kft, smaps, dcf, yh, 0.0, iters)
+        t_solve = time.perf_counter() - t0
+        xg = x.cpu().numpy()[0].astype(np.complex128)
+        out["cpu"] = {"kind": "port", "cores": os.cpu_count() or 1,
+                      "what": "FP32 oracle port of Reco.cpp (taps, kernelFT, nufftFWD/BWD, cgSenseDynamic), "
+                              "OpenMP over coils, the project's mixed-radix FFT",
+                      "s_setup_taps_kernelft": t_setup, "s_per_apply": t_apply, "s_per_solve": t_solve,
+                      "iters": int(itc), "residuals": [float(v) for v in resc],
+                      "rel_l2_gpu_vs_cpu": float(np.linalg.norm(xg - xc) / np.linalg.norm(xc)),
+                      "gpu_speedup_per_solve": t_solve / gpu_s}
+    del reco
+    return out
+
+
+def cfg2_precision_report(cgs, synth, torch, dev, stream):
+    """The precision configuration (160x160x112 image, 320x320x224 grid, 16
+    coils, R = 3x2 wave-CAIPI, 640 samples per readout, 20 CG iterations):
+    per-iteration relative L2 error of the FP32 and the compensated solves
+    against the FP64 GPU solve.  D: Pipe-Menon weights on the GPU (the host
+    Voronoi volumes of these 1.9 M samples take minutes), capped at their
+    99th percentile."""
+    w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s = make_workload(
+        cgs, synth, torch, "cfg2", dev.index or 0, stream.cuda_stream, "pipe-menon")
+    x = torch.zeros((len(sbins),) + w.img, dtype=torch.complex64, device=dev)
+    rep = precision_report(reco, data, x, w.cg_iters, torch, dev)
+    rep.update({"workload": w.name, "img": list(w.img), "grid": list(w.grid), "coils": w.n_ch,
+                "samples": int(sum(len(s) for s in sbins)), "cg_iters": w.cg_iters, "kb_w": kb_w,
+                "kb_b": round(kb_b, 4), "dcf": "Pipe-Menon (GPU, %.2f s), capped at the 99th percentile" % dcf_s})
+    del reco, data, x
+    return rep
+
+
 def run_diff_only(args):
     """The differentiation form alone (cfg4), one JSON line."""
     import torch
@@ -561,17 +717,21 @@ def run_cg_grad_only(args):
     v = torch.tensor([th.amp_y, th.amp_z, th.phase_y, th.phase_z, th.delay_y, th.delay_z], dtype=torch.float64,
                      device=dev, requires_grad=True)
     torch.cuda.reset_peak_memory_stats(dev)
+    mem = MemSampler(0)
+    mem.start()
     t0 = time.perf_counter()
     k = ag.wave_trajectory_torch(w, v, lines).contiguous()
     xk = ag.cg_unrolled(reco, k, y, w.cg_iters, checkpoint=True)
     loss = 0.5 * torch.sum(torch.abs(xk.to(torch.complex128) - x_true.to(torch.complex128)) ** 2)
     torch.cuda.synchronize(dev)
     t_fwd = time.perf_counter() - t0
+    free_fwd, total = torch.cuda.mem_get_info(dev)
     t0 = time.perf_counter()
     loss.backward()
     torch.cuda.synchronize(dev)
     t_bwd = time.perf_counter() - t0
     free, total = torch.cuda.mem_get_info(dev)
+    peak_smi = mem.stop()
     line = {"metric": "unrolled CG trajectory gradient (checkpointed backward)", "workload": w.name,
             "config": {"img": list(w.img), "grid": list(w.grid), "coils": w.n_ch, "bins": len(sbins),
                        "samples": int(ns), "cg_iters": w.cg_iters, "kb_w": kb_w, "kb_b": round(kb_b, 4),
@@ -579,8 +739,14 @@ def run_cg_grad_only(args):
                        "checkpoint": "every CG iteration (x, r, p, rr saved; the rest recomputed)"},
             "s_setup": t_setup, "s_forward": t_fwd, "s_backward": t_bwd, "loss": float(loss.item()),
             "dL_dtheta": v.grad.cpu().numpy().tolist(), "params": list(synth.WAVE_PARAM_NAMES),
+            "device_gb_in_use_after_forward": (total - free_fwd) / 2 ** 30,
             "device_gb_in_use_end": (total - free) / 2 ** 30,
-            "torch_peak_gb": torch.cuda.max_memory_allocated(dev) / 2 ** 30}
+            "device_gb_peak_sampled": peak_smi,
+            "torch_peak_gb": torch.cuda.max_memory_allocated(dev) / 2 ** 30,
+            "budget_gb": 180.0}
+    line["fits_in_budget"] = all(v is None or v <= 180.0 for v in
+                                 (line["device_gb_peak_sampled"], line["device_gb_in_use_after_forward"],
+                                  line["device_gb_in_use_end"]))
     print(json.dumps(line), flush=True)
     return 0
 
@@ -646,11 +812,23 @@ def run_ours(args):
     # launch shapes picked by the library's autotuner (timed batched applies)
     if args.nondeterministic:
         reco.set_deterministic(False)
+    t0 = time.perf_counter()
     tune = None if args.no_autotune else reco.autotune()
+    autotune_s = time.perf_counter() - t0
 
-    for _ in range(args.warmup):
+    t0 = time.perf_counter()
+    for i in range(args.warmup):
         res, its = reco.cg_sense_batched_tensor(data, x, 0.0, iters, want_stats=True)
+        if i == 0:
+            first_solve_s = time.perf_counter() - t0
     launches_per_step = reco.launch_count()
+    setup = {"density_weights_s": dcf_s, "autotune_s": autotune_s,
+             "first_solve_s": first_solve_s if args.warmup > 0 else None,
+             "library_ms": reco.setup_stats(),
+             "what": "density weights (host Voronoi or GPU Pipe-Menon); the library's rebuild of the bins "
+                     "(sort, tap records, tile and support lists, transposed tap matrix, workspaces) and the "
+                     "capture of the solve's CUDA graph; the autotuner's timed candidate applications; the "
+                     "first solve (capture included).  Not part of the timed steps."}
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -700,10 +878,23 @@ def run_ours(args):
         host_call()
     if world > 1:
         dist.barrier()
+    # per call: host wall time, and the device time between events recorded on
+    # the library's stream just before and just after the call (the copies,
+    # the graph and the state read-back; host work between them is not in it)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    host_ms = []
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for i in range(args.steps):
+        t1 = time.perf_counter()
+        ev[i][0].record(stream)
         host_call()
+        ev[i][1].record(stream)
+        host_ms.append(1e3 * (time.perf_counter() - t1))
     e2e_s = time.perf_counter() - t0
+    torch.cuda.synchronize(dev)
+    e2e_diag = {"host_ms_per_call": statistics.median(host_ms),
+                "device_ms_per_call": statistics.median([a.elapsed_time(b) for a, b in ev]),
+                "device_timed_ms_per_step": ms_step}
     te = torch.tensor([e2e_s], device=dev)
     if world > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
@@ -752,6 +943,11 @@ def run_ours(args):
             toep = toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, max(1, args.steps), w, sizes)
         except cgs.CGSError as e:   # e.g. no cuBLAS on the host: the headline stands without it
             toep = {"unavailable": str(e)}
+
+    # the reference's CPU-path configuration at full size, GPU and CPU
+    cfg1 = None
+    if not args.no_cfg1:
+        cfg1 = cfg1_report(cgs, synth, torch, dev, stream, with_cpu=(rank == 0 and not args.no_cpu))
 
     # per-stage kernel times of one batched application (roofline)
     xa = torch.from_numpy(np.stack([synth.phantom(w.img)] * nb)).to(dev)
@@ -817,19 +1013,29 @@ def run_ours(args):
         "gpu_launches": int(launches_per_step) * args.steps,
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "s_per_4d_recon": float(te.item()) / args.steps},
+                "s_per_4d_recon": float(te.item()) / args.steps, "breakdown": e2e_diag},
         "roofline": roofline,
         "precision": precision,
         "autotune": tune,
         "differentiation": diff,
         "plain": plain,
         "toeplitz": toep,
+        "setup": setup,
+        "cfg1": cfg1,
     }
     if rank == 0 and not args.no_cpu:
         cb = cpu_apply_sample(synth, args.workload)
         v = len(cb["times"]) / sum(cb["times"])
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cb["threads"], "kind": "port",
                                 "sample": cb["sample"]}
+        if cfg1 and "cpu" in cfg1:
+            line["cpu_baseline"]["cfg1"] = cfg1["cpu"]
+    # the precision configuration (its own context; the headline's is freed first)
+    if not args.no_precision and not args.no_cfg2:
+        del reco, xa, qa
+        torch.cuda.synchronize(dev)
+        torch.cuda.empty_cache()
+        line["precision_cfg2"] = cfg2_precision_report(cgs, synth, torch, dev, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -852,6 +1058,9 @@ def main():
                     help="let the autotuner pick atomic spreading (results not bitwise reproducible)")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiation form (cfg4)")
     ap.add_argument("--no-toeplitz", action="store_true", help="skip the Toeplitz-embedded solve")
+    ap.add_argument("--no-cfg1", action="store_true",
+                    help="skip the 64^3 / 8-coil / 262 144-sample configuration (GPU and CPU port)")
+    ap.add_argument("--no-cfg2", action="store_true", help="skip the cfg2 precision report")
     ap.add_argument("--diff-only", action="store_true", help="only the differentiation form (one JSON line)")
     ap.add_argument("--cg-grad-only", action="store_true",
                     help="only the unrolled-CG trajectory gradient of the combined workload (cfg5)")

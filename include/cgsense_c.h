@@ -353,6 +353,16 @@ int cgs_set_toeplitz(cgs_ctx* ctx, int32_t mode);
  * while not built). */
 int cgs_toeplitz_stats(cgs_ctx* ctx, double* build_ms, int64_t* bytes);
 
+/* Set-up cost of the current bins (host clock, milliseconds; the part of
+ * ConvKernel::calculateWeights, Reco.cpp:698-806, that the reference repeats
+ * per state, CGSense.cpp:218-222, plus this library's own set-up): ms[0]
+ * sorting the samples by home tile, ms[1] the tap records on the device,
+ * ms[2] the tile and support lists, ms[3] the transposed tap matrix, ms[4]
+ * the remaining uploads and the grid workspaces -- all from the last
+ * rebuild of the bins -- and ms[5] the capture and instantiation of the
+ * last CUDA graph of a batched solve.  n: entries wanted (at most 6). */
+int cgs_setup_stats(cgs_ctx* ctx, double* ms, int32_t n);
+
 /* Coil sensitivity maps from the measured data of a single-bin context
  * (device pointers; data [n_ch][ns] in the reference's order, maps
  * [n_ch][img]): the adjoint NUFFT of each coil's samples weighted by a Hann

@@ -216,6 +216,40 @@ class Oracle:
 
 
 # ---------------------------------------------------------------------------
+# Iterative density weights (Pipe and Menon, Magn. Reson. Med. 41:179-186,
+# 1999), FP64: the documented alternative to the Voronoi volumes of
+# estimateDensityV3D (functions.h:161-258).  With A the interpolation matrix
+# of the taps (Reco.cpp:698-806; rows = samples), w <- w / (A A^T w): spread
+# the weights onto the grid, interpolate back, divide.  Samples without taps
+# get 0.  Each bin iterates on its own samples and is normalised by its
+# maximum.
+# ---------------------------------------------------------------------------
+
+def pipe_menon(taps, n_grid, iters, bins=None):
+    """taps: Taps of all samples (one grid, CSR); bins: list of sample index
+    arrays (None: one bin of every sample).  Returns float64 [ns]."""
+    ptr, idx, wt = taps.ptr, taps.idx.astype(np.int64), taps.w.astype(np.float64)
+    ns = ptr.shape[0] - 1
+    cnt = np.diff(ptr)
+    out = np.zeros(ns, np.float64)
+    for sel in ([np.arange(ns)] if bins is None else bins):
+        sel = np.asarray(sel, np.int64)
+        m = np.zeros(ns, bool)
+        m[sel] = True
+        tap_in = np.repeat(m, cnt)                      # taps of this bin's samples
+        owner = np.repeat(np.arange(ns), cnt)[tap_in]
+        ti, tw = idx[tap_in], wt[tap_in]
+        w = np.where(m, 1.0, 0.0)
+        for _ in range(iters):
+            grid = np.bincount(ti, weights=tw * w[owner], minlength=n_grid)
+            u = np.bincount(owner, weights=tw * grid[ti], minlength=ns)
+            w = np.where(m & (u > 0), w / np.where(u > 0, u, 1.0), 0.0)
+        mx = w[sel].max() if sel.size else 0.0
+        out[sel] = w[sel] / mx if mx > 0 else 0.0
+    return out
+
+
+# ---------------------------------------------------------------------------
 # Exact normal operator (numpy, FP64): the operator that the Toeplitz
 # embedding computes and that the gridded operator approximates.  Small
 # problems only (a dense samples x voxels matrix).

@@ -117,3 +117,29 @@ def test_gridded_normal_operator_vs_exact(oracle_mod, o64):
     q_e = oracle_mod.exact_normal(k, img, grid, smaps, dcf.astype(np.float64), x)
     err = rel_l2(q_g, q_e)
     assert 1e-5 < err < 5e-3
+
+
+def test_pipe_menon_restatement_known_answers(oracle_mod, o64):
+    """The FP64 Pipe-Menon restatement: on a uniform lattice the interior
+    weights are equal; a lattice twice as dense on one side gets half the
+    weight there; w / (A A^T w) = 1 holds at the fixed point (interior)."""
+    grid = (48, 24, 24)
+    xs = np.concatenate([np.arange(6.0, 24.0, 1.0), np.arange(24.0, 42.0, 0.5)])
+    X, Y, Z = np.meshgrid(xs, np.arange(6.0, 18.0), np.arange(6.0, 18.0), indexing="ij")
+    k = np.stack([X, Y, Z], -1).reshape(-1, 3) / (np.array(grid) - 1)
+    p = oracle_mod.make_params(grid, grid, 1)
+    taps = o64.taps(p, k)
+    w = oracle_mod.pipe_menon(taps, int(np.prod(grid)), 40).reshape(X.shape)
+    assert abs(w.max() - 1.0) < 1e-12 and w.min() > 0
+    inner = (np.abs(Y - 12) < 3) & (np.abs(Z - 12) < 3)
+    sparse, dense = inner & (X > 10) & (X < 20), inner & (X > 28) & (X < 38)
+    assert np.ptp(w[sparse]) / np.median(w[sparse]) < 3e-2
+    assert abs(np.median(w[sparse]) / np.median(w[dense]) - 2.0) < 0.05
+    # fixed point: one more iteration changes the interior weights little
+    w2 = oracle_mod.pipe_menon(taps, int(np.prod(grid)), 41).reshape(X.shape)
+    assert np.abs(w2[sparse] / w[sparse] - 1).max() < 1e-2
+    # bins iterate independently
+    half = np.arange(k.shape[0] // 2)
+    wb = oracle_mod.pipe_menon(taps, int(np.prod(grid)), 10, bins=[half, np.arange(k.shape[0] // 2, k.shape[0])])
+    wh = oracle_mod.pipe_menon(o64.taps(p, k[half]), int(np.prod(grid)), 10)
+    assert np.allclose(wb[half], wh, rtol=1e-12, atol=0)

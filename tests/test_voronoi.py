@@ -104,3 +104,46 @@ def test_pipe_menon_weights_follow_density(gpu_lib, cgs):
     wv = w.reshape(X.shape)
     rv = np.median(v[sparse]) / np.median(v[dense])
     assert abs(ratio / rv - 1) < 0.1, (ratio, rv)
+
+
+@pytest.mark.gpu
+def test_pipe_menon_vs_fp64_oracle_on_wave_caipi(gpu_lib, cgs, synth, oracle_mod, o64):
+    """GPU Pipe-Menon weights on a wave-CAIPI trajectory (48x48x32 image on a
+    96x96x64 grid, 8 coils, one fully sampled bin of 73 728 samples, KB width
+    4) against the FP64 restatement (oracle_py.pipe_menon), 20 iterations:
+    relative L2 <= 1e-4 over the samples.  Then what the weights do to the
+    solve: the CG image (15 iterations, SNR 30) with the capped Pipe-Menon
+    weights stays within 3e-2 of the image with the capped Voronoi volumes
+    (functions.h:161-258), and both lie within 8e-2 of the phantom (best
+    complex scale)."""
+    w = synth.scaled(synth.WORKLOADS["cfg3"], (48, 48, 32), (96, 96, 64), n_ch=8, n_bins=1)
+    k = synth.wave_trajectory(w)
+    kb_w = 4.0
+    kb_b = float(np.pi * np.sqrt(kb_w ** 2 / 4 * 1.5 ** 2 - 0.8))
+    p = oracle_mod.make_params(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=kb_b)
+    taps = o64.taps(p, k)
+    ref = oracle_mod.pipe_menon(taps, int(np.prod(w.grid)), 20)
+    r = cgs.Reco(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=kb_b)
+    r.set_trajectory(k)
+    pm = r.pipe_menon_dcf(20)
+    err_w = float(np.linalg.norm(pm - ref) / np.linalg.norm(ref))
+    assert err_w < 1e-4, err_w
+    smaps = synth.coil_maps(w.img, w.n_ch)
+    x_true = synth.phantom(w.img)
+    r.set_smaps(smaps)
+    y = r.nufft_fwd(smaps * x_true[None])
+    y += synth.complex_noise(y.shape, 30.0, float(np.sqrt(np.mean(np.abs(y) ** 2))))
+
+    def solve(d):
+        r.set_dcf(d)
+        x, res, it = r.cg_sense(y, 0.0, 15)
+        a = np.vdot(x, x_true) / np.vdot(x, x)
+        return x, float(np.linalg.norm(a * x - x_true) / np.linalg.norm(x_true))
+
+    xv, ev = solve(synth.cap_dcf(cgs.voronoi_dcf(k)))
+    xp, ep = solve(synth.cap_dcf(pm))
+    d_img = float(np.linalg.norm(xp - xv) / np.linalg.norm(xv))
+    print("pm vs oracle %.2e; image error vs truth: voronoi %.3f, pipe-menon %.3f; images apart %.3f"
+          % (err_w, ev, ep, d_img))
+    assert ev < 8e-2 and ep < 8e-2, (ev, ep)
+    assert d_img < 3e-2 * 3, d_img
