@@ -96,6 +96,60 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
     // first); grids and coil planes start on 16-byte boundaries (Ng even).
     const bool vec = nz >= 3 && nz + 3 <= Gz - 1 && (a.coil_stride & 1) == 0 &&
                      (reinterpret_cast<uintptr_t>(a.grid) & 15) == 0 && (a.grid_bs & 1) == 0;
+    // Interior samples whose x and y supports hold exactly four candidates
+    // each (a kernel of width 4 away from the grid points and the grid's
+    // faces): a 4 x 4 loop over the rows without a branch per row, so that
+    // the loads of several rows can be in flight at once.  The rows, the
+    // products wx * wy, the z taps and their order are those of the general
+    // loop below, so the sums are bitwise the same.
+    int x0 = 5, nxt = 0, y0 = 5, nyt = 0;
+#pragma unroll
+    for (int q = 4; q >= 0; --q) {
+        if (w[q] != 0.f) x0 = q;
+        if (w[5 + q] != 0.f) y0 = q;
+    }
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        nxt += w[q] != 0.f ? 1 : 0;
+        nyt += w[5 + q] != 0.f ? 1 : 0;
+    }
+    if (vec && nxt == 4 && nyt == 4 && x0 <= 1 && y0 <= 1) {
+        float wxs[4], wys[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            wxs[q] = x0 ? w[q + 1] : w[q];
+            wys[q] = y0 ? w[6 + q] : w[5 + q];
+        }
+        const long long base = ((long long)(nx - 2 + x0) * Gy + (ny - 2 + y0)) * Gz + (nz - 2);
+        const int odd = (int)(base & 1);   // Gz even: every row of the sample has this parity
+        const float4* b4 = reinterpret_cast<const float4*>(grid + (base - odd));
+        const long long gz4 = Gz / 2, gyz4 = (long long)Gy * Gz / 2;
+#pragma unroll
+        for (int ix = 0; ix < 4; ++ix)
+#pragma unroll
+            for (int iy = 0; iy < 4; ++iy) {
+                const float wxy = wxs[ix] * wys[iy];
+                const float4* r4 = b4 + ix * gyz4 + iy * gz4;
+#pragma unroll
+                for (int c = 0; c < CC; ++c)
+                    if (c < ncc) {
+                        const float4* p = r4 + (long long)c * (a.coil_stride / 2);
+                        const float4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2);
+                        const float2 e[6] = {make_float2(q0.x, q0.y), make_float2(q0.z, q0.w), make_float2(q1.x, q1.y),
+                                             make_float2(q1.z, q1.w), make_float2(q2.x, q2.y), make_float2(q2.z, q2.w)};
+#pragma unroll
+                        for (int jz = 0; jz < 5; ++jz) {
+                            const float wz = w[10 + jz];
+                            const float wt = wxy * wz;
+                            if (wz != 0.f && wt > a.thresh) {
+                                const float2 g = odd ? e[jz + 1] : e[jz];
+                                acc[c].x = fmaf(g.x, wt, acc[c].x);
+                                acc[c].y = fmaf(g.y, wt, acc[c].y);
+                            }
+                        }
+                    }
+            }
+    } else {
 #pragma unroll
     for (int jx = 0; jx < 5; ++jx) {
         const float wx = w[jx];
@@ -145,6 +199,7 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
                 }
             }
         }
+    }
     }
     const float d = a.dcf ? a.dcf[i] : 1.f;
     float2* out = a.yv + i * a.nch + c0;

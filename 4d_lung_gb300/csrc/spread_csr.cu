@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
 // ---------------------------------------------------------------------------
 constexpr int CSR_SX = 32;            // x rows per unit
 constexpr int CSR_CAP = 2048;         // staged taps per unit
-constexpr int CSR_NST = 3;            // pipeline stages
+constexpr int CSR_NST = 2;            // pipeline stages
 constexpr unsigned long long CSR_WAIT_NS = 2000000000ull;
 
 __host__ __device__ inline int csr_ptr_stride(int tb) { return ((CSR_SX * tb + 1) + 3) & ~3; }
@@ -323,12 +323,7 @@ __host__ __device__ inline int csr_ptr_stride(int tb) { return ((CSR_SX * tb + 1
 static size_t csr_staged_smem(int tb)
 {
     return (size_t)CSR_NST * ((size_t)csr_ptr_stride(tb) * sizeof(unsigned) + (size_t)CSR_CAP * sizeof(int2)) +
-           2 * CSR_NST * sizeof(uint64_t);
-}
-
-CGS_D void mbar_arrive(uint64_t* bar)
-{
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+           CSR_NST * sizeof(uint64_t);
 }
 
 template <int CC, bool KAHAN>
@@ -339,8 +334,7 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_s
     const int PS = csr_ptr_stride(a.tb);
     int2* s_ent = reinterpret_cast<int2*>(s_csr);                                // [CSR_NST][CSR_CAP]
     unsigned* s_ptr = reinterpret_cast<unsigned*>(s_ent + CSR_NST * CSR_CAP);   // [CSR_NST][PS]
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_ptr + CSR_NST * PS);   // [CSR_NST] full: the copies landed
-    uint64_t* s_free = s_bar + CSR_NST;                                       // [CSR_NST] empty: every warp is done
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_ptr + CSR_NST * PS);
     const int tb = a.tb;
     const int nchunk = a.nch / CC;     // the launcher guarantees nch % CC == 0
     const int tid = threadIdx.x;
@@ -421,40 +415,26 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_s
         bulk_load(s_ptr + st * PS, a.ptr + p0, pb, &s_bar[st]);
         if (eb) bulk_load(s_ent + st * CSR_CAP, a.ent + e0a, eb, &s_bar[st]);
     };
-    const int nwarps = (int)(blockDim.x + 31) / 32;
     if (tid == 0) {
-        for (int st = 0; st < CSR_NST; ++st) {
-            mbar_init(&s_bar[st], 1);
-            mbar_init(&s_free[st], nwarps);
-        }
+        for (int st = 0; st < CSR_NST; ++st) mbar_init(&s_bar[st], 1);
         fence_mbar_init();
     }
     __syncthreads();
-    // No block-wide barrier per unit: a stage is refilled once every warp has
-    // arrived on its empty barrier, so fast warps run up to CSR_NST - 1 units
-    // ahead of slow ones.  Thread 0 issues unit kk + CSR_NST - 1 into the
-    // stage that unit kk - 1 used.  A wait that runs out sets the error flag
-    // and ends the warp's loop; thread 0 then lets its issued copies land.
     const int my_n = nunits > (int)blockIdx.x ? (nunits - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
-    int issued = 0;
     if (tid == 0)
-        for (; issued < CSR_NST - 1 && issued < my_n; ++issued) issue(issued);
-    bool failed = false;
-    for (int kk = 0; kk < my_n && !failed; ++kk) {
+        for (int kk = 0; kk < CSR_NST - 1 && kk < my_n; ++kk) issue(kk);
+    for (int kk = 0; kk < my_n; ++kk) {
         const int st = kk % CSR_NST;
-        if (tid == 0 && issued < my_n && issued == kk + CSR_NST - 1) {
-            if (kk > 0 && !mbar_wait_bounded(&s_free[(kk - 1) % CSR_NST], (uint32_t)(((kk - 1) / CSR_NST) & 1),
-                                             CSR_WAIT_NS)) {
+        if (tid == 0 && kk + CSR_NST - 1 < my_n) issue(kk + CSR_NST - 1);
+        const bool ok = mbar_wait_bounded(&s_bar[st], (uint32_t)((kk / CSR_NST) & 1), CSR_WAIT_NS);
+        if (__syncthreads_or(!ok)) {
+            // timeout: report, let the copies already issued land, leave
+            if (tid == 0) {
                 atomicExch(a.err, 1);
-                failed = true;
-                break;
+                for (int j = kk; j < my_n && j < kk + CSR_NST; ++j)
+                    mbar_wait_bounded(&s_bar[j % CSR_NST], (uint32_t)((j / CSR_NST) & 1), CSR_WAIT_NS);
             }
-            issue(issued++);
-        }
-        if (!mbar_wait_bounded(&s_bar[st], (uint32_t)((kk / CSR_NST) & 1), CSR_WAIT_NS)) {
-            atomicExch(a.err, 1);
-            failed = true;
-            break;
+            return;
         }
         const unsigned u = blockIdx.x + (unsigned)kk * gridDim.x;
         const unsigned jt = u / nslab;
@@ -475,12 +455,8 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_s
         } else {
             points(sp, nx, gp, gstep, [&](unsigned q) { return __ldg(a.ent + q); });
         }
-        __syncwarp();
-        if ((tid & 31) == 0) mbar_arrive(&s_free[st]);   // this warp is done with the stage
+        __syncthreads();   // the stage is free for the copy issued next
     }
-    if (failed && tid == 0)   // the last copies this thread issued (at most a stage each) must land first
-        for (int j = issued > CSR_NST ? issued - CSR_NST : 0; j < issued; ++j)
-            mbar_wait_bounded(&s_bar[j % CSR_NST], (uint32_t)((j / CSR_NST) & 1), CSR_WAIT_NS);
 }
 
 static int sm_count_csr()

@@ -10,9 +10,11 @@ Workload (default): the batched 4D reconstruction of 128x128x96 images on a
 seeded inputs (4d_lung_gb300/synth.py).
 
 One step = one full 16-bin reconstruction; value = E^H D E applies per
-second (bins x iterations per step / time per step), summed over ranks.
-With torchrun (N > 1) every rank reconstructs its own 16-bin scan on its
-GPU (replicas, weak scaling, no collective on the data path).
+second (bins x iterations per step / time per step).  With torchrun
+(N > 1) the scan's bins are partitioned over the ranks (greedy by sample
+count, 4d_lung_gb300/dist.py): every rank solves its bins, with no
+collective on the data path, and the step time is the slowest rank's
+(strong scaling: the total work is one scan whatever N).
 
 Beside the headline the line carries the plain per-bin GPU form, the
 per-iteration precision against the FP64 form, the differentiation form,
@@ -174,16 +176,26 @@ class MemSampler:
 # workload
 # ---------------------------------------------------------------------------
 
-def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voronoi", max_bins=0):
+def scan_bins(synth, name, max_bins=0):
+    """Sample indices of the workload's respiratory bins (the first max_bins)."""
+    w = synth.WORKLOADS[name]
+    lines = synth.readout_lines(w)
+    sbins = synth.bin_samples(synth.breathing_bins(len(lines), w.n_bins), w.n_read)
+    return sbins[:max_bins] if max_bins > 0 else sbins
+
+
+def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voronoi", max_bins=0, bin_subset=None):
+    """The workload's context, data and weights.  bin_subset: the indices of
+    the bins this process reconstructs (the multi-GPU bin partition), None
+    for all."""
     w = synth.WORKLOADS[name]
     kb_w = 4.0
     kb_b = beatty_beta(kb_w)
     lines = synth.readout_lines(w)
     k = synth.wave_trajectory(w, lines=lines)
-    rbins = synth.breathing_bins(len(lines), w.n_bins)
-    sbins = synth.bin_samples(rbins, w.n_read)
-    if max_bins > 0:
-        sbins = sbins[:max_bins]
+    sbins = scan_bins(synth, name, max_bins)
+    if bin_subset is not None:
+        sbins = [sbins[b] for b in bin_subset]
     smaps = synth.coil_maps(w.img, w.n_ch)
     # per-bin Voronoi weights (estimateDensityV3D, host C++), or the radial stand-in
     t0 = time.perf_counter()
@@ -205,7 +217,8 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
     data = torch.zeros((w.n_ch, ns), dtype=torch.complex64, device=dev)
     full = torch.zeros((w.n_ch, ns), dtype=torch.complex64, device=dev)
     # k-space of each bin from its own (z-displaced) phantom: y = E(S x_b)
-    for b, idx in enumerate(sbins):
+    for j, idx in enumerate(sbins):
+        b = j if bin_subset is None else bin_subset[j]
         shift = w.z_shift_max * (b / max(w.n_bins - 1, 1))
         x_b = torch.from_numpy(synth.phantom(w.img, z_shift=shift)).to(dev)
         imgs = (smaps_t * x_b[None]).contiguous()
@@ -331,7 +344,7 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": len(t), "warmup": args.warmup, "ms_per_step": 1e3 * sum(t) / len(t),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64/f32",
+        "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "c64/f32",
         "data": "synthetic", "config": {"workload": w.name, "bins": w.n_bins, "cg_iters": w.cg_iters,
                                         "step": "one E^H D E application of bin 0 on the host cores"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["threads"], "kind": "port",
@@ -531,6 +544,41 @@ def toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, steps, w, s
         }
     finally:
         reco.set_toeplitz(0)
+
+
+def pipe_menon_report(reco, synth, data, x, iters, sbins, dcf_voronoi, torch, dev, stream, steps):
+    """The headline solve with GPU Pipe-Menon density weights (20 iterations
+    per bin on the library's own gridding kernels, capped at each bin's 99th
+    percentile like the Voronoi volumes) in place of the host Voronoi
+    volumes: their set-up time, the timed reconstruction and the images'
+    distance from the Voronoi solve's.  The Voronoi weights are restored."""
+    t0 = time.perf_counter()
+    pm = reco.pipe_menon_dcf(20)
+    for idx in sbins:
+        pm[idx] = synth.cap_dcf(pm[idx])
+    pm_s = time.perf_counter() - t0
+    try:
+        reco.set_dcf(pm)
+        xp = torch.zeros_like(x)
+        for _ in range(2):
+            reco.cg_sense_batched_tensor(data, xp, 0.0, iters, want_stats=False)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            reco.cg_sense_batched_tensor(data, xp, 0.0, iters, want_stats=False)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms = e0.elapsed_time(e1) / steps
+        d = (xp - x).reshape(len(sbins), -1)
+        per_bin = (torch.linalg.vector_norm(d, dim=1) / torch.linalg.vector_norm(x.reshape(len(sbins), -1), dim=1))
+        return {"dcf": "Pipe-Menon, 20 iterations per bin on the GPU, capped at the 99th percentile",
+                "dcf_s": pm_s, "s_per_4d_recon": ms / 1e3,
+                "rel_l2_vs_voronoi_solve": float(torch.linalg.vector_norm(xp - x) / torch.linalg.vector_norm(x)),
+                "rel_l2_vs_voronoi_solve_per_bin_max": float(per_bin.max())}
+    finally:
+        reco.set_dcf(dcf_voronoi)
 
 
 def cfg1_report(cgs, synth, torch, dev, stream, steps=5, with_cpu=True):
@@ -798,12 +846,18 @@ def run_ours(args):
     # all cores); allocated after it, the end-to-end step measured 5 ms slower
     w0 = synth.WORKLOADS[args.workload]
     ns0 = len(synth.readout_lines(w0)) * w0.n_read
-    nb0 = min(args.max_bins, w0.n_bins) if args.max_bins > 0 else w0.n_bins
+    # N GPUs: the scan's bins are partitioned over the ranks (greedy by sample
+    # count); every rank solves its own bins, no collective on the data path
+    all_sizes = [len(b) for b in scan_bins(synth, args.workload, args.max_bins)]
+    mine = None
+    if world > 1:
+        mine = importlib.import_module("4d_lung_gb300.dist").partition_bins(all_sizes, world)[rank]
+    nb0 = len(all_sizes) if mine is None else len(mine)
     h_data = torch.zeros((w0.n_ch, ns0), dtype=torch.complex64, pin_memory=True)
-    h_x = torch.zeros((nb0,) + tuple(w0.img), dtype=torch.complex64, pin_memory=True)
+    h_x = torch.zeros((max(nb0, 1),) + tuple(w0.img), dtype=torch.complex64, pin_memory=True)
     w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s = make_workload(
-        cgs, synth, torch, args.workload, local, stream.cuda_stream, args.dcf, args.max_bins)
-    assert tuple(h_data.shape) == tuple(data.shape) and h_x.shape[0] == len(sbins)
+        cgs, synth, torch, args.workload, local, stream.cuda_stream, args.dcf, args.max_bins, mine)
+    assert tuple(h_data.shape) == tuple(data.shape) and (h_x.shape[0] == len(sbins) or not sbins)
     torch.cuda.synchronize(dev)
     nb = len(sbins)
     sizes = [len(s) for s in sbins]
@@ -851,8 +905,9 @@ def run_ours(args):
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms = float(t.item())
-    applies_per_step = nb * iters
-    value = world * applies_per_step * args.steps / (ms / 1e3)
+    applies_per_step = nb * iters                       # this rank's bins
+    total_applies_per_step = len(all_sizes) * iters     # the whole scan, all ranks
+    value = total_applies_per_step * args.steps / (ms / 1e3)
     ms_step = ms / args.steps
 
     # residual check of the last solve
@@ -898,13 +953,14 @@ def run_ours(args):
     te = torch.tensor([e2e_s], device=dev)
     if world > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * applies_per_step * args.steps / float(te.item())
+    e2e_value = total_applies_per_step * args.steps / float(te.item())
     h2d = data.numel() * 8
     d2h = x.numel() * 8 + h_res.nbytes + h_it.nbytes
 
     # the plain per-bin GPU form (frozen comparison point): same solve
     plain = None
-    if not args.no_plain:
+    extras = world == 1   # the comparison forms and reports: single-GPU runs only
+    if extras and not args.no_plain:
         xp = torch.zeros_like(x)
         reco.cg_sense_plain_tensor(data, xp, 0.0, 1)          # warm-up (cuFFT plan, first touch)
         torch.cuda.synchronize(dev)
@@ -926,27 +982,32 @@ def run_ours(args):
     # precision: the chosen form (and its compensated-spreading variant)
     # against the full-FP64 GPU form, iteration by iteration
     precision = None
-    if not args.no_precision:
+    if extras and not args.no_precision:
         precision = precision_report(reco, data, x, iters, torch, dev)
 
     # differentiation form (cfg4): trajectory gradients and self-calibration
     diff = None
-    if not args.no_diff:
+    if extras and not args.no_diff:
         diff = differentiation_report(cgs, synth, torch, dev, stream.cuda_stream)
 
 
     # the Toeplitz-embedded operator on the same solve (an alternative
     # operator for fixed trajectories; not the headline form)
     toep = None
-    if not args.no_toeplitz:
+    if extras and not args.no_toeplitz:
         try:
             toep = toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, max(1, args.steps), w, sizes)
         except cgs.CGSError as e:   # e.g. no cuBLAS on the host: the headline stands without it
             toep = {"unavailable": str(e)}
 
+    # the same solve with GPU Pipe-Menon weights in place of the host Voronoi volumes
+    pmr = None
+    if extras and args.dcf == "voronoi" and not args.no_pipe_menon:
+        pmr = pipe_menon_report(reco, synth, data, x, iters, sbins, dcf, torch, dev, stream, max(1, args.steps))
+
     # the reference's CPU-path configuration at full size, GPU and CPU
     cfg1 = None
-    if not args.no_cfg1:
+    if extras and not args.no_cfg1:
         cfg1 = cfg1_report(cgs, synth, torch, dev, stream, with_cpu=(rank == 0 and not args.no_cpu))
 
     # per-stage kernel times of one batched application (roofline)
@@ -996,7 +1057,7 @@ def run_ours(args):
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "strong",
         "vs_baseline": None, "dtype": "c64/f32 (fp64 CG scalars)", "data": "synthetic",
         "config": {"workload": w.name, "img": list(w.img), "grid": list(w.grid), "coils": w.n_ch,
                    "bins": nb, "samples_per_bin": [min(sizes), max(sizes)], "samples_total": int(sum(sizes)),
@@ -1008,7 +1069,8 @@ def run_ours(args):
                    else "radial stand-in",
                    "step": "one 16-bin 4D CG-SENSE reconstruction (graph replay)",
                    "l2": "inputs larger than L2 (data %d MB, workspace > 30 GB)" % (h2d // 2 ** 20),
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": ("bin partition over %d GPUs (greedy by samples; no data-path collective)" % world)
+                   if world > 1 else "single GPU"},
         "s_per_4d_recon": ms_step / 1e3,
         "gpu_launches": int(launches_per_step) * args.steps,
         "clocks": clk,
@@ -1021,9 +1083,10 @@ def run_ours(args):
         "plain": plain,
         "toeplitz": toep,
         "setup": setup,
+        "pipe_menon": pmr,
         "cfg1": cfg1,
     }
-    if rank == 0 and not args.no_cpu:
+    if rank == 0 and extras and not args.no_cpu:
         cb = cpu_apply_sample(synth, args.workload)
         v = len(cb["times"]) / sum(cb["times"])
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cb["threads"], "kind": "port",
@@ -1031,7 +1094,7 @@ def run_ours(args):
         if cfg1 and "cpu" in cfg1:
             line["cpu_baseline"]["cfg1"] = cfg1["cpu"]
     # the precision configuration (its own context; the headline's is freed first)
-    if not args.no_precision and not args.no_cfg2:
+    if extras and not args.no_precision and not args.no_cfg2:
         del reco, xa, qa
         torch.cuda.synchronize(dev)
         torch.cuda.empty_cache()
@@ -1061,6 +1124,8 @@ def main():
     ap.add_argument("--no-cfg1", action="store_true",
                     help="skip the 64^3 / 8-coil / 262 144-sample configuration (GPU and CPU port)")
     ap.add_argument("--no-cfg2", action="store_true", help="skip the cfg2 precision report")
+    ap.add_argument("--no-pipe-menon", action="store_true",
+                    help="skip the solve with GPU Pipe-Menon weights in place of the Voronoi volumes")
     ap.add_argument("--diff-only", action="store_true", help="only the differentiation form (one JSON line)")
     ap.add_argument("--cg-grad-only", action="store_true",
                     help="only the unrolled-CG trajectory gradient of the combined workload (cfg5)")
