@@ -867,7 +867,13 @@ def run_ours(args):
     if args.nondeterministic:
         reco.set_deterministic(False)
     t0 = time.perf_counter()
-    tune = None if args.no_autotune else reco.autotune()
+    tune = None
+    if args.spread_variant:   # launch shape by hand (profiling a variant), no autotuning
+        reco.set_launch_shape(args.spread_cc, args.spread_variant, args.interp_cc)
+        tune = {"spread_coils_per_block": args.spread_cc, "spread_variant": args.spread_variant,
+                "interp_coils_per_thread": args.interp_cc, "candidates_ms": [], "by_hand": True}
+    elif not args.no_autotune:
+        tune = reco.autotune()
     autotune_s = time.perf_counter() - t0
 
     t0 = time.perf_counter()
@@ -1117,6 +1123,10 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain per-bin GPU form")
     ap.add_argument("--no-precision", action="store_true", help="skip the per-iteration FP64 comparison")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
+    ap.add_argument("--spread-variant", type=int, default=0,
+                    help="launch shape by hand instead of the autotuner: spreading variant (cgs_set_launch_shape)")
+    ap.add_argument("--spread-cc", type=int, default=6, help="with --spread-variant: its coils per block / thread")
+    ap.add_argument("--interp-cc", type=int, default=2, help="with --spread-variant: coils per interpolation thread")
     ap.add_argument("--nondeterministic", action="store_true",
                     help="let the autotuner pick atomic spreading (results not bitwise reproducible)")
     ap.add_argument("--no-diff", action="store_true", help="skip the differentiation form (cfg4)")
