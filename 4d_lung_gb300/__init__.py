@@ -57,7 +57,7 @@ EXPORTS = [
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
     "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic", "cgs_set_launch_shape",
     "cgs_set_support_pruning", "cgs_support_stats", "cgs_spread_matrix_stats", "cgs_estimate_smaps_d",
-    "cgs_forward_y_listed_rows", "cgs_set_toeplitz", "cgs_toeplitz_stats", "cgs_setup_stats",
+    "cgs_forward_y_listed_rows", "cgs_set_toeplitz", "cgs_toeplitz_stats", "cgs_setup_stats", "cgs_e2e_stats",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -185,6 +185,7 @@ def lib():
         "cgs_set_toeplitz": (C.c_int, [vp, C.c_int32]),
         "cgs_toeplitz_stats": (C.c_int, [vp, vp, vp]),
         "cgs_setup_stats": (C.c_int, [vp, vp, C.c_int32]),
+        "cgs_e2e_stats": (C.c_int, [vp, vp]),
         "cgs_estimate_smaps_d": (C.c_int, [vp, vp, C.c_double, C.c_double, vp]),
         "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
                                              C.c_double, C.c_int32, C.c_int32, vp]),
@@ -600,6 +601,13 @@ class Reco:
         self._check(self._L.cgs_setup_stats(self._ctx, _p(v), 6))
         return dict(zip(("sort", "tap_records", "lists", "transposed_matrix", "workspace", "graph_capture"),
                         [float(x) for x in v]))
+
+    def e2e_stats(self):
+        """Device time (ms) of the parts of the last host-buffer batched
+        solve (see cgs_e2e_stats): {upload, solve, download}."""
+        v = np.zeros(3, np.float64)
+        self._check(self._L.cgs_e2e_stats(self._ctx, _p(v)))
+        return dict(zip(("upload", "solve", "download"), [float(x) for x in v]))
 
     def spread_matrix_stats(self):
         """(taps, grid points) of the transposed tap matrix (0, 0 when not built)."""

@@ -21,6 +21,9 @@ namespace cgs {
 
 constexpr int CG_FCHUNK = 4;   // elements per FP32 partial of a dot product
 
+// |v|^2 with a fixed rounding (one fused multiply-add), the same in every kernel
+CGS_D float cg_abs2(float2 v) { return __fmaf_rn(v.x, v.x, __fmul_rn(v.y, v.y)); }
+
 CGS_D void block_reduce2(double& a, double& b, double* s_red /* [2][RED_THREADS/32] */)
 {
 #pragma unroll
@@ -61,7 +64,7 @@ k_cg_init(const float2* __restrict__ b, float2* r, float2* p, float2* x, long lo
         r[off + i] = v;
         p[off + i] = v;
         x[off + i] = make_float2(0.f, 0.f);
-        fa += v.x * v.x + v.y * v.y;
+        fa = __fadd_rn(fa, cg_abs2(v));
         if (++cnt == CG_FCHUNK) {
             acc += (double)fa;
             fa = 0.f;
@@ -75,6 +78,16 @@ k_cg_init(const float2* __restrict__ b, float2* r, float2* p, float2* x, long lo
         o[0] = acc;
         o[1] = 0.0;
     }
+}
+
+// alpha = rr / pq (complexDivision, Reco.cpp:145-151), every product and
+// sum rounded on its own, so that the separate alpha kernel and the fused
+// residual update compute the same bits.
+CGS_D void cg_alpha(const double* rr, double pr, double pim, double* alpha)
+{
+    const double d = __dadd_rn(__dmul_rn(pr, pr), __dmul_rn(pim, pim));
+    alpha[0] = __ddiv_rn(__dadd_rn(__dmul_rn(rr[0], pr), __dmul_rn(rr[1], pim)), d);
+    alpha[1] = __ddiv_rn(__dsub_rn(__dmul_rn(rr[1], pr), __dmul_rn(rr[0], pim)), d);
 }
 
 // Sum of a bin's nblk (re, im) partials by one warp: lane l adds the
@@ -116,6 +129,7 @@ __global__ void k_cg_arm(CgState* st, const double* partials, int nblk, int nbin
     S.iter = 0;
     S.max_iter = max_iter;
     S.error = 0;
+    S.xpend = 0;
     // A zero right-hand side (empty bin, all-zero data) would make the
     // reference divide 0/0 and return NaN; here the solve stops at x = 0.
     S.active = (S.res > thresh && max_iter > 0 && s > 0.0) ? 1 : 0;
@@ -140,9 +154,7 @@ __global__ void k_cg_alpha(CgState* st, const double* partials, int nblk, int nb
         S.active = 0;
         return;
     }
-    const double d = pr * pr + pim * pim;
-    S.alpha[0] = (S.rr[0] * pr + S.rr[1] * pim) / d;
-    S.alpha[1] = (S.rr[1] * pr - S.rr[0] * pim) / d;
+    cg_alpha(S.rr, pr, pim, S.alpha);
 }
 
 // x += alpha p ; r -= alpha q ; partial sums of |r|^2  (Reco.cpp:285-298)
@@ -162,13 +174,11 @@ k_cg_update_xr(float2* x, float2* r, const float2* __restrict__ p, const float2*
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 pv = p[off + i], qv = q[off + i];
         float2 xv = x[off + i], rv = r[off + i];
-        xv.x += ar * pv.x - ai * pv.y;
-        xv.y += ar * pv.y + ai * pv.x;
-        rv.x -= ar * qv.x - ai * qv.y;
-        rv.y -= ar * qv.y + ai * qv.x;
+        xv = cg_axpy(xv, ar, ai, pv);
+        rv = cg_axmy(rv, ar, ai, qv);
         x[off + i] = xv;
         r[off + i] = rv;
-        fa += rv.x * rv.x + rv.y * rv.y;
+        fa = __fadd_rn(fa, cg_abs2(rv));
         if (++cnt == CG_FCHUNK) {
             acc += (double)fa;
             fa = 0.f;
@@ -184,6 +194,20 @@ k_cg_update_xr(float2* x, float2* r, const float2* __restrict__ p, const float2*
     }
 }
 
+// residual, beta = rr_new / rr_old (rr_new real), iteration count
+// (Reco.cpp:292-309); residuals: the bin's row of the residual record
+CGS_D void cg_residual_beta(CgState& S, double s, double* residuals)
+{
+    S.res = sqrt(s);
+    if (residuals) residuals[S.iter] = S.res;
+    const double d = __dadd_rn(__dmul_rn(S.rr[0], S.rr[0]), __dmul_rn(S.rr[1], S.rr[1]));
+    S.beta[0] = __ddiv_rn(__dmul_rn(s, S.rr[0]), d);
+    S.beta[1] = __ddiv_rn(__dmul_rn(-s, S.rr[1]), d);
+    S.rr[0] = s;
+    S.rr[1] = 0.0;
+    S.iter += 1;
+}
+
 // residual, beta = rr_new / rr, loop control (Reco.cpp:292-309)
 __global__ void k_cg_beta(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
                           int res_stride)
@@ -195,15 +219,7 @@ __global__ void k_cg_beta(CgState* st, const double* partials, int nblk, int nbi
     double s, unused;
     warp_partials(partials, (long long)bin * nblk, nblk, s, unused);
     if (threadIdx.x != 0) return;
-    S.res = sqrt(s);
-    if (residuals) residuals[(long long)bin * res_stride + S.iter] = S.res;
-    // beta = rr_new / rr_old with rr_new real
-    const double d = S.rr[0] * S.rr[0] + S.rr[1] * S.rr[1];
-    S.beta[0] = (s * S.rr[0]) / d;
-    S.beta[1] = (-s * S.rr[1]) / d;
-    S.rr[0] = s;
-    S.rr[1] = 0.0;
-    S.iter += 1;
+    cg_residual_beta(S, s, residuals ? residuals + (long long)bin * res_stride : nullptr);
     // p is updated in this same iteration before the loop test
 }
 
@@ -216,11 +232,7 @@ __global__ void k_cg_update_p(float2* p, const float2* __restrict__ r, long long
     const float br = (float)S.beta[0], bi = (float)S.beta[1];
     const long long off = (long long)bin * bs;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const float2 pv = p[off + i], rv = r[off + i];
-        float2 o;
-        o.x = rv.x + (br * pv.x - bi * pv.y);
-        o.y = rv.y + (br * pv.y + bi * pv.x);
-        p[off + i] = o;
+        p[off + i] = cg_axpy(r[off + i], br, bi, p[off + i]);
     }
 }
 
@@ -231,6 +243,116 @@ __global__ void k_cg_loop_test(CgState* st, int nbins)
     CgState& S = st[bin];
     if (!S.active) return;
     S.active = (S.res > S.thresh && S.iter < S.max_iter) ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Fused solve.  Per iteration: the forward z pass forms p = r + beta p and
+// x = x + alpha p of the previous iteration while it reads p (FwdZArgs::cg);
+// the adjoint z pass sums <p, q>; k_cg_update_r computes alpha from those
+// partial sums (in every block, in the order of k_cg_alpha) and updates r
+// with the partial sums of <r, r>; k_cg_beta_test computes the residual,
+// beta and the loop test.  After the loop k_cg_finish_x applies the last
+// pending x update.  Same arithmetic as the separate kernels above, hence
+// the same bits; two graph nodes per iteration besides the operator instead
+// of five, and x and p are read and written in the pass that reads p anyway.
+// ---------------------------------------------------------------------------
+
+// alpha from the <p, q> partials; r -= alpha q; partial sums of |r|^2.
+// grid: (nblk, nbins).  Block 0 of a bin records pq, alpha (or the error)
+// and marks the x / p updates pending.
+__global__ void __launch_bounds__(RED_THREADS)
+k_cg_update_r(float2* r, const float2* __restrict__ q, long long n, long long bs, CgState* st,
+              const double* pq_partials, int nblk_pq, double* partials)
+{
+    __shared__ double s_red[2 * RED_THREADS / 32];
+    __shared__ float s_alpha[2];
+    __shared__ int s_ok;
+    const int bin = blockIdx.y;
+    CgState& S = st[bin];
+    // Block 0 may clear S.active (non-finite values): the flag is read once,
+    // by thread 0, before that write, and the whole block follows s_ok.
+    if (threadIdx.x < 32) {
+        int act = 0;
+        if (threadIdx.x == 0) act = S.active;
+        act = __shfl_sync(0xffffffffu, act, 0);
+        double pr = 0.0, pim = 0.0;
+        if (act) warp_partials(pq_partials, (long long)bin * nblk_pq, nblk_pq, pr, pim);
+        if (threadIdx.x == 0 && !act) s_ok = 0;
+        if (threadIdx.x == 0 && act) {
+            const float2 qv = q[(long long)bin * bs];
+            const bool ok = isfinite(qv.x) && isfinite(qv.y) && isfinite(pr) && isfinite(pim);
+            double alpha[2] = {0.0, 0.0};
+            if (ok) cg_alpha(S.rr, pr, pim, alpha);
+            s_alpha[0] = (float)alpha[0];
+            s_alpha[1] = (float)alpha[1];
+            s_ok = ok ? 1 : 0;
+            if (blockIdx.x == 0) {
+                S.pq[0] = pr;
+                S.pq[1] = pim;
+                if (ok) {
+                    S.alpha[0] = alpha[0];
+                    S.alpha[1] = alpha[1];
+                    S.xpend = 1;
+                } else {
+                    S.error = 1;
+                    S.active = 0;
+                    S.xpend = 0;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const float ar = s_alpha[0], ai = s_alpha[1];
+    const long long off = (long long)bin * bs;
+    double acc = 0.0, dummy = 0.0;
+    float fa = 0.f;
+    int cnt = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float2 rv = r[off + i];
+        rv = cg_axmy(rv, ar, ai, q[off + i]);
+        r[off + i] = rv;
+        fa = __fadd_rn(fa, cg_abs2(rv));
+        if (++cnt == CG_FCHUNK) {
+            acc += (double)fa;
+            fa = 0.f;
+            cnt = 0;
+        }
+    }
+    acc += (double)fa;
+    block_reduce2(acc, dummy, s_red);
+    if (threadIdx.x == 0) {
+        double* o = partials + 2 * ((long long)bin * gridDim.x + blockIdx.x);
+        o[0] = acc;
+        o[1] = 0.0;
+    }
+}
+
+// residual, beta and the loop test in one step.  One warp per bin.
+__global__ void k_cg_beta_test(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
+                               int res_stride)
+{
+    const int bin = blockIdx.x;
+    if (bin >= nbins) return;
+    CgState& S = st[bin];
+    if (!S.active) return;
+    double s, unused;
+    warp_partials(partials, (long long)bin * nblk, nblk, s, unused);
+    if (threadIdx.x != 0) return;
+    cg_residual_beta(S, s, residuals ? residuals + (long long)bin * res_stride : nullptr);
+    S.active = (S.res > S.thresh && S.iter < S.max_iter) ? 1 : 0;
+}
+
+// x += alpha p for the bins whose last update is still pending.  grid: (nblk, nbins)
+__global__ void k_cg_finish_x(float2* x, const float2* __restrict__ p, long long n, long long bs, const CgState* st)
+{
+    const int bin = blockIdx.y;
+    const CgState& S = st[bin];
+    if (!S.xpend) return;
+    const float ar = (float)S.alpha[0], ai = (float)S.alpha[1];
+    const long long off = (long long)bin * bs;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        x[off + i] = cg_axpy(x[off + i], ar, ai, p[off + i]);
 }
 
 }  // namespace cgs

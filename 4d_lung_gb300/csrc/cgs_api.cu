@@ -159,6 +159,13 @@ struct cgs_ctx {
     DevBuf d_zbuf, d_ybuf, d_grid, d_yv, d_img, d_data;
     // CG
     DevBuf d_b, d_x, d_r, d_pv, d_q, d_state, d_partials, d_partials2, d_res;
+    // while a fused solve is recorded: the vectors whose pending updates the
+    // forward z pass applies (FwdZArgs::cg); all null otherwise
+    struct {
+        CgState* st = nullptr;
+        float2 *p = nullptr, *x = nullptr;
+        const float2* r = nullptr;
+    } cgf;
     std::map<GraphKey, cudaGraphExec_t> graphs;
     std::map<GraphKey, long long> graph_launches;
     // adjoint y-buffer slot records at the start and at the end of each graph
@@ -175,6 +182,10 @@ struct cgs_ctx {
     // per-stage timing (cgs_profile_apply): events recorded after each pass
     cudaEvent_t* prof_ev = nullptr;
     int prof_n = 0;
+    // parts of the last host-buffer solve (cgs_e2e_stats): events before the
+    // upload, after it, after the graph launch and after the download
+    cudaEvent_t e2e_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool e2e_mark = false;       // solve_d records e2e_ev[2] after its graph launch
     std::string err;
 };
 
@@ -656,6 +667,18 @@ void set_support_tiles(const cgs_ctx* c, StridedPassArgs& a, int b0, int nb)
     a.sup_nsub = c->nch;
 }
 
+// In a fused solve the forward z pass of bins [b0, ...) applies their pending
+// CG updates while it reads the search direction x (== cgf.p + offset).
+void set_cg_fusion(const cgs_ctx* c, FwdZArgs& fz, int b0, const float2* x)
+{
+    if (!c->cgf.st) return;
+    const long long off = x - c->cgf.p;
+    fz.cg = c->cgf.st + b0;
+    fz.cg_p = c->cgf.p + off;
+    fz.cg_r = c->cgf.r + off;
+    fz.cg_x = c->cgf.x + off;
+}
+
 // Forward half for bins [b0, b0+nb) (nb <= ws_bins): image(s) -> grid -> samples (yv).
 // x: per bin [Ni] (x_bs) shared by the coils, or per coil (x_cs) without coil maps.
 int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long long x_cs, bool use_smaps,
@@ -683,6 +706,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fz.coil_in = c->Ni;
     fz.coil_out = zb;
     fz.tw = c->tw[2].as<float2>();
+    if (x_cs == 0) set_cg_fusion(c, fz, b0, x);
     CGS_LAUNCH(c, launch_fwd_z(Gz, fz, nb, c->stream));
 
     StridedPassArgs fy{};
@@ -960,6 +984,7 @@ int toep_chain(cgs_ctx* c, int b0, int nb, const float2* x, float2* q, const flo
     fz.coil_in = c->Ni;
     fz.coil_out = zb;
     fz.tw = c->tw[2].as<float2>();
+    set_cg_fusion(c, fz, b0, x);
     CGS_LAUNCH(c, launch_fwd_z(Gz, fz, nb, c->stream));
 
     StridedPassArgs fy{};
@@ -1273,6 +1298,8 @@ void cgs_destroy(cgs_ctx* c)
     if (c->plain_plan_ok) cufftDestroy(c->plain_plan);
     if (c->z_plan_ok) cufftDestroy(c->z_plan);
     if (c->blas) toeplitz_release(c->blas);
+    for (cudaEvent_t& e : c->e2e_ev)
+        if (e) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -1562,6 +1589,30 @@ static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh
     CGS_LAUNCH(c, launch_cg_init(c->d_b.as<float2>(), c->d_r.as<float2>(), c->d_pv.as<float2>(), x, Ni, Ni,
                                  c->d_partials2.as<double>(), st, nb, c->stream));
     CGS_LAUNCH(c, launch_cg_arm(st, c->d_partials2.as<double>(), nblk_cg, nb, thresh, max_iter, c->stream));
+    if (!x_trace) {
+        // fused iteration: operator (its forward z pass applies the previous
+        // iteration's x and p updates), alpha + r update, beta + loop test
+        struct Scope {   // the fusion pointers never outlive the recording
+            cgs_ctx* c;
+            ~Scope() { c->cgf = {}; }
+        } scope{c};
+        c->cgf.st = st;
+        c->cgf.p = c->d_pv.as<float2>();
+        c->cgf.r = c->d_r.as<float2>();
+        c->cgf.x = x;
+        for (int it = 0; it < max_iter; ++it) {
+            CGS_TRY(apply_bins(c, 0, nb, c->d_pv.as<float2>(), c->d_q.as<float2>(), c->d_pv.as<float2>(),
+                               c->d_partials.as<double>(), nblk_adj));
+            CGS_LAUNCH(c, launch_cg_update_r(c->d_r.as<float2>(), c->d_q.as<float2>(), Ni, Ni, st,
+                                             c->d_partials.as<double>(), nblk_adj, c->d_partials2.as<double>(), nb,
+                                             c->stream));
+            CGS_LAUNCH(c, launch_cg_beta_test(st, c->d_partials2.as<double>(), nblk_cg, nb, c->d_res.as<double>(),
+                                              max_iter, c->stream));
+        }
+        c->cgf = {};
+        CGS_LAUNCH(c, launch_cg_finish_x(x, c->d_pv.as<float2>(), Ni, Ni, st, nb, c->stream));
+        return CGS_OK;
+    }
     for (int it = 0; it < max_iter; ++it) {
         CGS_TRY(apply_bins(c, 0, nb, c->d_pv.as<float2>(), c->d_q.as<float2>(), c->d_pv.as<float2>(),
                            c->d_partials.as<double>(), nblk_adj));
@@ -1645,6 +1696,7 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
     }
     c->launches = c->graph_launches[key];
     CGS_CUDA(c, cudaGraphLaunch(exec, c->stream));
+    if (c->e2e_mark) CGS_CUDA(c, cudaEventRecord(c->e2e_ev[2], c->stream));
     if (residuals || iters) {
         std::vector<CgState> hs(nb);
         CGS_CUDA(c, cudaMemcpyAsync(hs.data(), c->d_state.p, nb * sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
@@ -1764,12 +1816,19 @@ int cgs_cg_solve_batched(cgs_ctx* c, const float* data, float* x, double thresh,
     const size_t bx = (size_t)c->nbins * c->Ni * sizeof(float2);
     CGS_CUDA(c, c->d_data.ensure(bd));
     CGS_CUDA(c, c->d_x.ensure(bx));
+    for (cudaEvent_t& e : c->e2e_ev)
+        if (!e) CGS_CUDA(c, cudaEventCreate(&e));
+    CGS_CUDA(c, cudaEventRecord(c->e2e_ev[0], c->stream));
     CGS_CUDA(c, cudaMemcpyAsync(c->d_data.p, data, bd, cudaMemcpyHostToDevice, c->stream));
+    CGS_CUDA(c, cudaEventRecord(c->e2e_ev[1], c->stream));
     std::vector<int32_t> it_local(c->nbins);
+    c->e2e_mark = true;
     int st = cgs_cg_solve_batched_d(c, c->d_data.as<float>(), c->d_x.as<float>(), thresh, max_iter, residuals,
                                     iters ? iters : it_local.data());
+    c->e2e_mark = false;
     if (st != CGS_OK && st != CGS_ERR_NONFINITE) return st;
     CGS_CUDA(c, cudaMemcpyAsync(x, c->d_x.p, bx, cudaMemcpyDeviceToHost, c->stream));
+    CGS_CUDA(c, cudaEventRecord(c->e2e_ev[3], c->stream));
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
     return st;
 }
@@ -2493,6 +2552,19 @@ int cgs_setup_stats(cgs_ctx* c, double* ms, int32_t n)
 {
     if (!c || (!ms && n > 0) || n < 0) return CGS_ERR_ARG;
     for (int i = 0; i < n && i < 6; ++i) ms[i] = c->setup_ms[i];
+    return CGS_OK;
+}
+
+int cgs_e2e_stats(cgs_ctx* c, double* ms)
+{
+    if (!c || !ms) return CGS_ERR_ARG;
+    for (const cudaEvent_t& e : c->e2e_ev)
+        if (!e) return fail(c, CGS_ERR_STATE, "no host-buffer solve has run (cgs_cg_solve_batched)");
+    for (int i = 0; i < 3; ++i) {
+        float t = 0.f;
+        CGS_CUDA(c, cudaEventElapsedTime(&t, c->e2e_ev[i], c->e2e_ev[i + 1]));
+        ms[i] = t;
+    }
     return CGS_OK;
 }
 

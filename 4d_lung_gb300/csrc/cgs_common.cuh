@@ -22,6 +22,26 @@ CGS_HD float2 cmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b
 CGS_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 CGS_HD float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
 
+// CG vector updates (addToArrayScaled / addArraysScaled, Reco.cpp:153-173)
+// with the step size (ar, ai) rounded to float.  Every product and sum is
+// rounded on its own (no fused multiply-add), so that the separate update
+// kernels and the forward z pass that applies the same updates in a fused
+// solve store the same bits.
+// y + a v
+CGS_D float2 cg_axpy(float2 y, float ar, float ai, float2 v)
+{
+    const float re = __fsub_rn(__fmul_rn(ar, v.x), __fmul_rn(ai, v.y));
+    const float im = __fadd_rn(__fmul_rn(ar, v.y), __fmul_rn(ai, v.x));
+    return make_float2(__fadd_rn(y.x, re), __fadd_rn(y.y, im));
+}
+// y - a v
+CGS_D float2 cg_axmy(float2 y, float ar, float ai, float2 v)
+{
+    const float re = __fsub_rn(__fmul_rn(ar, v.x), __fmul_rn(ai, v.y));
+    const float im = __fadd_rn(__fmul_rn(ar, v.y), __fmul_rn(ai, v.x));
+    return make_float2(__fsub_rn(y.x, re), __fsub_rn(y.y, im));
+}
+
 // ---------------------------------------------------------------------------
 // Compile-time helpers
 // ---------------------------------------------------------------------------

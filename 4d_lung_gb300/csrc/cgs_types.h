@@ -29,6 +29,10 @@ struct CgState {
     int max_iter;
     int active;        // 1 while the loop runs
     int error;         // 1: non-finite value detected (Reco.cpp:264-268)
+    int xpend;         // fused solve: x += alpha p and p = r + beta p of the last
+                       // iteration still to be applied (by the next forward z
+                       // pass, or by the final x update once the loop stopped)
+    int pad_;
 };
 
 struct StridedPassArgs {
@@ -80,6 +84,14 @@ struct FwdZArgs {
     long long coil_in, coil_out;  // coil strides of smaps and out
     const float2* tw;
     int* err;               // timeout flag of the pipelined variant (null: plain kernel)
+    // Fused CG step: with cg set, the image read is the search direction p of
+    // bin cg[blockIdx.y]; when that bin's xpend is set the pass first forms
+    // p = r + beta p and x = x + alpha p (the previous iteration's updates,
+    // Reco.cpp:285-290,306-307) and stores both.
+    const CgState* cg;
+    float2* cg_p;           // == x (stored back)
+    const float2* cg_r;     // residual, same layout as x
+    float2* cg_x;           // the solution, same layout as x
 };
 
 struct AdjZArgs {

@@ -38,6 +38,42 @@ CGS_D float2 table_twiddle(float2 v, float2 w)
 
 CGS_D float2 parity(float2 v, int l) { return (l & 1) ? cneg(v) : v; }
 
+// Image value read by a forward z pass.  In a fused CG solve (a.cg set) the
+// pass reads the search direction p and, while its bin has updates pending,
+// first applies them: x = x + alpha p, p = r + beta p (Reco.cpp:285-290,
+// 306-307); both are stored back.  Each image element is read by one thread
+// of one block, so each update is applied once.
+struct FwdZCg {
+    bool upd;
+    float ar, ai, br, bi;
+};
+CGS_D FwdZCg fwd_z_cg(const FwdZArgs& a)
+{
+    FwdZCg u{false, 0.f, 0.f, 0.f, 0.f};
+    if (a.cg) {
+        const CgState& S = a.cg[blockIdx.y];
+        if (S.active && S.xpend) {
+            u.upd = true;
+            u.ar = (float)S.alpha[0];
+            u.ai = (float)S.alpha[1];
+            u.br = (float)S.beta[0];
+            u.bi = (float)S.beta[1];
+        }
+    }
+    return u;
+}
+// e: element index within the batch (blockIdx.y * x_bs + line * Iz + z)
+CGS_D float2 fwd_z_value(const FwdZArgs& a, const FwdZCg& u, long long e)
+{
+    float2 p = a.x[e];
+    if (u.upd) {
+        a.cg_x[e] = cg_axpy(a.cg_x[e], u.ar, u.ai, p);
+        p = cg_axpy(a.cg_r[e], u.br, u.bi, p);
+        a.cg_p[e] = p;
+    }
+    return p;
+}
+
 // ---------------------------------------------------------------------------
 // Strided pass: lines along a non-contiguous axis of an [A][Lrows][B] array.
 // One block handles TB consecutive columns b of one outer index a.
@@ -581,7 +617,6 @@ k_fwd_z(FwdZArgs a)
     const int tid = threadIdx.x;
     for (int m = tid; m < L; m += blockDim.x) s_tw[m] = a.tw[m];
     const long long line0 = (long long)blockIdx.x * LPB;
-    const float2* xin = a.x + (long long)blockIdx.y * a.x_bs;
     float2* outb = a.out + (long long)blockIdx.y * a.out_bs;
 
     // stage-1 role
@@ -598,18 +633,20 @@ k_fwd_z(FwdZArgs a)
     const int ln2 = tid / R1, k1 = tid % R1;
     const long long line2 = line0 + ln2;
     const bool act2 = ln2 < LPB && line2 < a.nl;
+    const FwdZCg cg = fwd_z_cg(a);
 
     for (int c = 0; c < a.nch; ++c) {
         __syncthreads();   // s_tw ready / previous coil's stage 2 finished
         if (act1) {
             if (c == 0 || a.x_cs != 0) {
-                const float2* xl = xin + (long long)c * a.x_cs + line1 * a.Iz;
+                // a.cg is only set with x_cs == 0: each element is read once
+                const long long eb = (long long)blockIdx.y * a.x_bs + (long long)c * a.x_cs + line1 * a.Iz;
 #pragma unroll
                 for (int n1 = 0; n1 < R1; ++n1) {
                     const int l = R2 * n1 + n2;
                     const int zi = l - a.lo_z;
                     float2 v = make_float2(0.f, 0.f);
-                    if (zi >= 0 && zi < a.Iz) v = parity(cscale(xl[zi], axy * a.apz[zi]), l);
+                    if (zi >= 0 && zi < a.Iz) v = parity(cscale(fwd_z_value(a, cg, eb + zi), axy * a.apz[zi]), l);
                     xa[n1] = v;
                 }
             }
@@ -838,7 +875,6 @@ k_fwd_z_pipe(FwdZArgs a)
     if (tid == 0)
         for (int c = 0; c < NST - 1 && c < a.nch; ++c) issue(c);
 
-    const float2* xin = a.x + (long long)blockIdx.y * a.x_bs;
     float2* outb = a.out + (long long)blockIdx.y * a.out_bs;
     const int ln1 = tid / R2, n2 = tid % R2;
     const long long line1 = line0 + ln1;
@@ -847,12 +883,13 @@ k_fwd_z_pipe(FwdZArgs a)
     if (act1) {
         const int ix = (int)(line1 / a.Iy), iy = (int)(line1 - (long long)ix * a.Iy);
         const float axy = a.apx[ix] * a.apy[iy];
-        const float2* xl = xin + line1 * a.Iz;
+        const FwdZCg cg = fwd_z_cg(a);
+        const long long eb = (long long)blockIdx.y * a.x_bs + line1 * a.Iz;
 #pragma unroll
         for (int n1 = 0; n1 < R1; ++n1) {
             const int l = R2 * n1 + n2;
             const int zi = l - a.lo_z;
-            if (zi >= 0 && zi < a.Iz) xa[zi] = parity(cscale(xl[zi], axy * a.apz[zi]), l);
+            if (zi >= 0 && zi < a.Iz) xa[zi] = parity(cscale(fwd_z_value(a, cg, eb + zi), axy * a.apz[zi]), l);
         }
     }
     const int ln2 = tid / R1, k1 = tid % R1;

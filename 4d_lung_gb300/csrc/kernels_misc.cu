@@ -313,4 +313,27 @@ cudaError_t launch_cg_loop_test(CgState* st, int nbins, cudaStream_t s)
     return cudaGetLastError();
 }
 
+cudaError_t launch_cg_update_r(float2* r, const float2* q, long long n, long long bs, CgState* st,
+                               const double* pq_partials, int nblk_pq, double* partials, int nbins, cudaStream_t s)
+{
+    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    k_cg_update_r<<<grid, RED_THREADS, 0, s>>>(r, q, n, bs, st, pq_partials, nblk_pq, partials);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_beta_test(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
+                                int res_stride, cudaStream_t s)
+{
+    k_cg_beta_test<<<nbins, 32, 0, s>>>(st, partials, nblk, nbins, residuals, res_stride);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cg_finish_x(float2* x, const float2* p, long long n, long long bs, const CgState* st, int nbins,
+                               cudaStream_t s)
+{
+    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    k_cg_finish_x<<<grid, RED_THREADS, 0, s>>>(x, p, n, bs, st);
+    return cudaGetLastError();
+}
+
 }  // namespace cgs

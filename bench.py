@@ -955,7 +955,8 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     e2e_diag = {"host_ms_per_call": statistics.median(host_ms),
                 "device_ms_per_call": statistics.median([a.elapsed_time(b) for a, b in ev]),
-                "device_timed_ms_per_step": ms_step}
+                "device_timed_ms_per_step": ms_step,
+                "last_call_parts_ms": reco.e2e_stats()}
     te = torch.tensor([e2e_s], device=dev)
     if world > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)

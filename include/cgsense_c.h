@@ -363,6 +363,14 @@ int cgs_toeplitz_stats(cgs_ctx* ctx, double* build_ms, int64_t* bytes);
  * last CUDA graph of a batched solve.  n: entries wanted (at most 6). */
 int cgs_setup_stats(cgs_ctx* ctx, double* ms, int32_t n);
 
+/* Device time of the parts of the last cgs_cg_solve_batched call (CUDA
+ * events on the context's stream, ms): ms[0] the upload of the samples,
+ * ms[1] the solve's graph, ms[2] the read-back of the iteration record and
+ * the download of the images, including the host's wait in between.  A
+ * diagnostic of the host-buffer path of CGSense.cpp:226-266 (import, solve,
+ * export) with no counterpart call in the reference. */
+int cgs_e2e_stats(cgs_ctx* ctx, double* ms);
+
 /* Coil sensitivity maps from the measured data of a single-bin context
  * (device pointers; data [n_ch][ns] in the reference's order, maps
  * [n_ch][img]): the adjoint NUFFT of each coil's samples weighted by a Hann

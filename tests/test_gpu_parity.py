@@ -402,3 +402,53 @@ def test_precision_form_against_fp64(gpu_lib, cgs, oracle_mod, o64, synth, compe
     st, xo, reso, ito = o64.cg_sense(p, taps, o64.kernel_ft(p), smaps, dcf, data, 0.0, iters)
     assert rel_l2(x64.cpu().numpy()[0], xo) < 1e-6
     assert np.allclose(res64[0, :iters], reso, rtol=1e-6)
+
+
+@pytest.mark.parametrize("groups,toeplitz", [(False, False), (True, False), (False, True)])
+def test_fused_cg_updates_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, groups, toeplitz):
+    """The solve whose forward z pass applies the previous iteration's
+    x += alpha p and p = r + beta p (Reco.cpp:285-290,306-307), with alpha
+    folded into the residual update and beta into the loop test, gives the
+    same bits as the solve with a kernel per update (the trace form): images,
+    residuals and iteration counts -- with a bin that stops on the threshold
+    before the others, an empty bin, several workspace groups and the
+    Toeplitz operator."""
+    import torch
+    img, grid, nch = (16, 16, 12), (32, 32, 24), 3
+    k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 48)
+    rb = [np.arange(0, 10), np.arange(10, 32), np.arange(32, 35), np.arange(35, 60)]
+    bins = synth.bin_samples(rb, 48) + [np.array([], np.int64)]
+    smaps = synth.coil_maps(img, nch)
+    rng = np.random.default_rng(16)
+    data = (rng.standard_normal((nch, k.shape[0])) + 1j * rng.standard_normal((nch, k.shape[0]))).astype(np.complex64)
+    dcf = rng.uniform(0.5, 1.5, k.shape[0]).astype(np.float32)
+    per_bin = nch * (img[0] * img[1] * grid[2] + 2 * img[0] * grid[1] * grid[2] + int(np.prod(grid))) * 8
+    r = make_reco(cgs, img, grid, nch, kb_w=w, kb_b=b, workspace_bytes=2 * per_bin if groups else 0)
+    r.set_trajectory(k)
+    r.set_dcf(dcf)
+    r.set_bins(bins)
+    r.set_smaps(smaps)
+    if toeplitz:
+        r.set_toeplitz(1)
+    iters, nb = 8, len(bins)
+    stream = torch.cuda.Stream()
+    r.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        d = torch.from_numpy(data).cuda()
+        xf = torch.zeros((nb,) + img, dtype=torch.complex64, device="cuda")
+        xs = torch.zeros_like(xf)
+        tr = torch.zeros((iters, nb) + img, dtype=torch.complex64, device="cuda")
+    stream.synchronize()
+    res0, _ = r.cg_sense_trace_tensor(d, xs, 0.0, iters, tr)
+    # a threshold between bin 1's residuals after its 3rd and 4th iterations
+    # stops it early; the other bins may stop at other iterations
+    thresh = float(0.5 * (res0[1, 2] + res0[1, 3]))
+    for _ in range(2):   # the second call replays the captured graph
+        resf, itf = r.cg_sense_batched_tensor(d, xf, thresh, iters)
+        ress, its = r.cg_sense_trace_tensor(d, xs, thresh, iters, tr)
+        stream.synchronize()
+        assert np.array_equal(itf, its) and itf[1] == 4 and itf[nb - 1] == 0
+        assert np.array_equal(resf, ress)
+        assert torch.equal(xf, xs)
+        assert torch.count_nonzero(xf[nb - 1]) == 0 and torch.count_nonzero(xf[0]) > 0
+    r.close()
