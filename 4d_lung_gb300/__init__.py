@@ -57,7 +57,7 @@ EXPORTS = [
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
     "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic", "cgs_set_launch_shape",
     "cgs_set_support_pruning", "cgs_support_stats", "cgs_spread_matrix_stats", "cgs_estimate_smaps_d",
-    "cgs_forward_y_listed_rows", "cgs_set_toeplitz", "cgs_toeplitz_stats", "cgs_setup_stats", "cgs_e2e_stats",
+    "cgs_forward_y_listed_rows", "cgs_set_toeplitz", "cgs_toeplitz_stats", "cgs_setup_stats", "cgs_e2e_stats", "cgs_set_toeplitz_spectrum", "cgs_toeplitz_spectrum_method",
 ]
 
 # Stage names of cgs_profile_apply, in launch order (one group of bins).
@@ -186,6 +186,8 @@ def lib():
         "cgs_toeplitz_stats": (C.c_int, [vp, vp, vp]),
         "cgs_setup_stats": (C.c_int, [vp, vp, C.c_int32]),
         "cgs_e2e_stats": (C.c_int, [vp, vp]),
+        "cgs_set_toeplitz_spectrum": (C.c_int, [vp, C.c_int32]),
+        "cgs_toeplitz_spectrum_method": (C.c_int, [vp]),
         "cgs_estimate_smaps_d": (C.c_int, [vp, vp, C.c_double, C.c_double, vp]),
         "cgs_reconstruct_states": (C.c_int, [vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_char_p,
                                              C.c_double, C.c_int32, C.c_int32, vp]),
@@ -586,6 +588,16 @@ class Reco:
         """Toeplitz embedding of E^H D E: 0 off (gridded operator), 1 on, 2 on
         with the unfused x stage (see cgs_set_toeplitz)."""
         self._check(self._L.cgs_set_toeplitz(self._ctx, int(mode)))
+
+    def set_toeplitz_spectrum(self, method):
+        """Spectrum build: 0 through the point-spread function (adjoint NUFFT)
+        where the fine grid has FFT kernels, 1 the Dirichlet product (see
+        cgs_set_toeplitz_spectrum)."""
+        self._check(self._L.cgs_set_toeplitz_spectrum(self._ctx, int(method)))
+
+    def toeplitz_spectrum_method(self):
+        """1 point-spread function, 2 Dirichlet product, 0 not built."""
+        return int(self._L.cgs_toeplitz_spectrum_method(self._ctx))
 
     def toeplitz_stats(self):
         """(build time of the spectra in ms, bytes they hold)."""

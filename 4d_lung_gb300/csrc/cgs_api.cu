@@ -145,6 +145,8 @@ struct cgs_ctx {
     bool toep_valid = false;
     uint64_t toep_serial = 0;    // traj_serial the spectra were built from
     double toep_build_ms = 0.0;
+    int toep_method = 0;         // spectrum build: 0 through the PSF where possible, 1 Dirichlet product
+    int toep_used = 0;           // method of the last build: 1 PSF (adjoint NUFFT), 2 Dirichlet product
     // set-up cost of the last rebuild of the bins and of the last graph
     // capture (host clock, ms): sort, tap records, tile and support lists,
     // transposed tap matrix, workspaces, graph capture + instantiation
@@ -895,6 +897,130 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
     return CGS_OK;
 }
 
+int centred_fft_dev(cgs_ctx* c, float2* a, int sign, int rescale);
+int check_timeout(cgs_ctx* c);
+
+// Fine grid of the PSF build: per axis the shortest line length with FFT
+// kernels that is at least 4 I_a (two-fold oversampling of the 2 I_a modes
+// of the point-spread function); false when an axis has none.
+bool psf_fine_grid(const cgs_ctx* c, int nf[3])
+{
+    int n = 0;
+    const int* list = fft_supported_list(&n);
+    for (int a = 0; a < 3; ++a) {
+        nf[a] = 0;
+        for (int i = 0; i < n; ++i)
+            if (list[i] >= 4 * c->I[a] && (nf[a] == 0 || list[i] < nf[a])) nf[a] = list[i];
+        if (nf[a] == 0) return false;
+    }
+    return true;
+}
+
+// Spectra through the point-spread function of each bin (toeplitz.cu,
+// k_psf_*): FP64 Kaiser-Bessel spreading of D onto the fine grid, the
+// centred transform (sign +1) keeping the 2 I_a central positions per axis,
+// deapodisation into the grid, the grid's centred transform (sign -1).
+int build_toeplitz_psf(cgs_ctx* c, const int nf[3])
+{
+    constexpr double kW = 7.0;   // window width (window error ~5e-7 relative)
+    const double beta = 0.5 * kTwoPi * std::sqrt(kW * kW / 4.0 * 1.5 * 1.5 - 0.8);
+    const int* I = c->I;
+    const long long nft = (long long)nf[0] * nf[1] * nf[2];
+    const long long Ng = c->Ng;
+    DevBuf bufA, bufB, bufG, tw[3], rcp[3];
+    // A: FP64 fine grid, then the z pass's output, then the box R; B: the
+    // complex fine grid, then the y pass's output, then the grid (when it fits)
+    CGS_CUDA(c, bufA.ensure((size_t)nft * sizeof(double)));
+    CGS_CUDA(c, bufB.ensure((size_t)nft * sizeof(float2)));
+    float2* gbuf = bufB.as<float2>();
+    if (Ng > nft) {
+        CGS_CUDA(c, bufG.ensure((size_t)Ng * sizeof(float2)));
+        gbuf = bufG.as<float2>();
+    }
+    for (int a = 0; a < 3; ++a) {
+        std::vector<float2> t(nf[a]);
+        for (int m = 0; m < nf[a]; ++m) {
+            const double ang = -kTwoPi * (double)m / (double)nf[a];
+            t[m] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+        }
+        CGS_TRY(upload(c, tw[a], t.data(), t.size() * sizeof(float2)));
+        // 1 / window transform at d / nf, d in [-I, I)
+        std::vector<float> r(2 * I[a]);
+        for (int j = 0; j < 2 * I[a]; ++j) {
+            const double xi = (double)(j - I[a]) / (double)nf[a];
+            const double z = beta * beta - (0.5 * kTwoPi * kW * xi) * (0.5 * kTwoPi * kW * xi);
+            const double rt = std::sqrt(std::fabs(z));
+            const double ft = rt == 0.0 ? kW : kW * (z > 0 ? std::sinh(rt) / rt : std::sin(rt) / rt);
+            r[j] = (float)(1.0 / ft);
+        }
+        CGS_TRY(upload(c, rcp[a], r.data(), r.size() * sizeof(float)));
+    }
+    int sf = 0, sg = 0;
+    for (int a = 0; a < 3; ++a) {
+        sf += nf[a] / 2;
+        sg += c->G[a] / 2;
+    }
+    const float sgn_f = (sf & 1) ? -1.f : 1.f;
+    const float scale = (float)(c->adj_scale_total / (double)Ng) * ((sg & 1) ? -1.f : 1.f);
+    for (int b = 0; b < c->nbins; ++b) {
+        PsfSpreadArgs ps{};
+        ps.k = c->d_k.as<double>();
+        ps.sorted = c->d_sorted.as<int>();
+        ps.dcf = c->has_dcf ? c->d_dcf_sorted.as<float>() : nullptr;
+        ps.s0 = c->h_bin_off[b];
+        ps.n = c->h_bin_off[b + 1] - c->h_bin_off[b];
+        for (int a = 0; a < 3; ++a) {
+            ps.G[a] = c->G[a];
+            ps.nf[a] = nf[a];
+        }
+        ps.w = kW;
+        ps.beta = beta;
+        ps.out = bufA.as<double>();
+        CGS_CUDA(c, cudaMemsetAsync(bufA.p, 0, (size_t)nft * sizeof(double), c->stream));
+        CGS_LAUNCH(c, launch_psf_spread(ps, c->stream));
+        CGS_LAUNCH(c, launch_psf_convert(bufA.as<double>(), bufB.as<float2>(), nft, c->stream));
+        ContigPassArgs cz{};
+        cz.in = bufB.as<float2>();
+        cz.out = bufA.as<float2>();
+        cz.nl = (long long)nf[0] * nf[1];
+        cz.Lin = nf[2];
+        cz.in_off = 0;
+        cz.Lout = 2 * I[2];
+        cz.out_off = nf[2] / 2 - I[2];
+        cz.tw = tw[2].as<float2>();
+        CGS_LAUNCH(c, launch_contig(nf[2], +1, cz, 1, c->stream));
+        StridedPassArgs sy{};
+        sy.in = bufA.as<float2>();
+        sy.out = bufB.as<float2>();
+        sy.in_as = (long long)nf[1] * 2 * I[2];
+        sy.out_as = (long long)2 * I[1] * 2 * I[2];
+        sy.B = 2 * I[2];
+        sy.Lin = nf[1];
+        sy.in_off = 0;
+        sy.Lout = 2 * I[1];
+        sy.out_off = nf[1] / 2 - I[1];
+        sy.tw = tw[1].as<float2>();
+        sy.err = c->d_err.as<int>();
+        CGS_LAUNCH(c, launch_strided(nf[1], +1, sy, nf[0], 1, c->stream));
+        StridedPassArgs sx{};
+        sx.in = bufB.as<float2>();
+        sx.out = bufA.as<float2>();
+        sx.B = 2 * I[1] * 2 * I[2];
+        sx.Lin = nf[0];
+        sx.in_off = 0;
+        sx.Lout = 2 * I[0];
+        sx.out_off = nf[0] / 2 - I[0];
+        sx.tw = tw[0].as<float2>();
+        sx.err = c->d_err.as<int>();
+        CGS_LAUNCH(c, launch_strided(nf[0], +1, sx, 1, 1, c->stream));
+        CGS_LAUNCH(c, launch_psf_place(bufA.as<float2>(), rcp[0].as<float>(), rcp[1].as<float>(), rcp[2].as<float>(),
+                                       c->G, I, sgn_f, gbuf, c->stream));
+        CGS_TRY(centred_fft_dev(c, gbuf, -1, 0));
+        CGS_LAUNCH(c, launch_psf_spectrum(gbuf, scale, Ng, c->d_toep.as<float>() + (long long)b * Ng, c->stream));
+    }
+    return CGS_OK;
+}
+
 // Toeplitz embedding: per bin the spectrum P of the point-spread function
 // of its samples (current coordinates and density weights), scaled so that
 // F_c^H P F_c between the unscaled passes is the gridded operator's
@@ -906,6 +1032,28 @@ int build_toeplitz(cgs_ctx* c)
             return fail(c, CGS_ERR_ARG, "the Toeplitz embedding needs grid >= 2 x image - 1 on every axis");
     const long long Ng = c->Ng;
     CGS_CUDA(c, c->d_toep.ensure((size_t)std::max(c->nbins, 1) * Ng * sizeof(float)));
+    int nf[3];
+    if (c->toep_method == 0 && psf_fine_grid(c, nf)) {
+        cudaEvent_t e0, e1;
+        CGS_CUDA(c, cudaEventCreate(&e0));
+        CGS_CUDA(c, cudaEventCreate(&e1));
+        cudaEventRecord(e0, c->stream);
+        int st = build_toeplitz_psf(c, nf);
+        cudaEventRecord(e1, c->stream);
+        const cudaError_t es = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (es == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (st != CGS_OK) return st;
+        CGS_CUDA(c, es);
+        CGS_TRY(check_timeout(c));
+        c->toep_build_ms = ms;
+        c->toep_used = 1;
+        c->toep_valid = true;
+        c->toep_serial = c->traj_serial;
+        return CGS_OK;
+    }
     const int gmax = std::max(c->G[0], std::max(c->G[1], c->G[2]));
     if (c->d_ones.bytes < (size_t)gmax * sizeof(float)) {
         std::vector<float> one(gmax, 1.f);
@@ -950,6 +1098,7 @@ int build_toeplitz(cgs_ctx* c)
     if (st != CGS_OK) return st;
     CGS_CUDA(c, es);
     c->toep_build_ms = ms;
+    c->toep_used = 2;
     c->toep_valid = true;
     c->toep_serial = c->traj_serial;
     return CGS_OK;
@@ -2509,6 +2658,21 @@ int cgs_toeplitz_stats(cgs_ctx* c, double* build_ms, int64_t* bytes)
     if (bytes) *bytes = c->toep_valid ? (int64_t)c->nbins * c->Ng * (int64_t)sizeof(float) : 0;
     return CGS_OK;
 }
+
+int cgs_set_toeplitz_spectrum(cgs_ctx* c, int32_t method)
+{
+    if (!c) return CGS_ERR_ARG;
+    if (method < 0 || method > 1) return fail(c, CGS_ERR_ARG, "spectrum method must be 0 or 1");
+    if (c->toep_method != method) {
+        c->toep_method = method;
+        c->toep_valid = false;
+        drop_graphs(c);
+        if (c->toep_mode && c->ns > 0 && !c->bins.empty()) return check_ready(c, false, false);
+    }
+    return CGS_OK;
+}
+
+int cgs_toeplitz_spectrum_method(const cgs_ctx* c) { return c && c->toep_valid ? c->toep_used : 0; }
 
 int cgs_set_support_pruning(cgs_ctx* c, int32_t on)
 {

@@ -215,6 +215,21 @@ struct ToepBuildArgs {
     float* P;                  // out: [Gx][Gy * Gz]
 };
 
+// Point-spread function of one bin by an adjoint NUFFT (toeplitz.cu): the
+// density weights spread with a Kaiser-Bessel window of width w onto a fine
+// grid nf (periodic, sample at nf nu + nf/2), accumulated in FP64.
+constexpr int PSF_TAPS = 8;        // candidate points per axis (window width <= 7)
+struct PsfSpreadArgs {
+    const double* k;           // coordinates [ns][3] (global index)
+    const int* sorted;         // sorted position -> global sample index
+    const float* dcf;          // sorted density weights, or null
+    long long s0, n;
+    int G[3];                  // grid of the operator (defines nu)
+    int nf[3];                 // fine grid
+    double w, beta;            // window width and shape
+    double* out;               // [nf0][nf1][nf2]
+};
+
 // Loss gradient pass (grad.cu): one bin's samples [s0, s0 + n) in sorted order.
 struct InterpGradArgs {
     const float2* grid;        // coil c at grid + c * coil_stride (one bin)

@@ -136,6 +136,15 @@ long long toeplitz_chunk(const int G[3], long long work_elems);
 int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, void** handle, cudaStream_t s,
                    std::string* err);
 void toeplitz_release(void* handle);
+// Spectrum through the point-spread function (toeplitz.cu): FP64 window
+// spreading of one bin's density weights onto the fine grid, conversion to
+// complex, placement of the deapodised central box into the grid, and the
+// real spectrum of the grid's transform.
+cudaError_t launch_psf_spread(const PsfSpreadArgs& a, cudaStream_t s);
+cudaError_t launch_psf_convert(const double* in, float2* out, long long n, cudaStream_t s);
+cudaError_t launch_psf_place(const float2* R, const float* rx, const float* ry, const float* rz, const int G[3],
+                             const int I[3], float sgn, float2* grid, cudaStream_t s);
+cudaError_t launch_psf_spectrum(const float2* grid, float scale, long long n, float* P, cudaStream_t s);
 // grid[item][j] *= P[item / nch][j] over items grids of Ng points
 cudaError_t launch_toep_mul(float2* grid, const float* P, long long Ng, int nch, int items, cudaStream_t s);
 // Fused x stage in place: forward x transform of the Lin = L/2 stored rows,

@@ -213,6 +213,135 @@ int toeplitz_build(const ToepBuildArgs& a, float* work, long long work_elems, vo
     return rc;
 }
 
+// ---------------------------------------------------------------------------
+// Spectrum through the point-spread function (the default where the fine
+// grid's line lengths have FFT kernels).  h(d) = sum_i D_i exp(2 pi i nu_i.d)
+// on |d_a| < I_a is an adjoint (type-1) NUFFT of the density weights:
+//   1. k_psf_spread: D_i times a Kaiser-Bessel window of width w <= 7 on the
+//      fine grid nf (nf_a >= 4 I_a, two-fold oversampling of the 2 I_a
+//      modes), sample at nf nu + nf/2, periodic; FP64 accumulation;
+//   2. k_psf_convert: to complex float;
+//   3. the library's centred FFT passes (sign +1) keeping the 2 I_a central
+//      output positions per axis (d in [-I_a, I_a));
+//   4. k_psf_place: divide by the window's Fourier transform, times
+//      (-1)^(sum nf_a / 2), into the grid at d + G/2 (zero outside |d_a| < I_a);
+//   5. the centred FFT of the grid (sign -1);
+//   6. k_psf_spectrum: P = s/Ng (-1)^(sum G_a / 2) Re(.).
+// Cost O(M w^3 + N_fine log N_fine) per bin instead of the Dirichlet
+// product's 2 Ng M flops; the window error at w = 7 is ~5e-7 relative.
+// ---------------------------------------------------------------------------
+
+// One warp per sample: lanes 0..23 evaluate the 3 x PSF_TAPS window factors
+// (FP64 I0), then the warp adds the PSF_TAPS^3 products (z fastest, so
+// consecutive lanes hit consecutive addresses) with FP64 atomics.
+__global__ void __launch_bounds__(256) k_psf_spread(PsfSpreadArgs a)
+{
+    __shared__ double s_f[8][3 * PSF_TAPS];
+    __shared__ int s_g[8][3 * PSF_TAPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long i = (long long)blockIdx.x * 8 + warp;
+    if (i >= a.n) return;                       // whole warp
+    const long long g = a.sorted[a.s0 + i];
+    const double d = a.dcf ? (double)a.dcf[a.s0 + i] : 1.0;
+    if (lane < 3 * PSF_TAPS) {
+        const int ax = lane / PSF_TAPS, t = lane % PSF_TAPS;
+        const double G = (double)a.G[ax], nf = (double)a.nf[ax];
+        const double nu = (a.k[3 * g + ax] * (G - 1.0) - 0.5 * G) / G;
+        const double u = nf * nu + 0.5 * nf;
+        const double g0 = ceil(u - 0.5 * a.w);
+        const double x = g0 + (double)t - u;
+        const double q = 1.0 - (2.0 * x / a.w) * (2.0 * x / a.w);
+        double f = q >= 0.0 ? cyl_bessel_i0(a.beta * sqrt(q)) : 0.0;
+        if (ax == 0) f *= d;
+        int gi = (int)g0 + t;
+        gi %= a.nf[ax];
+        if (gi < 0) gi += a.nf[ax];
+        s_f[warp][lane] = f;
+        s_g[warp][lane] = gi;
+    }
+    __syncwarp();
+    const double* f = s_f[warp];
+    const int* gg = s_g[warp];
+    constexpr int T3 = PSF_TAPS * PSF_TAPS * PSF_TAPS;
+    for (int c = lane; c < T3; c += 32) {
+        const int tx = c / (PSF_TAPS * PSF_TAPS), ty = (c / PSF_TAPS) % PSF_TAPS, tz = c % PSF_TAPS;
+        const double v = f[tx] * f[PSF_TAPS + ty] * f[2 * PSF_TAPS + tz];
+        if (v == 0.0) continue;
+        const long long e = ((long long)gg[tx] * a.nf[1] + gg[PSF_TAPS + ty]) * a.nf[2] + gg[2 * PSF_TAPS + tz];
+        atomicAdd(a.out + e, v);
+    }
+}
+
+__global__ void k_psf_convert(const double* __restrict__ in, float2* __restrict__ out, long long n)
+{
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        out[e] = make_float2((float)in[e], 0.f);
+}
+
+// grid[k] = sgn * R[d + I] * rx[dx + I] ry[..] rz[..] for |d_a| < I_a, d = k - G/2; else 0.
+// R: [2Ix][2Iy][2Iz]; r*: reciprocal window transforms at d / nf, d in [-I, I).
+__global__ void k_psf_place(const float2* __restrict__ R, const float* __restrict__ rx, const float* __restrict__ ry,
+                            const float* __restrict__ rz, int Gx, int Gy, int Gz, int Ix, int Iy, int Iz, float sgn,
+                            float2* __restrict__ grid)
+{
+    const long long n = (long long)Gx * Gy * Gz;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        const int kz = (int)(e % Gz);
+        const long long t = e / Gz;
+        const int ky = (int)(t % Gy), kx = (int)(t / Gy);
+        const int dx = kx - Gx / 2, dy = ky - Gy / 2, dz = kz - Gz / 2;
+        float2 v = make_float2(0.f, 0.f);
+        if (dx > -Ix && dx < Ix && dy > -Iy && dy < Iy && dz > -Iz && dz < Iz) {
+            const int jx = dx + Ix, jy = dy + Iy, jz = dz + Iz;
+            const float2 r = R[((long long)jx * (2 * Iy) + jy) * (2 * Iz) + jz];
+            const float m = sgn * rx[jx] * ry[jy] * rz[jz];
+            v = make_float2(r.x * m, r.y * m);
+        }
+        grid[e] = v;
+    }
+}
+
+// P[k] = scale * Re(grid[k])
+__global__ void k_psf_spectrum(const float2* __restrict__ grid, float scale, long long n, float* __restrict__ P)
+{
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        P[e] = scale * grid[e].x;
+}
+
+namespace {
+unsigned grid_stride_blocks(long long n)
+{
+    return (unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 16));
+}
+}  // namespace
+
+cudaError_t launch_psf_spread(const PsfSpreadArgs& a, cudaStream_t s)
+{
+    if (a.n <= 0) return cudaSuccess;
+    k_psf_spread<<<(unsigned)((a.n + 7) / 8), 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_psf_convert(const double* in, float2* out, long long n, cudaStream_t s)
+{
+    k_psf_convert<<<grid_stride_blocks(n), 256, 0, s>>>(in, out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_psf_place(const float2* R, const float* rx, const float* ry, const float* rz, const int G[3],
+                             const int I[3], float sgn, float2* grid, cudaStream_t s)
+{
+    const long long n = (long long)G[0] * G[1] * G[2];
+    k_psf_place<<<grid_stride_blocks(n), 256, 0, s>>>(R, rx, ry, rz, G[0], G[1], G[2], I[0], I[1], I[2], sgn, grid);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_psf_spectrum(const float2* grid, float scale, long long n, float* P, cudaStream_t s)
+{
+    k_psf_spectrum<<<grid_stride_blocks(n), 256, 0, s>>>(grid, scale, n, P);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_toep_mul(float2* grid, const float* P, long long Ng, int nch, int items, cudaStream_t s)
 {
     const long long total = Ng * items;

@@ -342,8 +342,8 @@ int cgs_set_support_pruning(cgs_ctx* ctx, int32_t on);
  * right-hand side stays the gridded adjoint of the data; the trajectory
  * derivatives keep the gridded operator.  The spectra (4 bytes per grid
  * point and bin) are built from the current coordinates, bins and density
- * weights (one FP32 matrix product per chunk of samples, cuBLAS opened at
- * run time) and rebuilt after any of them changes.  Mode 2: the same
+ * weights (cgs_set_toeplitz_spectrum says how) and rebuilt after any of
+ * them changes.  Mode 2: the same
  * operator with the x stage unfused (forward x pass, multiply, adjoint x
  * pass; for comparison).  Mode 0 (default): the gridded operator; the
  * spectra are released.  cgs_apply_vjp_k_d (the derivative of the gridded
@@ -352,6 +352,23 @@ int cgs_set_toeplitz(cgs_ctx* ctx, int32_t mode);
 /* Time of the last spectrum build (ms) and the bytes the spectra hold (0
  * while not built). */
 int cgs_toeplitz_stats(cgs_ctx* ctx, double* build_ms, int64_t* bytes);
+
+/* How the Toeplitz spectra are built (an extension; the reference has no
+ * Toeplitz embedding, and its normal operator is the gridded one of
+ * Reco.cpp:175-321).  method 0 (default): through each bin's point-spread
+ * function h(d) = sum_i D_i exp(2 pi i nu_i . d), computed by an adjoint
+ * NUFFT of the density weights -- Kaiser-Bessel window of width 7 on a
+ * fine grid of at least 4 I points per axis, FP64 accumulation, the
+ * library's FFT passes -- then the grid's transform; O(M w^3 + N log N) per
+ * bin, window error ~5e-7 relative.  Used when every fine-grid axis has an
+ * FFT line length (4 I <= 512), else the Dirichlet product.  method 1: the
+ * Dirichlet-kernel product of every sample with every grid point (exact to
+ * FP32 rounding, 2 Ng M flops per bin, cuBLAS).  Changing the method
+ * rebuilds the spectra. */
+int cgs_set_toeplitz_spectrum(cgs_ctx* ctx, int32_t method);
+/* Method of the last spectrum build: 1 point-spread function, 2 Dirichlet
+ * product, 0 while no spectra are built. */
+int cgs_toeplitz_spectrum_method(const cgs_ctx* ctx);
 
 /* Set-up cost of the current bins (host clock, milliseconds; the part of
  * ConvKernel::calculateWeights, Reco.cpp:698-806, that the reference repeats

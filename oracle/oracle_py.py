@@ -301,6 +301,63 @@ def toeplitz_spectrum(k, img, grid, dcf, adj_scale=ADJ_SCALE):
     return np.einsum("i,ia,ib,ic->abc", d, K[0], K[1], K[2]) * (s / np.prod(grid))
 
 
+def kb_window(x, W, beta):
+    """Kaiser-Bessel window I0(beta sqrt(1 - (2x/W)^2)) on |x| <= W/2, 0 outside."""
+    x = np.asarray(x, np.float64)
+    t = 1.0 - (2.0 * x / W) ** 2
+    return np.where(t >= 0.0, np.i0(beta * np.sqrt(np.clip(t, 0.0, None))), 0.0)
+
+
+def kb_window_ft(xi, W, beta):
+    """Continuous Fourier transform of kb_window at frequency xi (cycles per
+    unit): W sinh(sqrt(beta^2 - (pi W xi)^2)) / sqrt(beta^2 - (pi W xi)^2)."""
+    z = beta ** 2 - (np.pi * W * np.asarray(xi, np.float64)) ** 2
+    r = np.sqrt(np.abs(z))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        v = np.where(z > 0, np.sinh(r) / r, np.sin(r) / r)
+    return W * np.where(r == 0.0, 1.0, v)
+
+
+def toeplitz_spectrum_nufft(k, img, grid, dcf, adj_scale=ADJ_SCALE, W=7.0, fine=None):
+    """The spectrum of toeplitz_spectrum through the point-spread function
+    h(d) = sum_i D_i exp(2 pi i nu_i . d), |d_a| < I_a, computed by an adjoint
+    (type-1) NUFFT, as the library's set-up does it: D spread with a
+    Kaiser-Bessel window of width W onto a 2x oversampled fine grid of
+    n_a = 4 I_a points (sample position n nu + n/2, periodic), the centred
+    transform (sign +1) of the fine grid, division by the window's Fourier
+    transform, then h placed at d + G/2 of the grid and the centred
+    transform (sign -1): P = s/N_grid (-1)^(sum G/2) Re(...).  FP64, small
+    problems only (a Python loop over samples)."""
+    nu = sample_frequencies(k, grid)
+    M = nu.shape[0]
+    d = np.ones(M) if dcf is None else np.asarray(dcf, np.float64)
+    n = [4 * i for i in img] if fine is None else list(fine)
+    beta = np.pi * np.sqrt(W * W / 4.0 * 1.5 ** 2 - 0.8)
+    b = np.zeros(n)
+    for i in range(M):
+        idx, wts = [], []
+        for a in range(3):
+            u = n[a] * nu[i, a] + n[a] / 2.0
+            g = np.arange(int(np.ceil(u - W / 2.0)), int(np.floor(u + W / 2.0)) + 1)
+            idx.append(np.mod(g, n[a]))
+            wts.append(kb_window(g - u, W, beta))
+        np.add.at(b, np.ix_(*idx), d[i] * np.einsum("a,b,c->abc", *wts))
+    L = centred_fft_np(b, +1)
+    box = []
+    deap = []
+    for a in range(3):
+        dd = np.arange(-(img[a] - 1), img[a])
+        box.append(dd + n[a] // 2)
+        deap.append(kb_window_ft(dd / n[a], W, beta))
+    h = L[np.ix_(*box)] / np.einsum("a,b,c->abc", *deap)
+    h *= (-1.0) ** sum(v // 2 for v in n)
+    buf = np.zeros(tuple(grid), np.complex128)
+    buf[np.ix_(*[np.arange(-(img[a] - 1), img[a]) + grid[a] // 2 for a in range(3)])] = h
+    L2 = centred_fft_np(buf, -1)
+    s = adj_scale / np.sqrt(np.prod(grid))
+    return (L2.real * ((-1.0) ** sum(g // 2 for g in grid))) * (s / np.prod(grid))
+
+
 def centred_fft_np(a, sign):
     """Fourier::transformFWD (sign -1) / transformBWD (+1) without scaling:
     (-1)^n before and (-1)^k after an unnormalised transform on each axis."""
