@@ -62,16 +62,30 @@ CGS_D FwdZCg fwd_z_cg(const FwdZArgs& a)
     }
     return u;
 }
-// e: element index within the batch (blockIdx.y * x_bs + line * Iz + z)
-CGS_D float2 fwd_z_value(const FwdZArgs& a, const FwdZCg& u, long long e)
+
+// Fused form of a thread's image reads: for each of its line positions the
+// pending updates are applied and stored, and p * apod * parity is handed to
+// `put`.  Pointers are restrict-qualified copies, so that the loads of
+// later positions can be issued before the stores of earlier ones.
+// eb: element index of the line start within the batch.
+template <int R1, int R2, class Put>
+CGS_D void fwd_z_fused_line(const FwdZArgs& a, const FwdZCg& u, long long eb, int n2, float axy, Put put)
 {
-    float2 p = a.x[e];
-    if (u.upd) {
-        a.cg_x[e] = cg_axpy(a.cg_x[e], u.ar, u.ai, p);
-        p = cg_axpy(a.cg_r[e], u.br, u.bi, p);
-        a.cg_p[e] = p;
+    float2* __restrict__ P = a.cg_p + eb;
+    const float2* __restrict__ Rr = a.cg_r + eb;
+    float2* __restrict__ X = a.cg_x + eb;
+#pragma unroll
+    for (int n1 = 0; n1 < R1; ++n1) {
+        const int l = R2 * n1 + n2;
+        const int zi = l - a.lo_z;
+        if (zi >= 0 && zi < a.Iz) {
+            const float2 p0 = P[zi];
+            X[zi] = cg_axpy(X[zi], u.ar, u.ai, p0);
+            const float2 p1 = cg_axpy(Rr[zi], u.br, u.bi, p0);
+            P[zi] = p1;
+            put(n1, zi, parity(cscale(p1, axy * a.apz[zi]), l));
+        }
     }
-    return p;
 }
 
 // ---------------------------------------------------------------------------
@@ -641,13 +655,20 @@ k_fwd_z(FwdZArgs a)
             if (c == 0 || a.x_cs != 0) {
                 // a.cg is only set with x_cs == 0: each element is read once
                 const long long eb = (long long)blockIdx.y * a.x_bs + (long long)c * a.x_cs + line1 * a.Iz;
+                if (cg.upd) {
 #pragma unroll
-                for (int n1 = 0; n1 < R1; ++n1) {
-                    const int l = R2 * n1 + n2;
-                    const int zi = l - a.lo_z;
-                    float2 v = make_float2(0.f, 0.f);
-                    if (zi >= 0 && zi < a.Iz) v = parity(cscale(fwd_z_value(a, cg, eb + zi), axy * a.apz[zi]), l);
-                    xa[n1] = v;
+                    for (int n1 = 0; n1 < R1; ++n1) xa[n1] = make_float2(0.f, 0.f);
+                    fwd_z_fused_line<R1, R2>(a, cg, eb, n2, axy, [&](int n1, int, float2 v) { xa[n1] = v; });
+                } else {
+                    const float2* xl = a.x + eb;
+#pragma unroll
+                    for (int n1 = 0; n1 < R1; ++n1) {
+                        const int l = R2 * n1 + n2;
+                        const int zi = l - a.lo_z;
+                        float2 v = make_float2(0.f, 0.f);
+                        if (zi >= 0 && zi < a.Iz) v = parity(cscale(xl[zi], axy * a.apz[zi]), l);
+                        xa[n1] = v;
+                    }
                 }
             }
             float2 v[R1];
@@ -885,11 +906,16 @@ k_fwd_z_pipe(FwdZArgs a)
         const float axy = a.apx[ix] * a.apy[iy];
         const FwdZCg cg = fwd_z_cg(a);
         const long long eb = (long long)blockIdx.y * a.x_bs + line1 * a.Iz;
+        if (cg.upd) {
+            fwd_z_fused_line<R1, R2>(a, cg, eb, n2, axy, [&](int, int zi, float2 v) { xa[zi] = v; });
+        } else {
+            const float2* xl = a.x + eb;
 #pragma unroll
-        for (int n1 = 0; n1 < R1; ++n1) {
-            const int l = R2 * n1 + n2;
-            const int zi = l - a.lo_z;
-            if (zi >= 0 && zi < a.Iz) xa[zi] = parity(cscale(fwd_z_value(a, cg, eb + zi), axy * a.apz[zi]), l);
+            for (int n1 = 0; n1 < R1; ++n1) {
+                const int l = R2 * n1 + n2;
+                const int zi = l - a.lo_z;
+                if (zi >= 0 && zi < a.Iz) xa[zi] = parity(cscale(xl[zi], axy * a.apz[zi]), l);
+            }
         }
     }
     const int ln2 = tid / R1, k1 = tid % R1;
