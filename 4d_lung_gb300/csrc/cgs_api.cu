@@ -1032,6 +1032,12 @@ int build_toeplitz(cgs_ctx* c)
             return fail(c, CGS_ERR_ARG, "the Toeplitz embedding needs grid >= 2 x image - 1 on every axis");
     const long long Ng = c->Ng;
     CGS_CUDA(c, c->d_toep.ensure((size_t)std::max(c->nbins, 1) * Ng * sizeof(float)));
+    // unit deapodisation vectors of the operator's z passes (either method)
+    const int gmax = std::max(c->G[0], std::max(c->G[1], c->G[2]));
+    if (c->d_ones.bytes < (size_t)gmax * sizeof(float)) {
+        std::vector<float> one(gmax, 1.f);
+        CGS_TRY(upload(c, c->d_ones, one.data(), one.size() * sizeof(float)));
+    }
     int nf[3];
     if (c->toep_method == 0 && psf_fine_grid(c, nf)) {
         cudaEvent_t e0, e1;
@@ -1053,11 +1059,6 @@ int build_toeplitz(cgs_ctx* c)
         c->toep_valid = true;
         c->toep_serial = c->traj_serial;
         return CGS_OK;
-    }
-    const int gmax = std::max(c->G[0], std::max(c->G[1], c->G[2]));
-    if (c->d_ones.bytes < (size_t)gmax * sizeof(float)) {
-        std::vector<float> one(gmax, 1.f);
-        CGS_TRY(upload(c, c->d_ones, one.data(), one.size() * sizeof(float)));
     }
     // work: a chunk of samples' Dirichlet tables and their (y, z) products (W
     // of at most 2^28 floats, the whole bin when it fits)

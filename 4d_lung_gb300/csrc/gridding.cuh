@@ -79,9 +79,14 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
 {
     const int bin = a.bin0 + blockIdx.z;
     const long long s0 = a.bin_off[bin], s1 = a.bin_off[bin + 1];
-    const long long i = s0 + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    // blockIdx.x = sample block * chunks + coil chunk: the chunks of a sample
+    // block run side by side, so the blocks in flight cover a short run of
+    // samples (a compact region of the grid) for all coils, which L2 holds
+    const int nchunk = (a.nch + CC - 1) / CC;
+    const int chunk = (int)(blockIdx.x % (unsigned)nchunk);
+    const long long i = s0 + (long long)(blockIdx.x / (unsigned)nchunk) * blockDim.x + threadIdx.x;
     if (i >= s1) return;
-    const int c0 = blockIdx.y * CC;
+    const int c0 = chunk * CC;
     const float2* grid = a.grid + (long long)blockIdx.z * a.grid_bs + (long long)c0 * a.coil_stride;
     float w[15];
     int nx, ny, nz;

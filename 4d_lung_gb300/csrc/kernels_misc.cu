@@ -92,7 +92,9 @@ cudaError_t launch_tap_records(const double* k, const int* sample_idx, long long
 cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, int cc, cudaStream_t s)
 {
     if (max_bin_samples == 0 || nbins == 0) return cudaSuccess;
-    dim3 grid((unsigned)((max_bin_samples + 127) / 128), (unsigned)((a.nch + cc - 1) / cc), (unsigned)nbins);
+    const long long nblk = ((max_bin_samples + 127) / 128) * ((a.nch + cc - 1) / cc);
+    if (nblk > 0x7fffffffLL) return cudaErrorInvalidValue;
+    dim3 grid((unsigned)nblk, 1u, (unsigned)nbins);
     switch (cc) {
     case 2: k_interp<2><<<grid, 128, 0, s>>>(a); break;
     case 4: k_interp<4><<<grid, 128, 0, s>>>(a); break;

@@ -944,6 +944,7 @@ def run_ours(args):
     # the graph and the state read-back; host work between them is not in it)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     host_ms = []
+    parts = []
     t0 = time.perf_counter()
     for i in range(args.steps):
         t1 = time.perf_counter()
@@ -951,12 +952,25 @@ def run_ours(args):
         host_call()
         ev[i][1].record(stream)
         host_ms.append(1e3 * (time.perf_counter() - t1))
+        parts.append(reco.e2e_stats())
     e2e_s = time.perf_counter() - t0
+    # the same upload by PyTorch from the same pinned buffer, for comparison
+    d_tmp = torch.empty_like(data)
+    raw = []
+    for _ in range(3):
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(stream)
+        d_tmp.copy_(h_data, non_blocking=True)
+        r1.record(stream)
+        torch.cuda.synchronize(dev)
+        raw.append(r0.elapsed_time(r1))
+    del d_tmp
     torch.cuda.synchronize(dev)
     e2e_diag = {"host_ms_per_call": statistics.median(host_ms),
                 "device_ms_per_call": statistics.median([a.elapsed_time(b) for a, b in ev]),
                 "device_timed_ms_per_step": ms_step,
-                "last_call_parts_ms": reco.e2e_stats()}
+                "parts_ms": {k: statistics.median([p[k] for p in parts]) for k in parts[0]},
+                "torch_upload_ms": statistics.median(raw)}
     te = torch.tensor([e2e_s], device=dev)
     if world > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
