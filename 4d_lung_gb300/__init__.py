@@ -185,7 +185,7 @@ def lib():
         "cgs_set_toeplitz": (C.c_int, [vp, C.c_int32]),
         "cgs_toeplitz_stats": (C.c_int, [vp, vp, vp]),
         "cgs_setup_stats": (C.c_int, [vp, vp, C.c_int32]),
-        "cgs_e2e_stats": (C.c_int, [vp, vp]),
+        "cgs_e2e_stats": (C.c_int, [vp, vp, vp]),
         "cgs_set_toeplitz_spectrum": (C.c_int, [vp, C.c_int32]),
         "cgs_toeplitz_spectrum_method": (C.c_int, [vp]),
         "cgs_estimate_smaps_d": (C.c_int, [vp, vp, C.c_double, C.c_double, vp]),
@@ -616,10 +616,14 @@ class Reco:
 
     def e2e_stats(self):
         """Device time (ms) of the parts of the last host-buffer batched
-        solve (see cgs_e2e_stats): {upload, solve, download}."""
+        solve and whether its buffers were page-locked (see cgs_e2e_stats):
+        {upload, solve, download, pinned: [data, x]}."""
         v = np.zeros(3, np.float64)
-        self._check(self._L.cgs_e2e_stats(self._ctx, _p(v)))
-        return dict(zip(("upload", "solve", "download"), [float(x) for x in v]))
+        pin = np.zeros(2, np.int32)
+        self._check(self._L.cgs_e2e_stats(self._ctx, _p(v), _p(pin)))
+        out = dict(zip(("upload", "solve", "download"), [float(x) for x in v]))
+        out["pinned"] = [int(pin[0]), int(pin[1])]
+        return out
 
     def spread_matrix_stats(self):
         """(taps, grid points) of the transposed tap matrix (0, 0 when not built)."""

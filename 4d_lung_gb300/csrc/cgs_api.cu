@@ -188,6 +188,7 @@ struct cgs_ctx {
     // upload, after it, after the graph launch and after the download
     cudaEvent_t e2e_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool e2e_mark = false;       // solve_d records e2e_ev[2] after its graph launch
+    int e2e_pinned[2] = {0, 0};  // host buffers of the last call page-locked (as this runtime sees them)
     std::string err;
 };
 
@@ -1968,6 +1969,12 @@ int cgs_cg_solve_batched(cgs_ctx* c, const float* data, float* x, double thresh,
     CGS_CUDA(c, c->d_x.ensure(bx));
     for (cudaEvent_t& e : c->e2e_ev)
         if (!e) CGS_CUDA(c, cudaEventCreate(&e));
+    const void* hp[2] = {data, x};
+    for (int j = 0; j < 2; ++j) {
+        cudaPointerAttributes pa{};
+        c->e2e_pinned[j] = cudaPointerGetAttributes(&pa, hp[j]) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+        cudaGetLastError();
+    }
     CGS_CUDA(c, cudaEventRecord(c->e2e_ev[0], c->stream));
     CGS_CUDA(c, cudaMemcpyAsync(c->d_data.p, data, bd, cudaMemcpyHostToDevice, c->stream));
     CGS_CUDA(c, cudaEventRecord(c->e2e_ev[1], c->stream));
@@ -2720,9 +2727,13 @@ int cgs_setup_stats(cgs_ctx* c, double* ms, int32_t n)
     return CGS_OK;
 }
 
-int cgs_e2e_stats(cgs_ctx* c, double* ms)
+int cgs_e2e_stats(cgs_ctx* c, double* ms, int32_t* pinned)
 {
     if (!c || !ms) return CGS_ERR_ARG;
+    if (pinned) {
+        pinned[0] = c->e2e_pinned[0];
+        pinned[1] = c->e2e_pinned[1];
+    }
     for (const cudaEvent_t& e : c->e2e_ev)
         if (!e) return fail(c, CGS_ERR_STATE, "no host-buffer solve has run (cgs_cg_solve_batched)");
     for (int i = 0; i < 3; ++i) {

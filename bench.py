@@ -184,6 +184,24 @@ def scan_bins(synth, name, max_bins=0):
     return sbins[:max_bins] if max_bins > 0 else sbins
 
 
+_HOST_BUFS = []
+
+
+def host_buffer(cgs, torch, shape):
+    """A complex64 host tensor in page-locked memory from the library's own
+    allocator (cgs_alloc_host), the buffer a C-ABI caller hands to the
+    host-buffer calls; kept until the process exits."""
+    import ctypes as C
+    n = int(np.prod(shape))
+    p = cgs.lib().cgs_alloc_host(n * 8)
+    if not p:
+        raise MemoryError("cgs_alloc_host failed")
+    _HOST_BUFS.append(p)
+    a = np.ctypeslib.as_array((C.c_float * (2 * n)).from_address(p)).view(np.complex64).reshape(shape)
+    a[...] = 0
+    return torch.from_numpy(a)
+
+
 def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voronoi", max_bins=0, bin_subset=None):
     """The workload's context, data and weights.  bin_subset: the indices of
     the bins this process reconstructs (the multi-GPU bin partition), None
@@ -853,8 +871,8 @@ def run_ours(args):
     if world > 1:
         mine = importlib.import_module("4d_lung_gb300.dist").partition_bins(all_sizes, world)[rank]
     nb0 = len(all_sizes) if mine is None else len(mine)
-    h_data = torch.zeros((w0.n_ch, ns0), dtype=torch.complex64, pin_memory=True)
-    h_x = torch.zeros((max(nb0, 1),) + tuple(w0.img), dtype=torch.complex64, pin_memory=True)
+    h_data = host_buffer(cgs, torch, (w0.n_ch, ns0))
+    h_x = host_buffer(cgs, torch, (max(nb0, 1),) + tuple(w0.img))
     w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s = make_workload(
         cgs, synth, torch, args.workload, local, stream.cuda_stream, args.dcf, args.max_bins, mine)
     assert tuple(h_data.shape) == tuple(data.shape) and (h_x.shape[0] == len(sbins) or not sbins)
@@ -969,7 +987,8 @@ def run_ours(args):
     e2e_diag = {"host_ms_per_call": statistics.median(host_ms),
                 "device_ms_per_call": statistics.median([a.elapsed_time(b) for a, b in ev]),
                 "device_timed_ms_per_step": ms_step,
-                "parts_ms": {k: statistics.median([p[k] for p in parts]) for k in parts[0]},
+                "parts_ms": {k: statistics.median([p[k] for p in parts]) for k in ("upload", "solve", "download")},
+                "host_buffers_pinned": parts[-1]["pinned"],
                 "torch_upload_ms": statistics.median(raw)}
     te = torch.tensor([e2e_s], device=dev)
     if world > 1:
