@@ -1781,8 +1781,12 @@ static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh
     return CGS_OK;
 }
 
+// x_host / x_bytes: the host-buffer call's download of x, enqueued right
+// after the graph, ahead of the iteration record's read-back, so that one
+// synchronisation covers both.
 static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32_t max_iter, double* residuals,
-                   int32_t* iters, bool rhs_from_images, float* x_trace = nullptr)
+                   int32_t* iters, bool rhs_from_images, float* x_trace = nullptr, void* x_host = nullptr,
+                   size_t x_bytes = 0)
 {
     CGS_TRY(check_ready(c, true));
     if (!data || !x) return fail(c, CGS_ERR_ARG, "null pointer");
@@ -1848,6 +1852,8 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
     c->launches = c->graph_launches[key];
     CGS_CUDA(c, cudaGraphLaunch(exec, c->stream));
     if (c->e2e_mark) CGS_CUDA(c, cudaEventRecord(c->e2e_ev[2], c->stream));
+    if (x_host) CGS_CUDA(c, cudaMemcpyAsync(x_host, x, x_bytes, cudaMemcpyDeviceToHost, c->stream));
+    if (c->e2e_mark) CGS_CUDA(c, cudaEventRecord(c->e2e_ev[3], c->stream));
     if (residuals || iters) {
         std::vector<CgState> hs(nb);
         CGS_CUDA(c, cudaMemcpyAsync(hs.data(), c->d_state.p, nb * sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
@@ -1980,13 +1986,9 @@ int cgs_cg_solve_batched(cgs_ctx* c, const float* data, float* x, double thresh,
     CGS_CUDA(c, cudaEventRecord(c->e2e_ev[1], c->stream));
     std::vector<int32_t> it_local(c->nbins);
     c->e2e_mark = true;
-    int st = cgs_cg_solve_batched_d(c, c->d_data.as<float>(), c->d_x.as<float>(), thresh, max_iter, residuals,
-                                    iters ? iters : it_local.data());
+    const int st = solve_d(c, c->d_data.as<float>(), c->d_x.as<float>(), thresh, max_iter, residuals,
+                           iters ? iters : it_local.data(), false, nullptr, x, bx);
     c->e2e_mark = false;
-    if (st != CGS_OK && st != CGS_ERR_NONFINITE) return st;
-    CGS_CUDA(c, cudaMemcpyAsync(x, c->d_x.p, bx, cudaMemcpyDeviceToHost, c->stream));
-    CGS_CUDA(c, cudaEventRecord(c->e2e_ev[3], c->stream));
-    CGS_CUDA(c, cudaStreamSynchronize(c->stream));
     return st;
 }
 

@@ -72,8 +72,11 @@ struct SizeImpl {
                                          (int)ToepLayout<R1, R2, TBT, NSTAGE>::smem_bytes(L / 2));
         // the z extent of an image never exceeds the grid's: size for Iz = L
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_fwd_z_pipe<R1, R2, LPB, ZNST_F>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)ZF::smem_bytes(L, false));
+            e = cudaFuncSetAttribute(k_fwd_z_pipe<R1, R2, LPB, ZNST_F, false>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZF::smem_bytes(L, false));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_fwd_z_pipe<R1, R2, LPB, ZNST_F, true>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZF::smem_bytes(L, false));
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_adj_z_pipe<R1, R2, LPB, ZNST_A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)ZA::smem_bytes(L, true));
@@ -166,10 +169,12 @@ struct SizeImpl {
         // bulk copies need 16-byte aligned tiles: even Iz and coil strides
         if (a.err && a.smaps && a.x_cs == 0 && a.Iz <= L && (a.Iz & 1) == 0 && (a.coil_in & 1) == 0 &&
             al16(a.smaps)) {
-            k_fwd_z_pipe<R1, R2, LPB, ZNST_F><<<grid, NT_C, ZF::smem_bytes(a.Iz, false), s>>>(a);
+            if (a.cg) k_fwd_z_pipe<R1, R2, LPB, ZNST_F, true><<<grid, NT_C, ZF::smem_bytes(a.Iz, false), s>>>(a);
+            else k_fwd_z_pipe<R1, R2, LPB, ZNST_F, false><<<grid, NT_C, ZF::smem_bytes(a.Iz, false), s>>>(a);
             return cudaGetLastError();
         }
-        k_fwd_z<R1, R2, LPB><<<grid, NT_C, 0, s>>>(a);
+        if (a.cg) k_fwd_z<R1, R2, LPB, true><<<grid, NT_C, 0, s>>>(a);
+        else k_fwd_z<R1, R2, LPB, false><<<grid, NT_C, 0, s>>>(a);
         return cudaGetLastError();
     }
     static int adj_blocks(long long nl) { return (int)((nl + LPB - 1) / LPB); }

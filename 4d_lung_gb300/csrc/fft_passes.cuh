@@ -619,7 +619,7 @@ k_fft_contig(ContigPassArgs a)
 // and the x/y parities are applied here and in the later passes respectively.
 // ---------------------------------------------------------------------------
 
-template <int R1, int R2, int LPB>
+template <int R1, int R2, int LPB, bool CGF>
 __global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX)
 k_fwd_z(FwdZArgs a)
 {
@@ -647,7 +647,7 @@ k_fwd_z(FwdZArgs a)
     const int ln2 = tid / R1, k1 = tid % R1;
     const long long line2 = line0 + ln2;
     const bool act2 = ln2 < LPB && line2 < a.nl;
-    const FwdZCg cg = fwd_z_cg(a);
+    const FwdZCg cg = CGF ? fwd_z_cg(a) : FwdZCg{false, 0.f, 0.f, 0.f, 0.f};
 
     for (int c = 0; c < a.nch; ++c) {
         __syncthreads();   // s_tw ready / previous coil's stage 2 finished
@@ -655,7 +655,7 @@ k_fwd_z(FwdZArgs a)
             if (c == 0 || a.x_cs != 0) {
                 // a.cg is only set with x_cs == 0: each element is read once
                 const long long eb = (long long)blockIdx.y * a.x_bs + (long long)c * a.x_cs + line1 * a.Iz;
-                if (cg.upd) {
+                if (CGF && cg.upd) {
 #pragma unroll
                     for (int n1 = 0; n1 < R1; ++n1) xa[n1] = make_float2(0.f, 0.f);
                     fwd_z_fused_line<R1, R2>(a, cg, eb, n2, axy, [&](int n1, int, float2 v) { xa[n1] = v; });
@@ -862,7 +862,9 @@ struct ZPipeLayout {
     }
 };
 
-template <int R1, int R2, int LPB, int NST>
+// CGF: the fused CG form (a.cg set); a separate instantiation, so that the
+// plain pass compiles without the update path.
+template <int R1, int R2, int LPB, int NST, bool CGF>
 __global__ void __launch_bounds__(LPB * ContigLayout<R1, R2>::RMAX, (R1 > 16 || R2 > 16) ? 2 : 3)
 k_fwd_z_pipe(FwdZArgs a)
 {
@@ -904,9 +906,9 @@ k_fwd_z_pipe(FwdZArgs a)
     if (act1) {
         const int ix = (int)(line1 / a.Iy), iy = (int)(line1 - (long long)ix * a.Iy);
         const float axy = a.apx[ix] * a.apy[iy];
-        const FwdZCg cg = fwd_z_cg(a);
+        const FwdZCg cg = CGF ? fwd_z_cg(a) : FwdZCg{false, 0.f, 0.f, 0.f, 0.f};
         const long long eb = (long long)blockIdx.y * a.x_bs + line1 * a.Iz;
-        if (cg.upd) {
+        if (CGF && cg.upd) {
             fwd_z_fused_line<R1, R2>(a, cg, eb, n2, axy, [&](int, int zi, float2 v) { xa[zi] = v; });
         } else {
             const float2* xl = a.x + eb;

@@ -70,8 +70,10 @@ FAMILY = {"fwd_z": "k_fwd_z_pipe+k_adj_z_pipe", "adj_z": "k_fwd_z_pipe+k_adj_z_p
 
 
 def traffic_record():
-    """DRAM bytes (read + write) of each kernel family per application, from
-    an ncu capture (profiles/traffic.json, written by hand from the capture)."""
+    """DRAM bytes (read + write) against algorithmic bytes of each kernel
+    family in one application of the first two cfg3 bins, from an ncu capture
+    small enough for a shared GPU (profiles/traffic.json); a run's traffic is
+    its own algorithmic bytes times that ratio."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
@@ -894,6 +896,21 @@ def run_ours(args):
         tune = reco.autotune()
     autotune_s = time.perf_counter() - t0
 
+    if args.applies_only:
+        # profiling mode: the operator alone, args.applies_only applications of
+        # all bins (8 launches each: fwd z / y / x, interp, spread, adj x / y / z
+        # when one workspace group holds the bins), then the algorithmic bytes
+        xa = torch.from_numpy(np.stack([synth.phantom(w.img)] * nb)).to(dev)
+        qa = torch.empty_like(xa)
+        for _ in range(args.applies_only):
+            reco.apply_ehde_tensor(xa, qa, 0, nb)
+        torch.cuda.synchronize(dev)
+        support = reco.support_stats()
+        taps, points = reco.spread_matrix_stats()
+        print(json.dumps({"applies": args.applies_only, "bins": nb, "algorithmic_bytes": stage_bytes(
+            w, sizes, support, (taps, points) if taps > 0 else None, reco.forward_y_listed_rows())}))
+        return 0
+
     t0 = time.perf_counter()
     for i in range(args.warmup):
         res, its = reco.cg_sense_batched_tensor(data, x, 0.0, iters, want_stats=True)
@@ -1075,14 +1092,18 @@ def run_ours(args):
     dom_bytes = sum(sb[s] for s in fam[dom])
     peak, peak_kind = measured_peaks()
     achieved = dom_bytes / (fam_ms[dom] / 1e3) / 1e9
-    tkey = args.workload + ("_%dbin" % args.max_bins if args.max_bins > 0 else "")
-    tr = traffic_record().get(tkey, {}).get(dom)
+    rec = traffic_record()
+    tr = rec.get("families", {}).get(dom) if args.workload == "cfg3" else None
     roofline = {
         "bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
         "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"
         if peak_kind == "measured" else "fallback 6800 GB/s",
-        "traffic": None if tr is None else tr["dram_bytes_per_apply"],
-        "traffic_source": None if tr is None else tr["source"],
+        "traffic": None if tr is None else tr["ratio"] * dom_bytes,
+        "traffic_source": None if tr is None else (
+            "DRAM read + write bytes / algorithmic bytes = %.3f for this kernel family in one application of the "
+            "first two cfg3 bins (ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/traffic.json, "
+            "profiles/traffic_cfg3_2bin.md), times this run's algorithmic bytes" % tr["ratio"]),
+        "traffic_ratio_by_family": {k: v["ratio"] for k, v in rec.get("families", {}).items()},
         "launches_per_apply": len(fam[dom]),
         "algorithmic_bytes_per_apply": dom_bytes,
         "kernel_ms": fam_ms,
@@ -1174,6 +1195,8 @@ def main():
     ap.add_argument("--cg-grad-only", action="store_true",
                     help="only the unrolled-CG trajectory gradient of the combined workload (cfg5)")
     ap.add_argument("--workspace-gb", type=float, default=56.0, help="grid workspace budget (--cg-grad-only)")
+    ap.add_argument("--applies-only", type=int, default=0,
+                    help="profiling mode: only this many operator applications of all bins, then exit")
     ap.add_argument("--max-bins", type=int, default=0,
                     help="keep only the first N respiratory bins (small cases for profiling)")
     ap.add_argument("--precision-only", action="store_true",

@@ -382,8 +382,7 @@ int cgs_setup_stats(cgs_ctx* ctx, double* ms, int32_t n);
 
 /* Device time of the parts of the last cgs_cg_solve_batched call (CUDA
  * events on the context's stream, ms): ms[0] the upload of the samples,
- * ms[1] the solve's graph, ms[2] the read-back of the iteration record and
- * the download of the images, including the host's wait in between.
+ * ms[1] the solve's graph, ms[2] the download of the images.
  * pinned (optional, 2 entries): 1 where the call's data / image buffer was
  * page-locked memory as the library's CUDA runtime sees it (cgs_alloc_host
  * gives such memory); copies from other memory are staged and slower.  A
