@@ -186,6 +186,26 @@ def scan_bins(synth, name, max_bins=0):
     return sbins[:max_bins] if max_bins > 0 else sbins
 
 
+def torch_copy_ms(torch, dev, stream, data, x, h_data, h_x):
+    """Device times (ms) of PyTorch's upload of h_data and download into h_x
+    (the end-to-end call's buffers), medians of three."""
+    out = {}
+    d_tmp = torch.empty_like(data)
+    for name, f in (("upload", lambda: d_tmp.copy_(h_data, non_blocking=True)),
+                    ("download", lambda: h_x.copy_(x, non_blocking=True))):
+        t = []
+        for _ in range(3):
+            r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            r0.record(stream)
+            f()
+            r1.record(stream)
+            torch.cuda.synchronize(dev)
+            t.append(r0.elapsed_time(r1))
+        out[name] = round(statistics.median(t), 3)
+    del d_tmp
+    return out
+
+
 _HOST_BUFS = []
 
 
@@ -972,6 +992,7 @@ def run_ours(args):
 
     for _ in range(max(1, args.warmup)):
         host_call()
+    raw_before = torch_copy_ms(torch, dev, stream, data, x, h_data, h_x)
     if world > 1:
         dist.barrier()
     # per call: host wall time, and the device time between events recorded on
@@ -989,24 +1010,16 @@ def run_ours(args):
         host_ms.append(1e3 * (time.perf_counter() - t1))
         parts.append(reco.e2e_stats())
     e2e_s = time.perf_counter() - t0
-    # the same upload by PyTorch from the same pinned buffer, for comparison
-    d_tmp = torch.empty_like(data)
-    raw = []
-    for _ in range(3):
-        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        r0.record(stream)
-        d_tmp.copy_(h_data, non_blocking=True)
-        r1.record(stream)
-        torch.cuda.synchronize(dev)
-        raw.append(r0.elapsed_time(r1))
-    del d_tmp
+    # the same copies by PyTorch from / to the same page-locked buffers
+    raw = torch_copy_ms(torch, dev, stream, data, x, h_data, h_x)
     torch.cuda.synchronize(dev)
     e2e_diag = {"host_ms_per_call": statistics.median(host_ms),
                 "device_ms_per_call": statistics.median([a.elapsed_time(b) for a, b in ev]),
                 "device_timed_ms_per_step": ms_step,
                 "parts_ms": {k: statistics.median([p[k] for p in parts]) for k in ("upload", "solve", "download")},
+                "parts_ms_per_call": [[round(p[k], 3) for k in ("upload", "solve", "download")] for p in parts],
                 "host_buffers_pinned": parts[-1]["pinned"],
-                "torch_upload_ms": statistics.median(raw)}
+                "torch_copies_ms_before": raw_before, "torch_copies_ms_after": raw}
     te = torch.tensor([e2e_s], device=dev)
     if world > 1:
         dist.all_reduce(te, op=dist.ReduceOp.MAX)
