@@ -188,6 +188,8 @@ struct cgs_ctx {
     // upload, after it, after the graph launch and after the download
     cudaEvent_t e2e_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool e2e_mark = false;       // solve_d records e2e_ev[2] after its graph launch
+    void* h_stage = nullptr;     // page-locked staging of the solve's iteration record
+    size_t h_stage_bytes = 0;
     int e2e_pinned[2] = {0, 0};  // host buffers of the last call page-locked (as this runtime sees them)
     std::string err;
 };
@@ -1451,6 +1453,7 @@ void cgs_destroy(cgs_ctx* c)
     if (c->blas) toeplitz_release(c->blas);
     for (cudaEvent_t& e : c->e2e_ev)
         if (e) cudaEventDestroy(e);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
 }
@@ -1855,12 +1858,21 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
     if (x_host) CGS_CUDA(c, cudaMemcpyAsync(x_host, x, x_bytes, cudaMemcpyDeviceToHost, c->stream));
     if (c->e2e_mark) CGS_CUDA(c, cudaEventRecord(c->e2e_ev[3], c->stream));
     if (residuals || iters) {
-        std::vector<CgState> hs(nb);
-        CGS_CUDA(c, cudaMemcpyAsync(hs.data(), c->d_state.p, nb * sizeof(CgState), cudaMemcpyDeviceToHost, c->stream));
-        std::vector<double> hr((size_t)nb * std::max(max_iter, 1));
-        if (residuals)
-            CGS_CUDA(c, cudaMemcpyAsync(hr.data(), c->d_res.p, hr.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                                        c->stream));
+        // the iteration record goes through a page-locked staging buffer of
+        // the context (a copy into pageable memory would be staged by the
+        // driver behind the call's other copies)
+        const size_t sb = nb * sizeof(CgState), rb = (size_t)nb * std::max(max_iter, 1) * sizeof(double);
+        if (c->h_stage_bytes < sb + rb) {
+            if (c->h_stage) cudaFreeHost(c->h_stage);
+            c->h_stage = nullptr;
+            c->h_stage_bytes = 0;
+            CGS_CUDA(c, cudaMallocHost(&c->h_stage, sb + rb));
+            c->h_stage_bytes = sb + rb;
+        }
+        CgState* hs = reinterpret_cast<CgState*>(c->h_stage);
+        double* hr = reinterpret_cast<double*>(static_cast<char*>(c->h_stage) + sb);
+        CGS_CUDA(c, cudaMemcpyAsync(hs, c->d_state.p, sb, cudaMemcpyDeviceToHost, c->stream));
+        if (residuals) CGS_CUDA(c, cudaMemcpyAsync(hr, c->d_res.p, rb, cudaMemcpyDeviceToHost, c->stream));
         CGS_CUDA(c, cudaStreamSynchronize(c->stream));
         for (int b = 0; b < nb; ++b) {
             if (iters) iters[b] = hs[b].iter;

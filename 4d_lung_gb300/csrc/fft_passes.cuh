@@ -65,25 +65,42 @@ CGS_D FwdZCg fwd_z_cg(const FwdZArgs& a)
 
 // Fused form of a thread's image reads: for each of its line positions the
 // pending updates are applied and stored, and p * apod * parity is handed to
-// `put`.  Pointers are restrict-qualified copies, so that the loads of
-// later positions can be issued before the stores of earlier ones.
+// `put`.  The loads of a group of positions are issued together before any
+// of the group's stores (restrict-qualified pointers), so that the loads'
+// latency is paid once per group.
 // eb: element index of the line start within the batch.
+constexpr int fwd_z_group(int r1) { return r1 % 8 == 0 ? 8 : (r1 % 4 == 0 ? 4 : (r1 % 2 == 0 ? 2 : 1)); }
+
 template <int R1, int R2, class Put>
 CGS_D void fwd_z_fused_line(const FwdZArgs& a, const FwdZCg& u, long long eb, int n2, float axy, Put put)
 {
+    constexpr int GRP = fwd_z_group(R1);
     float2* __restrict__ P = a.cg_p + eb;
     const float2* __restrict__ Rr = a.cg_r + eb;
     float2* __restrict__ X = a.cg_x + eb;
 #pragma unroll
-    for (int n1 = 0; n1 < R1; ++n1) {
-        const int l = R2 * n1 + n2;
-        const int zi = l - a.lo_z;
-        if (zi >= 0 && zi < a.Iz) {
-            const float2 p0 = P[zi];
-            X[zi] = cg_axpy(X[zi], u.ar, u.ai, p0);
-            const float2 p1 = cg_axpy(Rr[zi], u.br, u.bi, p0);
-            P[zi] = p1;
-            put(n1, zi, parity(cscale(p1, axy * a.apz[zi]), l));
+    for (int g0 = 0; g0 < R1; g0 += GRP) {
+        float2 pv[GRP], rv[GRP], xv[GRP];
+#pragma unroll
+        for (int j = 0; j < GRP; ++j) {
+            const int zi = R2 * (g0 + j) + n2 - a.lo_z;
+            if (zi >= 0 && zi < a.Iz) {
+                pv[j] = P[zi];
+                rv[j] = Rr[zi];
+                xv[j] = X[zi];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < GRP; ++j) {
+            const int n1 = g0 + j;
+            const int l = R2 * n1 + n2;
+            const int zi = l - a.lo_z;
+            if (zi >= 0 && zi < a.Iz) {
+                X[zi] = cg_axpy(xv[j], u.ar, u.ai, pv[j]);
+                const float2 p1 = cg_axpy(rv[j], u.br, u.bi, pv[j]);
+                P[zi] = p1;
+                put(n1, zi, parity(cscale(p1, axy * a.apz[zi]), l));
+            }
         }
     }
 }
