@@ -256,10 +256,14 @@ cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan
 // CG
 // ---------------------------------------------------------------------------
 
+// Blocks per bin of the CG vector kernels: at most one per SM and bin, so
+// that the fused residual update's per-block sum of the <p, q> partials
+// (the same fixed order in every block) is repeated few times; with 16 bins
+// that is still 16 blocks per SM.
 int cg_blocks(long long n)
 {
     long long b = (n + RED_THREADS - 1) / RED_THREADS;
-    if (b > 4 * 152) b = 4 * 152;
+    if (b > 152) b = 152;
     if (b < 1) b = 1;
     return (int)b;
 }
