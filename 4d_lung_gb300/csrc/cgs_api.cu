@@ -1725,7 +1725,7 @@ static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh
     const int nb = c->nbins;
     const long long Ni = c->Ni;
     const int nblk_adj = adj_z_blocks(c->G[2], c->Nl);
-    const int nblk_cg = cg_blocks(Ni);
+    const int nblk_cg = cg_blocks(Ni, nb);
     if (rhs_from_images) {
         // b = sum_c conj(S_c) img_c from given coil images (Reco.cpp:182-190)
         CGS_LAUNCH(c, launch_coil_combine(data, c->d_smaps.as<float2>(), c->nch, Ni, c->d_b.as<float2>(), c->stream));
@@ -1799,7 +1799,7 @@ static int solve_d(cgs_ctx* c, const float* data, float* x, double thresh, int32
     const long long Ni = c->Ni;
     const size_t vb = (size_t)nb * Ni * sizeof(float2);
     const int nblk_adj = adj_z_blocks(c->G[2], c->Nl);
-    const int nblk_cg = cg_blocks(Ni);
+    const int nblk_cg = cg_blocks(Ni, nb);
     CGS_CUDA(c, c->d_b.ensure(vb));
     CGS_CUDA(c, c->d_r.ensure(vb));
     CGS_CUDA(c, c->d_pv.ensure(vb));
@@ -2013,8 +2013,8 @@ int cgs_cg_solve_plain_d(cgs_ctx* c, const float* data, float* x, double thresh,
     if (max_iter < 0 || max_iter > 10000) return fail(c, CGS_ERR_ARG, "max_iter out of range");
     const int nb = c->nbins;
     const long long Ni = c->Ni;
-    const int nblk_cg = cg_blocks(Ni);
-    const int nblk_dot = cg_blocks(Ni);
+    const int nblk_cg = cg_blocks(Ni, 1);
+    const int nblk_dot = cg_blocks(Ni, 1);
     if (!c->plain_plan_ok) {
         if (cufftPlan3d(&c->plain_plan, c->G[0], c->G[1], c->G[2], CUFFT_C2C) != CUFFT_SUCCESS)
             return fail(c, CGS_ERR_CUDA, "cufftPlan3d failed");

@@ -256,14 +256,16 @@ cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan
 // CG
 // ---------------------------------------------------------------------------
 
-// Blocks per bin of the CG vector kernels: at most one per SM and bin, so
-// that the fused residual update's per-block sum of the <p, q> partials
-// (the same fixed order in every block) is repeated few times; with 16 bins
-// that is still 16 blocks per SM.
-int cg_blocks(long long n)
+// Blocks per bin of the CG vector kernels: about 16 per SM over all bins
+// (152 x 16 in total, at least 152 per bin), so that the fused residual
+// update's per-block sum of the <p, q> partials (the same fixed order in
+// every block) is repeated few times while a single-bin solve still fills
+// the GPU.
+int cg_blocks(long long n, int nbins)
 {
+    const long long cap = std::max<long long>(152, (152LL * 16) / std::max(nbins, 1));
     long long b = (n + RED_THREADS - 1) / RED_THREADS;
-    if (b > 152) b = 152;
+    if (b > cap) b = cap;
     if (b < 1) b = 1;
     return (int)b;
 }
@@ -271,7 +273,7 @@ int cg_blocks(long long n)
 cudaError_t launch_cg_init(const float2* b, float2* r, float2* p, float2* x, long long n, long long bs,
                            double* partials, const CgState* st, int nbins, cudaStream_t s)
 {
-    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    dim3 grid((unsigned)cg_blocks(n, nbins), (unsigned)nbins);
     k_cg_init<<<grid, RED_THREADS, 0, s>>>(b, r, p, x, n, bs, partials, st);
     return cudaGetLastError();
 }
@@ -293,7 +295,7 @@ cudaError_t launch_cg_alpha(CgState* st, const double* partials, int nblk, int n
 cudaError_t launch_cg_update_xr(float2* x, float2* r, const float2* p, const float2* q, long long n, long long bs,
                                 const CgState* st, double* partials, int nbins, cudaStream_t s)
 {
-    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    dim3 grid((unsigned)cg_blocks(n, nbins), (unsigned)nbins);
     k_cg_update_xr<<<grid, RED_THREADS, 0, s>>>(x, r, p, q, n, bs, st, partials);
     return cudaGetLastError();
 }
@@ -308,7 +310,7 @@ cudaError_t launch_cg_beta(CgState* st, const double* partials, int nblk, int nb
 cudaError_t launch_cg_update_p(float2* p, const float2* r, long long n, long long bs, const CgState* st, int nbins,
                                cudaStream_t s)
 {
-    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    dim3 grid((unsigned)cg_blocks(n, nbins), (unsigned)nbins);
     k_cg_update_p<<<grid, RED_THREADS, 0, s>>>(p, r, n, bs, st);
     return cudaGetLastError();
 }
@@ -322,7 +324,7 @@ cudaError_t launch_cg_loop_test(CgState* st, int nbins, cudaStream_t s)
 cudaError_t launch_cg_update_r(float2* r, const float2* q, long long n, long long bs, CgState* st,
                                const double* pq_partials, int nblk_pq, double* partials, int nbins, cudaStream_t s)
 {
-    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    dim3 grid((unsigned)cg_blocks(n, nbins), (unsigned)nbins);
     k_cg_update_r<<<grid, RED_THREADS, 0, s>>>(r, q, n, bs, st, pq_partials, nblk_pq, partials);
     return cudaGetLastError();
 }
@@ -337,7 +339,7 @@ cudaError_t launch_cg_beta_test(CgState* st, const double* partials, int nblk, i
 cudaError_t launch_cg_finish_x(float2* x, const float2* p, long long n, long long bs, const CgState* st, int nbins,
                                cudaStream_t s)
 {
-    dim3 grid((unsigned)cg_blocks(n), (unsigned)nbins);
+    dim3 grid((unsigned)cg_blocks(n, nbins), (unsigned)nbins);
     k_cg_finish_x<<<grid, RED_THREADS, 0, s>>>(x, p, n, bs, st);
     return cudaGetLastError();
 }

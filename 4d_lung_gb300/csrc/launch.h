@@ -63,7 +63,7 @@ cudaError_t launch_coil_combine(const float2* imgs, const float2* smaps, int nch
                                 cudaStream_t s);
 
 // CG
-int cg_blocks(long long n);
+int cg_blocks(long long n, int nbins);
 cudaError_t launch_cg_init(const float2* b, float2* r, float2* p, float2* x, long long n, long long bs,
                            double* partials, const CgState* st, int nbins, cudaStream_t s);
 cudaError_t launch_cg_arm(CgState* st, const double* partials, int nblk, int nbins, double thresh, int max_iter,
