@@ -22,10 +22,6 @@ CGS_HD float2 cmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b
 CGS_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 CGS_HD float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
 
-// Request the 128-byte line holding p into L2 (no register is held and
-// nothing waits for it).
-CGS_D void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
-
 // CG vector updates (addToArrayScaled / addArraysScaled, Reco.cpp:153-173)
 // with the step size (ar, ai) rounded to float.  Every product and sum is
 // rounded on its own (no fused multiply-add), so that the separate update

@@ -129,18 +129,6 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
         const int odd = (int)(base & 1);   // Gz even: every row of the sample has this parity
         const float4* b4 = reinterpret_cast<const float4*>(grid + (base - odd));
         const long long gz4 = Gz / 2, gyz4 = (long long)Gy * Gz / 2;
-        // the 16 rows of every coil of the chunk are requested into L2 first
-        // (no registers held), so that the row loads below, issued a few at a
-        // time, mostly wait for L2 rather than DRAM
-#pragma unroll 1
-        for (int r = 0; r < 16 * CC; ++r) {
-            const int ix = r / (4 * CC), iy = (r / CC) % 4, c = r % CC;
-            if (c < ncc) {   // a row's 48 bytes may straddle two 128-byte lines
-                const float4* p = b4 + ix * gyz4 + iy * gz4 + (long long)c * (a.coil_stride / 2);
-                prefetch_l2(p);
-                prefetch_l2(p + 2);
-            }
-        }
 #pragma unroll
         for (int ix = 0; ix < 4; ++ix)
 #pragma unroll

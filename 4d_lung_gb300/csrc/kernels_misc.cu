@@ -256,14 +256,13 @@ cudaError_t launch_spread(const SpreadArgs& a, int ntiles, int nbins, bool kahan
 // CG
 // ---------------------------------------------------------------------------
 
-// Blocks per bin of the CG vector kernels: about 16 per SM over all bins
-// (152 x 16 in total, at least 152 per bin), so that the fused residual
-// update's per-block sum of the <p, q> partials (the same fixed order in
-// every block) is repeated few times while a single-bin solve still fills
-// the GPU.
+// Blocks per bin of the CG vector kernels: 152 x 16 / nbins, between 152
+// and 608 per bin, so that the fused residual update's per-block sum of the
+// <p, q> partials (the same fixed order in every block) is repeated few
+// times while a single-bin solve still fills the GPU.
 int cg_blocks(long long n, int nbins)
 {
-    const long long cap = std::max<long long>(152, (152LL * 16) / std::max(nbins, 1));
+    const long long cap = std::min<long long>(4 * 152, std::max<long long>(152, (152LL * 16) / std::max(nbins, 1)));
     long long b = (n + RED_THREADS - 1) / RED_THREADS;
     if (b > cap) b = cap;
     if (b < 1) b = 1;
