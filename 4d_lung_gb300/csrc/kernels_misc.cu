@@ -96,6 +96,7 @@ cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nb
     if (nblk > 0x7fffffffLL) return cudaErrorInvalidValue;
     dim3 grid((unsigned)nblk, 1u, (unsigned)nbins);
     switch (cc) {
+    case 1: k_interp<1><<<grid, 128, 0, s>>>(a); break;
     case 2: k_interp<2><<<grid, 128, 0, s>>>(a); break;
     case 4: k_interp<4><<<grid, 128, 0, s>>>(a); break;
     case 6: k_interp<6><<<grid, 128, 0, s>>>(a); break;
