@@ -308,7 +308,28 @@ k_cg_update_r(float2* r, const float2* __restrict__ q, long long n, long long bs
     double acc = 0.0, dummy = 0.0;
     float fa = 0.f;
     int cnt = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    // CG_FCHUNK consecutive elements of the thread at a time: their loads in
+    // flight together; the same elements, order and partial sums as the
+    // one-at-a-time loop below (and k_cg_update_xr)
+    for (; i + (CG_FCHUNK - 1) * stride < n; i += CG_FCHUNK * stride) {
+        float2 rv[CG_FCHUNK], qv[CG_FCHUNK];
+#pragma unroll
+        for (int j = 0; j < CG_FCHUNK; ++j) {
+            rv[j] = r[off + i + j * stride];
+            qv[j] = q[off + i + j * stride];
+        }
+#pragma unroll
+        for (int j = 0; j < CG_FCHUNK; ++j) {
+            rv[j] = cg_axmy(rv[j], ar, ai, qv[j]);
+            r[off + i + j * stride] = rv[j];
+            fa = __fadd_rn(fa, cg_abs2(rv[j]));
+        }
+        acc += (double)fa;
+        fa = 0.f;
+    }
+    for (; i < n; i += stride) {
         float2 rv = r[off + i];
         rv = cg_axmy(rv, ar, ai, q[off + i]);
         r[off + i] = rv;
