@@ -107,18 +107,16 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
     // the loads of several rows can be in flight at once.  The rows, the
     // products wx * wy, the z taps and their order are those of the general
     // loop below, so the sums are bitwise the same.
-    int x0 = 5, nxt = 0, y0 = 5, nyt = 0, z0 = 5, nzt = 0;
+    int x0 = 5, nxt = 0, y0 = 5, nyt = 0;
 #pragma unroll
     for (int q = 4; q >= 0; --q) {
         if (w[q] != 0.f) x0 = q;
         if (w[5 + q] != 0.f) y0 = q;
-        if (w[10 + q] != 0.f) z0 = q;
     }
 #pragma unroll
     for (int q = 0; q < 5; ++q) {
         nxt += w[q] != 0.f ? 1 : 0;
         nyt += w[5 + q] != 0.f ? 1 : 0;
-        nzt += w[10 + q] != 0.f ? 1 : 0;
     }
     if (vec && nxt == 4 && nyt == 4 && x0 <= 1 && y0 <= 1) {
         float wxs[4], wys[4];
@@ -131,41 +129,6 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
         const int odd = (int)(base & 1);   // Gz even: every row of the sample has this parity
         const float4* b4 = reinterpret_cast<const float4*>(grid + (base - odd));
         const long long gz4 = Gz / 2, gyz4 = (long long)Gy * Gz / 2;
-        // Four z taps starting on an even index (about half the interior
-        // samples): two 16-byte loads per row instead of three; the taps,
-        // their tests and their order are those of the loop below.
-        if (nzt == 4 && z0 <= 1 && ((base + z0) & 1) == 0) {
-            const float4* a4 = reinterpret_cast<const float4*>(grid + (base + z0));
-            auto rows = [&](auto zoff) {
-                constexpr int Z0 = decltype(zoff)::value;
-#pragma unroll
-                for (int ix = 0; ix < 4; ++ix)
-#pragma unroll
-                    for (int iy = 0; iy < 4; ++iy) {
-                        const float wxy = wxs[ix] * wys[iy];
-                        const float4* r4 = a4 + ix * gyz4 + iy * gz4;
-#pragma unroll
-                        for (int c = 0; c < CC; ++c)
-                            if (c < ncc) {
-                                const float4* p = r4 + (long long)c * (a.coil_stride / 2);
-                                const float4 q0 = __ldg(p), q1 = __ldg(p + 1);
-                                const float2 e[4] = {make_float2(q0.x, q0.y), make_float2(q0.z, q0.w),
-                                                     make_float2(q1.x, q1.y), make_float2(q1.z, q1.w)};
-#pragma unroll
-                                for (int jz = Z0; jz < Z0 + 4; ++jz) {
-                                    const float wz = w[10 + jz];
-                                    const float wt = wxy * wz;
-                                    if (wz != 0.f && wt > a.thresh) {
-                                        acc[c].x = fmaf(e[jz - Z0].x, wt, acc[c].x);
-                                        acc[c].y = fmaf(e[jz - Z0].y, wt, acc[c].y);
-                                    }
-                                }
-                            }
-                    }
-            };
-            if (z0 == 0) rows(std::integral_constant<int, 0>{});
-            else rows(std::integral_constant<int, 1>{});
-        } else {
 #pragma unroll
         for (int ix = 0; ix < 4; ++ix)
 #pragma unroll
@@ -191,7 +154,6 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
                         }
                     }
             }
-        }
     } else {
 #pragma unroll
     for (int jx = 0; jx < 5; ++jx) {
