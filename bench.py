@@ -578,7 +578,9 @@ def toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, steps, w, s
             # that it cannot pass for a solve that converged
             "final_residual_rel": [float(r[-1] / r[0]) if r[0] > 0 else None for r in res],
             "rel_l2_vs_gridded_solve": rel,
-            "apply_ms": apply_ms, "stage_ms": stage_ms,
+            "apply_ms": apply_ms,
+        "rhs_ms": rhs_ms,
+        "cg_update_ms_per_iter": (ms_step - iters * apply_ms - rhs_ms) / max(iters, 1), "stage_ms": stage_ms,
             "stage_frac_of_peak": {s: tb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
             "apply_achieved_gbs": (sum(tb.values()) + 56 * int(np.prod(w.img)) * nb) / (apply_ms / 1e3) / 1e9,
         }
@@ -1101,6 +1103,22 @@ def run_ours(args):
     st = np.median(np.stack(reps), axis=0)
     groups = len(st) // 8
     stage_ms = {s: float(sum(st[g * 8 + i] for g in range(groups))) for i, s in enumerate(STAGES)}
+    # the right-hand side alone (sample gather + adjoint chain of all bins),
+    # to split the step into applications, right-hand side and CG updates
+    import ctypes as C
+    b_rhs = torch.empty_like(xa)
+    rhs_t = []
+    for _ in range(4):
+        r0, r1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r0.record(stream)
+        st_rhs = cgs.lib().cgs_rhs_d(reco.ctx, 0, nb, C.c_void_p(data.data_ptr()), C.c_void_p(b_rhs.data_ptr()))
+        r1.record(stream)
+        torch.cuda.synchronize(dev)
+        if st_rhs != 0:
+            raise RuntimeError(cgs.lib().cgs_last_error(reco.ctx).decode())
+        rhs_t.append(r0.elapsed_time(r1))
+    rhs_ms = float(np.median(rhs_t[1:]))
+    del b_rhs
     support = reco.support_stats()
     taps, points = reco.spread_matrix_stats()
     variant = tune.get("spread_variant") if tune else 6   # the library's default is the gather
