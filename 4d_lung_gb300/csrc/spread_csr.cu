@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
 // ---------------------------------------------------------------------------
 constexpr int CSR_SX = 32;            // x rows per unit
 constexpr int CSR_CAP = 2048;         // staged taps per unit
-constexpr int CSR_NST = 3;            // pipeline stages
+constexpr int CSR_NST = 2;            // pipeline stages
 constexpr unsigned long long CSR_WAIT_NS = 2000000000ull;
 
 __host__ __device__ inline int csr_ptr_stride(int tb) { return ((CSR_SX * tb + 1) + 3) & ~3; }

@@ -578,9 +578,7 @@ def toeplitz_report(reco, synth, data, x, iters, torch, dev, stream, steps, w, s
             # that it cannot pass for a solve that converged
             "final_residual_rel": [float(r[-1] / r[0]) if r[0] > 0 else None for r in res],
             "rel_l2_vs_gridded_solve": rel,
-            "apply_ms": apply_ms,
-        "rhs_ms": rhs_ms,
-        "cg_update_ms_per_iter": (ms_step - iters * apply_ms - rhs_ms) / max(iters, 1), "stage_ms": stage_ms,
+            "apply_ms": apply_ms, "stage_ms": stage_ms,
             "stage_frac_of_peak": {s: tb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
             "apply_achieved_gbs": (sum(tb.values()) + 56 * int(np.prod(w.img)) * nb) / (apply_ms / 1e3) / 1e9,
         }
@@ -1153,6 +1151,8 @@ def run_ours(args):
         "stage_ms": stage_ms,
         "stage_frac_of_peak": {s: sb[s] / (stage_ms[s] / 1e3) / 1e9 / peak for s in stage_ms},
         "apply_ms": apply_ms,
+        "rhs_ms": rhs_ms,
+        "cg_update_ms_per_iter": (ms_step - iters * apply_ms - rhs_ms) / max(iters, 1),
         "apply_achieved_gbs": apply_bytes(w, sizes, support, matrix, y_listed) / (apply_ms / 1e3) / 1e9,
         "apply_bytes": apply_bytes(w, sizes, support, matrix, y_listed),
         "support": {"listed_column_fraction": float(sum(support[0])) / (nb * w.grid[1] * w.grid[2]),
