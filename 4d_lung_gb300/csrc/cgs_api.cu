@@ -2360,7 +2360,7 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
     c->spread_cc = best_sc;
     best = 1e30f;
     int best_ic = c->interp_cc;
-    for (int v : {1, 2, 4, 6, 8, -1, -2}) {
+    for (int v : {1, 2, 4, 6, 8}) {
         c->interp_cc = v;
         float ms;
         CGS_TRY(time_apply(ms));
@@ -2765,9 +2765,8 @@ int cgs_set_launch_shape(cgs_ctx* c, int32_t spread_cc, int32_t spread_variant, 
     if (spread_variant < 1 || spread_variant > 7 || (spread_variant >= 3 && spread_variant <= 5 && c->kahan) ||
         (spread_variant == 3 && c->deterministic))
         return fail(c, CGS_ERR_ARG, "spreading variant not allowed here");
-    if (interp_cc != 1 && interp_cc != 2 && interp_cc != 4 && interp_cc != 6 && interp_cc != 8 && interp_cc != -1 &&
-        interp_cc != -2)
-        return fail(c, CGS_ERR_ARG, "interp_cc must be 1, 2, 4, 6, 8, -1 or -2");
+    if (interp_cc != 1 && interp_cc != 2 && interp_cc != 4 && interp_cc != 6 && interp_cc != 8)
+        return fail(c, CGS_ERR_ARG, "interp_cc must be 1, 2, 4, 6 or 8");
     c->spread_cc = spread_cc;
     c->spread_wpp = spread_variant;
     c->interp_cc = interp_cc;

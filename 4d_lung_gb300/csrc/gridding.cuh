@@ -18,7 +18,6 @@
 #include "cgs_common.cuh"
 #include "cgs_types.h"
 #include "gridding_common.cuh"
-#include "ptx_async.cuh"
 
 namespace cgs {
 
@@ -75,13 +74,7 @@ __global__ void k_tap_records(const double* __restrict__ k, const int* __restric
 // sample values are written coil-interleaved, yv[i][c].
 // ---------------------------------------------------------------------------
 
-// STAGED: the 48 bytes of each of an interior sample's 16 rows per coil are
-// first copied into the thread's own slots of shared memory by cp.async
-// (all 16 x 3 x CC copies in flight at once, no register held for them),
-// then read from there: the same values, taps and order, so the sums are
-// bitwise those of the register form.  Shared memory: [CC][16][3][128]
-// float4 per block (CC x 96 KiB).
-template <int CC, bool STAGED = false>
+template <int CC>
 __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
 {
     const int bin = a.bin0 + blockIdx.z;
@@ -136,21 +129,6 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
         const int odd = (int)(base & 1);   // Gz even: every row of the sample has this parity
         const float4* b4 = reinterpret_cast<const float4*>(grid + (base - odd));
         const long long gz4 = Gz / 2, gyz4 = (long long)Gy * Gz / 2;
-        extern __shared__ float4 s_rows[];   // STAGED only: [CC][16 rows][3][128 threads]
-        if constexpr (STAGED) {
-#pragma unroll
-            for (int c = 0; c < CC; ++c)
-                if (c < ncc)
-#pragma unroll
-                    for (int r = 0; r < 16; ++r) {
-                        const float4* p = b4 + (r / 4) * gyz4 + (r % 4) * gz4 + (long long)c * (a.coil_stride / 2);
-#pragma unroll
-                        for (int j = 0; j < 3; ++j)
-                            cp_async16(&s_rows[((c * 16 + r) * 3 + j) * 128 + threadIdx.x], p + j);
-                    }
-            cp_async_commit();
-            cp_async_wait_all();
-        }
 #pragma unroll
         for (int ix = 0; ix < 4; ++ix)
 #pragma unroll
@@ -161,17 +139,7 @@ __global__ void __launch_bounds__(128) k_interp(InterpArgs a)
                 for (int c = 0; c < CC; ++c)
                     if (c < ncc) {
                         const float4* p = r4 + (long long)c * (a.coil_stride / 2);
-                        float4 q0, q1, q2;
-                        if constexpr (STAGED) {
-                            const float4* sp = &s_rows[((c * 16 + ix * 4 + iy) * 3) * 128 + threadIdx.x];
-                            q0 = sp[0];
-                            q1 = sp[128];
-                            q2 = sp[256];
-                        } else {
-                            q0 = __ldg(p);
-                            q1 = __ldg(p + 1);
-                            q2 = __ldg(p + 2);
-                        }
+                        const float4 q0 = __ldg(p), q1 = __ldg(p + 1), q2 = __ldg(p + 2);
                         const float2 e[6] = {make_float2(q0.x, q0.y), make_float2(q0.z, q0.w), make_float2(q1.x, q1.y),
                                              make_float2(q1.z, q1.w), make_float2(q2.x, q2.y), make_float2(q2.z, q2.w)};
 #pragma unroll

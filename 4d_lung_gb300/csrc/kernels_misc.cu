@@ -89,22 +89,13 @@ cudaError_t launch_tap_records(const double* k, const int* sample_idx, long long
 }
 
 // coils per interpolation thread: one of 2, 4, 6, 8 (autotuned per context)
-// shared memory of the staged interpolation (cc < 0): 16 rows x 3 x 16 bytes
-// per coil and thread, 128 threads
-static size_t interp_staged_smem(int cc) { return (size_t)cc * 16 * 3 * 16 * 128; }
-
-// cc: coils per interpolation thread (1, 2, 4, 6, 8), or -1 / -2 for the
-// shared-memory staged form with 1 / 2 coils per thread
 cudaError_t launch_interp(const InterpArgs& a, long long max_bin_samples, int nbins, int cc, cudaStream_t s)
 {
-    const int ccabs = cc < 0 ? -cc : cc;
     if (max_bin_samples == 0 || nbins == 0) return cudaSuccess;
-    const long long nblk = ((max_bin_samples + 127) / 128) * ((a.nch + ccabs - 1) / ccabs);
+    const long long nblk = ((max_bin_samples + 127) / 128) * ((a.nch + cc - 1) / cc);
     if (nblk > 0x7fffffffLL) return cudaErrorInvalidValue;
     dim3 grid((unsigned)nblk, 1u, (unsigned)nbins);
     switch (cc) {
-    case -1: k_interp<1, true><<<grid, 128, interp_staged_smem(1), s>>>(a); break;
-    case -2: k_interp<2, true><<<grid, 128, interp_staged_smem(2), s>>>(a); break;
     case 1: k_interp<1><<<grid, 128, 0, s>>>(a); break;
     case 2: k_interp<2><<<grid, 128, 0, s>>>(a); break;
     case 4: k_interp<4><<<grid, 128, 0, s>>>(a); break;
@@ -204,10 +195,6 @@ cudaError_t kernels_init()
                             (const void*)k_spread_pipe<4, 2>, (const void*)k_spread_pipe<6, 2>};
     for (int i = 0; i < 6 && e == cudaSuccess; ++i)
         e = cudaFuncSetAttribute(pipes[i], cudaFuncAttributeMaxDynamicSharedMemorySize, spp);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_interp<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)interp_staged_smem(1));
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_interp<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)interp_staged_smem(2));
     if (e == cudaSuccess) e = fft_init_all();
     return e;
 }

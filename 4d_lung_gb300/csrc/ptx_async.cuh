@@ -105,13 +105,4 @@ CGS_D void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::
 CGS_D void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 CGS_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Per-thread asynchronous 16-byte copies global -> shared (cp.async, cached
-// in L1 as well), committed as a group and waited for by the issuing thread.
-CGS_D void cp_async16(void* dst_smem, const void* src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst_smem)), "l"(src) : "memory");
-}
-CGS_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-CGS_D void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
 }  // namespace cgs

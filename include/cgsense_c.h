@@ -317,9 +317,8 @@ int cgs_set_deterministic(cgs_ctx* ctx, int32_t on);
  * row offsets and taps are staged in shared memory by bulk copies; 7: the
  * same gather reading the matrix from global memory; for 6 and 7 spread_cc
  * is the coils per thread, 2, 4, 6 or 8, 0 by the coil count), coils per
- * interpolation thread (1, 2, 4, 6, 8; -1 / -2: 1 / 2 coils with each
- * interior sample's rows first copied into shared memory by cp.async).
- * Variants 1, 2, 4, 5, 6, 7 and every interpolation shape give
+ * interpolation thread (1, 2, 4, 6, 8).  Variants 1, 2, 4, 5, 6, 7 and every
+ * interpolation shape give
  * bitwise-identical results. */
 int cgs_set_launch_shape(cgs_ctx* ctx, int32_t spread_cc, int32_t spread_variant, int32_t interp_cc);
 
