@@ -152,6 +152,7 @@ __global__ void k_cg_alpha(CgState* st, const double* partials, int nblk, int nb
     if (!isfinite(qv.x) || !isfinite(qv.y) || !isfinite(pr) || !isfinite(pim)) {
         S.error = 1;
         S.active = 0;
+        S.xpend = 0;   // fused solve: x already holds the last applied update
         return;
     }
     cg_alpha(S.rr, pr, pim, S.alpha);
@@ -248,62 +249,26 @@ __global__ void k_cg_loop_test(CgState* st, int nbins)
 // ---------------------------------------------------------------------------
 // Fused solve.  Per iteration: the forward z pass forms p = r + beta p and
 // x = x + alpha p of the previous iteration while it reads p (FwdZArgs::cg);
-// the adjoint z pass sums <p, q>; k_cg_update_r computes alpha from those
-// partial sums (in every block, in the order of k_cg_alpha) and updates r
-// with the partial sums of <r, r>; k_cg_beta_test computes the residual,
-// beta and the loop test.  After the loop k_cg_finish_x applies the last
+// the adjoint z pass sums <p, q>; k_cg_alpha computes alpha from those
+// partial sums; k_cg_update_r updates r with the partial sums of <r, r>;
+// k_cg_beta_test computes the residual, beta and the loop test.  After the loop k_cg_finish_x applies the last
 // pending x update.  Same arithmetic as the separate kernels above, hence
-// the same bits; two graph nodes per iteration besides the operator instead
+// the same bits; three graph nodes per iteration besides the operator instead
 // of five, and x and p are read and written in the pass that reads p anyway.
 // ---------------------------------------------------------------------------
 
-// alpha from the <p, q> partials; r -= alpha q; partial sums of |r|^2.
-// grid: (nblk, nbins).  Block 0 of a bin records pq, alpha (or the error)
-// and marks the x / p updates pending.
+// r -= alpha q with the alpha that k_cg_alpha recorded; partial sums of
+// |r|^2.  grid: (nblk, nbins).  Block 0 of a bin marks the x / p updates
+// pending (k_cg_alpha has already stopped a bin with non-finite values).
 __global__ void __launch_bounds__(RED_THREADS)
-k_cg_update_r(float2* r, const float2* __restrict__ q, long long n, long long bs, CgState* st,
-              const double* pq_partials, int nblk_pq, double* partials)
+k_cg_update_r(float2* r, const float2* __restrict__ q, long long n, long long bs, CgState* st, double* partials)
 {
     __shared__ double s_red[2 * RED_THREADS / 32];
-    __shared__ float s_alpha[2];
-    __shared__ int s_ok;
     const int bin = blockIdx.y;
     CgState& S = st[bin];
-    // Block 0 may clear S.active (non-finite values): the flag is read once,
-    // by thread 0, before that write, and the whole block follows s_ok.
-    if (threadIdx.x < 32) {
-        int act = 0;
-        if (threadIdx.x == 0) act = S.active;
-        act = __shfl_sync(0xffffffffu, act, 0);
-        double pr = 0.0, pim = 0.0;
-        if (act) warp_partials(pq_partials, (long long)bin * nblk_pq, nblk_pq, pr, pim);
-        if (threadIdx.x == 0 && !act) s_ok = 0;
-        if (threadIdx.x == 0 && act) {
-            const float2 qv = q[(long long)bin * bs];
-            const bool ok = isfinite(qv.x) && isfinite(qv.y) && isfinite(pr) && isfinite(pim);
-            double alpha[2] = {0.0, 0.0};
-            if (ok) cg_alpha(S.rr, pr, pim, alpha);
-            s_alpha[0] = (float)alpha[0];
-            s_alpha[1] = (float)alpha[1];
-            s_ok = ok ? 1 : 0;
-            if (blockIdx.x == 0) {
-                S.pq[0] = pr;
-                S.pq[1] = pim;
-                if (ok) {
-                    S.alpha[0] = alpha[0];
-                    S.alpha[1] = alpha[1];
-                    S.xpend = 1;
-                } else {
-                    S.error = 1;
-                    S.active = 0;
-                    S.xpend = 0;
-                }
-            }
-        }
-    }
-    __syncthreads();
-    if (!s_ok) return;
-    const float ar = s_alpha[0], ai = s_alpha[1];
+    if (!S.active) return;   // not written by this kernel
+    if (blockIdx.x == 0 && threadIdx.x == 0) S.xpend = 1;
+    const float ar = (float)S.alpha[0], ai = (float)S.alpha[1];
     const long long off = (long long)bin * bs;
     double acc = 0.0, dummy = 0.0;
     float fa = 0.f;

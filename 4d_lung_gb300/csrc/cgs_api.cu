@@ -1745,7 +1745,7 @@ static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh
     CGS_LAUNCH(c, launch_cg_arm(st, c->d_partials2.as<double>(), nblk_cg, nb, thresh, max_iter, c->stream));
     if (!x_trace) {
         // fused iteration: operator (its forward z pass applies the previous
-        // iteration's x and p updates), alpha + r update, beta + loop test
+        // iteration's x and p updates), alpha, r update, beta + loop test
         struct Scope {   // the fusion pointers never outlive the recording
             cgs_ctx* c;
             ~Scope() { c->cgf = {}; }
@@ -1757,9 +1757,10 @@ static int record_solve(cgs_ctx* c, const float2* data, float2* x, double thresh
         for (int it = 0; it < max_iter; ++it) {
             CGS_TRY(apply_bins(c, 0, nb, c->d_pv.as<float2>(), c->d_q.as<float2>(), c->d_pv.as<float2>(),
                                c->d_partials.as<double>(), nblk_adj));
+            CGS_LAUNCH(c, launch_cg_alpha(st, c->d_partials.as<double>(), nblk_adj, nb, c->d_q.as<float2>(), Ni,
+                                          c->stream));
             CGS_LAUNCH(c, launch_cg_update_r(c->d_r.as<float2>(), c->d_q.as<float2>(), Ni, Ni, st,
-                                             c->d_partials.as<double>(), nblk_adj, c->d_partials2.as<double>(), nb,
-                                             c->stream));
+                                             c->d_partials2.as<double>(), nb, c->stream));
             CGS_LAUNCH(c, launch_cg_beta_test(st, c->d_partials2.as<double>(), nblk_cg, nb, c->d_res.as<double>(),
                                               max_iter, c->stream));
         }

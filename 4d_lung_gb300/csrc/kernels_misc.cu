@@ -322,10 +322,10 @@ cudaError_t launch_cg_loop_test(CgState* st, int nbins, cudaStream_t s)
 }
 
 cudaError_t launch_cg_update_r(float2* r, const float2* q, long long n, long long bs, CgState* st,
-                               const double* pq_partials, int nblk_pq, double* partials, int nbins, cudaStream_t s)
+                               double* partials, int nbins, cudaStream_t s)
 {
     dim3 grid((unsigned)cg_blocks(n, nbins), (unsigned)nbins);
-    k_cg_update_r<<<grid, RED_THREADS, 0, s>>>(r, q, n, bs, st, pq_partials, nblk_pq, partials);
+    k_cg_update_r<<<grid, RED_THREADS, 0, s>>>(r, q, n, bs, st, partials);
     return cudaGetLastError();
 }
 

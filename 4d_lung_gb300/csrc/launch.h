@@ -77,9 +77,9 @@ cudaError_t launch_cg_beta(CgState* st, const double* partials, int nblk, int nb
 cudaError_t launch_cg_update_p(float2* p, const float2* r, long long n, long long bs, const CgState* st, int nbins,
                                cudaStream_t s);
 cudaError_t launch_cg_loop_test(CgState* st, int nbins, cudaStream_t s);
-// fused solve: alpha + r update, beta + loop test, the final pending x update
+// fused solve: r update (after launch_cg_alpha), beta + loop test, the final pending x update
 cudaError_t launch_cg_update_r(float2* r, const float2* q, long long n, long long bs, CgState* st,
-                               const double* pq_partials, int nblk_pq, double* partials, int nbins, cudaStream_t s);
+                               double* partials, int nbins, cudaStream_t s);
 cudaError_t launch_cg_beta_test(CgState* st, const double* partials, int nblk, int nbins, double* residuals,
                                 int res_stride, cudaStream_t s);
 cudaError_t launch_cg_finish_x(float2* x, const float2* p, long long n, long long bs, const CgState* st, int nbins,
