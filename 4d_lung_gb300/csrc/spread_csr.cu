@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
 // Every wait is bounded: on a timeout the block sets the error flag, lets
 // its issued copies land and leaves.
 // ---------------------------------------------------------------------------
-constexpr int CSR_SX = 32;            // x rows per unit
+constexpr int CSR_SX = 64;            // x rows per unit
 constexpr int CSR_CAP = 2048;         // staged taps per unit
 constexpr int CSR_NST = 2;            // pipeline stages
 constexpr unsigned long long CSR_WAIT_NS = 2000000000ull;
