@@ -2343,7 +2343,7 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
         if ((wpp == 4 || wpp == 5) && c->kahan) continue;
         if (wpp >= 6 && !(c->csr_valid && support_pruned(c))) continue;
         // the gather's shape parameter is its coils per thread
-        const std::vector<int> cand = wpp >= 6 ? std::vector<int>{2, 4, 6, 8} : sc;
+        const std::vector<int> cand = wpp >= 6 ? std::vector<int>{4, 6, 8} : sc;
         for (int v : cand) {
             if (wpp == 2 && v < 2) continue;
             c->spread_cc = v;
