@@ -332,7 +332,12 @@ def apply_bytes(w, sizes, support=None, matrix=None, y_listed=False):
 # CPU baseline (oracle port)
 # ---------------------------------------------------------------------------
 
-def cpu_apply_sample(synth, name, budget_s=12.0, max_reps=3, warmup=0):
+def cpu_apply_sample(synth, name, budget_s=12.0, max_reps=3, warmup=0, all_bins=False):
+    """The FP32 oracle port (the reference's arithmetic, OpenMP over coils)
+    on the host cores.  all_bins: a step is one E^H D E application of every
+    bin of the scan (the unit the GPU arm's value counts), else one
+    application of the bin whose size is the median of the scan's.  At most
+    max_reps timed steps, fewer when budget_s runs out."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py
     threads = os.cpu_count() or 1
@@ -343,28 +348,39 @@ def cpu_apply_sample(synth, name, budget_s=12.0, max_reps=3, warmup=0):
     lines = synth.readout_lines(w)
     k = synth.wave_trajectory(w, lines=lines)
     rbins = synth.breathing_bins(len(lines), w.n_bins)
-    sb = synth.bin_samples(rbins, w.n_read)[0]
-    kb = k[sb]
+    sbins = synth.bin_samples(rbins, w.n_read)
+    sizes = [len(b) for b in sbins]
+    order = np.argsort(sizes, kind="stable")
+    chosen = list(range(len(sbins))) if all_bins else [int(order[len(order) // 2])]
     p = oracle_py.make_params(w.img, w.grid, w.n_ch, kb_w=kb_w, kb_b=beatty_beta(kb_w))
-    taps = o.taps(p, kb)                     # ConvKernel::calculateWeights (set-up)
     kft = o.kernel_ft(p)                     # ConvKernel::calculateKernelFT (set-up)
+    prep = []
+    for b in chosen:
+        kb = k[sbins[b]]
+        prep.append((o.taps(p, kb), synth.radial_dcf(kb, w.grid)))   # calculateWeights (set-up)
     smaps = synth.coil_maps(w.img, w.n_ch)
-    dcf = synth.radial_dcf(kb, w.grid)
     x = synth.phantom(w.img)
+
+    def step():
+        for taps, dcf in prep:
+            o.apply_ehde(p, taps, kft, smaps, dcf, x)
+
     for _ in range(warmup):
-        o.apply_ehde(p, taps, kft, smaps, dcf, x)
+        step()
     times = []
     t_all = time.perf_counter()
     while len(times) < max_reps:
         t0 = time.perf_counter()
-        o.apply_ehde(p, taps, kft, smaps, dcf, x)
+        step()
         times.append(time.perf_counter() - t0)
         if time.perf_counter() - t_all > budget_s:
             break
+    what = ("one E^H D E application of each of the %d bins (%d samples in all)" % (len(chosen), sum(sizes))
+            if all_bins else "E^H D E applications of the median-size bin %d (%d samples)" % (chosen[0], sizes[chosen[0]]))
     return {
-        "times": times, "threads": threads, "samples_in_bin": int(len(sb)),
-        "sample": "E^H D E applications of bin 0 (%d samples, %d coils, %s grid), %d timed" % (
-            len(sb), w.n_ch, "x".join(map(str, w.grid)), len(times)),
+        "times": times, "threads": threads, "applies_per_step": len(chosen),
+        "samples_in_bin": int(sizes[chosen[0]]),
+        "sample": "%s, %d coils, %s grid, %d timed" % (what, w.n_ch, "x".join(map(str, w.grid)), len(times)),
     }
 
 
@@ -378,19 +394,21 @@ def run_reference(args):
         return 0
     synth = importlib.import_module("4d_lung_gb300.synth")
     w = synth.WORKLOADS[args.workload]
-    res = cpu_apply_sample(synth, args.workload, budget_s=1e9, max_reps=args.steps, warmup=args.warmup)
+    res = cpu_apply_sample(synth, args.workload, budget_s=1e9, max_reps=args.steps, warmup=args.warmup,
+                           all_bins=True)
     t = res["times"]
-    value = len(t) / sum(t)
+    value = res["applies_per_step"] * len(t) / sum(t)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": len(t), "warmup": args.warmup, "ms_per_step": 1e3 * sum(t) / len(t),
         "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": "c64/f32",
         "data": "synthetic", "config": {"workload": w.name, "bins": w.n_bins, "cg_iters": w.cg_iters,
-                                        "step": "one E^H D E application of bin 0 on the host cores"},
+                                        "step": "one E^H D E application of every bin of the scan on the "
+                                                "host cores (the GPU arm's unit: bin-applies)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["threads"], "kind": "port",
                          "sample": res["sample"]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "s_per_4d_recon_extrapolated": w.n_bins * w.cg_iters * sum(t) / len(t),
+        "s_per_4d_recon_extrapolated": w.cg_iters * sum(t) / len(t),
     }
     print(json.dumps(line), flush=True)
     return 0
