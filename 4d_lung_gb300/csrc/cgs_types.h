@@ -92,6 +92,7 @@ struct FwdZArgs {
     float2* cg_p;           // == x (stored back)
     const float2* cg_r;     // residual, same layout as x
     float2* cg_x;           // the solution, same layout as x
+    int nbatch;             // batch items of the launch (set by the launcher; see zp_item)
 };
 
 struct AdjZArgs {
@@ -111,6 +112,7 @@ struct AdjZArgs {
     long long q_cs;         // coil stride of q when smaps is null
     const float2* tw;
     int* err;               // timeout flag of the pipelined variant (null: plain kernel)
+    int nbatch;             // batch items of the launch (set by the launcher; see zp_item)
 };
 
 struct TapRecord {

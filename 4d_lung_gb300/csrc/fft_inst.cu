@@ -163,9 +163,12 @@ struct SizeImpl {
         else k_fft_contig<R1, R2, +1, LPB><<<grid, NT_C, 0, s>>>(a);
         return cudaGetLastError();
     }
-    static cudaError_t fwd_z(const FwdZArgs& a, int batch, cudaStream_t s)
+    // z passes: one block per (line block, batch item), items fastest (zp_item)
+    static cudaError_t fwd_z(const FwdZArgs& a0, int batch, cudaStream_t s)
     {
-        dim3 grid((unsigned)((a.nl + LPB - 1) / LPB), (unsigned)batch);
+        FwdZArgs a = a0;
+        a.nbatch = batch;
+        dim3 grid((unsigned)(((a.nl + LPB - 1) / LPB) * batch));
         // bulk copies need 16-byte aligned tiles: even Iz and coil strides
         if (a.err && a.smaps && a.x_cs == 0 && a.Iz <= L && (a.Iz & 1) == 0 && (a.coil_in & 1) == 0 &&
             al16(a.smaps)) {
@@ -178,9 +181,11 @@ struct SizeImpl {
         return cudaGetLastError();
     }
     static int adj_blocks(long long nl) { return (int)((nl + LPB - 1) / LPB); }
-    static cudaError_t adj_z(const AdjZArgs& a, int batch, cudaStream_t s)
+    static cudaError_t adj_z(const AdjZArgs& a0, int batch, cudaStream_t s)
     {
-        dim3 grid((unsigned)adj_blocks(a.nl), (unsigned)batch);
+        AdjZArgs a = a0;
+        a.nbatch = batch;
+        dim3 grid((unsigned)((long long)adj_blocks(a.nl) * batch));
         if (a.err && a.smaps && a.Iz <= L && (a.Iz & 1) == 0 && (a.coil_s & 1) == 0 && (a.coil_in & 1) == 0 &&
             (a.in_bs & 1) == 0 && al16(a.smaps) && al16(a.in)) {
             k_adj_z_pipe<R1, R2, LPB, ZNST_A><<<grid, NT_C, ZA::smem_bytes(a.Iz, true), s>>>(a);

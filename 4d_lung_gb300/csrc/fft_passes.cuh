@@ -38,6 +38,13 @@ CGS_D float2 table_twiddle(float2 v, float2 w)
 
 CGS_D float2 parity(float2 v, int l) { return (l & 1) ? cneg(v) : v; }
 
+// Block order of the z passes: block b of a launch over nbatch items (bins)
+// is line block b / nbatch of item b % nbatch.  The blocks of one line block
+// run side by side for every bin, so its coil-map tiles, which all bins
+// share, come from DRAM once and from L2 for the other bins.
+CGS_D int zp_item(int nbatch) { return (int)(blockIdx.x % (unsigned)nbatch); }
+CGS_D long long zp_lblk(int nbatch) { return (long long)(blockIdx.x / (unsigned)nbatch); }
+
 // Image value read by a forward z pass.  In a fused CG solve (a.cg set) the
 // pass reads the search direction p and, while its bin has updates pending,
 // first applies them: x = x + alpha p, p = r + beta p (Reco.cpp:285-290,
@@ -47,11 +54,11 @@ struct FwdZCg {
     bool upd;
     float ar, ai, br, bi;
 };
-CGS_D FwdZCg fwd_z_cg(const FwdZArgs& a)
+CGS_D FwdZCg fwd_z_cg(const FwdZArgs& a, int item)
 {
     FwdZCg u{false, 0.f, 0.f, 0.f, 0.f};
     if (a.cg) {
-        const CgState& S = a.cg[blockIdx.y];
+        const CgState& S = a.cg[item];
         if (S.active && S.xpend) {
             u.upd = true;
             u.ar = (float)S.alpha[0];
@@ -647,8 +654,9 @@ k_fwd_z(FwdZArgs a)
     __shared__ float2 s_y[LPB * Lay::LINE];
     const int tid = threadIdx.x;
     for (int m = tid; m < L; m += blockDim.x) s_tw[m] = a.tw[m];
-    const long long line0 = (long long)blockIdx.x * LPB;
-    float2* outb = a.out + (long long)blockIdx.y * a.out_bs;
+    const int item = zp_item(a.nbatch);
+    const long long line0 = zp_lblk(a.nbatch) * LPB;
+    float2* outb = a.out + (long long)item * a.out_bs;
 
     // stage-1 role
     const int ln1 = tid / R2, n2 = tid % R2;
@@ -664,14 +672,14 @@ k_fwd_z(FwdZArgs a)
     const int ln2 = tid / R1, k1 = tid % R1;
     const long long line2 = line0 + ln2;
     const bool act2 = ln2 < LPB && line2 < a.nl;
-    const FwdZCg cg = CGF ? fwd_z_cg(a) : FwdZCg{false, 0.f, 0.f, 0.f, 0.f};
+    const FwdZCg cg = CGF ? fwd_z_cg(a, item) : FwdZCg{false, 0.f, 0.f, 0.f, 0.f};
 
     for (int c = 0; c < a.nch; ++c) {
         __syncthreads();   // s_tw ready / previous coil's stage 2 finished
         if (act1) {
             if (c == 0 || a.x_cs != 0) {
                 // a.cg is only set with x_cs == 0: each element is read once
-                const long long eb = (long long)blockIdx.y * a.x_bs + (long long)c * a.x_cs + line1 * a.Iz;
+                const long long eb = (long long)item * a.x_bs + (long long)c * a.x_cs + line1 * a.Iz;
                 if (CGF && cg.upd) {
 #pragma unroll
                     for (int n1 = 0; n1 < R1; ++n1) xa[n1] = make_float2(0.f, 0.f);
@@ -730,7 +738,7 @@ k_fwd_z(FwdZArgs a)
 //   q[line][z] = scale * apod * sum_c conj(S_c) * F^H_z(zbuf[c][line])[z + lo_z]
 // The coil sum is accumulated in registers in coil order (no atomics).
 // When p != nullptr, the block also accumulates <p, q> = sum conj(p) q in
-// double precision and writes it to partials[blockIdx] (re, im).
+// double precision and writes it to partials[item][line block] (re, im).
 // ---------------------------------------------------------------------------
 
 template <int R1, int R2, int LPB>
@@ -746,9 +754,11 @@ k_adj_z(AdjZArgs a)
     __shared__ double s_red[2][NT / 32];
     const int tid = threadIdx.x;
     for (int m = tid; m < L; m += blockDim.x) s_tw[m] = a.tw[m];
-    const long long line0 = (long long)blockIdx.x * LPB;
-    const float2* inb = a.in + (long long)blockIdx.y * a.in_bs;
-    float2* qb = a.q + (long long)blockIdx.y * a.q_bs;
+    const int item = zp_item(a.nbatch);
+    const long long lblk = zp_lblk(a.nbatch);
+    const long long line0 = lblk * LPB;
+    const float2* inb = a.in + (long long)item * a.in_bs;
+    float2* qb = a.q + (long long)item * a.q_bs;
 
     const int ln1 = tid / R2, n2 = tid % R2;
     const long long line1 = line0 + ln1;
@@ -821,7 +831,7 @@ k_adj_z(AdjZArgs a)
                 const float2 qv = cscale(acc[k2], sxy * a.apz[zi]);
                 qb[line2 * a.Iz + zi] = qv;
                 if (a.p) {
-                    const float2 pv = a.p[(long long)blockIdx.y * a.q_bs + line2 * a.Iz + zi];
+                    const float2 pv = a.p[(long long)item * a.q_bs + line2 * a.Iz + zi];
                     fre += pv.x * qv.x + pv.y * qv.y;
                     fim += pv.x * qv.y - pv.y * qv.x;
                 }
@@ -847,7 +857,7 @@ k_adj_z(AdjZArgs a)
                 r0 += s_red[0][w];
                 r1 += s_red[1][w];
             }
-            double* out = a.partials + 2 * ((long long)blockIdx.y * gridDim.x + blockIdx.x);
+            double* out = a.partials + 2 * ((long long)item * (gridDim.x / a.nbatch) + lblk);
             out[0] = r0;
             out[1] = r1;
         }
@@ -898,7 +908,8 @@ k_fwd_z_pipe(FwdZArgs a)
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_xa + (size_t)LPB * a.Iz);
     const int tid = threadIdx.x;
     for (int m = tid; m < L; m += ZL::NT) s_tw[m] = a.tw[m];
-    const long long line0 = (long long)blockIdx.x * LPB;
+    const int item = zp_item(a.nbatch);
+    const long long line0 = zp_lblk(a.nbatch) * LPB;
     const int rows = (int)min((long long)LPB, a.nl - line0);
     const uint32_t tile_bytes = (uint32_t)rows * (uint32_t)a.Iz * (uint32_t)sizeof(float2);
     const float2* Sb = a.smaps + line0 * a.Iz;
@@ -915,7 +926,7 @@ k_fwd_z_pipe(FwdZArgs a)
     if (tid == 0)
         for (int c = 0; c < NST - 1 && c < a.nch; ++c) issue(c);
 
-    float2* outb = a.out + (long long)blockIdx.y * a.out_bs;
+    float2* outb = a.out + (long long)item * a.out_bs;
     const int ln1 = tid / R2, n2 = tid % R2;
     const long long line1 = line0 + ln1;
     const bool act1 = ln1 < LPB && line1 < a.nl;
@@ -923,8 +934,8 @@ k_fwd_z_pipe(FwdZArgs a)
     if (act1) {
         const int ix = (int)(line1 / a.Iy), iy = (int)(line1 - (long long)ix * a.Iy);
         const float axy = a.apx[ix] * a.apy[iy];
-        const FwdZCg cg = CGF ? fwd_z_cg(a) : FwdZCg{false, 0.f, 0.f, 0.f, 0.f};
-        const long long eb = (long long)blockIdx.y * a.x_bs + line1 * a.Iz;
+        const FwdZCg cg = CGF ? fwd_z_cg(a, item) : FwdZCg{false, 0.f, 0.f, 0.f, 0.f};
+        const long long eb = (long long)item * a.x_bs + line1 * a.Iz;
         if (CGF && cg.upd) {
             fwd_z_fused_line<R1, R2>(a, cg, eb, n2, axy, [&](int, int zi, float2 v) { xa[zi] = v; });
         } else {
@@ -1006,13 +1017,15 @@ k_adj_z_pipe(AdjZArgs a)
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_y + LPB * Lay::LINE);
     const int tid = threadIdx.x;
     for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
-    const long long line0 = (long long)blockIdx.x * LPB;
+    const int item = zp_item(a.nbatch);
+    const long long lblk = zp_lblk(a.nbatch);
+    const long long line0 = lblk * LPB;
     const int rows = (int)min((long long)LPB, a.nl - line0);
     const uint32_t in_bytes = (uint32_t)rows * (uint32_t)L * (uint32_t)sizeof(float2);
     const uint32_t s_bytes = (uint32_t)rows * (uint32_t)a.Iz * (uint32_t)sizeof(float2);
-    const float2* inb = a.in + (long long)blockIdx.y * a.in_bs + line0 * L;
+    const float2* inb = a.in + (long long)item * a.in_bs + line0 * L;
     const float2* Sb = a.smaps + line0 * a.Iz;
-    float2* qb = a.q + (long long)blockIdx.y * a.q_bs;
+    float2* qb = a.q + (long long)item * a.q_bs;
     if (tid == 0) {
         for (int s = 0; s < NST; ++s) mbar_init(&s_bar[s], 1);
         fence_mbar_init();
@@ -1098,7 +1111,7 @@ k_adj_z_pipe(AdjZArgs a)
                 const float2 qv = cscale(acc[k2], sxy * a.apz[zi]);
                 qb[line2 * a.Iz + zi] = qv;
                 if (a.p) {
-                    const float2 pv = a.p[(long long)blockIdx.y * a.q_bs + line2 * a.Iz + zi];
+                    const float2 pv = a.p[(long long)item * a.q_bs + line2 * a.Iz + zi];
                     fre += pv.x * qv.x + pv.y * qv.y;
                     fim += pv.x * qv.y - pv.y * qv.x;
                 }
@@ -1124,7 +1137,7 @@ k_adj_z_pipe(AdjZArgs a)
                 r0 += s_red[0][w];
                 r1 += s_red[1][w];
             }
-            double* out = a.partials + 2 * ((long long)blockIdx.y * gridDim.x + blockIdx.x);
+            double* out = a.partials + 2 * ((long long)item * (gridDim.x / a.nbatch) + lblk);
             out[0] = r0;
             out[1] = r1;
         }
