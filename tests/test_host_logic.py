@@ -114,14 +114,15 @@ def test_roofline_byte_model(synth):
     Ni, Nl, C8 = Ix * Iy * Iz, Ix * Iy, 8 * w.n_ch
     sizes = [10, 30]
     full = bench.stage_bytes(w, sizes)
-    assert full["fwd_z"] == 2 * (8 * Ni + C8 * Ni + C8 * Nl * Gz)
+    assert full["fwd_z"] == 2 * (8 * Ni + C8 * Nl * Gz) + C8 * Ni   # coil maps once (L2 across bins)
     assert full["fwd_y"] == 2 * C8 * (Nl * Gz + Ix * Gy * Gz)
     assert full["fwd_x"] == C8 * 2 * Gy * Gz * (Ix + Gx)
-    assert full["adj_x"] == full["fwd_x"] and full["adj_y"] == full["fwd_y"] and full["adj_z"] == full["fwd_z"]
+    assert full["adj_x"] == full["fwd_x"] and full["adj_y"] == full["fwd_y"]
+    assert full["adj_z"] == 2 * (C8 * Nl * Gz + 8 * Ni) + C8 * Ni
     cols, tiles = [40, 60], [3, 5]
     pruned = bench.stage_bytes(w, sizes, (cols, tiles), matrix=(500, 100 * Gx), y_listed=True)
     assert pruned["fwd_x"] == C8 * 100 * (Ix + Gx)
     assert pruned["fwd_y"] == C8 * (2 * Nl * Gz + Ix * 100)
     assert pruned["spread"] == C8 * 100 * Gx + 4 * 100 * Gx + 8 * 500 + 40 * C8
     assert pruned["interp"] == C8 * 100 * Gx + 40 * (64 + 4 + C8)
-    assert bench.apply_bytes(w, sizes) == sum(full.values()) + 56 * Ni * 2
+    assert bench.apply_bytes(w, sizes) == sum(full.values())
