@@ -125,6 +125,10 @@ struct cgs_ctx {
     // built when the x and y passes' column tiles coincide
     DevBuf d_sup_rowmask;
     long long sup_rowmask_bs = 0;            // words per bin (0: not built)
+    int sup_tb = 0;                          // columns per listed tile: forward x pass, spreading
+    int sup_tb_adj = 0;                      // columns per listed tile: adjoint x pass (fft_listed_cols)
+    std::vector<long long> h_sup_off_adj;    // per bin: first entry in d_sup_tiles_adj
+    DevBuf d_sup_tiles_adj;                  // the adjoint x pass's listed tiles {bin, first column}
     // transposed tap matrix of the listed tiles' points (spreading variant 6)
     bool csr_valid = false;
     long long csr_pts = 0;
@@ -273,6 +277,7 @@ struct BinPrep {
     std::vector<int> tile_idx;
     std::vector<int> plane_rng;   // [ntiles][TILE_X][2]
     std::vector<int> sup_cols;        // first column of each x-pass tile the samples touch
+    std::vector<int> sup_cols_adj;    // the same for the adjoint x pass's (narrower) tiles
     std::vector<int> live;            // spreading tiles holding a supported column
 };
 
@@ -377,7 +382,7 @@ void tile_lists(const cgs_ctx* c, const unsigned* nearest, long long n, BinPrep&
 // columns of the flattened [Gy][Gz] plane: the tiles holding a supported
 // column are listed (sup_cols); the spreading stores the grid tiles whose
 // (y, z) extent meets a listed column (live).
-void support_lists(const cgs_ctx* c, const unsigned* nearest, long long n, int tb, BinPrep& out)
+void support_lists(const cgs_ctx* c, const unsigned* nearest, long long n, int tb, int tb_adj, BinPrep& out)
 {
     const int Gy = c->G[1], Gz = c->G[2];
     const long long ncol = (long long)Gy * Gz;
@@ -398,6 +403,16 @@ void support_lists(const cgs_ctx* c, const unsigned* nearest, long long n, int t
         if (!any) continue;
         out.sup_cols.push_back((int)b0);
         for (long long b = b0; b < b1; ++b) listed[b] = 1;
+    }
+    // the adjoint x pass reads the grid only where a sample reaches: its own
+    // tiles, each inside a listed forward tile (tb_adj divides tb), so that
+    // the spreading has stored every column it reads
+    out.sup_cols_adj.clear();
+    for (long long b0 = 0; b0 < ncol; b0 += tb_adj) {
+        const long long b1 = std::min(ncol, b0 + tb_adj);
+        bool any = false;
+        for (long long b = b0; b < b1 && !any; ++b) any = col[b] != 0;
+        if (any) out.sup_cols_adj.push_back((int)b0);
     }
     // spreading tiles whose (y, z) extent holds a masked column: the adjoint
     // x pass reads those columns at every x, so these tiles are stored (with
@@ -434,7 +449,7 @@ int build_csr(cgs_ctx* c)
     c->csr_valid = false;
     c->csr_entries = 0;
     if (!c->sup_built || c->total == 0) return CGS_OK;
-    const int tbx = fft_strided_cols(c->G[0]);
+    const int tbx = c->sup_tb;
     const long long ncol = (long long)c->G[1] * c->G[2];
     const long long ntl = c->h_sup_off[c->nbins];
     const long long npts = ntl * c->G[0] * tbx;
@@ -549,40 +564,49 @@ int rebuild_bins(cgs_ctx* c)
     c->setup_ms[1] = ms_since(t0);
     t0 = clk::now();
     const int tbx = fft_strided_cols(c->G[0]);
+    int tba = fft_listed_cols(c->G[0], c->lo[0], c->I[0]);
+    if (tba <= 0 || tbx % tba != 0) tba = tbx;
+    c->sup_tb = tbx;
+    c->sup_tb_adj = tba;
 #pragma omp parallel for schedule(dynamic, 1)
     for (int b = 0; b < c->nbins; ++b) {
         tile_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], prep[b]);
         if (tbx > 0)
-            support_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], tbx, prep[b]);
+            support_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], tbx, tba,
+                          prep[b]);
     }
     c->sup_built = false;
     c->h_sup_off.assign(c->nbins + 1, 0);
+    c->h_sup_off_adj.assign(c->nbins + 1, 0);
     if (tbx > 0) {
-        std::vector<int2> tiles;
+        std::vector<int2> tiles, tiles_adj;
         std::vector<int> live;
         c->h_live_off.assign(c->nbins + 1, 0);
         for (int b = 0; b < c->nbins; ++b) {
             for (int b0 : prep[b].sup_cols) tiles.push_back(make_int2(b, b0));
             c->h_sup_off[b + 1] = (long long)tiles.size();
+            for (int b0 : prep[b].sup_cols_adj) tiles_adj.push_back(make_int2(b, b0));
+            c->h_sup_off_adj[b + 1] = (long long)tiles_adj.size();
             live.insert(live.end(), prep[b].live.begin(), prep[b].live.end());
             c->h_live_off[b + 1] = (long long)live.size();
         }
         CGS_TRY(upload(c, c->d_sup_tiles, tiles.data(), std::max<size_t>(tiles.size(), 1) * sizeof(int2)));
         c->h_sup_tiles = tiles;
+        CGS_TRY(upload(c, c->d_sup_tiles_adj, tiles_adj.data(), std::max<size_t>(tiles_adj.size(), 1) * sizeof(int2)));
         CGS_TRY(upload(c, c->d_live, live.data(), std::max<size_t>(live.size(), 1) * sizeof(int)));
         CGS_TRY(upload(c, c->d_live_off, c->h_live_off.data(), c->h_live_off.size() * sizeof(long long)));
         c->sup_built = true;
-        // row masks of the forward y pass: its tile (z tile zs, all y) stores row y only
-        // when the x pass lists the column tile starting at y * Gz + zs * tb
+        // row masks of the forward y pass: it stores row y of column z only
+        // when the x pass lists the column tile starting at y * Gz + zs * tb,
+        // zs = z / tb (the x-pass tiles never straddle two rows: Gz % tb == 0)
         c->sup_rowmask_bs = 0;
-        const int tby = fft_strided_cols(c->G[1]);
-        if (tby == tbx && c->G[2] % tby == 0 && c->G[1] % 32 == 0) {
-            const int nzs = c->G[2] / tby, wpr = c->G[1] / 32;
+        if (c->G[2] % tbx == 0 && c->G[1] % 32 == 0) {
+            const int nzs = c->G[2] / tbx, wpr = c->G[1] / 32;
             const long long bs = (long long)nzs * wpr;
             std::vector<unsigned> rm((size_t)c->nbins * bs, 0u);
             for (int b = 0; b < c->nbins; ++b)
                 for (long long J = c->h_sup_off[b]; J < c->h_sup_off[b + 1]; ++J) {
-                    const int f = tiles[J].y, y = f / c->G[2], zs = (f % c->G[2]) / tby;
+                    const int f = tiles[J].y, y = f / c->G[2], zs = (f % c->G[2]) / tbx;
                     rm[(size_t)b * bs + (size_t)zs * wpr + y / 32] |= 1u << (y % 32);
                 }
             CGS_TRY(upload(c, c->d_sup_rowmask, rm.data(), rm.size() * sizeof(unsigned)));
@@ -663,11 +687,14 @@ int prepare_adj_slots(cgs_ctx* c, int b0, int nb, bool pruned)
     return CGS_OK;
 }
 
-// x pass over bins [b0, b0 + nb): only the listed tiles
-void set_support_tiles(const cgs_ctx* c, StridedPassArgs& a, int b0, int nb)
+// x pass over bins [b0, b0 + nb): only the listed tiles (the forward
+// pass's, or the adjoint pass's narrower ones)
+void set_support_tiles(const cgs_ctx* c, StridedPassArgs& a, int b0, int nb, bool adjoint)
 {
-    a.sup_tiles = c->d_sup_tiles.as<int2>() + c->h_sup_off[b0];
-    a.sup_ntiles = c->h_sup_off[b0 + nb] - c->h_sup_off[b0];
+    const std::vector<long long>& off = adjoint ? c->h_sup_off_adj : c->h_sup_off;
+    a.sup_tiles = (adjoint ? c->d_sup_tiles_adj : c->d_sup_tiles).as<int2>() + off[b0];
+    a.sup_ntiles = off[b0 + nb] - off[b0];
+    a.sup_tb = adjoint ? c->sup_tb_adj : c->sup_tb;
     a.sup_bin0 = b0;
     a.sup_nsub = c->nch;
 }
@@ -733,6 +760,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     if (sup && c->sup_rowmask_bs > 0) {
         fy.sup_rowmask = c->d_sup_rowmask.as<unsigned>() + (long long)b0 * c->sup_rowmask_bs;
         fy.sup_rowmask_bs = c->sup_rowmask_bs;
+        fy.sup_rowmask_tb = c->sup_tb;
         fy.sup_nsub = c->nch;
     }
     CGS_LAUNCH(c, launch_strided(Gy, -1, fy, Ix, nb * c->nch, c->stream));
@@ -751,7 +779,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fx.out_off = 0;
     fx.err = c->d_err.as<int>();
     fx.tw = c->tw[0].as<float2>();
-    if (sup) set_support_tiles(c, fx, b0, nb);
+    if (sup) set_support_tiles(c, fx, b0, nb, false);
     CGS_LAUNCH(c, launch_strided(Gx, -1, fx, 1, nb * c->nch, c->stream));
 
     InterpArgs ia{};
@@ -828,7 +856,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
             ca.nch = c->nch;
             ca.Gx = Gx;
             ca.B = (long long)Gy * Gz;
-            ca.tb = fft_strided_cols(Gx);
+            ca.tb = c->sup_tb;
             ca.cc = c->spread_cc;   // coils per thread of the gather (0: by the coil count)
             if (ca.cc != 2 && ca.cc != 4 && ca.cc != 6 && ca.cc != 8) ca.cc = 0;
             ca.err = c->d_err.as<int>();
@@ -854,7 +882,7 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
         ax.out_off = c->lo[0];
         ax.err = c->d_err.as<int>();
         ax.tw = c->tw[0].as<float2>();
-        if (sup) set_support_tiles(c, ax, b0, nb);
+        if (sup) set_support_tiles(c, ax, b0, nb, true);
         CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
     }
 
@@ -2710,12 +2738,24 @@ int cgs_support_stats(cgs_ctx* c, int64_t* listed_cols, int64_t* live_tiles)
     CGS_TRY(check_ready(c, false));
     const bool sup = support_pruned(c);
     const long long ncol = (long long)c->G[1] * c->G[2];
-    const int tbx = fft_strided_cols(c->G[0]);
+    const int tbx = c->sup_tb;
     for (int b = 0; b < c->nbins; ++b) {
         if (listed_cols)
             listed_cols[b] = sup ? std::min(ncol, (c->h_sup_off[b + 1] - c->h_sup_off[b]) * (long long)tbx) : ncol;
         if (live_tiles) live_tiles[b] = sup ? c->h_live_off[b + 1] - c->h_live_off[b] : c->ntiles;
     }
+    return CGS_OK;
+}
+
+int cgs_support_stats_adjoint(cgs_ctx* c, int64_t* listed_cols)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!listed_cols) return fail(c, CGS_ERR_ARG, "null pointer");
+    const bool sup = support_pruned(c);
+    const long long ncol = (long long)c->G[1] * c->G[2];
+    for (int b = 0; b < c->nbins; ++b)
+        listed_cols[b] = sup ? std::min(ncol, (c->h_sup_off_adj[b + 1] - c->h_sup_off_adj[b]) * (long long)c->sup_tb_adj)
+                             : ncol;
     return CGS_OK;
 }
 

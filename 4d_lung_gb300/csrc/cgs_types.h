@@ -53,12 +53,15 @@ struct StridedPassArgs {
     // (bin - sup_bin0) * sup_nsub + sub.
     const int2* sup_tiles;
     long long sup_ntiles;
+    int sup_tb;                // columns per listed tile
     int sup_bin0, sup_nsub;
     // Forward y pass: only the rows that the x pass reads are stored.  Per
-    // bin and column tile (b0 / TB), L / 32 words of row bits; bin of item
-    // = item / sup_nsub, words per bin sup_rowmask_bs.
+    // bin and x-pass tile of the row's column (column / sup_rowmask_tb),
+    // L / 32 words of row bits; bin of item = item / sup_nsub, words per bin
+    // sup_rowmask_bs.
     const unsigned* sup_rowmask;
     long long sup_rowmask_bs;
+    int sup_rowmask_tb;
 };
 
 struct ContigPassArgs {

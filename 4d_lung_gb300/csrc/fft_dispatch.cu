@@ -51,7 +51,8 @@ static EncodeTiledFn encode_fn()
     return fn;
 }
 
-bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int batch, int TB, int* box_rows)
+bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int batch, int TB, int* box_rows,
+                        int promo)
 {
     // TMA rows start on 16-byte boundaries: base pointer, row pitch and
     // strides must be multiples of 16 bytes (even element counts)
@@ -69,9 +70,11 @@ bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int b
     const cuuint64_t strides[3] = {(cuuint64_t)a.B * 8, (cuuint64_t)as * 8, (cuuint64_t)bs * 8};
     const cuuint32_t box[4] = {(cuuint32_t)TB, (cuuint32_t)br, 1, 1};
     const cuuint32_t es[4] = {1, 1, 1, 1};
+    const CUtensorMapL2promotion pr = promo <= 64    ? CU_TENSOR_MAP_L2_PROMOTION_L2_64B
+                                      : promo <= 128 ? CU_TENSOR_MAP_L2_PROMOTION_L2_128B
+                                                     : CU_TENSOR_MAP_L2_PROMOTION_L2_256B;
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 4, const_cast<float2*>(a.in), dims, strides, box, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, pr, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return false;
     *box_rows = br;
     return true;
@@ -110,6 +113,18 @@ int fft_strided_cols(int L)
 {
     switch (L) {
 #define CGS_CASE(L_, R1_, R2_, G_) case L_: return fft_strided_tile_cols(R1_, R2_);
+        CGS_FFT_SIZES(CGS_CASE)
+#undef CGS_CASE
+    }
+    return 0;
+}
+
+int fft_listed_cols(int L, int lo, int I)
+{
+    const bool half = 4 * lo == L && 2 * I == L;
+    switch (L) {
+#define CGS_CASE(L_, R1_, R2_, G_) \
+    case L_: return half ? fft_listed_tile_cols(R1_, R2_) : fft_strided_tile_cols(R1_, R2_);
         CGS_FFT_SIZES(CGS_CASE)
 #undef CGS_CASE
     }

@@ -49,11 +49,16 @@ struct SizeImpl {
     // the TMA strided variants instantiated: forward (input-pruned or not),
     // adjoint (output-pruned or not)
     static constexpr bool HAS_IN = R1 % 4 == 0, HAS_OUT = R2 % 4 == 0;
+    // x passes over listed tiles of the sample support: narrower tiles
+    // (fft_listed_tile_cols) when both pruned forms exist
+    static constexpr int TBN = fft_listed_tile_cols(R1, R2);
+    static constexpr bool NARROW = HAS_IN && HAS_OUT && TBN != TB;
+    static_assert(!(HAS_IN && HAS_OUT) || fft_has_narrow_tiles(R1, R2), "listed width and pruned forms agree");
 
-    template <int SIGN, int MODE>
+    template <int SIGN, int MODE, int TBK = TB>
     static cudaError_t tma_attr(int smem)
     {
-        return cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, SIGN, TB, NSTAGE, MODE>,
+        return cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, SIGN, TBK, NSTAGE, MODE>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     }
 
@@ -66,6 +71,11 @@ struct SizeImpl {
             if (e == cudaSuccess) e = tma_attr<-1, PRUNE_IN>(smem);
         if constexpr (HAS_OUT)
             if (e == cudaSuccess) e = tma_attr<+1, PRUNE_OUT>(smem);
+        if constexpr (NARROW) {
+            const int smem_n = (int)PipeLayout<R1, R2, TBN, NSTAGE>::smem_bytes(L);
+            if (e == cudaSuccess) e = tma_attr<-1, PRUNE_IN, TBN>(smem_n);
+            if (e == cudaSuccess) e = tma_attr<+1, PRUNE_OUT, TBN>(smem_n);
+        }
         if constexpr (HAS_IN)
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(k_toep_x_tma<R1, R2, TBT, NSTAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -86,33 +96,47 @@ struct SizeImpl {
     static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
     // persistent launch: as many blocks as fit, at most one per tile
-    template <int SIGN, int MODE>
+    template <int SIGN, int MODE, int TBK = TB>
     static cudaError_t tma_run(const StridedPassArgs& a, const CUtensorMap& map, int A, int batch, int box_rows,
                                cudaStream_t s)
     {
-        const size_t smem = Pipe::smem_bytes(a.Lin);
+        using P = PipeLayout<R1, R2, TBK, NSTAGE>;
+        const size_t smem = P::smem_bytes(a.Lin);
         int per_sm = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_fft_strided_tma<R1, R2, SIGN, TB, NSTAGE, MODE>, Pipe::NT, smem);
+            &per_sm, k_fft_strided_tma<R1, R2, SIGN, TBK, NSTAGE, MODE>, P::NT, smem);
         if (e != cudaSuccess) return e;
         const long long tiles_per_item = (long long)A * a.ntb;
         const long long ntiles = a.sup_tiles ? a.sup_ntiles * a.sup_nsub : tiles_per_item * batch;
         if (ntiles <= 0) return cudaSuccess;   // no listed tile: nothing to transform
         long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
         if (nblk > ntiles) nblk = ntiles;
-        k_fft_strided_tma<R1, R2, SIGN, TB, NSTAGE, MODE><<<(unsigned)nblk, Pipe::NT, smem, s>>>(
+        k_fft_strided_tma<R1, R2, SIGN, TBK, NSTAGE, MODE><<<(unsigned)nblk, P::NT, smem, s>>>(
             a, map, ntiles, (int)tiles_per_item, box_rows);
         return cudaGetLastError();
     }
 
     static cudaError_t strided(int sign, StridedPassArgs a, int A, int batch, cudaStream_t s)
     {
-        a.ntb = (a.B + TB - 1) / TB;
+        const bool half_in = 4 * a.in_off == L && 2 * a.Lin == L;
+        const bool half_out = 4 * a.out_off == L && 2 * a.Lout == L;
         CUtensorMap map;
         int box_rows = 0;
+        // listed tiles are visited at the width they were listed with
+        if (a.sup_tiles && a.sup_tb != TB && !(NARROW && a.sup_tb == TBN)) return cudaErrorInvalidValue;
+        if constexpr (NARROW) {
+            // tiles of fft_listed_cols' width: 64-byte rows, promoted to L2
+            // as 64-byte requests
+            if (a.sup_tiles && a.sup_tb == TBN) {
+                if (!a.err || !(sign < 0 ? half_in : half_out)) return cudaErrorInvalidValue;
+                a.ntb = (a.B + TBN - 1) / TBN;
+                if (!encode_strided_map(&map, a, A, batch, TBN, &box_rows, TBN * 8)) return cudaErrorInvalidValue;
+                if (sign < 0) return tma_run<-1, PRUNE_IN, TBN>(a, map, A, batch, box_rows, s);
+                return tma_run<+1, PRUNE_OUT, TBN>(a, map, A, batch, box_rows, s);
+            }
+        }
+        a.ntb = (a.B + TB - 1) / TB;
         if (a.err && encode_strided_map(&map, a, A, batch, TB, &box_rows)) {
-            const bool half_in = 4 * a.in_off == L && 2 * a.Lin == L;
-            const bool half_out = 4 * a.out_off == L && 2 * a.Lout == L;
             if (sign < 0) {
                 if constexpr (HAS_IN)
                     if (half_in) return tma_run<-1, PRUNE_IN>(a, map, A, batch, box_rows, s);

@@ -219,8 +219,17 @@ struct SignFold {
     static constexpr bool value = (R1 % 2 == 0) && (R2 % 2 == 0);
 };
 
+// resident blocks the compiler must allow: 3 (input-pruned, L <= 320) or 2
+// blocks of 256 threads, twice as many of 128 threads
+template <int R1, int R2, int TB, int NSTAGE, int MODE>
+constexpr int strided_tma_min_blocks()
+{
+    constexpr int NT = PipeLayout<R1, R2, TB, NSTAGE>::NT;
+    return ((MODE == PRUNE_IN && R1 * R2 <= 320) ? 3 : 2) * (256 / NT > 1 ? 256 / NT : 1);
+}
+
 template <int R1, int R2, int SIGN, int TB, int NSTAGE, int MODE>
-__global__ void __launch_bounds__(PipeLayout<R1, R2, TB, NSTAGE>::NT, (MODE == PRUNE_IN && R1 * R2 <= 320) ? 3 : 2)
+__global__ void __launch_bounds__(PipeLayout<R1, R2, TB, NSTAGE>::NT, strided_tma_min_blocks<R1, R2, TB, NSTAGE, MODE>())
 k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, long long ntiles,
                   int tiles_per_item, int box_rows)
 {
@@ -371,8 +380,9 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
                     bool done = false;
                     if constexpr (RM) {
                         if (a.sup_rowmask && a.out_off == 0 && a.Lout == L) {
+                            // the x-pass tile of this thread's column (in range: b0 < B)
                             const unsigned* mw = a.sup_rowmask + (item / a.sup_nsub) * a.sup_rowmask_bs +
-                                                 (long long)(b0 / TB) * (L / 32);
+                                                 (long long)((bok ? b : b0) / a.sup_rowmask_tb) * (L / 32);
                             unsigned rm[L / 32];
 #pragma unroll
                             for (int q = 0; q < L / 32; ++q) rm[q] = __ldg(mw + q);

@@ -12,3 +12,12 @@
 
 // columns per tile of the strided passes of a line length L = R1 * R2
 constexpr int fft_strided_tile_cols(int r1, int r2) { return (r1 > r2 ? r1 : r2) > 16 ? 8 : 16; }
+// columns per listed tile of the sample-support-pruned x passes (input-pruned
+// forward, output-pruned adjoint; both need R1 and R2 multiples of 4): 8
+// columns (64-byte rows), so that a listed tile carries fewer columns no
+// sample reaches than a 16-column one
+constexpr bool fft_has_narrow_tiles(int r1, int r2) { return r1 % 4 == 0 && r2 % 4 == 0; }
+constexpr int fft_listed_tile_cols(int r1, int r2)
+{
+    return fft_has_narrow_tiles(r1, r2) ? 8 : fft_strided_tile_cols(r1, r2);
+}

@@ -14,14 +14,21 @@ bool fft_supported(int L);
 // per-device kernel attributes of the FFT passes (dynamic shared memory)
 cudaError_t fft_init_all();
 // 4-D tensor map [batch][A][Lin][B] of a strided pass's input with a
-// TB x box_rows box; false when the buffer or strides are not 16-byte aligned
-bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int batch, int TB, int* box_rows);
+// TB x box_rows box; false when the buffer or strides are not 16-byte aligned.
+// promo: L2 promotion of the box's rows in bytes (64, 128 or 256)
+bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int batch, int TB, int* box_rows,
+                        int promo = 256);
 // 3-D tensor map [nbins][L][B] of 4-byte spectrum values with a TB x
 // box_rows box; false when the buffer or pitch is not 16-byte aligned
 bool encode_spectrum_map(CUtensorMap* map, const float* P, long long B, int L, int nbins, int TB, int* box_rows);
 const int* fft_supported_list(int* n);
 // columns per tile of the strided passes of line length L (0: unsupported)
 int fft_strided_cols(int L);
+// columns per listed tile of the x passes over the sample support of a grid
+// of L points along x holding an image of I points from row lo: the narrow
+// tiles when both x passes run half-pruned (4 lo == L, 2 I == L), else the
+// strided passes' width (0: unsupported)
+int fft_listed_cols(int L, int lo, int I);
 
 // One launch per pass; `batch` items along blockIdx.y.
 cudaError_t launch_strided(int L, int sign, const StridedPassArgs& a, int A, int batch, cudaStream_t s);

@@ -300,7 +300,7 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
 
 // ---------------------------------------------------------------------------
 // The same gather with the matrix staged in shared memory.  Work unit: a
-// slab of CSR_SX consecutive x rows of one listed tile (CSR_SX * tb points,
+// slab of csr_slab_rows(tb) consecutive x rows of one listed tile (CSR_PTS points,
 // consecutive in the matrix, so their row offsets and their taps are two
 // contiguous ranges).  One thread per block issues both ranges of the unit
 // CSR_NST - 1 ahead as bulk copies (cp.async.bulk, completion on an
@@ -313,12 +313,14 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
 // Every wait is bounded: on a timeout the block sets the error flag, lets
 // its issued copies land and leaves.
 // ---------------------------------------------------------------------------
-constexpr int CSR_SX = 64;            // x rows per unit
+constexpr int CSR_PTS = 1024;         // points per unit (64 rows of 16-column tiles)
 constexpr int CSR_CAP = 2048;         // staged taps per unit
 constexpr int CSR_NST = 2;            // pipeline stages
 constexpr unsigned long long CSR_WAIT_NS = 2000000000ull;
 
-__host__ __device__ inline int csr_ptr_stride(int tb) { return ((CSR_SX * tb + 1) + 3) & ~3; }
+// x rows per unit for tiles of tb columns (tb divides CSR_PTS: 4, 8, 16 or 32)
+__host__ __device__ inline int csr_slab_rows(int tb) { return CSR_PTS / tb; }
+__host__ __device__ inline int csr_ptr_stride(int tb) { return ((CSR_PTS + 1) + 3) & ~3; }
 
 static size_t csr_staged_smem(int tb)
 {
@@ -341,7 +343,8 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_s
     const int k = tid % tb;
     const int ch = (tid / tb) % nchunk;
     const int xo = tid / (tb * nchunk), xs = blockDim.x / (tb * nchunk);
-    const unsigned nslab = (unsigned)((a.Gx + CSR_SX - 1) / CSR_SX);
+    const int sx = csr_slab_rows(tb);
+    const unsigned nslab = (unsigned)((a.Gx + sx - 1) / sx);
     const float4* yv4 = reinterpret_cast<const float4*>(a.yv) + ch * (CC / 2);
     const int yv4_stride = a.nch / 2;
     const long long cs = a.coil_stride;
@@ -402,8 +405,8 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_s
     auto issue = [&](int kk) {   // thread 0 only
         const unsigned u = blockIdx.x + (unsigned)kk * gridDim.x;
         const unsigned jt = u / nslab;
-        const int xa = (int)(u - jt * nslab) * CSR_SX;
-        const int nx = min(CSR_SX, a.Gx - xa);
+        const int xa = (int)(u - jt * nslab) * sx;
+        const int nx = min(sx, a.Gx - xa);
         const long long p0 = ((a.j0 + jt) * a.Gx + xa) * tb;
         const int np = nx * tb;
         const unsigned e0a = __ldg(a.ptr + p0) & ~1u, e1 = __ldg(a.ptr + p0 + np);
@@ -438,8 +441,8 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr_s
         }
         const unsigned u = blockIdx.x + (unsigned)kk * gridDim.x;
         const unsigned jt = u / nslab;
-        const int xa = (int)(u - jt * nslab) * CSR_SX;
-        const int nx = min(CSR_SX, a.Gx - xa);
+        const int xa = (int)(u - jt * nslab) * sx;
+        const int nx = min(sx, a.Gx - xa);
         const unsigned* sp = s_ptr + st * PS;
         const int2 t = a.tiles[a.j0 + jt];
         // store pointer of (x = xa + xo, column t.y + k, first coil of the chunk); null: no column
@@ -504,7 +507,8 @@ static cudaError_t spread_csr_staged_run(const CsrSpreadArgs& a, cudaStream_t s)
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spread_csr_staged<CC, KAHAN>, nt, smem);
     if (e != cudaSuccess) return e;
-    const long long nunits = a.nj * ((a.Gx + CSR_SX - 1) / CSR_SX);
+    const int sx = csr_slab_rows(a.tb);
+    const long long nunits = a.nj * ((a.Gx + sx - 1) / sx);
     if (nunits >= 0x7fffffffLL) return cudaErrorInvalidValue;
     const long long nblk = std::min<long long>(nunits, (long long)sm_count_csr() * std::max(per_sm, 1));
     k_spread_csr_staged<CC, KAHAN><<<(unsigned)nblk, nt, smem, s>>>(a, (int)nunits);
@@ -523,7 +527,7 @@ cudaError_t launch_spread_csr(const CsrSpreadArgs& a, bool kahan, bool staged, c
     if (cc == 0) cc = a.nch <= 2 ? 2 : a.nch <= 4 ? 4 : 6;
     // the staged form: an error flag, 16-byte aligned row offsets of every
     // slab (tb a multiple of 4), whole coil chunks of 16-byte coil pairs
-    staged = staged && a.err && (a.tb % 4) == 0 && (reinterpret_cast<uintptr_t>(a.ptr) & 15) == 0 &&
+    staged = staged && a.err && (a.tb % 4) == 0 && (CSR_PTS % a.tb) == 0 && (reinterpret_cast<uintptr_t>(a.ptr) & 15) == 0 &&
              (reinterpret_cast<uintptr_t>(a.ent) & 15) == 0 && (reinterpret_cast<uintptr_t>(a.yv) & 15) == 0 &&
              (cc % 2) == 0 && (a.nch % cc) == 0;
     if (staged) {

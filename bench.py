@@ -288,10 +288,12 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
 def stage_bytes(w, sizes, support=None, matrix=None, y_listed=False):
     """Algorithmic bytes of each stage of one E^H D E application over all
     bins: every stage reads its input and writes its output once.
-    support = (listed columns, stored spreading tiles) per bin, from
-    Reco.support_stats(): with sample-support pruning the x passes move only
-    the listed (y, z) columns, the interpolation reads within them and the
-    spreading stores only the listed tiles.  None: the full grid.
+    support = (listed columns, stored spreading tiles[, the adjoint x pass's
+    listed columns]) per bin, from Reco.support_stats() (and
+    Reco.support_stats_adjoint()): with sample-support pruning the x passes
+    move only their listed (y, z) columns, the interpolation reads within
+    them and the spreading stores only the listed tiles.  None: the full
+    grid.
     matrix = (taps, points) of the transposed tap matrix when the spreading
     is its gather: it stores every point of the listed columns and reads the
     row offsets (4 bytes per point), the taps (8 bytes each) and the coil
@@ -308,7 +310,8 @@ def stage_bytes(w, sizes, support=None, matrix=None, y_listed=False):
         tiles = [Ng // 512] * nb
     else:
         cols, tiles = [int(v) for v in support[0]], [int(v) for v in support[1]]
-    scol, stile = sum(cols), sum(tiles)
+    acols = [int(v) for v in support[2]] if support is not None and len(support) > 2 else cols
+    scol, stile, sacol = sum(cols), sum(tiles), sum(acols)
     return {
         # the coil maps once per application: the z passes run the bins of a
         # line block side by side, so the other bins read the maps from L2
@@ -318,7 +321,7 @@ def stage_bytes(w, sizes, support=None, matrix=None, y_listed=False):
         "interp": C8 * scol * Gx + M * (64 + 4 + C8),
         "spread": (C8 * scol * Gx + 4 * matrix[1] + 8 * matrix[0] + M * C8) if matrix
         else C8 * stile * 512 + M * (64 + C8),   # tiled kernels: 4 x 8 x 16 points per tile
-        "adj_x": C8 * scol * (Gx + Ix),
+        "adj_x": C8 * sacol * (Gx + Ix),
         "adj_y": nb * C8 * (Ix * Gy * Gz + Nl * Gz),
         "adj_z": nb * (C8 * Nl * Gz + 8 * Ni) + C8 * Ni,
     }
@@ -442,6 +445,26 @@ def precision_report(reco, data, x, iters, torch, dev):
             errs.append(float(e.max()))
         out["rel_l2_per_iter_" + name] = errs
         del tr
+        if comp:
+            # the compensated form's own speed: its graph-captured batched
+            # solve, timed like the headline (warm-up replays, then events)
+            stream = torch.cuda.current_stream(dev)
+            xx.zero_()
+            for _ in range(3):
+                reco.cg_sense_batched_tensor(data, xx, 0.0, iters, want_stats=False)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            reps = 5
+            torch.cuda.synchronize(dev)
+            e0.record(stream)
+            for _ in range(reps):
+                reco.cg_sense_batched_tensor(data, xx, 0.0, iters, want_stats=False)
+            e1.record(stream)
+            torch.cuda.synchronize(dev)
+            ms = e0.elapsed_time(e1) / reps
+            out["compensated_s_per_recon"] = ms / 1e3
+            out["compensated_applies_per_s"] = nb * iters / (ms / 1e3)
+        del xx
     reco.set_precision(False)
     out["max_rel_l2_fp32"] = max(out["rel_l2_per_iter_fp32"])
     out["max_rel_l2_compensated"] = max(out["rel_l2_per_iter_compensated"])
@@ -958,7 +981,7 @@ def run_ours(args):
         for _ in range(args.applies_only):
             reco.apply_ehde_tensor(xa, qa, 0, nb)
         torch.cuda.synchronize(dev)
-        support = reco.support_stats()
+        support = reco.support_stats() + (reco.support_stats_adjoint(),)
         taps, points = reco.spread_matrix_stats()
         print(json.dumps({"applies": args.applies_only, "bins": nb, "algorithmic_bytes": stage_bytes(
             w, sizes, support, (taps, points) if taps > 0 else None, reco.forward_y_listed_rows())}))
@@ -1138,7 +1161,7 @@ def run_ours(args):
         rhs_t.append(r0.elapsed_time(r1))
     rhs_ms = float(np.median(rhs_t[1:]))
     del b_rhs
-    support = reco.support_stats()
+    support = reco.support_stats() + (reco.support_stats_adjoint(),)
     taps, points = reco.spread_matrix_stats()
     variant = tune.get("spread_variant") if tune else 6   # the library's default is the gather
     gather = variant in (6, 7) and taps > 0

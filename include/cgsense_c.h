@@ -408,6 +408,12 @@ int cgs_estimate_smaps_d(cgs_ctx* ctx, const void* data, double radius, double e
  * (without pruning: every column, every tile). */
 int cgs_support_stats(cgs_ctx* ctx, int64_t* listed_cols, int64_t* live_tiles);
 
+/* Per bin (cgs_num_bins entries): the (y, z) grid columns the adjoint x
+ * pass transforms.  With pruning it lists narrower tiles than the forward
+ * x pass (8 columns where the grid is twice the image along x), each inside
+ * a forward tile; without pruning: every column. */
+int cgs_support_stats_adjoint(cgs_ctx* ctx, int64_t* listed_cols);
+
 /* 1 when the forward y pass stores only the rows of the x pass's listed
  * tiles (sample-support pruning on and the passes' column tiles coincide),
  * else 0. */

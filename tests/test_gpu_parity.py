@@ -262,8 +262,10 @@ def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, g
                                           # x passes with 8-column tiles (L = 320), Gz % 16 != 0
                                           ((160, 16, 12), (320, 32, 24), 3),
                                           ((48, 40, 24), (96, 80, 48), 4),
-                                          # x and y tiles coincide: the forward y pass stores listed rows only
-                                          ((32, 32, 16), (64, 64, 32), 3)])
+                                          # the forward y pass stores listed rows only
+                                          ((32, 32, 16), (64, 64, 32), 3),
+                                          # listed rows with 8-column x tiles inside 16-column y tiles
+                                          ((32, 32, 20), (64, 64, 40), 3)])
 def test_support_pruning_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid, nch):
     """Sample-support pruning (x passes over the supported column tiles only,
     masked y passes, spreading tiles of supported columns only) leaves every
