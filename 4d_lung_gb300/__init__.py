@@ -56,7 +56,7 @@ EXPORTS = [
     "cgs_rhs_vjp_k_d", "cgs_trajectory_serial", "cgs_get_stream", "cgs_import_data_bin", "cgs_permute_samples_d",
     "cgs_export_complex_bin", "cgs_export_float_bin", "cgs_import_smaps_bin", "cgs_import_density_bin", "cgs_rss_d",
     "cgs_reconstruct_states", "cgs_pipe_menon_dcf", "cgs_set_deterministic", "cgs_set_launch_shape",
-    "cgs_set_support_pruning", "cgs_support_stats", "cgs_support_stats_adjoint", "cgs_spread_matrix_stats", "cgs_estimate_smaps_d",
+    "cgs_set_support_pruning", "cgs_support_stats", "cgs_spread_matrix_stats", "cgs_spread_fused", "cgs_estimate_smaps_d",
     "cgs_forward_y_listed_rows", "cgs_set_toeplitz", "cgs_toeplitz_stats", "cgs_setup_stats", "cgs_e2e_stats", "cgs_set_toeplitz_spectrum", "cgs_toeplitz_spectrum_method",
 ]
 
@@ -180,8 +180,8 @@ def lib():
         "cgs_set_launch_shape": (C.c_int, [vp, C.c_int32, C.c_int32, C.c_int32]),
         "cgs_set_support_pruning": (C.c_int, [vp, C.c_int32]),
         "cgs_support_stats": (C.c_int, [vp, vp, vp]),
-        "cgs_support_stats_adjoint": (C.c_int, [vp, vp]),
         "cgs_spread_matrix_stats": (C.c_int, [vp, vp, vp]),
+        "cgs_spread_fused": (C.c_int, [vp, vp]),
         "cgs_forward_y_listed_rows": (C.c_int, [vp, vp]),
         "cgs_set_toeplitz": (C.c_int, [vp, C.c_int32]),
         "cgs_toeplitz_stats": (C.c_int, [vp, vp, vp]),
@@ -573,13 +573,6 @@ class Reco:
         self._check(self._L.cgs_support_stats(self._ctx, _p(cols), _p(live)))
         return cols, live
 
-    def support_stats_adjoint(self):
-        """Per bin: grid (y, z) columns the adjoint x pass transforms (see
-        cgs_support_stats_adjoint)."""
-        cols = np.zeros(self.num_bins(), np.int64)
-        self._check(self._L.cgs_support_stats_adjoint(self._ctx, _p(cols)))
-        return cols
-
     def estimate_smaps_tensor(self, data, maps, radius, eps=0.05):
         """Coil maps from low-resolution coil images (see cgs_estimate_smaps_d):
         data complex64 [n_ch][ns], maps complex64 [n_ch][img], device tensors."""
@@ -639,6 +632,13 @@ class Reco:
         p = np.zeros(1, np.int64)
         self._check(self._L.cgs_spread_matrix_stats(self._ctx, _p(t), _p(p)))
         return int(t[0]), int(p[0])
+
+    def spread_fused(self):
+        """True when the last application ran the spreading fused with the
+        adjoint x pass (see cgs_spread_fused)."""
+        v = np.zeros(1, np.int32)
+        self._check(self._L.cgs_spread_fused(self._ctx, _p(v)))
+        return bool(v[0])
 
     def set_deterministic(self, on):
         """Fixed summation order (default); off lets the autotuner pick

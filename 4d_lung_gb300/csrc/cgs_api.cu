@@ -6,6 +6,7 @@
 // the reference functions each one stands for.
 #include "cgsense_c.h"
 #include "launch.h"
+#include "fft_sizes.h"
 
 #include <algorithm>
 #include <chrono>
@@ -106,10 +107,12 @@ struct cgs_ctx {
     // launch shapes (cgs_autotune): coils per spreading block (0: as many as
     // fit), coils per interpolation thread
     int spread_cc = 0;
-    int spread_wpp = 6;          // spreading variant: warps per x plane 1 / 2, 3 atomics, 4 / 5 pipelined,
+    int spread_wpp = 8;          // spreading variant: warps per x plane 1 / 2, 3 atomics, 4 / 5 pipelined,
                                  // 6 / 7 gather over the transposed tap matrix, staged in shared memory /
-                                 // read from global memory (2 when it is not built)
+                                 // read from global memory (2 when it is not built), 8 the staged gather
+                                 // fused with the adjoint x pass (6 where that does not apply)
     bool deterministic = true;   // fixed summation order everywhere (cgs_set_deterministic)
+    bool spread_fused = false;   // the last adjoint half ran the fused spreading + x pass
     int interp_cc = 4;
     bool k_host_stale = false;   // d_k updated on the device (cgs_update_trajectory_d)
     uint64_t traj_serial = 0;    // incremented whenever the coordinates change
@@ -125,10 +128,16 @@ struct cgs_ctx {
     // built when the x and y passes' column tiles coincide
     DevBuf d_sup_rowmask;
     long long sup_rowmask_bs = 0;            // words per bin (0: not built)
-    int sup_tb = 0;                          // columns per listed tile: forward x pass, spreading
-    int sup_tb_adj = 0;                      // columns per listed tile: adjoint x pass (fft_listed_cols)
-    std::vector<long long> h_sup_off_adj;    // per bin: first entry in d_sup_tiles_adj
-    DevBuf d_sup_tiles_adj;                  // the adjoint x pass's listed tiles {bin, first column}
+    int sup_tb = 0;                          // columns per listed x-pass tile (fft_listed_cols)
+    // the spreading gather's listing (variants 6, 7): tiles of the strided
+    // passes' width, each a union of x-pass tiles, so that it stores every
+    // column the adjoint x pass reads, in 128-byte rows
+    int spr_tb = 0;
+    std::vector<long long> h_spr_off;
+    std::vector<int2> h_spr_tiles;
+    DevBuf d_spr_tiles;
+    int csr_list = -1;                       // listing of the transposed tap matrix: 0 the spreading's,
+                                             // 1 the x passes' (fused variant 8); -1 not built
     // transposed tap matrix of the listed tiles' points (spreading variant 6)
     bool csr_valid = false;
     long long csr_pts = 0;
@@ -277,7 +286,7 @@ struct BinPrep {
     std::vector<int> tile_idx;
     std::vector<int> plane_rng;   // [ntiles][TILE_X][2]
     std::vector<int> sup_cols;        // first column of each x-pass tile the samples touch
-    std::vector<int> sup_cols_adj;    // the same for the adjoint x pass's (narrower) tiles
+    std::vector<int> spr_cols;        // the same for the spreading gather's wider tiles
     std::vector<int> live;            // spreading tiles holding a supported column
 };
 
@@ -382,7 +391,7 @@ void tile_lists(const cgs_ctx* c, const unsigned* nearest, long long n, BinPrep&
 // columns of the flattened [Gy][Gz] plane: the tiles holding a supported
 // column are listed (sup_cols); the spreading stores the grid tiles whose
 // (y, z) extent meets a listed column (live).
-void support_lists(const cgs_ctx* c, const unsigned* nearest, long long n, int tb, int tb_adj, BinPrep& out)
+void support_lists(const cgs_ctx* c, const unsigned* nearest, long long n, int tb, int tbs, BinPrep& out)
 {
     const int Gy = c->G[1], Gz = c->G[2];
     const long long ncol = (long long)Gy * Gz;
@@ -404,15 +413,13 @@ void support_lists(const cgs_ctx* c, const unsigned* nearest, long long n, int t
         out.sup_cols.push_back((int)b0);
         for (long long b = b0; b < b1; ++b) listed[b] = 1;
     }
-    // the adjoint x pass reads the grid only where a sample reaches: its own
-    // tiles, each inside a listed forward tile (tb_adj divides tb), so that
-    // the spreading has stored every column it reads
-    out.sup_cols_adj.clear();
-    for (long long b0 = 0; b0 < ncol; b0 += tb_adj) {
-        const long long b1 = std::min(ncol, b0 + tb_adj);
+    // the spreading gather's tiles (tb divides tbs)
+    out.spr_cols.clear();
+    for (long long b0 = 0; b0 < ncol; b0 += tbs) {
+        const long long b1 = std::min(ncol, b0 + tbs);
         bool any = false;
         for (long long b = b0; b < b1 && !any; ++b) any = col[b] != 0;
-        if (any) out.sup_cols_adj.push_back((int)b0);
+        if (any) out.spr_cols.push_back((int)b0);
     }
     // spreading tiles whose (y, z) extent holds a masked column: the adjoint
     // x pass reads those columns at every x, so these tiles are stored (with
@@ -440,25 +447,28 @@ int upload(cgs_ctx* c, DevBuf& b, const void* h, size_t bytes)
     return CGS_OK;
 }
 
-// The transposed tap matrix over the points of the listed x-pass tiles
-// (spreading variant 6), from the current tap records and support lists.
-// Skipped (variant 6 then falls back to the tiled kernel) when the counts
-// could overflow 32-bit offsets.
-int build_csr(cgs_ctx* c)
+// The transposed tap matrix over the points of the listed tiles of the
+// spreading gather (list 0, variants 6 and 7) or of the x passes (list 1,
+// the gather fused with the adjoint x pass), from the current tap records
+// and support lists.  Skipped (the gather variants then fall back to the
+// tiled kernel) when the counts could overflow 32-bit offsets.
+int build_csr(cgs_ctx* c, int list)
 {
     c->csr_valid = false;
+    c->csr_list = -1;
     c->csr_entries = 0;
     if (!c->sup_built || c->total == 0) return CGS_OK;
-    const int tbx = c->sup_tb;
+    const int tbx = list == 1 ? c->sup_tb : c->spr_tb;
+    const std::vector<long long>& off = list == 1 ? c->h_sup_off : c->h_spr_off;
+    const std::vector<int2>& tl = list == 1 ? c->h_sup_tiles : c->h_spr_tiles;
     const long long ncol = (long long)c->G[1] * c->G[2];
-    const long long ntl = c->h_sup_off[c->nbins];
+    const long long ntl = off[c->nbins];
     const long long npts = ntl * c->G[0] * tbx;
     if (npts <= 0 || (unsigned long long)c->total * 125ull >= 0xffffffffull || npts + 1 >= 0x7fffffffLL) return CGS_OK;
     std::vector<int> ct((size_t)c->nbins * ncol, -1);
     for (int b = 0; b < c->nbins; ++b)
-        for (long long J = c->h_sup_off[b]; J < c->h_sup_off[b + 1]; ++J)
-            for (int k = 0; k < tbx && c->h_sup_tiles[J].y + k < ncol; ++k)
-                ct[(size_t)b * ncol + c->h_sup_tiles[J].y + k] = (int)J;
+        for (long long J = off[b]; J < off[b + 1]; ++J)
+            for (int k = 0; k < tbx && tl[J].y + k < ncol; ++k) ct[(size_t)b * ncol + tl[J].y + k] = (int)J;
     CGS_TRY(upload(c, c->d_col_tile, ct.data(), ct.size() * sizeof(int)));
     const size_t tmp = csr_scan_tmp_elems(npts + 1);
     CGS_CUDA(c, c->d_csr_cnt.ensure((size_t)(npts + 1) * sizeof(unsigned)));
@@ -493,7 +503,31 @@ int build_csr(cgs_ctx* c)
     c->csr_pts = npts;
     c->csr_entries = ne;
     c->csr_valid = true;
+    c->csr_list = list;
     return CGS_OK;
+}
+
+void drop_graphs(cgs_ctx* c);
+
+// The fused spreading + adjoint x pass (variant 8) applies: listed x-pass
+// tiles of 8 columns, both x passes half-pruned, a coil chunk (2, 4, 6) that
+// divides the coil count
+bool fused_spread_applies(const cgs_ctx* c)
+{
+    if (c->sup_tb != SAX_TB || 4 * c->lo[0] != c->G[0] || 2 * c->I[0] != c->G[0] || c->nch % 2 != 0) return false;
+    const int cc = c->spread_cc;
+    return !(cc == 2 || cc == 4 || cc == 6) || c->nch % cc == 0;
+}
+
+// The transposed tap matrix over the listing the current spreading variant
+// reads (rebuilt, and the captured graphs dropped, when it changes)
+int ensure_csr(cgs_ctx* c)
+{
+    if (!c->sup_built) return CGS_OK;
+    const int want = (c->spread_wpp == 8 && fused_spread_applies(c)) ? 1 : 0;
+    if (c->csr_list == want && c->csr_valid) return CGS_OK;
+    drop_graphs(c);
+    return build_csr(c, want);
 }
 
 void drop_graphs(cgs_ctx* c)
@@ -563,36 +597,39 @@ int rebuild_bins(cgs_ctx* c)
     }
     c->setup_ms[1] = ms_since(t0);
     t0 = clk::now();
-    const int tbx = fft_strided_cols(c->G[0]);
-    int tba = fft_listed_cols(c->G[0], c->lo[0], c->I[0]);
-    if (tba <= 0 || tbx % tba != 0) tba = tbx;
+    // the x passes' tiles: 8 columns (64-byte rows) where both passes run
+    // half-pruned, else the strided passes' width
+    const int tbx = fft_listed_cols(c->G[0], c->lo[0], c->I[0]);
+    int tbs = fft_strided_cols(c->G[0]);
+    if (tbx <= 0 || tbs % tbx != 0) tbs = tbx;
     c->sup_tb = tbx;
-    c->sup_tb_adj = tba;
+    c->spr_tb = tbs;
 #pragma omp parallel for schedule(dynamic, 1)
     for (int b = 0; b < c->nbins; ++b) {
         tile_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], prep[b]);
         if (tbx > 0)
-            support_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], tbx, tba,
+            support_lists(c, nearest.data() + c->h_bin_off[b], c->h_bin_off[b + 1] - c->h_bin_off[b], tbx, tbs,
                           prep[b]);
     }
     c->sup_built = false;
     c->h_sup_off.assign(c->nbins + 1, 0);
-    c->h_sup_off_adj.assign(c->nbins + 1, 0);
+    c->h_spr_off.assign(c->nbins + 1, 0);
     if (tbx > 0) {
-        std::vector<int2> tiles, tiles_adj;
+        std::vector<int2> tiles, spr;
         std::vector<int> live;
         c->h_live_off.assign(c->nbins + 1, 0);
         for (int b = 0; b < c->nbins; ++b) {
             for (int b0 : prep[b].sup_cols) tiles.push_back(make_int2(b, b0));
             c->h_sup_off[b + 1] = (long long)tiles.size();
-            for (int b0 : prep[b].sup_cols_adj) tiles_adj.push_back(make_int2(b, b0));
-            c->h_sup_off_adj[b + 1] = (long long)tiles_adj.size();
+            for (int b0 : prep[b].spr_cols) spr.push_back(make_int2(b, b0));
+            c->h_spr_off[b + 1] = (long long)spr.size();
             live.insert(live.end(), prep[b].live.begin(), prep[b].live.end());
             c->h_live_off[b + 1] = (long long)live.size();
         }
         CGS_TRY(upload(c, c->d_sup_tiles, tiles.data(), std::max<size_t>(tiles.size(), 1) * sizeof(int2)));
         c->h_sup_tiles = tiles;
-        CGS_TRY(upload(c, c->d_sup_tiles_adj, tiles_adj.data(), std::max<size_t>(tiles_adj.size(), 1) * sizeof(int2)));
+        CGS_TRY(upload(c, c->d_spr_tiles, spr.data(), std::max<size_t>(spr.size(), 1) * sizeof(int2)));
+        c->h_spr_tiles = spr;
         CGS_TRY(upload(c, c->d_live, live.data(), std::max<size_t>(live.size(), 1) * sizeof(int)));
         CGS_TRY(upload(c, c->d_live_off, c->h_live_off.data(), c->h_live_off.size() * sizeof(long long)));
         c->sup_built = true;
@@ -616,7 +653,8 @@ int rebuild_bins(cgs_ctx* c)
     CGS_CUDA(c, cudaStreamSynchronize(c->stream));
     c->setup_ms[2] = ms_since(t0);
     t0 = clk::now();
-    CGS_TRY(build_csr(c));
+    c->csr_list = -1;
+    CGS_TRY(ensure_csr(c));
     c->setup_ms[3] = ms_since(t0);
     t0 = clk::now();
     std::vector<int> tile_ptr;
@@ -687,14 +725,12 @@ int prepare_adj_slots(cgs_ctx* c, int b0, int nb, bool pruned)
     return CGS_OK;
 }
 
-// x pass over bins [b0, b0 + nb): only the listed tiles (the forward
-// pass's, or the adjoint pass's narrower ones)
-void set_support_tiles(const cgs_ctx* c, StridedPassArgs& a, int b0, int nb, bool adjoint)
+// x pass over bins [b0, b0 + nb): only the listed tiles
+void set_support_tiles(const cgs_ctx* c, StridedPassArgs& a, int b0, int nb)
 {
-    const std::vector<long long>& off = adjoint ? c->h_sup_off_adj : c->h_sup_off;
-    a.sup_tiles = (adjoint ? c->d_sup_tiles_adj : c->d_sup_tiles).as<int2>() + off[b0];
-    a.sup_ntiles = off[b0 + nb] - off[b0];
-    a.sup_tb = adjoint ? c->sup_tb_adj : c->sup_tb;
+    a.sup_tiles = c->d_sup_tiles.as<int2>() + c->h_sup_off[b0];
+    a.sup_ntiles = c->h_sup_off[b0 + nb] - c->h_sup_off[b0];
+    a.sup_tb = c->sup_tb;
     a.sup_bin0 = b0;
     a.sup_nsub = c->nch;
 }
@@ -779,7 +815,7 @@ int fwd_chain(cgs_ctx* c, int b0, int nb, const float2* x, long long x_bs, long 
     fx.out_off = 0;
     fx.err = c->d_err.as<int>();
     fx.tw = c->tw[0].as<float2>();
-    if (sup) set_support_tiles(c, fx, b0, nb, false);
+    if (sup) set_support_tiles(c, fx, b0, nb);
     CGS_LAUNCH(c, launch_strided(Gx, -1, fx, 1, nb * c->nch, c->stream));
 
     InterpArgs ia{};
@@ -840,7 +876,42 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
             for (int b = b0; b < b0 + nb; ++b)
                 sa.live_max = (int)std::max<long long>(sa.live_max, c->h_live_off[b + 1] - c->h_live_off[b]);
         }
-        if (sup && (c->spread_wpp == 6 || c->spread_wpp == 7) && c->csr_valid) {
+        // variant 8: the gather fused with the adjoint x pass (the listed
+        // tiles of 8 columns of a half-pruned x pass); where it does not
+        // apply, the staged gather and the x pass run as variant 6
+        bool fused = false;
+        if (sup && c->spread_wpp == 8 && c->csr_valid && c->csr_list == 1 && fused_spread_applies(c)) {
+            CGS_TRY(prepare_adj_slots(c, b0, nb, sup));
+            SpreadAdjxArgs fa{};
+            fa.ptr = c->d_csr_ptr.as<unsigned>();
+            fa.ent = c->d_csr_ent.as<int2>();
+            fa.yv = c->d_yv.as<float2>();
+            fa.tiles = c->d_sup_tiles.as<int2>();
+            fa.j0 = c->h_sup_off[b0];
+            fa.nj = c->h_sup_off[b0 + nb] - c->h_sup_off[b0];
+            fa.bin0 = b0;
+            fa.nch = c->nch;
+            fa.B = (long long)Gy * Gz;
+            fa.cc = (c->spread_cc == 2 || c->spread_cc == 4 || c->spread_cc == 6) ? c->spread_cc : 0;
+            fa.out = c->d_ybuf_adj.as<float2>();
+            fa.out_bs = yb;
+            fa.tw = c->tw[0].as<float2>();
+            fa.err = c->d_err.as<int>();
+            const cudaError_t e = launch_spread_adjx(Gx, fa, c->kahan, c->stream);
+            if (e == cudaSuccess) {
+                ++c->launches;
+                if (c->prof_ev) CGS_CUDA(c, cudaEventRecord(c->prof_ev[c->prof_n++], c->stream));
+                fused = true;
+            } else if (e == cudaErrorNotSupported) {
+                cudaGetLastError();
+            } else {
+                CGS_CUDA(c, e);
+            }
+        }
+        c->spread_fused = fused;
+        if (fused) {
+            // the adjoint y pass reads what the fused kernel stored
+        } else if (sup && c->spread_wpp >= 6 && c->csr_valid) {
             // gather over the transposed tap matrix: stores the listed tiles' points
             CsrSpreadArgs ca{};
             ca.grid = c->d_grid.as<float2>();
@@ -849,19 +920,22 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
             ca.ptr = c->d_csr_ptr.as<unsigned>();
             ca.ent = c->d_csr_ent.as<int2>();
             ca.yv = c->d_yv.as<float2>();
-            ca.tiles = c->d_sup_tiles.as<int2>();
-            ca.j0 = c->h_sup_off[b0];
-            ca.nj = c->h_sup_off[b0 + nb] - c->h_sup_off[b0];
+            // the listing the matrix was built on
+            const bool xl = c->csr_list == 1;
+            const std::vector<long long>& off = xl ? c->h_sup_off : c->h_spr_off;
+            ca.tiles = (xl ? c->d_sup_tiles : c->d_spr_tiles).as<int2>();
+            ca.j0 = off[b0];
+            ca.nj = off[b0 + nb] - off[b0];
             ca.bin0 = b0;
             ca.nch = c->nch;
             ca.Gx = Gx;
             ca.B = (long long)Gy * Gz;
-            ca.tb = c->sup_tb;
+            ca.tb = xl ? c->sup_tb : c->spr_tb;
             ca.cc = c->spread_cc;   // coils per thread of the gather (0: by the coil count)
             if (ca.cc != 2 && ca.cc != 4 && ca.cc != 6 && ca.cc != 8) ca.cc = 0;
             ca.err = c->d_err.as<int>();
-            // variant 6: the matrix staged in shared memory; 7: read from global memory
-            CGS_LAUNCH(c, launch_spread_csr(ca, c->kahan, c->spread_wpp == 6, c->stream));
+            // variants 6 (and 8): the matrix staged in shared memory; 7: read from global memory
+            CGS_LAUNCH(c, launch_spread_csr(ca, c->kahan, c->spread_wpp != 7, c->stream));
         } else {
             // variants 6 / 7 without their matrix: the two-warps-per-plane tiled kernel
             const int wpp = c->spread_wpp >= 6 ? 2 : c->spread_wpp;
@@ -869,21 +943,23 @@ int adj_chain(cgs_ctx* c, int b0, int nb, float2* q, long long q_bs, bool use_sm
             CGS_LAUNCH(c, launch_spread(sa, c->ntiles, nb, c->kahan, wpp, c->stream));
         }
 
-        CGS_TRY(prepare_adj_slots(c, b0, nb, sup));
-        StridedPassArgs ax{};
-        ax.in = c->d_grid.as<float2>();
-        ax.out = c->d_ybuf_adj.as<float2>();
-        ax.in_bs = c->Ng;
-        ax.out_bs = yb;
-        ax.B = Gy * Gz;
-        ax.Lin = Gx;
-        ax.in_off = 0;
-        ax.Lout = Ix;
-        ax.out_off = c->lo[0];
-        ax.err = c->d_err.as<int>();
-        ax.tw = c->tw[0].as<float2>();
-        if (sup) set_support_tiles(c, ax, b0, nb, true);
-        CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
+        if (!fused) {
+            CGS_TRY(prepare_adj_slots(c, b0, nb, sup));
+            StridedPassArgs ax{};
+            ax.in = c->d_grid.as<float2>();
+            ax.out = c->d_ybuf_adj.as<float2>();
+            ax.in_bs = c->Ng;
+            ax.out_bs = yb;
+            ax.B = Gy * Gz;
+            ax.Lin = Gx;
+            ax.in_off = 0;
+            ax.Lout = Ix;
+            ax.out_off = c->lo[0];
+            ax.err = c->d_err.as<int>();
+            ax.tw = c->tw[0].as<float2>();
+            if (sup) set_support_tiles(c, ax, b0, nb);
+            CGS_LAUNCH(c, launch_strided(Gx, +1, ax, 1, nb * c->nch, c->stream));
+        }
     }
 
     StridedPassArgs ay{};
@@ -2366,16 +2442,19 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
     }
     float best = 1e30f;
     int best_sc = sc[0], best_wpp = 1;
-    for (int wpp : {1, 2, 4, 5, 3, 7, 6}) {
+    for (int wpp : {1, 2, 4, 5, 3, 7, 6, 8}) {
         if (wpp == 3 && (c->deterministic || c->kahan)) continue;
         if ((wpp == 4 || wpp == 5) && c->kahan) continue;
-        if (wpp >= 6 && !(c->csr_valid && support_pruned(c))) continue;
-        // the gather's shape parameter is its coils per thread
-        const std::vector<int> cand = wpp >= 6 ? std::vector<int>{4, 6, 8} : sc;
+        if (wpp >= 6 && !support_pruned(c)) continue;
+        // the gather's shape parameter is its coils per thread (per block when fused)
+        const std::vector<int> cand = wpp == 8 ? std::vector<int>{2, 4, 6} : wpp >= 6 ? std::vector<int>{4, 6, 8} : sc;
         for (int v : cand) {
             if (wpp == 2 && v < 2) continue;
+            if (wpp == 8 && c->nch % v != 0) continue;
             c->spread_cc = v;
             c->spread_wpp = wpp;
+            CGS_TRY(ensure_csr(c));
+            if (wpp >= 6 && !c->csr_valid) continue;
             float ms;
             CGS_TRY(time_apply(ms));
             if (ms < best) {
@@ -2387,6 +2466,7 @@ int cgs_autotune(cgs_ctx* c, float* times_ms, int32_t max_times, int32_t* n_time
     }
     c->spread_wpp = best_wpp;
     c->spread_cc = best_sc;
+    CGS_TRY(ensure_csr(c));
     best = 1e30f;
     int best_ic = c->interp_cc;
     for (int v : {1, 2, 4, 6, 8}) {
@@ -2747,23 +2827,19 @@ int cgs_support_stats(cgs_ctx* c, int64_t* listed_cols, int64_t* live_tiles)
     return CGS_OK;
 }
 
-int cgs_support_stats_adjoint(cgs_ctx* c, int64_t* listed_cols)
-{
-    CGS_TRY(check_ready(c, false));
-    if (!listed_cols) return fail(c, CGS_ERR_ARG, "null pointer");
-    const bool sup = support_pruned(c);
-    const long long ncol = (long long)c->G[1] * c->G[2];
-    for (int b = 0; b < c->nbins; ++b)
-        listed_cols[b] = sup ? std::min(ncol, (c->h_sup_off_adj[b + 1] - c->h_sup_off_adj[b]) * (long long)c->sup_tb_adj)
-                             : ncol;
-    return CGS_OK;
-}
-
 int cgs_forward_y_listed_rows(cgs_ctx* c, int32_t* listed)
 {
     CGS_TRY(check_ready(c, false));
     if (!listed) return fail(c, CGS_ERR_ARG, "null pointer");
     *listed = (support_pruned(c) && c->sup_rowmask_bs > 0) ? 1 : 0;
+    return CGS_OK;
+}
+
+int cgs_spread_fused(cgs_ctx* c, int32_t* fused)
+{
+    CGS_TRY(check_ready(c, false));
+    if (!fused) return fail(c, CGS_ERR_ARG, "null pointer");
+    *fused = c->spread_fused ? 1 : 0;
     return CGS_OK;
 }
 
@@ -2803,7 +2879,7 @@ int cgs_set_launch_shape(cgs_ctx* c, int32_t spread_cc, int32_t spread_variant, 
 {
     if (!c) return CGS_ERR_ARG;
     if (spread_cc < 0 || spread_cc > spread_max_coils(c->kahan)) return fail(c, CGS_ERR_ARG, "spread_cc out of range");
-    if (spread_variant < 1 || spread_variant > 7 || (spread_variant >= 3 && spread_variant <= 5 && c->kahan) ||
+    if (spread_variant < 1 || spread_variant > 8 || (spread_variant >= 3 && spread_variant <= 5 && c->kahan) ||
         (spread_variant == 3 && c->deterministic))
         return fail(c, CGS_ERR_ARG, "spreading variant not allowed here");
     if (interp_cc != 1 && interp_cc != 2 && interp_cc != 4 && interp_cc != 6 && interp_cc != 8)
@@ -2812,7 +2888,7 @@ int cgs_set_launch_shape(cgs_ctx* c, int32_t spread_cc, int32_t spread_variant, 
     c->spread_wpp = spread_variant;
     c->interp_cc = interp_cc;
     drop_graphs(c);
-    return CGS_OK;
+    return ensure_csr(c);
 }
 
 }  // extern "C"

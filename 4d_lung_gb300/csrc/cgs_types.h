@@ -208,6 +208,27 @@ struct CsrSpreadArgs {
     int* err;                  // error flag (a bounded wait of the staged form ran out)
 };
 
+// Spreading fused with the adjoint x pass (spread_adjx.cuh): the gather of
+// CsrSpreadArgs over listed tiles of 8 columns and Gx = L rows (grid and
+// coil_stride unused), then the output-pruned x transform into the adjoint
+// y pass's input: coil c of bin slot s at out + (s * nch + c) * out_bs, row
+// l - L/4 of column b at (l - L/4) * B + b.
+struct SpreadAdjxArgs {
+    const unsigned* ptr;       // [P + 1] (+ 16-byte padding)
+    const int2* ent;
+    const float2* yv;          // [total samples][nch]
+    const int2* tiles;         // listed tiles {bin, first column}, global index
+    long long j0, nj;          // the tiles of this launch: [j0, j0 + nj)
+    int bin0;                  // bin of workspace slot 0
+    int nch;
+    long long B;               // Gy * Gz
+    int cc;                    // coils per block (2, 4, 6; 0: by the coil count)
+    float2* out;
+    long long out_bs;
+    const float2* tw;          // L twiddles
+    int* err;
+};
+
 // Toeplitz embedding (toeplitz.cu): the spectrum P of one bin's point-spread
 // function, from sorted samples [s0, s0 + n).
 struct ToepBuildArgs {

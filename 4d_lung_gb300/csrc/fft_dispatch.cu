@@ -13,7 +13,8 @@ namespace cgs {
     int fft_adj_blocks_##L_(long long nl);                                                             \
     cudaError_t fft_init_##L_();                                                                       \
     cudaError_t fft_toep_x_##L_(const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch, \
-                                cudaStream_t s);
+                                cudaStream_t s);                                                       \
+    cudaError_t fft_spread_adjx_##L_(const SpreadAdjxArgs& a, bool kahan, cudaStream_t s);
 CGS_FFT_SIZES(CGS_DECLARE)
 
 static const int kSizes[] = {
@@ -192,6 +193,17 @@ cudaError_t launch_toep_x(int L, const StridedPassArgs& a, const float* P, long 
 {
     switch (L) {
 #define CGS_CASE(L_, R1_, R2_, G_) case L_: return fft_toep_x_##L_(a, P, p_bs, nsub, batch, s);
+        CGS_FFT_SIZES(CGS_CASE)
+#undef CGS_CASE
+    }
+    return cudaErrorNotSupported;
+}
+
+cudaError_t launch_spread_adjx(int L, const SpreadAdjxArgs& a, bool kahan, cudaStream_t s)
+{
+    if (a.nj <= 0) return cudaSuccess;
+    switch (L) {
+#define CGS_CASE(L_, R1_, R2_, G_) case L_: return fft_spread_adjx_##L_(a, kahan, s);
         CGS_FFT_SIZES(CGS_CASE)
 #undef CGS_CASE
     }

@@ -3,6 +3,7 @@
 #include "fft_sizes.h"
 #include "launch.h"
 #include "fft_passes.cuh"
+#include "spread_adjx.cuh"
 
 #ifndef CGS_FFT_GROUP
 #define CGS_FFT_GROUP 0
@@ -55,10 +56,14 @@ struct SizeImpl {
     static constexpr bool NARROW = HAS_IN && HAS_OUT && TBN != TB;
     static_assert(!(HAS_IN && HAS_OUT) || fft_has_narrow_tiles(R1, R2), "listed width and pruned forms agree");
 
-    template <int SIGN, int MODE, int TBK = TB>
+    // pipeline stages of the narrow forward pass: its stages hold half as
+    // many bytes (Ix rows of 64 bytes), so one more keeps as many in flight
+    static constexpr int NSTAGE_NI = 3;
+
+    template <int SIGN, int MODE, int TBK = TB, int NS = NSTAGE>
     static cudaError_t tma_attr(int smem)
     {
-        return cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, SIGN, TBK, NSTAGE, MODE>,
+        return cudaFuncSetAttribute(k_fft_strided_tma<R1, R2, SIGN, TBK, NS, MODE>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     }
 
@@ -72,15 +77,24 @@ struct SizeImpl {
         if constexpr (HAS_OUT)
             if (e == cudaSuccess) e = tma_attr<+1, PRUNE_OUT>(smem);
         if constexpr (NARROW) {
-            const int smem_n = (int)PipeLayout<R1, R2, TBN, NSTAGE>::smem_bytes(L);
-            if (e == cudaSuccess) e = tma_attr<-1, PRUNE_IN, TBN>(smem_n);
-            if (e == cudaSuccess) e = tma_attr<+1, PRUNE_OUT, TBN>(smem_n);
+            if (e == cudaSuccess)
+                e = tma_attr<-1, PRUNE_IN, TBN, NSTAGE_NI>((int)PipeLayout<R1, R2, TBN, NSTAGE_NI>::smem_bytes(L));
+            if (e == cudaSuccess)
+                e = tma_attr<+1, PRUNE_OUT, TBN>((int)PipeLayout<R1, R2, TBN, NSTAGE>::smem_bytes(L));
         }
         if constexpr (HAS_IN)
             if (e == cudaSuccess)
                 e = cudaFuncSetAttribute(k_toep_x_tma<R1, R2, TBT, NSTAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)ToepLayout<R1, R2, TBT, NSTAGE>::smem_bytes(L / 2));
         // the z extent of an image never exceeds the grid's: size for Iz = L
+        if constexpr (HAS_IN && HAS_OUT) {
+            if (e == cudaSuccess) e = sax_attr<2, false>();
+            if (e == cudaSuccess) e = sax_attr<2, true>();
+            if (e == cudaSuccess) e = sax_attr<4, false>();
+            if (e == cudaSuccess) e = sax_attr<4, true>();
+            if (e == cudaSuccess) e = sax_attr<6, false>();
+            if (e == cudaSuccess) e = sax_attr<6, true>();
+        }
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_fwd_z_pipe<R1, R2, LPB, ZNST_F, false>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ZF::smem_bytes(L, false));
@@ -96,22 +110,22 @@ struct SizeImpl {
     static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
     // persistent launch: as many blocks as fit, at most one per tile
-    template <int SIGN, int MODE, int TBK = TB>
+    template <int SIGN, int MODE, int TBK = TB, int NS = NSTAGE>
     static cudaError_t tma_run(const StridedPassArgs& a, const CUtensorMap& map, int A, int batch, int box_rows,
                                cudaStream_t s)
     {
-        using P = PipeLayout<R1, R2, TBK, NSTAGE>;
+        using P = PipeLayout<R1, R2, TBK, NS>;
         const size_t smem = P::smem_bytes(a.Lin);
         int per_sm = 0;
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_fft_strided_tma<R1, R2, SIGN, TBK, NSTAGE, MODE>, P::NT, smem);
+            &per_sm, k_fft_strided_tma<R1, R2, SIGN, TBK, NS, MODE>, P::NT, smem);
         if (e != cudaSuccess) return e;
         const long long tiles_per_item = (long long)A * a.ntb;
         const long long ntiles = a.sup_tiles ? a.sup_ntiles * a.sup_nsub : tiles_per_item * batch;
         if (ntiles <= 0) return cudaSuccess;   // no listed tile: nothing to transform
         long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
         if (nblk > ntiles) nblk = ntiles;
-        k_fft_strided_tma<R1, R2, SIGN, TBK, NSTAGE, MODE><<<(unsigned)nblk, P::NT, smem, s>>>(
+        k_fft_strided_tma<R1, R2, SIGN, TBK, NS, MODE><<<(unsigned)nblk, P::NT, smem, s>>>(
             a, map, ntiles, (int)tiles_per_item, box_rows);
         return cudaGetLastError();
     }
@@ -131,7 +145,7 @@ struct SizeImpl {
                 if (!a.err || !(sign < 0 ? half_in : half_out)) return cudaErrorInvalidValue;
                 a.ntb = (a.B + TBN - 1) / TBN;
                 if (!encode_strided_map(&map, a, A, batch, TBN, &box_rows, TBN * 8)) return cudaErrorInvalidValue;
-                if (sign < 0) return tma_run<-1, PRUNE_IN, TBN>(a, map, A, batch, box_rows, s);
+                if (sign < 0) return tma_run<-1, PRUNE_IN, TBN, NSTAGE_NI>(a, map, A, batch, box_rows, s);
                 return tma_run<+1, PRUNE_OUT, TBN>(a, map, A, batch, box_rows, s);
             }
         }
@@ -178,6 +192,51 @@ struct SizeImpl {
             k_toep_x_tma<R1, R2, TBT, NSTAGE><<<(unsigned)nblk, Lay::NT, smem, s>>>(a, nsub, map, pmap, ntiles,
                                                                                    box_rows, pbox_rows);
             return cudaGetLastError();
+        }
+    }
+    // spreading fused with the adjoint x pass (tiles of 8 columns, output
+    // pruned); layouts above the opt-in shared-memory limit are not launched
+    static constexpr size_t SAX_SMEM_MAX = 227 * 1024;
+    template <int CC, bool K>
+    static cudaError_t sax_attr()
+    {
+        if (SaxLayout<R1, R2, CC>::bytes > SAX_SMEM_MAX) return cudaSuccess;   // not launched
+        return cudaFuncSetAttribute(k_spread_adjx<R1, R2, CC, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)SaxLayout<R1, R2, CC>::bytes);
+    }
+    template <int CC, bool K>
+    static cudaError_t sax_run(const SpreadAdjxArgs& a, cudaStream_t s)
+    {
+        constexpr size_t smem = SaxLayout<R1, R2, CC>::bytes;
+        if (smem > SAX_SMEM_MAX || a.nch % CC != 0) return cudaErrorNotSupported;
+        int per_sm = 0;
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_spread_adjx<R1, R2, CC, K>, SAX_NT,
+                                                                      smem);
+        if (e != cudaSuccess) return e;
+        const long long nunits = a.nj * (a.nch / CC);
+        if (nunits <= 0) return cudaSuccess;
+        if (nunits >= 0x7fffffffLL) return cudaErrorInvalidValue;
+        const long long nblk = std::min<long long>(nunits, (long long)sm_count() * std::max(per_sm, 1));
+        k_spread_adjx<R1, R2, CC, K><<<(unsigned)nblk, SAX_NT, smem, s>>>(a, (int)nunits);
+        return cudaGetLastError();
+    }
+    static cudaError_t spread_adjx(const SpreadAdjxArgs& a, bool kahan, cudaStream_t s)
+    {
+        if constexpr (!(HAS_IN && HAS_OUT)) {
+            return cudaErrorNotSupported;
+        } else {
+            // 16-byte aligned row offsets and taps (bulk copies), coil pairs
+            if (!a.err || (reinterpret_cast<uintptr_t>(a.ptr) & 15) || (reinterpret_cast<uintptr_t>(a.ent) & 15) ||
+                (reinterpret_cast<uintptr_t>(a.yv) & 15) || a.nch < 2)
+                return cudaErrorNotSupported;
+            int cc = a.cc;
+            if (cc == 0) cc = a.nch % 6 == 0 ? 6 : a.nch % 4 == 0 ? 4 : 2;
+            switch (cc) {
+            case 2: return kahan ? sax_run<2, true>(a, s) : sax_run<2, false>(a, s);
+            case 4: return kahan ? sax_run<4, true>(a, s) : sax_run<4, false>(a, s);
+            case 6: return kahan ? sax_run<6, true>(a, s) : sax_run<6, false>(a, s);
+            }
+            return cudaErrorNotSupported;
         }
     }
     static cudaError_t contig(int sign, const ContigPassArgs& a, int batch, cudaStream_t s)
@@ -229,6 +288,7 @@ struct SizeImpl {
     cudaError_t fft_init_##L_();                                                                       \
     cudaError_t fft_toep_x_##L_(const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch, \
                                 cudaStream_t s);                                                       \
+    cudaError_t fft_spread_adjx_##L_(const SpreadAdjxArgs& a, bool kahan, cudaStream_t s);             \
     CGS_DEFINE_IF_##G_(L_, R1_, R2_)
 
 #define CGS_BODY(L_, R1_, R2_)                                                                      \
@@ -244,7 +304,9 @@ struct SizeImpl {
     cudaError_t fft_init_##L_() { return SizeImpl<R1_, R2_>::init(); }                                 \
     cudaError_t fft_toep_x_##L_(const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch, \
                                 cudaStream_t s)                                                        \
-    { return SizeImpl<R1_, R2_>::toep_x(a, P, p_bs, nsub, batch, s); }
+    { return SizeImpl<R1_, R2_>::toep_x(a, P, p_bs, nsub, batch, s); }                                \
+    cudaError_t fft_spread_adjx_##L_(const SpreadAdjxArgs& a, bool kahan, cudaStream_t s)              \
+    { return SizeImpl<R1_, R2_>::spread_adjx(a, kahan, s); }
 
 #if CGS_FFT_GROUP == 0
 #define CGS_DEFINE_IF_0(L, R1, R2) CGS_BODY(L, R1, R2)

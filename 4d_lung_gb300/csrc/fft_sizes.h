@@ -21,3 +21,7 @@ constexpr int fft_listed_tile_cols(int r1, int r2)
 {
     return fft_has_narrow_tiles(r1, r2) ? 8 : fft_strided_tile_cols(r1, r2);
 }
+
+// spreading fused with the adjoint x pass (spread_adjx.cuh): threads per
+// block, columns per tile (the x passes' narrow tiles)
+constexpr int SAX_NT = 512, SAX_TB = 8;

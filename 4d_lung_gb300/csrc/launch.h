@@ -160,6 +160,10 @@ cudaError_t launch_toep_mul(float2* grid, const float* P, long long Ng, int nch,
 // when the pass does not apply (line length, pruning, alignment).
 cudaError_t launch_toep_x(int L, const StridedPassArgs& a, const float* P, long long p_bs, int nsub, int batch,
                           cudaStream_t s);
+// Spreading fused with the adjoint x pass of a grid of L points along x
+// (spread_adjx.cuh).  cudaErrorNotSupported when it does not apply (line
+// length without narrow tiles, coil count, alignment, shared memory).
+cudaError_t launch_spread_adjx(int L, const SpreadAdjxArgs& a, bool kahan, cudaStream_t s);
 
 // File IO (io.cu)
 cudaError_t launch_scale_samples(float2* data, const float* d, long long ns, int nch, cudaStream_t s);

@@ -47,6 +47,8 @@ sys.path.insert(0, ROOT)
 METRIC = "E^H D E applies/s; s per 16-bin 4D recon; chosen vs plain at <=1e-4 rel err"
 UNIT = "applies/s"
 STAGES = ["fwd_z", "fwd_y", "fwd_x", "interp", "spread", "adj_x", "adj_y", "adj_z"]
+# the stages when the spreading runs fused with the adjoint x pass (variant 8)
+STAGES_FUSED = ["fwd_z", "fwd_y", "fwd_x", "interp", "spread_adjx", "adj_y", "adj_z"]
 
 
 def beatty_beta(w, sigma=2.0):
@@ -66,7 +68,8 @@ def measured_peaks():
 # stage -> kernel family (the roofline's "kernel")
 FAMILY = {"fwd_z": "k_fwd_z_pipe+k_adj_z_pipe", "adj_z": "k_fwd_z_pipe+k_adj_z_pipe",
           "fwd_y": "k_fft_strided_tma", "fwd_x": "k_fft_strided_tma", "adj_x": "k_fft_strided_tma",
-          "adj_y": "k_fft_strided_tma", "interp": "k_interp", "spread": "k_spread"}
+          "adj_y": "k_fft_strided_tma", "interp": "k_interp", "spread": "k_spread",
+          "spread_adjx": "k_spread_adjx"}
 
 
 def traffic_record():
@@ -285,20 +288,21 @@ def make_workload(cgs, synth, torch, name, device, stream_handle, dcf_kind="voro
     return w, reco, data, sbins, smaps, dcf, k, kb_w, kb_b, dcf_s
 
 
-def stage_bytes(w, sizes, support=None, matrix=None, y_listed=False):
+def stage_bytes(w, sizes, support=None, matrix=None, y_listed=False, fused=False):
     """Algorithmic bytes of each stage of one E^H D E application over all
     bins: every stage reads its input and writes its output once.
-    support = (listed columns, stored spreading tiles[, the adjoint x pass's
-    listed columns]) per bin, from Reco.support_stats() (and
-    Reco.support_stats_adjoint()): with sample-support pruning the x passes
-    move only their listed (y, z) columns, the interpolation reads within
-    them and the spreading stores only the listed tiles.  None: the full
-    grid.
+    support = (listed columns, stored spreading tiles) per bin, from
+    Reco.support_stats(): with sample-support pruning the x passes move only
+    the listed (y, z) columns, the interpolation reads within them and the
+    spreading stores only the listed tiles.  None: the full grid.
     matrix = (taps, points) of the transposed tap matrix when the spreading
-    is its gather: it stores every point of the listed columns and reads the
-    row offsets (4 bytes per point), the taps (8 bytes each) and the coil
-    values of the samples.  y_listed: the forward y pass stores only the
-    listed columns' rows (8 bytes x Ix per listed column)."""
+    is its gather: it stores every point of its listed columns (its rows) and
+    reads the row offsets (4 bytes per point), the taps (8 bytes each) and
+    the coil values of the samples.  y_listed: the forward y pass stores only the
+    listed columns' rows (8 bytes x Ix per listed column).  fused: the
+    gather runs fused with the adjoint x pass (stage "spread_adjx"): the
+    matrix and the samples are read, the x pass's Ix output rows written,
+    the grid never stored or reloaded."""
     Ix, Iy, Iz = w.img
     Gx, Gy, Gz = w.grid
     Ni, Ng, Nl = Ix * Iy * Iz, Gx * Gy * Gz, Ix * Iy
@@ -310,8 +314,11 @@ def stage_bytes(w, sizes, support=None, matrix=None, y_listed=False):
         tiles = [Ng // 512] * nb
     else:
         cols, tiles = [int(v) for v in support[0]], [int(v) for v in support[1]]
-    acols = [int(v) for v in support[2]] if support is not None and len(support) > 2 else cols
-    scol, stile, sacol = sum(cols), sum(tiles), sum(acols)
+    scol, stile = sum(cols), sum(tiles)
+    if fused and matrix:
+        sb = stage_bytes(w, sizes, support, matrix, y_listed)
+        sb["spread_adjx"] = 4 * matrix[1] + 8 * matrix[0] + M * C8 + C8 * scol * Ix
+        return {k: sb[k] for k in STAGES_FUSED}
     return {
         # the coil maps once per application: the z passes run the bins of a
         # line block side by side, so the other bins read the maps from L2
@@ -319,19 +326,19 @@ def stage_bytes(w, sizes, support=None, matrix=None, y_listed=False):
         "fwd_y": C8 * (nb * Nl * Gz + Ix * scol) if y_listed else nb * C8 * (Nl * Gz + Ix * Gy * Gz),
         "fwd_x": C8 * scol * (Ix + Gx),
         "interp": C8 * scol * Gx + M * (64 + 4 + C8),
-        "spread": (C8 * scol * Gx + 4 * matrix[1] + 8 * matrix[0] + M * C8) if matrix
+        "spread": (C8 * matrix[1] + 4 * matrix[1] + 8 * matrix[0] + M * C8) if matrix
         else C8 * stile * 512 + M * (64 + C8),   # tiled kernels: 4 x 8 x 16 points per tile
-        "adj_x": C8 * sacol * (Gx + Ix),
+        "adj_x": C8 * scol * (Gx + Ix),
         "adj_y": nb * C8 * (Ix * Gy * Gz + Nl * Gz),
         "adj_z": nb * (C8 * Nl * Gz + 8 * Ni) + C8 * Ni,
     }
 
 
-def apply_bytes(w, sizes, support=None, matrix=None, y_listed=False):
+def apply_bytes(w, sizes, support=None, matrix=None, y_listed=False, fused=False):
     """Algorithmic bytes of one application of the operator (its eight
-    stages; the CG vector updates of a solve, 64 bytes per voxel and bin and
-    iteration, are not part of it)."""
-    return sum(stage_bytes(w, sizes, support, matrix, y_listed).values())
+    stages, seven fused; the CG vector updates of a solve, 64 bytes per voxel
+    and bin and iteration, are not part of it)."""
+    return sum(stage_bytes(w, sizes, support, matrix, y_listed, fused).values())
 
 
 # ---------------------------------------------------------------------------
@@ -975,16 +982,19 @@ def run_ours(args):
     if args.applies_only:
         # profiling mode: the operator alone, args.applies_only applications of
         # all bins (8 launches each: fwd z / y / x, interp, spread, adj x / y / z
-        # when one workspace group holds the bins), then the algorithmic bytes
+        # when one workspace group holds the bins; 7 with the spreading fused
+        # with the adjoint x pass), then the algorithmic bytes
         xa = torch.from_numpy(np.stack([synth.phantom(w.img)] * nb)).to(dev)
         qa = torch.empty_like(xa)
         for _ in range(args.applies_only):
             reco.apply_ehde_tensor(xa, qa, 0, nb)
         torch.cuda.synchronize(dev)
-        support = reco.support_stats() + (reco.support_stats_adjoint(),)
+        support = reco.support_stats()
         taps, points = reco.spread_matrix_stats()
-        print(json.dumps({"applies": args.applies_only, "bins": nb, "algorithmic_bytes": stage_bytes(
-            w, sizes, support, (taps, points) if taps > 0 else None, reco.forward_y_listed_rows())}))
+        fused = reco.spread_fused()
+        print(json.dumps({"applies": args.applies_only, "bins": nb, "spread_fused_with_adjoint_x": fused,
+                          "algorithmic_bytes": stage_bytes(w, sizes, support, (taps, points) if taps > 0 else None,
+                                                           reco.forward_y_listed_rows(), fused)}))
         return 0
 
     t0 = time.perf_counter()
@@ -1143,8 +1153,10 @@ def run_ours(args):
     for _ in range(5):
         reps.append(reco.profile_apply_tensor(xa, qa, 0, nb))
     st = np.median(np.stack(reps), axis=0)
-    groups = len(st) // 8
-    stage_ms = {s: float(sum(st[g * 8 + i] for g in range(groups))) for i, s in enumerate(STAGES)}
+    fused = reco.spread_fused()
+    names = STAGES_FUSED if fused else STAGES
+    groups = len(st) // len(names)
+    stage_ms = {s: float(sum(st[g * len(names) + i] for g in range(groups))) for i, s in enumerate(names)}
     # the right-hand side alone (sample gather + adjoint chain of all bins),
     # to split the step into applications, right-hand side and CG updates
     import ctypes as C
@@ -1161,17 +1173,17 @@ def run_ours(args):
         rhs_t.append(r0.elapsed_time(r1))
     rhs_ms = float(np.median(rhs_t[1:]))
     del b_rhs
-    support = reco.support_stats() + (reco.support_stats_adjoint(),)
+    support = reco.support_stats()
     taps, points = reco.spread_matrix_stats()
-    variant = tune.get("spread_variant") if tune else 6   # the library's default is the gather
-    gather = variant in (6, 7) and taps > 0
+    variant = tune.get("spread_variant") if tune else 8   # the library's default is the fused gather
+    gather = variant in (6, 7, 8) and taps > 0
     matrix = (taps, points) if gather else None
     y_listed = reco.forward_y_listed_rows()
-    sb = stage_bytes(w, sizes, support, matrix, y_listed)
+    sb = stage_bytes(w, sizes, support, matrix, y_listed, fused)
     apply_ms = float(sum(stage_ms.values()))
-    # kernel families: the four x/y passes are one kernel template
+    # kernel families: the x/y passes are one kernel template
     family = dict(FAMILY, spread="k_spread_csr" if gather else "k_spread")
-    fam = {k: [s for s in STAGES if family[s] == k] for k in dict.fromkeys(family.values())}
+    fam = {k: [s for s in names if family[s] == k] for k in dict.fromkeys(family[s] for s in names)}
     fam_ms = {k: sum(stage_ms[s] for s in v) for k, v in fam.items()}
     dom = max(fam_ms, key=fam_ms.get)
     dom_bytes = sum(sb[s] for s in fam[dom])
@@ -1197,8 +1209,9 @@ def run_ours(args):
         "apply_ms": apply_ms,
         "rhs_ms": rhs_ms,
         "cg_update_ms_per_iter": (ms_step - iters * apply_ms - rhs_ms) / max(iters, 1),
-        "apply_achieved_gbs": apply_bytes(w, sizes, support, matrix, y_listed) / (apply_ms / 1e3) / 1e9,
-        "apply_bytes": apply_bytes(w, sizes, support, matrix, y_listed),
+        "apply_achieved_gbs": apply_bytes(w, sizes, support, matrix, y_listed, fused) / (apply_ms / 1e3) / 1e9,
+        "apply_bytes": apply_bytes(w, sizes, support, matrix, y_listed, fused),
+        "spread_fused_with_adjoint_x": fused,
         "support": {"listed_column_fraction": float(sum(support[0])) / (nb * w.grid[1] * w.grid[2]),
                     "stored_tile_fraction": float(sum(support[1])) / (nb * int(np.prod(w.grid)) // 512)},
     }

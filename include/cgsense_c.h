@@ -312,14 +312,17 @@ int cgs_set_deterministic(cgs_ctx* ctx, int32_t on);
  * block (0: as many as fit), spreading variant (1 / 2: one / two warps per x
  * plane of a tile; 3: shared-memory atomics, only with determinism off;
  * 4 / 5: persistent and software-pipelined with one / two warps per plane;
- * 6 (default): a gather over the transposed tap matrix, built with the bins
- * when sample-support pruning is on -- without it variant 2 runs -- whose
- * row offsets and taps are staged in shared memory by bulk copies; 7: the
- * same gather reading the matrix from global memory; for 6 and 7 spread_cc
- * is the coils per thread, 2, 4, 6 or 8, 0 by the coil count), coils per
- * interpolation thread (1, 2, 4, 6, 8).  Variants 1, 2, 4, 5, 6, 7 and every
- * interpolation shape give
- * bitwise-identical results. */
+ * 6: a gather over the transposed tap matrix, built with the bins when
+ * sample-support pruning is on -- without it variant 2 runs -- whose row
+ * offsets and taps are staged in shared memory by bulk copies; 7: the same
+ * gather reading the matrix from global memory; for 6 and 7 spread_cc is the
+ * coils per thread, 2, 4, 6 or 8, 0 by the coil count; 8 (default): the
+ * staged gather fused with the adjoint x pass, one block per listed
+ * 8-column tile and chunk of spread_cc coils (2, 4 or 6, 0 by the coil
+ * count), the grid kept in shared memory -- where the grid is not twice the
+ * image along x, or the coil count has no such chunk, variant 6 runs),
+ * coils per interpolation thread (1, 2, 4, 6, 8).  Variants 1, 2, 4, 5, 6,
+ * 7, 8 and every interpolation shape give bitwise-identical results. */
 int cgs_set_launch_shape(cgs_ctx* ctx, int32_t spread_cc, int32_t spread_variant, int32_t interp_cc);
 
 /* Sample-support pruning of the oversampled FFT (default on): the x passes
@@ -408,26 +411,26 @@ int cgs_estimate_smaps_d(cgs_ctx* ctx, const void* data, double radius, double e
  * (without pruning: every column, every tile). */
 int cgs_support_stats(cgs_ctx* ctx, int64_t* listed_cols, int64_t* live_tiles);
 
-/* Per bin (cgs_num_bins entries): the (y, z) grid columns the adjoint x
- * pass transforms.  With pruning it lists narrower tiles than the forward
- * x pass (8 columns where the grid is twice the image along x), each inside
- * a forward tile; without pruning: every column. */
-int cgs_support_stats_adjoint(cgs_ctx* ctx, int64_t* listed_cols);
-
 /* 1 when the forward y pass stores only the rows of the x pass's listed
  * tiles (sample-support pruning on and the passes' column tiles coincide),
  * else 0. */
 int cgs_forward_y_listed_rows(cgs_ctx* ctx, int32_t* listed);
 
-/* The transposed tap matrix of spreading variant 6 (all bins): its taps
+/* The transposed tap matrix of spreading variants 6 to 8 (all bins): its taps
  * (entries) and grid points (rows); both 0 when it is not built. */
 int cgs_spread_matrix_stats(cgs_ctx* ctx, int64_t* taps, int64_t* points);
+
+/* *fused = 1 when the last operator application ran the spreading fused
+ * with the adjoint x pass (variant 8 where it applies; one launch in place
+ * of two), else 0. */
+int cgs_spread_fused(cgs_ctx* ctx, int32_t* fused);
 
 /* Autotuner: times one batched E^H D E application of every bin for each
  * candidate launch shape -- the spreading variants of cgs_set_launch_shape
  * (tiled kernels with coils per block all that fit, then 1/2, 1/3, 1/4 of
- * them; the transposed-matrix gather with 4, 6 or 8 coils per thread), then
- * coils per interpolation thread (2, 4, 6, 8) -- and keeps the fastest for
+ * them; the transposed-matrix gather with 4, 6 or 8 coils per thread; the
+ * gather fused with the adjoint x pass with 2, 4 or 6 coils per block), then
+ * coils per interpolation thread (1, 2, 4, 6, 8) -- and keeps the fastest for
  * this context.  times_ms (may be NULL) receives the median time of each
  * candidate in that order; the chosen shape is returned in *spread_cc,
  * *spread_wpp (the spreading variant) and *interp_cc (each may be NULL). */

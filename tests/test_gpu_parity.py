@@ -202,9 +202,11 @@ def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
     r.set_smaps(smaps)
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 5)
     tune = r.autotune()
-    assert tune["spread_variant"] in (1, 2, 4, 5, 6, 7)
+    assert tune["spread_variant"] in (1, 2, 4, 5, 6, 7, 8)
     if tune["spread_variant"] in (6, 7):   # the gather's parameter: coils per thread
         assert tune["spread_coils_per_block"] in (4, 6, 8)
+    elif tune["spread_variant"] == 8:      # fused with the adjoint x pass: coils per block
+        assert tune["spread_coils_per_block"] in (2, 4, 6)
     else:
         assert tune["spread_coils_per_block"] in range(1, nch + 1)
     assert tune["interp_coils_per_thread"] in (1, 2, 4, 6, 8)
@@ -218,9 +220,10 @@ def test_autotune_keeps_results_bitwise(gpu_lib, cgs, oracle_mod, o64, synth):
 def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid, nch):
     """The fixed-order spreading variants (one / two warps per x plane,
     plain or persistent and pipelined, the gather over the transposed tap
-    matrix with and without its shared-memory staging) and every coil chunk
-    size give bitwise-identical solves: each grid value is summed in the
-    same order."""
+    matrix with and without its shared-memory staging, the gather fused with
+    the adjoint x pass) and every coil chunk size give bitwise-identical
+    solves: each grid value is summed in the same order, and the fused x
+    transform does the unfused pass's operations."""
     k, p, taps_all, w, b = oversampled_case(oracle_mod, o64, img, grid, nch, 60, 48)
     bins = synth.bin_samples([np.arange(0, 7), np.arange(7, 41), np.arange(41, 60)], 48)
     smaps = synth.coil_maps(img, nch)
@@ -233,11 +236,17 @@ def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, g
     r.set_launch_shape(0, 1, 4)
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 4)
     for cc in (0, 3, 5):
-        for variant in (1, 2, 4, 5, 6, 7):
+        for variant in (1, 2, 4, 5, 6, 7, 8):
             r.set_launch_shape(cc, variant, 2)
             x1, res1, _ = r.cg_sense_batched(data, 0.0, 4)
             assert np.array_equal(x1, x0), (cc, variant)
             assert np.array_equal(res1, res0), (cc, variant)
+    # the fused kernel's coil chunks (with 7 coils none applies: variant 6 runs)
+    for cc in (2, 4, 6):
+        r.set_launch_shape(cc, 8, 2)
+        x1, res1, _ = r.cg_sense_batched(data, 0.0, 4)
+        assert np.array_equal(x1, x0) and np.array_equal(res1, res0), cc
+        assert r.spread_fused() == (nch % cc == 0), cc
     # compensated sums: the tiled kernel and the transposed-matrix gather agree bitwise
     r.set_precision("compensated")
     r.set_launch_shape(0, 1, 2)
@@ -248,6 +257,9 @@ def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, g
     r.set_launch_shape(0, 7, 2)
     xk7, rk7, _ = r.cg_sense_batched(data, 0.0, 4)
     assert np.array_equal(xk, xk7) and np.array_equal(rk, rk7)
+    r.set_launch_shape(0, 8, 2)
+    xk8, rk8, _ = r.cg_sense_batched(data, 0.0, 4)
+    assert np.array_equal(xk, xk8) and np.array_equal(rk, rk8)
     # every interpolation shape (coils per thread) sums each sample in the
     # same order
     r.set_precision(False)
@@ -288,7 +300,7 @@ def test_support_pruning_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid
     out = {}
     for on in (True, False):
         r.set_support_pruning(on)
-        for variant in (1, 2, 4, 6, 7):
+        for variant in (1, 2, 4, 6, 7, 8):
             r.set_launch_shape(0, variant, 2)
             out[on, variant] = r.cg_sense_batched(data, 0.0, 4)[:2]
     ref = out[False, 1]
@@ -324,7 +336,7 @@ def test_atomic_spreading_matches_fixed_order(gpu_lib, cgs, oracle_mod, o64, syn
     x0, res0, _ = r.cg_sense_batched(data, 0.0, 5)
     r.set_deterministic(False)
     tune = r.autotune()
-    assert tune["spread_variant"] in (1, 2, 3, 4, 5, 6, 7)
+    assert tune["spread_variant"] in (1, 2, 3, 4, 5, 6, 7, 8)
     x1, res1, _ = r.cg_sense_batched(data, 0.0, 5)
     assert rel_l2(x1, x0) < 1e-5
     assert np.allclose(res1, res0, rtol=1e-5)
