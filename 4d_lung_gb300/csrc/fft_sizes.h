@@ -24,4 +24,4 @@ constexpr int fft_listed_tile_cols(int r1, int r2)
 
 // spreading fused with the adjoint x pass (spread_adjx.cuh): threads per
 // block, columns per tile (the x passes' narrow tiles)
-constexpr int SAX_NT = 512, SAX_TB = 8;
+constexpr int SAX_NT = 1024, SAX_TB = 8;

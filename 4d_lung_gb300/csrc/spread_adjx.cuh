@@ -17,10 +17,10 @@
 //      the same operations on the same values.
 // So the adjoint y pass's input equals that of the unfused spreading + x
 // pass bit for bit, and the grid's store and reload (16 bytes per point and
-// coil) are gone.  Where shared memory allows, two blocks share an SM, so
-// that one block's transform and stores overlap the other's gather.  Every
-// wait is bounded: on a timeout the block sets the error flag, lets its
-// issued copies land and leaves.
+// coil) are gone.  One block of SAX_NT threads per SM (the unit's lines take
+// most of its shared memory): 32 warps for the gather's dependent loads,
+// three barriers per unit.  Every wait is bounded: on a timeout the block
+// sets the error flag, lets its issued copies land and leaves.
 #pragma once
 #include "fft_sizes.h"
 #include "fft_passes.cuh"
@@ -35,25 +35,28 @@ struct SaxLayout {
     static constexpr int L = R1 * R2;
     static constexpr int PTS = L * SAX_TB;              // points of a unit
     static constexpr int PS = ((PTS + 1) + 3) & ~3;     // staged row offsets per stage
+    // a coil's lines in shared memory: 8 float2 of padding after every 16
+    // rows of the 8 columns, so that the 4 row groups a warp reads in the
+    // transform's stage 2 fall in different halves of the banks
+    static constexpr int GS = PTS + PTS / 16;
     static constexpr long long fixed = (long long)SAX_NST * PS * sizeof(unsigned) +
-                                       (long long)CC * PTS * sizeof(float2) + (long long)L * sizeof(float2) +
+                                       (long long)CC * GS * sizeof(float2) + (long long)L * sizeof(float2) +
                                        SAX_NST * sizeof(uint64_t);
-    // blocks per SM: two when each can still stage 1024 taps per stage
-    // (an SM's 228 KiB less 1 KiB per block), else one
-    static constexpr long long room2 = ((233472 / 2 - 1024) - fixed) / (long long)(SAX_NST * sizeof(int2));
-    static constexpr int BPS = room2 >= 1024 ? 2 : 1;
-    static constexpr long long room = ((233472 / BPS - 1024) - fixed) / (long long)(SAX_NST * sizeof(int2));
-    // staged taps per stage (at most 8192, an even count; 0: never staged)
+    // staged taps per stage: what the 227 KiB of a block's shared memory
+    // leave (at most 8192, an even count; 0: never staged)
+    static constexpr long long room = (232448 - fixed) / (long long)(SAX_NST * sizeof(int2));
     static constexpr int CAP = room >= 8192 ? 8192 : room >= 2 ? (int)(room & ~1LL) : 0;
     static constexpr size_t bytes = (size_t)SAX_NST * CAP * sizeof(int2) + (size_t)fixed;
 };
 
 template <int R1, int R2, int CC, bool KAHAN>
-__global__ void __launch_bounds__(SAX_NT, SaxLayout<R1, R2, CC>::BPS) k_spread_adjx(SpreadAdjxArgs a, int nunits)
+__global__ void __launch_bounds__(SAX_NT, 1) k_spread_adjx(SpreadAdjxArgs a, int nunits)
 {
     constexpr int L = R1 * R2, TB = SAX_TB;
     using Lay = SaxLayout<R1, R2, CC>;
-    constexpr int PTS = Lay::PTS, PS = Lay::PS, CAP = Lay::CAP;
+    constexpr int PTS = Lay::PTS, PS = Lay::PS, CAP = Lay::CAP, GS = Lay::GS;
+    // shared-memory position of row l, column bi of a coil's lines
+    auto gi = [](int l, int bi) { return l * TB + bi + (l >> 4) * TB; };
     constexpr bool FOLD = SignFold<R1, R2>::value;
     constexpr int MR = R1 > R2 ? R1 : R2;
     constexpr int TPC = TB * MR;                               // transform threads per coil
@@ -65,7 +68,7 @@ __global__ void __launch_bounds__(SAX_NT, SaxLayout<R1, R2, CC>::BPS) k_spread_a
     int2* s_ent = reinterpret_cast<int2*>(s_sax);                             // [SAX_NST][CAP]
     unsigned* s_ptr = reinterpret_cast<unsigned*>(s_ent + SAX_NST * CAP);     // [SAX_NST][PS]
     float2* s_g = reinterpret_cast<float2*>(s_ptr + SAX_NST * PS);           // [CC][L][TB]
-    float2* s_tw = s_g + CC * PTS;                                            // W^m, or [n2][k1] signed (FOLD)
+    float2* s_tw = s_g + CC * GS;                                             // W^m, or [n2][k1] signed (FOLD)
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
     const int tid = threadIdx.x;
     if (FOLD) {
@@ -121,18 +124,22 @@ __global__ void __launch_bounds__(SAX_NT, SaxLayout<R1, R2, CC>::BPS) k_spread_a
         for (int kk = 0; kk < SAX_NST - 1 && kk < my_n; ++kk) issue(kk);
     for (int kk = 0; kk < my_n; ++kk) {
         const int st = kk % SAX_NST;
-        // the stage of unit kk - 1 is free (the barrier ending it): fetch
-        // unit kk + SAX_NST - 1 into it
-        if (tid == 0 && kk + SAX_NST - 1 < my_n) issue(kk + SAX_NST - 1);
         const bool ok = mbar_wait_bounded(&s_bar[st], (uint32_t)((kk / SAX_NST) & 1), SAX_WAIT_NS);
         if (__syncthreads_or(!ok)) {
             // timeout: report, let the copies already issued land, leave
             if (tid == 0) {
                 atomicExch(a.err, 1);
-                for (int j = kk; j < my_n && j < kk + SAX_NST; ++j)
+                for (int j = kk; j < my_n && j < kk + SAX_NST - 1; ++j)
                     mbar_wait_bounded(&s_bar[j % SAX_NST], (uint32_t)((j / SAX_NST) & 1), SAX_WAIT_NS);
             }
             return;
+        }
+        // every thread is past the previous unit (its transform's reads of
+        // the lines, its gather's reads of stage (kk - 1) % SAX_NST): fetch
+        // unit kk + SAX_NST - 1 into that stage
+        if (tid == 0 && kk + SAX_NST - 1 < my_n) {
+            fence_proxy_async_smem();
+            issue(kk + SAX_NST - 1);
         }
         const unsigned u = blockIdx.x + (unsigned)kk * gridDim.x;
         const unsigned jt = u / (unsigned)nchunk;
@@ -174,7 +181,7 @@ __global__ void __launch_bounds__(SAX_NT, SaxLayout<R1, R2, CC>::BPS) k_spread_a
             for (int c = 0; c < CC; ++c) {
                 float2 o = acc[c];
                 if (KAHAN) o = make_float2(__fsub_rn(o.x, cmp[c].x), __fsub_rn(o.y, cmp[c].y));
-                s_g[c * PTS + i] = o;
+                s_g[c * GS + gi(i / TB, i % TB)] = o;
             }
         }
         __syncthreads();
@@ -187,13 +194,13 @@ __global__ void __launch_bounds__(SAX_NT, SaxLayout<R1, R2, CC>::BPS) k_spread_a
         for (int c0 = 0; c0 < CC; c0 += CPP) {
             const int c = c0 + lc;
             const bool act = lc < CPP && c < CC;
-            float2* g = s_g + c * PTS;
+            float2* g = s_g + c * GS;
             if (act && rq < R2) {
                 const int n2 = rq;
                 float2 v[R1];
 #pragma unroll
                 for (int n1 = 0; n1 < R1; ++n1) {
-                    const float2 x = g[(R2 * n1 + n2) * TB + bi];
+                    const float2 x = g[gi(R2 * n1 + n2, bi)];
                     v[n1] = FOLD ? x : parity(x, R2 * n1 + n2);
                 }
                 Dft<R1, +1>::run(v);
@@ -202,7 +209,7 @@ __global__ void __launch_bounds__(SAX_NT, SaxLayout<R1, R2, CC>::BPS) k_spread_a
                     float2 tv = v[k1];
                     if (FOLD) tv = table_twiddle<+1>(tv, s_tw[n2 * R1 + k1]);
                     else if (k1 > 0) tv = table_twiddle<+1>(tv, s_tw[n2 * k1]);
-                    g[(k1 * R2 + n2) * TB + bi] = tv;
+                    g[gi(k1 * R2 + n2, bi)] = tv;
                 }
             }
             __syncthreads();
@@ -210,7 +217,7 @@ __global__ void __launch_bounds__(SAX_NT, SaxLayout<R1, R2, CC>::BPS) k_spread_a
                 const int k1 = rq;
                 float2 w[R2];
 #pragma unroll
-                for (int n2 = 0; n2 < R2; ++n2) w[n2] = g[(k1 * R2 + n2) * TB + bi];
+                for (int n2 = 0; n2 < R2; ++n2) w[n2] = g[gi(k1 * R2 + n2, bi)];
                 Dft<R2, +1>::run(w);
                 const long long item = (long long)(t.x - a.bin0) * a.nch + ch * CC + c;
                 float2* o = a.out + item * a.out_bs + (long long)k1 * a.B + b;
@@ -220,8 +227,8 @@ __global__ void __launch_bounds__(SAX_NT, SaxLayout<R1, R2, CC>::BPS) k_spread_a
                     o[(k2 - R2 / 4) * step] = FOLD ? w[k2] : parity(w[k2], k1 + R1 * k2);
             }
         }
-        // the unit's buffer and matrix stage are free for the next units
-        __syncthreads();
+        // the next wait's barrier orders this unit's reads of the lines and
+        // of its stage before the next unit's writes
     }
 }
 
