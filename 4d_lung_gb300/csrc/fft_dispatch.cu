@@ -67,6 +67,8 @@ bool encode_strided_map(CUtensorMap* map, const StridedPassArgs& a, int A, int b
     if (br > 256)
         for (br = 256; br > 1 && a.Lin % br != 0; --br) {
         }
+    // each box of a stage lands on a 128-byte boundary
+    if (br < a.Lin && ((long long)br * TB * 8) % 128 != 0) return false;
     const cuuint64_t dims[4] = {(cuuint64_t)a.B, (cuuint64_t)a.Lin, (cuuint64_t)A, (cuuint64_t)batch};
     const cuuint64_t strides[3] = {(cuuint64_t)a.B * 8, (cuuint64_t)as * 8, (cuuint64_t)bs * 8};
     const cuuint32_t box[4] = {(cuuint32_t)TB, (cuuint32_t)br, 1, 1};

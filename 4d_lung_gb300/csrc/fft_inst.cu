@@ -110,7 +110,7 @@ struct SizeImpl {
     static bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
 
     // persistent launch: as many blocks as fit, at most one per tile
-    template <int SIGN, int MODE, int TBK = TB, int NS = NSTAGE>
+    template <int SIGN, int MODE, int TBK = TB, int NS = NSTAGE, int MAXB = 0>
     static cudaError_t tma_run(const StridedPassArgs& a, const CUtensorMap& map, int A, int batch, int box_rows,
                                cudaStream_t s)
     {
@@ -123,6 +123,7 @@ struct SizeImpl {
         const long long tiles_per_item = (long long)A * a.ntb;
         const long long ntiles = a.sup_tiles ? a.sup_ntiles * a.sup_nsub : tiles_per_item * batch;
         if (ntiles <= 0) return cudaSuccess;   // no listed tile: nothing to transform
+        if (MAXB > 0 && per_sm > MAXB) per_sm = MAXB;
         long long nblk = (long long)sm_count() * (per_sm > 0 ? per_sm : 1);
         if (nblk > ntiles) nblk = ntiles;
         k_fft_strided_tma<R1, R2, SIGN, TBK, NS, MODE><<<(unsigned)nblk, P::NT, smem, s>>>(
@@ -145,7 +146,8 @@ struct SizeImpl {
                 if (!a.err || !(sign < 0 ? half_in : half_out)) return cudaErrorInvalidValue;
                 a.ntb = (a.B + TBN - 1) / TBN;
                 if (!encode_strided_map(&map, a, A, batch, TBN, &box_rows, TBN * 8)) return cudaErrorInvalidValue;
-                if (sign < 0) return tma_run<-1, PRUNE_IN, TBN, NSTAGE_NI>(a, map, A, batch, box_rows, s);
+                // four blocks per SM: five (what shared memory allows) measured 7 % slower
+                if (sign < 0) return tma_run<-1, PRUNE_IN, TBN, NSTAGE_NI, 4>(a, map, A, batch, box_rows, s);
                 return tma_run<+1, PRUNE_OUT, TBN>(a, map, A, batch, box_rows, s);
             }
         }

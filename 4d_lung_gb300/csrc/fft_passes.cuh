@@ -202,10 +202,19 @@ template <int R1, int R2, int TB, int NSTAGE>
 struct PipeLayout {
     static constexpr int L = R1 * R2;
     static constexpr int NT = TB * (R1 > R2 ? R1 : R2);
-    // 1 KiB slack to align the TMA destination to 1 KiB; two twiddle tables
+    // the stage exchange: rows of TB values; with 8-column tiles 8 float2 of
+    // padding after every R2 rows, so that the 4 row groups k1 a warp reads
+    // in stage 2 fall in different halves of the banks
+    static constexpr int YP = TB == 8 ? 8 : 0;
+    static constexpr int SY = L * TB + R1 * YP;
+    // a pipeline stage: Lin rows of TB values, rounded up to 128 bytes so
+    // that every stage starts on the 128-byte boundary a TMA destination needs
+    __host__ __device__ static int stage_elems(int Lin) { return (Lin * TB + 15) & ~15; }
+    // 128 bytes of slack to align the first stage (the tiles are not
+    // swizzled); the twiddle table
     static size_t smem_bytes(int Lin)
     {
-        return 1024 + ((size_t)NSTAGE * Lin * TB + (size_t)L * TB + 2 * L) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
+        return 128 + ((size_t)NSTAGE * stage_elems(Lin) + (size_t)SY + L) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
     }
 };
 
@@ -235,18 +244,19 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
 {
     constexpr int L = R1 * R2;
     constexpr int NT = PipeLayout<R1, R2, TB, NSTAGE>::NT;
+    constexpr int YP = PipeLayout<R1, R2, TB, NSTAGE>::YP;
     constexpr bool FOLD = SignFold<R1, R2>::value;
     static_assert(MODE != PRUNE_IN || R1 % 4 == 0, "input pruning needs R1 % 4 == 0");
     static_assert(MODE != PRUNE_OUT || R2 % 4 == 0, "output pruning needs R2 % 4 == 0");
     extern __shared__ float4 s_pipe[];
-    // 1 KiB-aligned start, derived from the shared array itself so that the
-    // compiler keeps shared-memory (not generic) loads and stores
-    const uint32_t pad = (1024u - (smem_addr(s_pipe) & 1023u)) & 1023u;
-    const int stage_elems = a.Lin * TB;
+    // 128-byte-aligned start, derived from the shared array itself so that
+    // the compiler keeps shared-memory (not generic) loads and stores
+    const uint32_t pad = (128u - (smem_addr(s_pipe) & 127u)) & 127u;
+    const int stage_elems = PipeLayout<R1, R2, TB, NSTAGE>::stage_elems(a.Lin);
     float2* s_in = reinterpret_cast<float2*>(reinterpret_cast<char*>(s_pipe) + pad);
     float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
-    float2* s_tw = s_y + L * TB;        // W^m, or the signed table [n2][k1] when FOLD
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + 2 * L);
+    float2* s_tw = s_y + PipeLayout<R1, R2, TB, NSTAGE>::SY;   // W^m, or the signed table [n2][k1] when FOLD
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
     const int tid = threadIdx.x;
     if (FOLD) {
         for (int m = tid; m < L; m += NT) {
@@ -287,7 +297,7 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
         int ai, b0;
         decode(t, item, ai, b0);
         const int s = (int)(k % NSTAGE);
-        mbar_arrive_expect_tx(&s_bar[s], (uint32_t)(stage_elems * sizeof(float2)));
+        mbar_arrive_expect_tx(&s_bar[s], (uint32_t)((size_t)a.Lin * TB * sizeof(float2)));   // the rows copied
         float2* dst = s_in + (size_t)s * stage_elems;
         for (int r0 = 0; r0 < a.Lin; r0 += box_rows)
             tma_load_4d(dst + (size_t)r0 * TB, &tmap, b0, r0, ai, (int)item, &s_bar[s]);
@@ -350,7 +360,7 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
                     float2 tv = v[k1];
                     if (FOLD) tv = table_twiddle<SIGN>(tv, s_tw[n2 * R1 + k1]);
                     else if (k1 > 0) tv = table_twiddle<SIGN>(tv, s_tw[n2 * k1]);
-                    s_y[(k1 * R2 + n2) * TB + bi] = tv;
+                    s_y[(k1 * R2 + n2) * TB + bi + k1 * YP] = tv;
                 }
             }
         }
@@ -360,7 +370,7 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
             if (k1 < R1) {
                 float2 u[R2];
 #pragma unroll
-                for (int n2 = 0; n2 < R2; ++n2) u[n2] = s_y[(k1 * R2 + n2) * TB + bi];
+                for (int n2 = 0; n2 < R2; ++n2) u[n2] = s_y[(k1 * R2 + n2) * TB + bi + k1 * YP];
                 Dft<R2, SIGN>::run(u);
                 float2* out = a.out + item * a.out_bs + (long long)ai * a.out_as + b;
                 if constexpr (MODE == PRUNE_OUT) {
