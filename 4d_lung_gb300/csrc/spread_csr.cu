@@ -2,9 +2,10 @@
 // transposed tap matrix.
 //
 // The tap set of a trajectory is fixed, so its transpose is built once per
-// set of tap records: for every grid point of the listed x-pass column tiles
-// (the only points the adjoint x pass reads), the (sample, weight) pairs of
-// the taps that land on it.  Rows are ordered by (nearest x, sorted sample
+// set of tap records: for every grid point of the listed column tiles (the
+// unfused gather's 16-column tiles, or the x passes' own tiles for the gather
+// fused with the adjoint x pass; either covers every point the adjoint x
+// pass reads), the (sample, weight) pairs of the taps that land on it.  Rows are ordered by (nearest x, sorted sample
 // position) -- the order in which the tiled spreading kernels add the
 // samples to a grid point -- so the gather sums every point in the same
 // order with the same fused multiply-adds and gives bitwise the same grid.
@@ -313,7 +314,7 @@ __global__ void __launch_bounds__(256, (KAHAN || CC > 6) ? 3 : 4) k_spread_csr(C
 // Every wait is bounded: on a timeout the block sets the error flag, lets
 // its issued copies land and leaves.
 // ---------------------------------------------------------------------------
-constexpr int CSR_PTS = 1024;         // points per unit (64 rows of 16-column tiles)
+constexpr int CSR_PTS = 1024;         // points per unit (64 rows of a 16-column tile)
 constexpr int CSR_CAP = 2048;         // staged taps per unit
 constexpr int CSR_NST = 2;            // pipeline stages
 constexpr unsigned long long CSR_WAIT_NS = 2000000000ull;
