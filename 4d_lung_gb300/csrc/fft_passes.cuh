@@ -211,10 +211,10 @@ struct PipeLayout {
     // that every stage starts on the 128-byte boundary a TMA destination needs
     __host__ __device__ static int stage_elems(int Lin) { return (Lin * TB + 15) & ~15; }
     // 128 bytes of slack to align the first stage (the tiles are not
-    // swizzled); the twiddle table
+    // swizzled); the twiddle table (R2 rows of R1 + 1 when signed)
     static size_t smem_bytes(int Lin)
     {
-        return 128 + ((size_t)NSTAGE * stage_elems(Lin) + (size_t)SY + L) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
+        return 128 + ((size_t)NSTAGE * stage_elems(Lin) + (size_t)SY + L + R2) * sizeof(float2) + NSTAGE * sizeof(uint64_t);
     }
 };
 
@@ -256,13 +256,13 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
     float2* s_in = reinterpret_cast<float2*>(reinterpret_cast<char*>(s_pipe) + pad);
     float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
     float2* s_tw = s_y + PipeLayout<R1, R2, TB, NSTAGE>::SY;   // W^m, or the signed table [n2][k1] when FOLD
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L + R2);
     const int tid = threadIdx.x;
     if (FOLD) {
         for (int m = tid; m < L; m += NT) {
             const int n2 = m / R1, k1 = m - n2 * R1;
             const float2 w = a.tw[n2 * k1];
-            s_tw[m] = ((n2 + k1) & 1) ? cneg(w) : w;
+            s_tw[n2 * (R1 + 1) + k1] = ((n2 + k1) & 1) ? cneg(w) : w;   // rows padded by one: no bank conflicts
         }
     } else {
         for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
@@ -358,7 +358,7 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
 #pragma unroll
                 for (int k1 = 0; k1 < R1; ++k1) {
                     float2 tv = v[k1];
-                    if (FOLD) tv = table_twiddle<SIGN>(tv, s_tw[n2 * R1 + k1]);
+                    if (FOLD) tv = table_twiddle<SIGN>(tv, s_tw[n2 * (R1 + 1) + k1]);
                     else if (k1 > 0) tv = table_twiddle<SIGN>(tv, s_tw[n2 * k1]);
                     s_y[(k1 * R2 + n2) * TB + bi + k1 * YP] = tv;
                 }

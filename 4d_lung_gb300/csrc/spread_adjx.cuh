@@ -40,7 +40,7 @@ struct SaxLayout {
     // transform's stage 2 fall in different halves of the banks
     static constexpr int GS = PTS + PTS / 16;
     static constexpr long long fixed = (long long)SAX_NST * PS * sizeof(unsigned) +
-                                       (long long)CC * GS * sizeof(float2) + (long long)L * sizeof(float2) +
+                                       (long long)CC * GS * sizeof(float2) + (long long)(L + R2) * sizeof(float2) +
                                        SAX_NST * sizeof(uint64_t);
     // staged taps per stage: what the 227 KiB of a block's shared memory
     // leave (at most 8192, an even count; 0: never staged)
@@ -69,13 +69,13 @@ __global__ void __launch_bounds__(SAX_NT, 1) k_spread_adjx(SpreadAdjxArgs a, int
     unsigned* s_ptr = reinterpret_cast<unsigned*>(s_ent + SAX_NST * CAP);     // [SAX_NST][PS]
     float2* s_g = reinterpret_cast<float2*>(s_ptr + SAX_NST * PS);           // [CC][L][TB]
     float2* s_tw = s_g + CC * GS;                                             // W^m, or [n2][k1] signed (FOLD)
-    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
+    uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L + R2);
     const int tid = threadIdx.x;
     if (FOLD) {
         for (int m = tid; m < L; m += SAX_NT) {
             const int n2 = m / R1, k1 = m - n2 * R1;
             const float2 w = a.tw[n2 * k1];
-            s_tw[m] = ((n2 + k1) & 1) ? cneg(w) : w;
+            s_tw[n2 * (R1 + 1) + k1] = ((n2 + k1) & 1) ? cneg(w) : w;   // rows padded by one: no bank conflicts
         }
     } else {
         for (int m = tid; m < L; m += SAX_NT) s_tw[m] = a.tw[m];
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(SAX_NT, 1) k_spread_adjx(SpreadAdjxArgs a, int
 #pragma unroll
                 for (int k1 = 0; k1 < R1; ++k1) {
                     float2 tv = v[k1];
-                    if (FOLD) tv = table_twiddle<+1>(tv, s_tw[n2 * R1 + k1]);
+                    if (FOLD) tv = table_twiddle<+1>(tv, s_tw[n2 * (R1 + 1) + k1]);
                     else if (k1 > 0) tv = table_twiddle<+1>(tv, s_tw[n2 * k1]);
                     g[gi(k1 * R2 + n2, bi)] = tv;
                 }
