@@ -901,9 +901,12 @@ struct ZPipeLayout {
     // elements of one stage: S tile (+ z-buffer tile for the adjoint)
     __host__ __device__ static size_t stage_elems(int Iz, bool adj) { return (size_t)LPB * Iz + (adj ? (size_t)LPB * L : 0); }
     // forward: the block's x * apod lines stay in shared memory across the coils
+    // twiddles W^(n2 k1) as R2 rows of R1 + 1 (padded: a warp's rows in
+    // different banks)
+    static constexpr int TW = R2 * (R1 + 1);
     static size_t smem_bytes(int Iz, bool adj)
     {
-        return (NST * stage_elems(Iz, adj) + L + (size_t)LPB * Lay::LINE + (adj ? 0 : (size_t)LPB * Iz)) *
+        return (NST * stage_elems(Iz, adj) + TW + (size_t)LPB * Lay::LINE + (adj ? 0 : (size_t)LPB * Iz)) *
                    sizeof(float2) +
                16 * NST;
     }
@@ -922,12 +925,15 @@ k_fwd_z_pipe(FwdZArgs a)
     extern __shared__ float4 s_dyn[];
     const size_t se = ZL::stage_elems(a.Iz, false);
     float2* s_stage = reinterpret_cast<float2*>(s_dyn);
-    float2* s_tw = s_stage + NST * se;
-    float2* s_y = s_tw + L;
+    float2* s_tw = s_stage + NST * se;      // [R2][R1 + 1]: W^(n2 k1)
+    float2* s_y = s_tw + ZL::TW;
     float2* s_xa = s_y + LPB * Lay::LINE;   // x * apod * parity of the block's lines, [LPB][Iz]
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_xa + (size_t)LPB * a.Iz);
     const int tid = threadIdx.x;
-    for (int m = tid; m < L; m += ZL::NT) s_tw[m] = a.tw[m];
+    for (int m = tid; m < L; m += ZL::NT) {
+        const int r = m / R1, q = m - r * R1;
+        s_tw[r * (R1 + 1) + q] = a.tw[r * q];
+    }
     const int item = zp_item(a.nbatch);
     const long long line0 = zp_lblk(a.nbatch) * LPB;
     const int rows = (int)min((long long)LPB, a.nl - line0);
@@ -998,7 +1004,7 @@ k_fwd_z_pipe(FwdZArgs a)
 #pragma unroll
             for (int kk = 0; kk < R1; ++kk) {
                 float2 t = v[kk];
-                if (kk > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * kk]);
+                if (kk > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * (R1 + 1) + kk]);
                 s_y[ln1 * Lay::LINE + n2 * Lay::R1P + kk] = t;
             }
         }
@@ -1032,11 +1038,14 @@ k_adj_z_pipe(AdjZArgs a)
     const size_t se = ZL::stage_elems(a.Iz, true);
     const size_t s_off = (size_t)LPB * L;   // S tile after the z-buffer tile
     float2* s_stage = reinterpret_cast<float2*>(s_dyn);
-    float2* s_tw = s_stage + NST * se;
-    float2* s_y = s_tw + L;
+    float2* s_tw = s_stage + NST * se;      // [R2][R1 + 1]: W^(n2 k1)
+    float2* s_y = s_tw + ZL::TW;
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_y + LPB * Lay::LINE);
     const int tid = threadIdx.x;
-    for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
+    for (int m = tid; m < L; m += NT) {
+        const int r = m / R1, q = m - r * R1;
+        s_tw[r * (R1 + 1) + q] = a.tw[r * q];
+    }
     const int item = zp_item(a.nbatch);
     const long long lblk = zp_lblk(a.nbatch);
     const long long line0 = lblk * LPB;
@@ -1099,7 +1108,7 @@ k_adj_z_pipe(AdjZArgs a)
 #pragma unroll
             for (int kk = 0; kk < R1; ++kk) {
                 float2 t = v[kk];
-                if (kk > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * kk]);
+                if (kk > 0) t = table_twiddle<SIGN>(t, s_tw[n2 * (R1 + 1) + kk]);
                 s_y[ln1 * Lay::LINE + n2 * Lay::R1P + kk] = t;
             }
         }
