@@ -257,6 +257,8 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
     float2* s_y = s_in + (size_t)NSTAGE * stage_elems;
     float2* s_tw = s_y + PipeLayout<R1, R2, TB, NSTAGE>::SY;   // W^m, or the signed table [n2][k1] when FOLD
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L + R2);
+    __shared__ long long s_item[NSTAGE];   // per stage: the tile's batch item,
+    __shared__ int2 s_ab[NSTAGE];          // outer index and first column
     const int tid = threadIdx.x;
     if (FOLD) {
         for (int m = tid; m < L; m += NT) {
@@ -297,6 +299,10 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
         int ai, b0;
         decode(t, item, ai, b0);
         const int s = (int)(k % NSTAGE);
+        // the tile's coordinates for the threads that transform it (read
+        // after the barriers that follow the copy's completion)
+        s_item[s] = item;
+        s_ab[s] = make_int2(ai, b0);
         mbar_arrive_expect_tx(&s_bar[s], (uint32_t)((size_t)a.Lin * TB * sizeof(float2)));   // the rows copied
         float2* dst = s_in + (size_t)s * stage_elems;
         for (int r0 = 0; r0 < a.Lin; r0 += box_rows)
@@ -319,10 +325,17 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
             }
             return;
         }
-        const long long t = blockIdx.x + k * gridDim.x;
+        // the tile's coordinates: from the issuing thread's arithmetic, or
+        // read from the list (listed tiles; measured faster than the slots)
         long long item;
         int ai, b0;
-        decode(t, item, ai, b0);
+        if (a.sup_tiles) {
+            decode(blockIdx.x + k * gridDim.x, item, ai, b0);
+        } else {
+            item = s_item[s];
+            ai = s_ab[s].x;
+            b0 = s_ab[s].y;
+        }
         const int bi = tid % TB;
         const int b = b0 + bi;
         const bool bok = b < a.B;
