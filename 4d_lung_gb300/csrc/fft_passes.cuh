@@ -483,6 +483,8 @@ k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tm
     float2* s_y = reinterpret_cast<float2*>(s_p + (size_t)NSTAGE * L * TB);
     float2* s_tw = s_y + L * TB;
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L);
+    __shared__ long long s_item[NSTAGE];   // per stage: the tile's batch item
+    __shared__ int s_b0[NSTAGE];           // and first column (left by the issuing thread)
     const int tid = threadIdx.x;
     for (int m = tid; m < L; m += NT) s_tw[m] = a.tw[m];
     if (tid == 0) {
@@ -505,6 +507,8 @@ k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tm
         int b0;
         decode(t, item, bin, b0);
         const int s = (int)(k % NSTAGE);
+        s_item[s] = item;
+        s_b0[s] = b0;
         mbar_arrive_expect_tx(&s_bar[s], (uint32_t)(stage_elems * sizeof(float2) + L * TB * sizeof(float)));
         float2* dst = s_in + (size_t)s * stage_elems;
         for (int r0 = 0; r0 < a.Lin; r0 += box_rows)
@@ -527,10 +531,10 @@ k_toep_x_tma(StridedPassArgs a, int nsub, const __grid_constant__ CUtensorMap tm
             }
             return;
         }
-        const long long t = blockIdx.x + k * gridDim.x;
-        long long item, bin;
-        int b0;
-        decode(t, item, bin, b0);
+        // the tile's coordinates, as the issuing thread decoded them (no
+        // per-thread 64-bit divisions)
+        const long long item = s_item[s];
+        const int b0 = s_b0[s];
         const int bi = tid % TB;
         const int b = b0 + bi;
         const bool bok = b < a.B;
