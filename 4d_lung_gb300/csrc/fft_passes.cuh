@@ -258,8 +258,11 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
     float2* s_tw = s_y + PipeLayout<R1, R2, TB, NSTAGE>::SY;   // W^m, or the signed table [n2][k1] when FOLD
     uint64_t* s_bar = reinterpret_cast<uint64_t*>(s_tw + L + R2);
     __shared__ long long s_item[NSTAGE];   // per stage: the tile's batch item,
-    __shared__ int2 s_ab[NSTAGE];          // outer index and first column
+    __shared__ int2 s_ab[NSTAGE];          // outer index and first column,
+    __shared__ long long s_rmb[NSTAGE];    // first row-mask word of its bin
     const int tid = threadIdx.x;
+    // columns per row-mask tile: a power of two (8 or 16)
+    const int rm_shift = a.sup_rowmask ? __ffs(a.sup_rowmask_tb) - 1 : 0;
     if (FOLD) {
         for (int m = tid; m < L; m += NT) {
             const int n2 = m / R1, k1 = m - n2 * R1;
@@ -303,6 +306,7 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
         // after the barriers that follow the copy's completion)
         s_item[s] = item;
         s_ab[s] = make_int2(ai, b0);
+        if (a.sup_rowmask) s_rmb[s] = (item / a.sup_nsub) * a.sup_rowmask_bs;
         mbar_arrive_expect_tx(&s_bar[s], (uint32_t)((size_t)a.Lin * TB * sizeof(float2)));   // the rows copied
         float2* dst = s_in + (size_t)s * stage_elems;
         for (int r0 = 0; r0 < a.Lin; r0 += box_rows)
@@ -404,11 +408,24 @@ k_fft_strided_tma(StridedPassArgs a, const __grid_constant__ CUtensorMap tmap, l
                     if constexpr (RM) {
                         if (a.sup_rowmask && a.out_off == 0 && a.Lout == L) {
                             // the x-pass tile of this thread's column (in range: b0 < B)
-                            const unsigned* mw = a.sup_rowmask + (item / a.sup_nsub) * a.sup_rowmask_bs +
-                                                 (long long)((bok ? b : b0) / a.sup_rowmask_tb) * (L / 32);
+                            const unsigned* mw = a.sup_rowmask + s_rmb[s] +
+                                                 (long long)((bok ? b : b0) >> rm_shift) * (L / 32);
                             unsigned rm[L / 32];
+                            if constexpr ((L / 32) % 4 == 0) {
+                                // 16-byte words: a bin's words and a tile's are multiples of 4
+                                const uint4* mw4 = reinterpret_cast<const uint4*>(mw);
 #pragma unroll
-                            for (int q = 0; q < L / 32; ++q) rm[q] = __ldg(mw + q);
+                                for (int q = 0; q < L / 128; ++q) {
+                                    const uint4 v4 = __ldg(mw4 + q);
+                                    rm[4 * q] = v4.x;
+                                    rm[4 * q + 1] = v4.y;
+                                    rm[4 * q + 2] = v4.z;
+                                    rm[4 * q + 3] = v4.w;
+                                }
+                            } else {
+#pragma unroll
+                                for (int q = 0; q < L / 32; ++q) rm[q] = __ldg(mw + q);
+                            }
 #pragma unroll
                             for (int k2 = 0; k2 < R2; ++k2) {
                                 const int l = k1 + R1 * k2;

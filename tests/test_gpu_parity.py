@@ -277,7 +277,9 @@ def test_spreading_variants_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, g
                                           # the forward y pass stores listed rows only
                                           ((32, 32, 16), (64, 64, 32), 3),
                                           # listed rows with 8-column x tiles inside 16-column y tiles
-                                          ((32, 32, 20), (64, 64, 40), 3)])
+                                          ((32, 32, 20), (64, 64, 40), 3),
+                                          # row masks read as 16-byte words (Gy / 32 a multiple of 4)
+                                          ((32, 64, 16), (64, 128, 32), 4)])
 def test_support_pruning_bitwise(gpu_lib, cgs, oracle_mod, o64, synth, img, grid, nch):
     """Sample-support pruning (x passes over the supported column tiles only,
     masked y passes, spreading tiles of supported columns only) leaves every
