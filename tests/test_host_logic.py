@@ -126,3 +126,11 @@ def test_roofline_byte_model(synth):
     assert pruned["spread"] == C8 * 100 * Gx + 4 * 100 * Gx + 8 * 500 + 40 * C8
     assert pruned["interp"] == C8 * 100 * Gx + 40 * (64 + 4 + C8)
     assert bench.apply_bytes(w, sizes) == sum(full.values())
+    # the spreading fused with the adjoint x pass: one stage that reads the
+    # matrix and the samples and writes the x pass's Ix output rows
+    fused = bench.stage_bytes(w, sizes, (cols, tiles), matrix=(500, 100 * Gx), y_listed=True, fused=True)
+    assert list(fused) == bench.STAGES_FUSED
+    assert fused["spread_adjx"] == 4 * 100 * Gx + 8 * 500 + 40 * C8 + C8 * 100 * Ix
+    assert all(fused[k] == pruned[k] for k in fused if k != "spread_adjx")
+    assert (bench.apply_bytes(w, sizes, (cols, tiles), (500, 100 * Gx), True, True) ==
+            bench.apply_bytes(w, sizes, (cols, tiles), (500, 100 * Gx), True) - C8 * 100 * Gx * 2)
