@@ -1013,9 +1013,7 @@ def run_ours(args):
 
     # end to end through the host-buffer C ABI call (pinned host memory),
     # before the device-timed solves and before the clock sampler polls the
-    # GPU: measured after the sampler's nvidia-smi had run, every other call
-    # boundary saw a 6-10 ms stall of the copies (upload 0.72 / download
-    # 1.05 ms otherwise, as measured here)
+    # GPU
     applies_per_step = nb * iters                       # this rank's bins
     total_applies_per_step = len(all_sizes) * iters     # the whole scan, all ranks
     h_data.copy_(data.cpu())
